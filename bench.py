@@ -1,0 +1,340 @@
+#!/usr/bin/env python
+"""Benchmark: Levenberg-Marquardt bundle adjustment on one GB300 (or N replicas).
+
+Workload (default): one large problem -- 88 cameras on a 200 m circle,
+64,298 points, about 385k observations with power-law views per point (mean
+about 6), 6-parameter cameras, fixed K, pixel noise N(0,1), 2% outliers --
+solved by plain FP64 Levenberg-Marquardt for up to 50 iterations (the
+LM->TR hand-over disabled).  A step is one full solve from the same initial
+estimate.  The metric is LM iterations per second.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+* value: iterations / device time of the K solves with the problem resident
+  in HBM (CUDA events on the solver's stream, bracketing each solve; the L2
+  is flushed between solves and the per-iteration working set is larger
+  than L2 anyway).
+* e2e: the same metric through the C ABI from host buffers: psba_create
+  (upload, index lists) + psba_levmar + psba_get_params per step, host clock.
+* roofline: the Schur-complement stage (k_schur_off + k_schur_diag +
+  k_schur_reduce), timed live with CUDA events inside the timed solves.
+* cpu_baseline: the FP64 CPU oracle (a C restatement of the reference's
+  path) on the host cores, on a bounded sample of the same problem.
+* --impl reference: the CPU oracle alone (the reference's OpenCL/MSVC path
+  does not build on this machine), one LM iteration per step.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "LM iterations/s (plain FP64 Levenberg-Marquardt, 88 cams x 64,298 pts)"
+UNIT = "iterations/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--points", type=int, default=64298)
+    ap.add_argument("--cams", type=int, default=88)
+    ap.add_argument("--max-iter", type=int, default=50)
+    ap.add_argument("--cpu-iters", type=int, default=2, help="oracle LM iterations in the CPU sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    return ap.parse_args()
+
+
+def workload_config(args, sc):
+    k = np.bincount(sc.obs_pt)
+    return {
+        "workload": "LM bundle adjustment, %d cameras x %d points, %d observations (power-law views, mean %.2f), "
+                    "6-param cameras, fixed K, %d iterations max, LM->TR switch off" % (
+                        sc.n_cams, sc.n_pts, sc.n_obs, k.mean(), args.max_iter),
+        "cameras": sc.n_cams, "points": sc.n_pts, "observations": sc.n_obs,
+        "pair_entries": int(((k * (k - 1)) // 2).sum()),
+        "max_iter": args.max_iter, "precision": "fp64",
+        "l2": "flushed between solves (256 MiB write); per-iteration working set > L2",
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons, power = [], [], set(), []
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm), "power_w_max": max(power) if power else None}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs"), "measured"
+    return 6800.0, "fallback"
+
+
+def schur_bytes(sc):
+    """Algorithmic bytes of the Schur stage per trial: Y and W of every
+    observation (FP64), a 4-byte index per observation, and S (6C)^2 FP64."""
+    O, C = sc.n_obs, sc.n_cams
+    return 2 * O * 18 * 8 + O * 4 + (6 * C) ** 2 * 8
+
+
+def schur_flops(cfg):
+    """FP64 flops of the Schur stage per trial: 6x6x3 FMAs per off-diagonal
+    pair entry, (21 + 6) x 3 FMAs per observation for the diagonal blocks and ea."""
+    return 2 * 108 * cfg["pair_entries"] + 2 * 81 * cfg["observations"]
+
+
+def flush_l2(torch, buf):
+    buf.zero_()
+    torch.cuda.synchronize()
+
+
+def cpu_baseline(sc, args):
+    import oracle
+    nthreads = os.cpu_count() or 1
+    sess = oracle.Session(sc)
+    out = {}
+    for tag, th in (("threads", nthreads), ("single", 1)):
+        iters = args.cpu_iters if tag == "threads" else 1
+        o = oracle.default_opts(allow_switch=0, max_iter=iters, n_threads=th)
+        t = time.perf_counter()
+        r = sess.levmar(o)
+        dt = time.perf_counter() - t
+        out[tag] = (r.iterations / dt, r, dt)
+    sess.close()
+    return out, nthreads
+
+
+def run_reference(args):
+    """The reference arm: the FP64 CPU restatement on all host cores, one LM
+    iteration of the same problem per step (restarted from the initial
+    estimate each step)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import oracle
+    from psba_gb300 import scenes
+    sc = scenes.circle_scene(seed=0, n_cams=args.cams, n_pts=args.points, name="circle")
+    cfg = workload_config(args, sc)
+    nthreads = os.cpu_count() or 1
+    sess = oracle.Session(sc)
+    o = oracle.default_opts(allow_switch=0, max_iter=1, n_threads=nthreads)
+    for _ in range(args.warmup):
+        sess.levmar(o)
+    t = time.perf_counter()
+    iters = 0
+    for _ in range(args.steps):
+        iters += sess.levmar(o).iterations
+    dt = time.perf_counter() - t
+    sess.close()
+    value = iters / dt
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+        "config": cfg, "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                         "sample": "1 LM iteration of the same problem per step, %d steps" % args.steps},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    import psba_gb300 as P
+    from psba_gb300 import scenes
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    P.lib()
+    sc = scenes.circle_scene(seed=rank, n_cams=args.cams, n_pts=args.points, name="circle")
+    cfg = workload_config(args, sc)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    opts = P.default_opts(allow_switch=0, max_iter=args.max_iter)
+
+    solver = P.Solver(sc)
+    for _ in range(args.warmup):
+        solver.reset_params()
+        solver.levmar(opts, fetch=False, trace_cap=0)
+
+    # ---- timed region: K solves from the same initial estimate, problem resident in HBM
+    solver.set_stage_timing(True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = P.kernel_launches()
+    barrier()
+    t0 = time.perf_counter()
+    dev_ms, iters, trials, costs = [], 0, 0, []
+    for _ in range(args.steps):
+        solver.reset_params()
+        flush_l2(torch, flush)
+        r = solver.levmar(opts, fetch=False, trace_cap=0)
+        dev_ms.append(r.device_ms)
+        iters += r.iterations
+        trials += r.n_trials
+        costs.append(r.final_cost)
+    barrier()
+    wall = time.perf_counter() - t0
+    launches = P.kernel_launches() - launches0
+    clk = clocks.stop()
+    stages = solver.stage_timing()
+    solver.set_stage_timing(False)
+
+    total_dev_s = sum(dev_ms) / 1e3
+    if dist:
+        t = torch.tensor([total_dev_s, wall], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        it = torch.tensor([iters], dtype=torch.float64, device="cuda")
+        dist.all_reduce(it, op=dist.ReduceOp.SUM)
+        total_dev_s, wall = float(t[0]), float(t[1])
+        iters_all = float(it[0])
+    else:
+        iters_all = iters
+    value = iters_all / total_dev_s
+
+    # ---- end to end through the C ABI from host buffers
+    e2e_s, e2e_iters, h2d, d2h = 0.0, 0, 0, 0
+    for _ in range(args.e2e_steps):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        with P.Solver(sc) as s2:
+            r2 = s2.levmar(opts, fetch=True, trace_cap=0)
+            a, b = s2.transfer_bytes()
+        e2e_s += time.perf_counter() - t
+        e2e_iters += r2.iterations
+        h2d, d2h = a, b
+    e2e_value = e2e_iters / e2e_s
+
+    # ---- roofline of the dominant stage (Schur complement)
+    schur_ms = sum(stages[k][0] for k in ("schur_off", "schur_diag", "schur_reduce"))
+    schur_n = max(stages["schur_off"][1], 1)
+    schur_avg_s = schur_ms / schur_n / 1e3
+    peak_gbs, peak_kind = measured_peaks()
+    achieved_gbs = schur_bytes(sc) / schur_avg_s / 1e9
+    fp64_peak = P.measure_peak("fp64")
+    fp64_achieved = schur_flops(cfg) / schur_avg_s / 1e12
+    stage_ms = {k: (v[0] / v[1] if v[1] else 0.0) for k, v in stages.items()}
+    total_stage = sum(v[0] for v in stages.values())
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": sum(dev_ms) / len(dev_ms), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded generator)",
+        "config": cfg, "parallelism": "replicas" if world > 1 else "single",
+        "solves_per_s": len(dev_ms) * world / total_dev_s,
+        "latency_ms": {"p50": float(np.percentile(dev_ms, 50)), "p99": float(np.percentile(dev_ms, 99))},
+        "iterations_per_solve": iters / len(dev_ms), "trials_per_solve": trials / len(dev_ms),
+        "final_cost": costs[-1], "wall_ms_per_step": 1e3 * wall / args.steps,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "steps": args.e2e_steps},
+        "roofline": {"kernel": "schur (k_schur_off + k_schur_diag + k_schur_reduce), per trial",
+                     "bound": "hbm", "achieved": achieved_gbs, "peak": peak_gbs, "unit": "GB/s",
+                     "frac": achieved_gbs / peak_gbs, "peak_source": peak_kind, "traffic": None,
+                     "algorithmic_bytes": schur_bytes(sc), "avg_ms": schur_avg_s * 1e3,
+                     "fp64": {"achieved_tflops": fp64_achieved, "peak_tflops": fp64_peak,
+                              "frac": fp64_achieved / fp64_peak, "flops": schur_flops(cfg),
+                              "peak_source": "measured FP64 FMA kernel (psba_measure_peak)"}},
+        "stage_ms": stage_ms,
+        "stage_share": {k: (v[0] / total_stage if total_stage else 0.0) for k, v in stages.items()},
+        "clocks": clk, "gpu_launches": int(launches),
+    }
+    if rank == 0 and not args.no_cpu:
+        cb, nthreads = cpu_baseline(sc, args)
+        v, r, dt = cb["threads"]
+        # the same iterations on the GPU for a cost comparison at equal iteration count
+        with P.Solver(sc) as s3:
+            g = s3.levmar(P.default_opts(allow_switch=0, max_iter=r.iterations), fetch=False, trace_cap=0)
+        line["cpu_baseline"] = {
+            "value": v, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": "%d LM iterations of the same problem (FP64 C oracle, OpenMP), %.1f s" % (r.iterations, dt),
+            "single_thread_value": cb["single"][0],
+            "cost_after_sample": r.final_cost, "gpu_cost_after_sample": g.final_cost,
+            "cost_rel_diff": abs(g.final_cost - r.final_cost) / r.final_cost,
+        }
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

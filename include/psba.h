@@ -1,0 +1,230 @@
+/*
+ * psba_gb300 — sparse bundle adjustment (Levenberg-Marquardt and trust-region
+ * dogleg) on one NVIDIA GB300 GPU.  C ABI.
+ *
+ * This is the drop-in boundary for the reference's solver path.  The
+ * reference (shenyan0712/PSBA) exposes its solver as two C++ driver calls
+ * over a pre-staged OpenCL buffer set:
+ *
+ *   int levmar(PSBA_structPtr, int cnp, int pnp, int mnp, int n3Dpts, int nCams,
+ *              int n2Dprojs, dtype *finalErr);                         PSBA/levmar.h:6-10
+ *   int trust_region(PSBA_structPtr, int cnp, int pnp, int mnp, int n3Dpts,
+ *                    int nCams, int n2Dprojs, int *blk_idx, dtype *finalErr);
+ *                                                                      PSBA/trust_region.h:5-11
+ * with the buffers filled by fill_initBuffer2 / fill_idxBuffer
+ * (PSBA/cl_psba.cpp:138-207) and the LM<->TR alternation of PSBA/main.cpp:193-208.
+ * Here the buffer set is an opaque handle created from host arrays, and the
+ * drivers take an options struct instead of compile-time constants
+ * (PSBA/psba.h:3-18).  Everything is plain C: pointers, sizes, status codes.
+ * No call exits the process; errors are returned and described by
+ * psba_last_error().
+ *
+ * Parameter layout (the reference's, PSBA/main.cpp:131-149):
+ *   K     5 per camera: fx, cx, cy, aspect ratio, skew (held fixed)
+ *   q0    4 per camera: initial rotation quaternion s, v1, v2, v3
+ *   cams  6 per camera: v1, v2, v3 (vector part of the local rotation
+ *         quaternion, composed as q(v) (x) q0) and translation t1, t2, t3
+ *   pts   3 per point
+ *   meas  2 per observation; observations sorted by (point, camera),
+ *         each (point, camera) pair at most once (PSBA/misc.cpp:189-197)
+ *
+ * Threading: one handle is used by one host thread at a time; handles are
+ * independent.  Each handle owns one CUDA stream and its device memory.
+ */
+#ifndef PSBA_GB300_H
+#define PSBA_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* return codes */
+#define PSBA_OK 0
+#define PSBA_ERR_ARG -1      /* invalid argument (sizes, ordering, null pointer) */
+#define PSBA_ERR_CUDA -2     /* CUDA runtime error (message in psba_last_error) */
+#define PSBA_ERR_NOMEM -3    /* device allocation failed */
+#define PSBA_ERR_STATE -4    /* handle in an unusable state */
+
+/* solver status codes, identical to PSBA/psba.h:12-18 */
+#define PSBA_ITER_TURN_TO_LM 1
+#define PSBA_ITER_TURN_TO_TR 2
+#define PSBA_ITER_CONTINUE 3
+#define PSBA_ITER_ERR 4
+#define PSBA_ITER_DP_NO_CHANGE 5
+#define PSBA_ITER_ERR_SMALL_ENOUGH 6
+#define PSBA_ITER_PASS 7
+
+/* trace record kinds */
+#define PSBA_TRACE_LM_TRIAL 1      /* LM trial that produced a step; rho computed */
+#define PSBA_TRACE_LM_SOLVE_FAIL 2 /* LM trial whose reduced camera system was not SPD */
+#define PSBA_TRACE_TR_TRIAL 3      /* dogleg trial */
+#define PSBA_TRACE_TR_PB_FAIL 4    /* TR Gauss-Newton step failed; lambda raised */
+#define PSBA_TRACE_LM_STOP 5       /* LM trial ended by the step-size tests */
+
+/* precision of the per-observation stages */
+#define PSBA_PREC_FP64 0  /* every stage in FP64 */
+#define PSBA_PREC_MIXED 1 /* Jacobian, residual, W, V^-1, Y in FP32; Schur accumulation,
+                             Cholesky, damping and gain ratio in FP64 */
+
+typedef struct psba_handle psba_handle;
+
+typedef struct {
+    int n_cams;
+    int n_pts;
+    int n_obs;
+    const double *K;    /* 5 * n_cams */
+    const double *q0;   /* 4 * n_cams */
+    const double *cams; /* 6 * n_cams */
+    const double *pts;  /* 3 * n_pts */
+    const double *meas; /* 2 * n_obs */
+    const int *obs_pt;  /* n_obs, non-decreasing */
+    const int *obs_cam; /* n_obs, increasing within a point */
+} psba_problem_desc;
+
+typedef struct {
+    double tau;         /* initial damping factor, PSBA_INIT_MU (psba.h:6), 1e-3 */
+    double stop_thresh; /* PSBA_STOP_THRESH (psba.h:7), 1e-12 */
+    double eps;         /* PSBA_EPSILON (psba.h:8), 1e-12 */
+    double eps2;        /* PSBA_EPSILON2 (psba.h:9), 1e-12 */
+    int max_iter;       /* shared iteration budget, 50 (levmar.cpp:100) */
+    int allow_switch;   /* 1: LM hands over to TR after 5 good steps (levmar.cpp:215-219) */
+    int precision;      /* PSBA_PREC_* */
+    int reserved;
+} psba_opts;
+
+typedef struct {
+    int itno;
+    int kind;     /* PSBA_TRACE_* */
+    int accepted; /* 1 if the parameters were updated */
+    int pad;
+    double damping; /* mu (LM) or trust radius before the trial (TR) */
+    double rho;     /* gain ratio, NaN when not computed */
+    double cost;    /* sum of squared residuals at the trial point, NaN when not computed */
+    double lambda;  /* TR: lambda of the Gauss-Newton step */
+} psba_trace_entry;
+
+typedef struct {
+    int status;           /* PSBA_ITER_* of the last driver */
+    int iterations;       /* shared iteration counter on return */
+    double initial_cost;  /* sum of squared residuals before the first step */
+    double final_cost;    /* the driver's finalErr */
+    int n_trace;          /* number of trace records produced (may exceed trace_cap) */
+    int trace_cap;        /* capacity of trace (caller-set) */
+    psba_trace_entry *trace; /* caller-owned buffer of trace_cap records, or NULL */
+    double device_ms;     /* GPU time of the solve, CUDA events on the handle's stream */
+    int n_trials;         /* damping trials run */
+    int n_linearizations; /* Jacobian evaluations run */
+} psba_result;
+
+/* ---- lifetime ---------------------------------------------------------- */
+
+/* Default options: the reference's compile-time constants (PSBA/psba.h:3-18). */
+void psba_default_opts(psba_opts *opts);
+
+/* Replaces setup_cl + fill_initBuffer2 + generate_idxs + fill_idxBuffer
+ * (PSBA/cl_psba.cpp:16-207, PSBA/misc.cpp:178-218): validates the problem,
+ * copies it to the device and builds the camera-sorted and camera-pair
+ * index lists there.  The host arrays may be freed afterwards. */
+int psba_create(const psba_problem_desc *desc, psba_handle **out);
+
+/* Replaces release of the PSBA_struct buffers. */
+int psba_destroy(psba_handle *h);
+
+/* Current parameters (the reference updates cams_buffer / pts3D_buffer in
+ * place, sba_func.cpp:1170-1214). */
+int psba_get_params(psba_handle *h, double *cams, double *pts);
+int psba_set_params(psba_handle *h, const double *cams, const double *pts);
+
+/* Restores the initial estimate given to psba_create, on the device (the
+ * reference re-reads its input files instead, PSBA/main.cpp:102-180). */
+int psba_reset_params(psba_handle *h);
+
+/* ---- drivers ----------------------------------------------------------- */
+
+/* levmar(), PSBA/levmar.cpp:45-256.  *itno is the shared iteration counter
+ * (the reference's global itno, main.cpp:27); it is advanced in place. */
+int psba_levmar(psba_handle *h, const psba_opts *opts, int *itno, psba_result *res);
+
+/* trust_region(), PSBA/trust_region.cpp:49-288 (dogleg / 2-D subspace step
+ * with the modified-Cholesky lambda fallback). */
+int psba_trust_region(psba_handle *h, const psba_opts *opts, int *itno, psba_result *res);
+
+/* The LM <-> TR alternation of PSBA/main.cpp:193-208, from itno = 0. */
+int psba_solve_hybrid(psba_handle *h, const psba_opts *opts, psba_result *res);
+
+/* ---- stage evaluation (parity checks; reference layouts, host buffers) -- */
+
+/* compute_exQT (sba_func.cpp:81-145): ex = meas - projection; *cost = sum ex^2. */
+int psba_eval_residual(psba_handle *h, double *ex, double *cost);
+
+/* compute_jacobiQT (sba_func.cpp:153-245): JA 2x6 and JB 2x3 per observation. */
+int psba_eval_jacobian(psba_handle *h, double *JA, double *JB);
+
+/* compute_U/V/Wblks/g (sba_func.cpp:252-617) with factor coeff: U 6x6 per
+ * camera, V 3x3 per point, W 6x3 per observation, g = [ga | gb]. */
+int psba_eval_normal(psba_handle *h, double coeff, double *U, double *V, double *W, double *g);
+
+/* After psba_eval_normal: one damping trial's reduced system
+ * (update_UV, compute_Vinv, compute_Yblks, compute_S, compute_ea;
+ * levmar.cpp:126-131): Vinv 3x3 per point, Y 6x3 per observation,
+ * S (6C x 6C, lower triangle defined, upper set to zero), ea (6C). */
+int psba_eval_reduced(psba_handle *h, double mu, double *Vinv, double *Y, double *S, double *ea);
+
+/* After psba_eval_reduced: the step dp = [dpa | dpb] of SPDinv + matVec_mul +
+ * compute_eb + compute_dpb (levmar.cpp:134-155).  *chol_status is 0 when S
+ * was factored, 1 when it was not SPD (dp untouched). */
+int psba_eval_step(psba_handle *h, double *dp, int *chol_status);
+
+/* compute_Jmultiply (sba_func.cpp:19-75) for the last Jacobian: out holds the
+ * 2 entries per observation (the reference's dense grid minus its zeros). */
+int psba_eval_jmultiply(psba_handle *h, const double *x, double *out);
+
+/* Modified Cholesky of cholmod_blk + compute_cholmod_E (cl_cholmod.cpp:25-202)
+ * on an n x n matrix (lower triangle read); writes the factor (lower) to S
+ * and the diagonal correction to E.  Runs on the device; n % 3 == 0. */
+int psba_eval_cholmod(int n, double *S, double *E);
+
+/* ---- measurement (no reference counterpart: the reference only keeps
+ * host clock() totals, PSBA/main.cpp:22-37,220-227) ---------------------- */
+
+/* Stage timing with CUDA events on the handle's stream.  enable != 0 turns
+ * it on and clears the totals.  Stage order: linearize (camera tables,
+ * residual, Jacobian, W), point blocks (V, gb), camera blocks (U, ga), V^-1,
+ * Y, Schur off-diagonal, Schur diagonal + ea, Schur reduction, Cholesky +
+ * solves, eb/dpb, trial cost. */
+#define PSBA_N_STAGES 11
+int psba_set_stage_timing(psba_handle *h, int enable);
+/* Fills total_ms[k] and counts[k] for k < n; returns the number of stages. */
+int psba_get_stage_timing(psba_handle *h, double *total_ms, long long *counts, int n);
+
+/* Host<->device bytes copied by the handle so far (problem upload, index
+ * lists, parameter read-back). */
+int psba_transfer_bytes(psba_handle *h, size_t *h2d, size_t *d2h);
+
+/* Kernels launched by this library in the process so far. */
+long long psba_kernel_launches(void);
+
+/* FMA throughput of the current device in TFLOP/s: which = 0 FP64, 1 FP32. */
+int psba_measure_peak(int which, double *tflops);
+
+/* ---- misc -------------------------------------------------------------- */
+
+/* Message of the last error on the calling thread. */
+const char *psba_last_error(void);
+
+/* CUDA stream (cudaStream_t) of the handle, for callers that time or order
+ * their own work around a solve. */
+void *psba_stream(psba_handle *h);
+
+/* Device bytes held by the handle. */
+size_t psba_device_bytes(psba_handle *h);
+
+/* Library version string. */
+const char *psba_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

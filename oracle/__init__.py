@@ -79,6 +79,11 @@ def lib():
                                        C.POINTER(Result)]
         L.orc_pair_count.argtypes = [C.POINTER(Problem)]
         L.orc_pair_count.restype = C.c_longlong
+        L.orc_session_new.argtypes = [C.POINTER(Problem)]
+        L.orc_session_new.restype = C.c_void_p
+        for f in ("orc_session_levmar", "orc_session_trust_region"):
+            getattr(L, f).argtypes = [C.c_void_p, _dp, _dp, C.POINTER(Opts), _ip, C.POINTER(Result)]
+        L.orc_session_free.argtypes = [C.c_void_p]
         _lib = L
     return _lib
 
@@ -268,3 +273,36 @@ def solve_hybrid(scene, opts=None, **kw):
 def pair_count(scene):
     pr = OracleProblem(scene)
     return lib().orc_pair_count(pr.ref)
+
+
+class Session:
+    """Oracle problem with index lists built once (for timing repeated LM calls)."""
+
+    def __init__(self, scene):
+        self.pr = OracleProblem(scene)
+        self.cams0 = _f64(scene.cams).copy()
+        self.pts0 = _f64(scene.pts).copy()
+        self.s = lib().orc_session_new(self.pr.ref)
+        if not self.s:
+            raise MemoryError("oracle session")
+
+    def levmar(self, opts, cams=None, pts=None, itno=0, trace_cap=256):
+        cams = self.cams0.copy() if cams is None else _f64(cams).copy()
+        pts = self.pts0.copy() if pts is None else _f64(pts).copy()
+        tr = np.zeros(trace_cap, dtype=TRACE_DTYPE)
+        res = Result(0, 0, 0.0, 0.0, 0, trace_cap, tr.ctypes.data_as(C.POINTER(Trace)))
+        it = C.c_int(itno)
+        lib().orc_session_levmar(self.s, _d(cams), _d(pts), C.byref(opts), C.byref(it), C.byref(res))
+        n = min(res.n_trace, trace_cap)
+        return Run(res.status, res.iterations, res.initial_cost, res.final_cost, tr[:n].copy(), cams, pts)
+
+    def close(self):
+        if self.s:
+            lib().orc_session_free(self.s)
+            self.s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

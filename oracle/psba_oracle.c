@@ -1358,3 +1358,38 @@ int orc_solve_hybrid(const orc_problem *p, double *cams, double *pts, const orc_
     ws_free(&w);
     return flag;
 }
+
+/* A problem with its index lists and work buffers built once, for timing
+ * repeated driver calls (the reference builds its index tables once too,
+ * PSBA/main.cpp:183-189). */
+struct orc_session {
+    orc_ws w;
+};
+
+orc_session *orc_session_new(const orc_problem *p)
+{
+    orc_session *s = (orc_session *)calloc(1, sizeof(orc_session));
+    if (s) ws_init(&s->w, p);
+    return s;
+}
+
+int orc_session_levmar(orc_session *s, double *cams, double *pts, const orc_opts *o, int *itno,
+                       orc_result *res)
+{
+    set_threads(o);
+    return levmar_ws(&s->w, cams, pts, o, itno, res);
+}
+
+int orc_session_trust_region(orc_session *s, double *cams, double *pts, const orc_opts *o, int *itno,
+                             orc_result *res)
+{
+    set_threads(o);
+    return trust_region_ws(&s->w, cams, pts, o, itno, res);
+}
+
+void orc_session_free(orc_session *s)
+{
+    if (!s) return;
+    ws_free(&s->w);
+    free(s);
+}

@@ -112,8 +112,16 @@ int orc_trust_region(const orc_problem *p, double *cams, double *pts, const orc_
 int orc_solve_hybrid(const orc_problem *p, double *cams, double *pts, const orc_opts *o,
                      orc_result *res);
 
-/* scene with its derived index lists; opaque handle for repeated driver calls */
 long long orc_pair_count(const orc_problem *p);
+
+/* problem with its index lists and buffers built once, for repeated driver calls */
+typedef struct orc_session orc_session;
+orc_session *orc_session_new(const orc_problem *p);
+int orc_session_levmar(orc_session *s, double *cams, double *pts, const orc_opts *o, int *itno,
+                       orc_result *res);
+int orc_session_trust_region(orc_session *s, double *cams, double *pts, const orc_opts *o, int *itno,
+                             orc_result *res);
+void orc_session_free(orc_session *s);
 
 #ifdef __cplusplus
 }

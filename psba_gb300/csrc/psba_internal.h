@@ -1,0 +1,180 @@
+// Internal declarations shared by the kernels, the dense solver and the host
+// drivers.  Not part of the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/psba.h"
+
+namespace psba {
+
+constexpr int CNP = 6;   // camera parameters (rotation vector part + translation)
+constexpr int PNP = 3;   // point parameters
+constexpr int MNP = 2;   // image coordinates
+constexpr int CAMTAB = 48;  // doubles per camera table entry (CamTab)
+constexpr int TILE = 32;    // dense Cholesky block size
+constexpr int SCHUR_CHUNK = 64;  // pair-list entries per Schur work unit
+constexpr int CAM_CHUNK = 512;   // observations per camera-reduction work unit
+constexpr int RED_THREADS = 256; // threads of the reduction kernels
+
+// Per-camera table, computed once per parameter vector on the device:
+// rotation M = R(q(v) (x) q0) (row-major), the derivative of M with
+// respect to each component of v (D[m]), translation and intrinsics.
+struct CamTab {
+    double M[9];
+    double D[27];
+    double t[3];
+    double fx, sk, cx, fy, cy;  // fy = fx * aspect
+    double pad[4];
+};
+static_assert(sizeof(CamTab) == CAMTAB * sizeof(double), "CamTab layout");
+
+// Scalars that one damping trial returns to the host in a single copy.
+struct TrialScalars {
+    double dp_L2;     // sum dp^2
+    double rho_den;   // sum dp (mu dp + g)
+    double new_cost;  // sum of squared residuals at p + dp
+    double dot_g_dp;  // sum g dp (trust region prediction)
+    int chol_status;  // 0: factored; 1: not SPD
+    int pad;
+    double extra[3];
+};
+
+// A unit of Schur work: a contiguous range of one camera pair's entry list
+// (or of one camera's observation list for the diagonal blocks).  Units run
+// in any order; `out` is the unit's position in the pair-major, chunk-ordered
+// partial array that the reduction sums in order.
+struct SchurUnit {
+    int slot;   // camera pair (off-diagonal) or camera (diagonal)
+    int begin;  // first entry
+    int count;  // number of entries (<= SCHUR_CHUNK)
+    int out;    // partial-sum slot
+};
+
+// Camera-reduction work unit (per-camera sums over the camera-sorted list).
+struct CamUnit {
+    int cam;
+    int begin;
+    int count;
+    int pad;
+};
+
+const char *set_error(const std::string &msg);
+void note_launch(int n);     // counts kernel launches (psba_kernel_launches)
+long long launch_count();
+
+// ---- kernel launchers (psba_kernels.cu) ---------------------------------
+
+struct DeviceProblem {
+    int nc = 0, np = 0, no = 0, N = 0, Np = 0;  // N = 6 nc, Np = N padded to TILE
+    // problem (immutable)
+    double *K = nullptr, *q0 = nullptr, *meas = nullptr;
+    int *obs_pt = nullptr, *obs_cam = nullptr;
+    int *pt_start = nullptr;   // np + 1
+    int *cam_obs = nullptr;    // observations sorted by (camera, point)
+    // camera pair lists for the off-diagonal Schur blocks (k > l)
+    int n_pairs = 0;           // nonempty pairs
+    int *pair_kl = nullptr;    // 2 per pair: k, l
+    int *pair_a = nullptr;     // entries: observation of camera k
+    int *pair_b = nullptr;     // entries: observation of camera l
+    long long n_pair_entries = 0;
+    SchurUnit *off_units = nullptr;
+    int n_off_units = 0;
+    int *off_unit_start = nullptr;  // per pair: first unit (n_pairs + 1)
+    SchurUnit *diag_units = nullptr;  // per camera chunks of cam_obs
+    int n_diag_units = 0;
+    int *diag_unit_start = nullptr;   // per camera (nc + 1)
+    CamUnit *cam_units = nullptr;
+    int n_cam_units = 0;
+    int *cam_unit_start = nullptr;    // per camera (nc + 1)
+    // parameters
+    double *cams = nullptr, *pts = nullptr;
+    double *cams0 = nullptr, *pts0 = nullptr;  // initial estimate as uploaded
+    // per-linearization
+    double *camtab = nullptr;     // nc CamTab
+    double *camtab_new = nullptr; // nc CamTab at p + dp
+    double *ex = nullptr;         // 2 per obs
+    double *A = nullptr;          // 12 per obs
+    double *B = nullptr;          // 6 per obs
+    double *W = nullptr;          // 18 per obs
+    double *U = nullptr;          // 36 per camera
+    double *V = nullptr;          // 6 per point (00 01 02 11 12 22)
+    double *g = nullptr;          // N + 3 np
+    double *uvdiag = nullptr;     // N + 3 np
+    double *cam_partial = nullptr;  // n_cam_units * 27
+    // per-trial
+    double *Vinv = nullptr;       // 6 per point
+    double *Y = nullptr;          // 18 per obs
+    double *schur_partial = nullptr;  // (n_off_units * 36 + n_diag_units * 27)
+    double *S = nullptr;          // Np x Np (lower)
+    double *Ssave = nullptr;      // copy of S (TR fallback, refinement)
+    double *rhs = nullptr;        // Np (ea on entry, y after the forward solve)
+    double *xsol = nullptr;       // Np
+    double *Linv = nullptr;       // (Np / TILE) * TILE * TILE inverses of the diagonal blocks
+    int *status = nullptr;        // Cholesky status word
+    double *dp = nullptr;         // N + 3 np
+    double *eb = nullptr;         // 3 np
+    double *red_partial = nullptr;  // reduction partials
+    int red_partial_cap = 0;
+    TrialScalars *scal = nullptr; // device scalars
+    TrialScalars *scal_host = nullptr;  // pinned host mirror
+    // trust region vectors
+    double *vecPU = nullptr, *vecPB = nullptr, *vecP = nullptr, *jx1 = nullptr, *jx2 = nullptr;
+    double *E = nullptr;
+    double *tmp9 = nullptr;       // 9 per point (full 3x3 copies for the parity interface)
+    size_t bytes = 0;
+};
+
+// Linearization: camera tables, residual, Jacobian, W, V, gb, U, ga.
+void launch_cam_tables(const DeviceProblem &d, const double *cams, const double *dpa,
+                       double *tab, cudaStream_t s);
+void launch_linearize(const DeviceProblem &d, double coeff, cudaStream_t s);
+void launch_point_blocks(const DeviceProblem &d, double coeff, cudaStream_t s);
+void launch_camera_blocks(const DeviceProblem &d, double coeff, cudaStream_t s);
+// Residual only (ex) at the current parameters, and its sum of squares.
+void launch_residual(const DeviceProblem &d, const double *tab, const double *pts,
+                     const double *dpb, double *ex_out, double *partial, int nblocks,
+                     cudaStream_t s);
+int residual_blocks(const DeviceProblem &d);
+
+// Damping trial: V^-1, Y, Schur complement, ea.
+void launch_vinv(const DeviceProblem &d, double mu, cudaStream_t s);
+void launch_yblocks(const DeviceProblem &d, cudaStream_t s);
+void launch_schur(const DeviceProblem &d, double mu, cudaStream_t s);
+void launch_schur_off(const DeviceProblem &d, cudaStream_t s);
+void launch_schur_diag(const DeviceProblem &d, cudaStream_t s);
+void launch_schur_reduce(const DeviceProblem &d, double mu, cudaStream_t s);
+// Back-substitution: eb, dpb and partial sums for |dp|^2 and dp.(mu dp + g).
+void launch_eb_dpb(const DeviceProblem &d, double mu, cudaStream_t s);
+int eb_blocks(const DeviceProblem &d);
+void launch_update_params(const DeviceProblem &d, cudaStream_t s);
+
+// Deterministic reductions and vector helpers.
+void launch_sum_partials(const double *partial, int n, double *dst, cudaStream_t s);
+void launch_finish_trial(const DeviceProblem &d, double mu, cudaStream_t s);
+void launch_max_uvdiag(const DeviceProblem &d, double *dst, cudaStream_t s);
+void launch_sumsq(const double *x, long long n, double *partial, int nblocks, double *dst,
+                  cudaStream_t s);
+void launch_dot(const double *x, const double *y, long long n, double *partial, int nblocks,
+                double *dst, cudaStream_t s);
+void launch_jmultiply(const DeviceProblem &d, const double *x, double *out, cudaStream_t s);
+void launch_axpby(double *out, const double *x, double a, const double *y, double b, long long n,
+                  cudaStream_t s);
+void launch_scale(double *out, const double *x, const double *num, const double *den,
+                  double den_scale, double sign, long long n, cudaStream_t s);
+
+// Dense reduced-camera solve (psba_dense.cu): Cholesky of S (Np x Np, lower),
+// forward solve of rhs in the same sweep, back solve into xsol.
+void launch_cholesky_solve(const DeviceProblem &d, cudaStream_t s);
+// Modified Cholesky (trust-region lambda fallback) and its diagonal correction.
+void launch_cholmod(double *S, int n, int ld, double *E, double *work, cudaStream_t s);
+
+// Copies for the parity interface.
+void launch_expand_V(const DeviceProblem &d, const double *V6, double *V9, cudaStream_t s);
+
+}  // namespace psba

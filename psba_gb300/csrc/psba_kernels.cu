@@ -1,0 +1,900 @@
+// Sparse stages of one Levenberg-Marquardt / dogleg iteration, FP64, sm_103a.
+//
+// Layout in HBM (all per-observation arrays follow the observation order,
+// which is (point, camera) sorted as the reference's generate_idxs,
+// PSBA/misc.cpp:189-197):
+//   ex 2, A 12 (2x6 row-major), B 6 (2x3), W 18 (6x3), Y 18 (6x3) doubles per
+//   observation; V and V^-1 6 doubles per point (upper triangle 00 01 02 11 12
+//   22); U 36 per camera; g = [ga (6C) | gb (3P)].
+// Every reduction runs in a fixed order (no floating-point atomics), so a
+// solve is bit-for-bit repeatable.
+#include "psba_internal.h"
+
+namespace psba {
+
+static inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// ---------------------------------------------------------------------------
+// Camera tables.  q = q(v) (x) q0 (compute_exQT.cl:82-87), M = matrix of
+// X -> q (0,X) conj(q), D[m] = dM/dv_m through q(v) with s = sqrt(1-|v|^2).
+__global__ void k_cam_tables(int nc, const double *__restrict__ K, const double *__restrict__ q0,
+                             const double *__restrict__ cams, const double *__restrict__ dpa,
+                             double *__restrict__ tab)
+{
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= nc) return;
+    double vl[3], t[3];
+    for (int m = 0; m < 3; ++m) {
+        vl[m] = dpa ? cams[6 * j + m] + dpa[6 * j + m] : cams[6 * j + m];
+        t[m] = dpa ? cams[6 * j + 3 + m] + dpa[6 * j + 3 + m] : cams[6 * j + 3 + m];
+    }
+    const double s0 = q0[4 * j], a1 = q0[4 * j + 1], a2 = q0[4 * j + 2], a3 = q0[4 * j + 3];
+    const double sl = sqrt(1.0 - vl[0] * vl[0] - vl[1] * vl[1] - vl[2] * vl[2]);
+    const double s = sl * s0 - (a1 * vl[0] + a2 * vl[1] + a3 * vl[2]);
+    const double a = s0 * vl[0] + sl * a1 + a3 * vl[1] - a2 * vl[2];
+    const double b = s0 * vl[1] + sl * a2 + a1 * vl[2] - a3 * vl[0];
+    const double c = s0 * vl[2] + sl * a3 + a2 * vl[0] - a1 * vl[1];
+    CamTab T;
+    const double d = s * s - (a * a + b * b + c * c);
+    T.M[0] = d + 2 * a * a;      T.M[1] = 2 * (a * b - s * c); T.M[2] = 2 * (a * c + s * b);
+    T.M[3] = 2 * (a * b + s * c); T.M[4] = d + 2 * b * b;      T.M[5] = 2 * (b * c - s * a);
+    T.M[6] = 2 * (a * c - s * b); T.M[7] = 2 * (b * c + s * a); T.M[8] = d + 2 * c * c;
+    // dM/d(s, a, b, c)
+    const double dS[9] = {2 * s, -2 * c, 2 * b, 2 * c, 2 * s, -2 * a, -2 * b, 2 * a, 2 * s};
+    const double dA[9] = {2 * a, 2 * b, 2 * c, 2 * b, -2 * a, -2 * s, 2 * c, 2 * s, -2 * a};
+    const double dB[9] = {-2 * b, 2 * a, 2 * s, 2 * a, 2 * b, 2 * c, -2 * s, 2 * c, -2 * b};
+    const double dC[9] = {-2 * c, -2 * s, 2 * a, 2 * s, -2 * c, 2 * b, 2 * a, 2 * b, 2 * c};
+    const double av[3] = {a1, a2, a3};
+    for (int m = 0; m < 3; ++m) {
+        const double ds = -vl[m] / sl;
+        // dq/dv_m = (s0 ds - a0_m,  a0 ds + s0 e_m + e_m x a0)
+        double e_x_a[3] = {0, 0, 0};
+        if (m == 0) { e_x_a[1] = -a3; e_x_a[2] = a2; }
+        if (m == 1) { e_x_a[0] = a3; e_x_a[2] = -a1; }
+        if (m == 2) { e_x_a[0] = -a2; e_x_a[1] = a1; }
+        const double dq0 = s0 * ds - av[m];
+        double dqv[3];
+        for (int r = 0; r < 3; ++r) dqv[r] = av[r] * ds + (r == m ? s0 : 0.0) + e_x_a[r];
+        for (int e = 0; e < 9; ++e)
+            T.D[9 * m + e] = dS[e] * dq0 + dA[e] * dqv[0] + dB[e] * dqv[1] + dC[e] * dqv[2];
+    }
+    T.t[0] = t[0]; T.t[1] = t[1]; T.t[2] = t[2];
+    const double *k = K + 5 * j;
+    T.fx = k[0]; T.cx = k[1]; T.cy = k[2]; T.fy = k[0] * k[3]; T.sk = k[4];
+    T.pad[0] = T.pad[1] = T.pad[2] = T.pad[3] = 0.0;
+    double *o = tab + (size_t)CAMTAB * j;
+    const double *src = reinterpret_cast<const double *>(&T);
+    for (int e = 0; e < CAMTAB; ++e) o[e] = src[e];
+}
+
+void launch_cam_tables(const DeviceProblem &d, const double *cams, const double *dpa, double *tab,
+                       cudaStream_t s)
+{
+    k_cam_tables<<<ceil_div(d.nc, 128), 128, 0, s>>>(d.nc, d.K, d.q0, cams, dpa, tab); note_launch(1);
+}
+
+// ---------------------------------------------------------------------------
+// Linearization, one thread per observation: residual (compute_exQT.cl),
+// Jacobian blocks A = d(x,y)/d(v,t), B = d(x,y)/dX (compute_jacobiQT.cl) by
+// the chain rule through the camera table, and W = coeff A^T B
+// (compute_Wblks.cl:28-33).
+__global__ void __launch_bounds__(256) k_linearize(int no, const int *__restrict__ obs_pt,
+                                                   const int *__restrict__ obs_cam,
+                                                   const double *__restrict__ meas,
+                                                   const double *__restrict__ pts,
+                                                   const double *__restrict__ tab, double coeff,
+                                                   double *__restrict__ ex, double *__restrict__ A,
+                                                   double *__restrict__ B, double *__restrict__ W)
+{
+    int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= no) return;
+    const int i = __ldg(obs_pt + o), j = __ldg(obs_cam + o);
+    const double X0 = __ldg(pts + 3 * i), X1 = __ldg(pts + 3 * i + 1), X2 = __ldg(pts + 3 * i + 2);
+    const double *T = tab + (size_t)CAMTAB * j;
+    double M[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) M[e] = __ldg(T + e);
+    const double xc = M[0] * X0 + M[1] * X1 + M[2] * X2 + __ldg(T + 36);
+    const double yc = M[3] * X0 + M[4] * X1 + M[5] * X2 + __ldg(T + 37);
+    const double zc = M[6] * X0 + M[7] * X1 + M[8] * X2 + __ldg(T + 38);
+    const double fx = __ldg(T + 39), sk = __ldg(T + 40), cx = __ldg(T + 41), fy = __ldg(T + 42),
+                 cy = __ldg(T + 43);
+    const double iz = 1.0 / zc;
+    const double2 m2 = *reinterpret_cast<const double2 *>(meas + 2 * (size_t)o);
+    const double nu = fx * xc + sk * yc;
+    const double u = (nu + cx * zc) * iz;
+    const double v = (fy * yc + cy * zc) * iz;
+    double2 e2;
+    e2.x = m2.x - u;
+    e2.y = m2.y - v;
+    *reinterpret_cast<double2 *>(ex + 2 * (size_t)o) = e2;
+    // d(x,y)/dXc
+    const double p00 = fx * iz, p01 = sk * iz, p02 = -nu * iz * iz;
+    const double p11 = fy * iz, p12 = -fy * yc * iz * iz;
+    // dXc/dv = D[m] X
+    double a0[6], a1[6];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+        const double *Dm = T + 9 + 9 * m;
+        const double g0 = __ldg(Dm + 0) * X0 + __ldg(Dm + 1) * X1 + __ldg(Dm + 2) * X2;
+        const double g1 = __ldg(Dm + 3) * X0 + __ldg(Dm + 4) * X1 + __ldg(Dm + 5) * X2;
+        const double g2 = __ldg(Dm + 6) * X0 + __ldg(Dm + 7) * X1 + __ldg(Dm + 8) * X2;
+        a0[m] = p00 * g0 + p01 * g1 + p02 * g2;
+        a1[m] = p11 * g1 + p12 * g2;
+    }
+    a0[3] = p00; a0[4] = p01; a0[5] = p02;
+    a1[3] = 0.0; a1[4] = p11; a1[5] = p12;
+    double b0[3], b1[3];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+        b0[m] = p00 * M[m] + p01 * M[3 + m] + p02 * M[6 + m];
+        b1[m] = p11 * M[3 + m] + p12 * M[6 + m];
+    }
+    double2 *Ao = reinterpret_cast<double2 *>(A + 12 * (size_t)o);
+    Ao[0] = make_double2(a0[0], a0[1]); Ao[1] = make_double2(a0[2], a0[3]);
+    Ao[2] = make_double2(a0[4], a0[5]); Ao[3] = make_double2(a1[0], a1[1]);
+    Ao[4] = make_double2(a1[2], a1[3]); Ao[5] = make_double2(a1[4], a1[5]);
+    double2 *Bo = reinterpret_cast<double2 *>(B + 6 * (size_t)o);
+    Bo[0] = make_double2(b0[0], b0[1]); Bo[1] = make_double2(b0[2], b1[0]);
+    Bo[2] = make_double2(b1[1], b1[2]);
+    double w[18];
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) w[r * 3 + c] = coeff * (a0[r] * b0[c] + a1[r] * b1[c]);
+    double2 *Wo = reinterpret_cast<double2 *>(W + 18 * (size_t)o);
+#pragma unroll
+    for (int e = 0; e < 9; ++e) Wo[e] = make_double2(w[2 * e], w[2 * e + 1]);
+}
+
+void launch_linearize(const DeviceProblem &d, double coeff, cudaStream_t s)
+{
+    if (d.no == 0) return;
+    k_linearize<<<ceil_div(d.no, 256), 256, 0, s>>>(d.no, d.obs_pt, d.obs_cam, d.meas, d.pts,
+                                                      d.camtab, coeff, d.ex, d.A, d.B, d.W); note_launch(1);
+}
+
+// ---------------------------------------------------------------------------
+// Residual and its squared norm at (camera table, pts [+ dpb]); block partials.
+__global__ void __launch_bounds__(256) k_residual(int no, const int *__restrict__ obs_pt,
+                                                  const int *__restrict__ obs_cam,
+                                                  const double *__restrict__ meas,
+                                                  const double *__restrict__ pts,
+                                                  const double *__restrict__ dpb,
+                                                  const double *__restrict__ tab,
+                                                  double *__restrict__ ex_out,
+                                                  double *__restrict__ partial)
+{
+    __shared__ double red[256];
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    double sq = 0.0;
+    if (o < no) {
+        const int i = __ldg(obs_pt + o), j = __ldg(obs_cam + o);
+        double X[3];
+#pragma unroll
+        for (int m = 0; m < 3; ++m)
+            X[m] = dpb ? __ldg(pts + 3 * i + m) + __ldg(dpb + 3 * i + m) : __ldg(pts + 3 * i + m);
+        const double *T = tab + (size_t)CAMTAB * j;
+        const double xc = __ldg(T + 0) * X[0] + __ldg(T + 1) * X[1] + __ldg(T + 2) * X[2] + __ldg(T + 36);
+        const double yc = __ldg(T + 3) * X[0] + __ldg(T + 4) * X[1] + __ldg(T + 5) * X[2] + __ldg(T + 37);
+        const double zc = __ldg(T + 6) * X[0] + __ldg(T + 7) * X[1] + __ldg(T + 8) * X[2] + __ldg(T + 38);
+        const double iz = 1.0 / zc;
+        const double u = (__ldg(T + 39) * xc + __ldg(T + 40) * yc + __ldg(T + 41) * zc) * iz;
+        const double v = (__ldg(T + 42) * yc + __ldg(T + 43) * zc) * iz;
+        const double2 m2 = *reinterpret_cast<const double2 *>(meas + 2 * (size_t)o);
+        const double e0 = m2.x - u, e1 = m2.y - v;
+        if (ex_out) *reinterpret_cast<double2 *>(ex_out + 2 * (size_t)o) = make_double2(e0, e1);
+        sq = e0 * e0 + e1 * e1;
+    }
+    red[threadIdx.x] = sq;
+    __syncthreads();
+    for (int st = 128; st > 0; st >>= 1) {
+        if (threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
+int residual_blocks(const DeviceProblem &d) { return ceil_div(d.no > 0 ? d.no : 1, 256); }
+
+void launch_residual(const DeviceProblem &d, const double *tab, const double *pts, const double *dpb,
+                     double *ex_out, double *partial, int nblocks, cudaStream_t s)
+{
+    k_residual<<<nblocks, 256, 0, s>>>(d.no, d.obs_pt, d.obs_cam, d.meas, pts, dpb, tab, ex_out,
+                                        partial); note_launch(1);
+}
+
+// ---------------------------------------------------------------------------
+// Per-point sums: V_i = coeff sum B^T B (compute_V.cl:24-37) and
+// gb_i = coeff sum B^T e (compute_g.cl:42-57), ascending camera order.
+__global__ void k_point_blocks(int np, int ncp, const int *__restrict__ pt_start,
+                               const double *__restrict__ B, const double *__restrict__ ex,
+                               double coeff, double *__restrict__ V, double *__restrict__ g,
+                               double *__restrict__ uvdiag)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    double v00 = 0, v01 = 0, v02 = 0, v11 = 0, v12 = 0, v22 = 0, g0 = 0, g1 = 0, g2 = 0;
+    const int e = pt_start[i + 1];
+    for (int o = pt_start[i]; o < e; ++o) {
+        const double *b = B + 6 * (size_t)o;
+        const double b0 = b[0], b1 = b[1], b2 = b[2], c0 = b[3], c1 = b[4], c2 = b[5];
+        const double e0 = ex[2 * (size_t)o], e1 = ex[2 * (size_t)o + 1];
+        v00 = v00 + b0 * b0 + c0 * c0;
+        v01 = v01 + b0 * b1 + c0 * c1;
+        v02 = v02 + b0 * b2 + c0 * c2;
+        v11 = v11 + b1 * b1 + c1 * c1;
+        v12 = v12 + b1 * b2 + c1 * c2;
+        v22 = v22 + b2 * b2 + c2 * c2;
+        g0 = g0 + b0 * e0 + c0 * e1;
+        g1 = g1 + b1 * e0 + c1 * e1;
+        g2 = g2 + b2 * e0 + c2 * e1;
+    }
+    double *Vi = V + 6 * (size_t)i;
+    Vi[0] = coeff * v00; Vi[1] = coeff * v01; Vi[2] = coeff * v02;
+    Vi[3] = coeff * v11; Vi[4] = coeff * v12; Vi[5] = coeff * v22;
+    uvdiag[ncp + 3 * (size_t)i] = Vi[0];
+    uvdiag[ncp + 3 * (size_t)i + 1] = Vi[3];
+    uvdiag[ncp + 3 * (size_t)i + 2] = Vi[5];
+    g[ncp + 3 * (size_t)i] = coeff * g0;
+    g[ncp + 3 * (size_t)i + 1] = coeff * g1;
+    g[ncp + 3 * (size_t)i + 2] = coeff * g2;
+}
+
+void launch_point_blocks(const DeviceProblem &d, double coeff, cudaStream_t s)
+{
+    if (d.np == 0) return;
+    k_point_blocks<<<ceil_div(d.np, 128), 128, 0, s>>>(d.np, d.N, d.pt_start, d.B, d.ex, coeff, d.V,
+                                                         d.g, d.uvdiag); note_launch(1);
+}
+
+// ---------------------------------------------------------------------------
+// Per-camera sums U_j = coeff sum A^T A (compute_U.cl:21-34) and
+// ga_j = coeff sum A^T e (compute_g.cl:25-41) over the camera-sorted list,
+// split in units of CAM_CHUNK observations; fixed-order tree per unit, then
+// units summed in order.
+constexpr int CAM_THREADS = 128;
+constexpr int CAM_NV = 27;  // 21 upper-triangle entries of A^T A + 6 of A^T e
+
+__global__ void __launch_bounds__(CAM_THREADS) k_camera_partial(const CamUnit *__restrict__ units,
+                                                                const int *__restrict__ cam_obs,
+                                                                const double *__restrict__ A,
+                                                                const double *__restrict__ ex,
+                                                                double *__restrict__ partial)
+{
+    __shared__ double red[CAM_NV][CAM_THREADS];
+    const CamUnit u = units[blockIdx.x];
+    double acc[CAM_NV];
+#pragma unroll
+    for (int v = 0; v < CAM_NV; ++v) acc[v] = 0.0;
+    for (int t = threadIdx.x; t < u.count; t += CAM_THREADS) {
+        const int o = cam_obs[u.begin + t];
+        double a[12];
+        const double2 *Ao = reinterpret_cast<const double2 *>(A + 12 * (size_t)o);
+#pragma unroll
+        for (int e = 0; e < 6; ++e) {
+            const double2 x = Ao[e];
+            a[2 * e] = x.x;
+            a[2 * e + 1] = x.y;
+        }
+        const double2 e2 = *reinterpret_cast<const double2 *>(ex + 2 * (size_t)o);
+        int v = 0;
+#pragma unroll
+        for (int r = 0; r < 6; ++r)
+#pragma unroll
+            for (int c = r; c < 6; ++c, ++v) acc[v] = acc[v] + a[r] * a[c] + a[6 + r] * a[6 + c];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) acc[21 + k] = acc[21 + k] + a[k] * e2.x + a[6 + k] * e2.y;
+    }
+#pragma unroll
+    for (int v = 0; v < CAM_NV; ++v) red[v][threadIdx.x] = acc[v];
+    __syncthreads();
+    for (int st = CAM_THREADS / 2; st > 0; st >>= 1) {
+        if (threadIdx.x < st)
+            for (int v = 0; v < CAM_NV; ++v) red[v][threadIdx.x] += red[v][threadIdx.x + st];
+        __syncthreads();
+    }
+    if (threadIdx.x < CAM_NV) partial[(size_t)blockIdx.x * CAM_NV + threadIdx.x] = red[threadIdx.x][0];
+}
+
+__global__ void k_camera_finish(int nc, const int *__restrict__ unit_start,
+                                const double *__restrict__ partial, double coeff,
+                                double *__restrict__ U, double *__restrict__ g,
+                                double *__restrict__ uvdiag)
+{
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= nc * CAM_NV) return;
+    const int j = id / CAM_NV, v = id % CAM_NV;
+    double sum = 0.0;
+    for (int u = unit_start[j]; u < unit_start[j + 1]; ++u) sum += partial[(size_t)u * CAM_NV + v];
+    sum = coeff * sum;
+    if (v >= 21) {
+        g[6 * j + (v - 21)] = sum;
+        return;
+    }
+    // v -> (r, c), r <= c, row-major over the upper triangle
+    int r = 0, c = 0, k = v;
+    for (r = 0; r < 6; ++r) {
+        if (k < 6 - r) {
+            c = r + k;
+            break;
+        }
+        k -= 6 - r;
+    }
+    U[36 * (size_t)j + r * 6 + c] = sum;
+    U[36 * (size_t)j + c * 6 + r] = sum;
+    if (r == c) uvdiag[6 * j + r] = sum;
+}
+
+void launch_camera_blocks(const DeviceProblem &d, double coeff, cudaStream_t s)
+{
+    if (d.n_cam_units > 0)
+        k_camera_partial<<<d.n_cam_units, CAM_THREADS, 0, s>>>(d.cam_units, d.cam_obs, d.A, d.ex,
+                                                                 d.cam_partial); note_launch(1);
+    k_camera_finish<<<ceil_div(d.nc * CAM_NV, 128), 128, 0, s>>>(d.nc, d.cam_unit_start,
+                                                                   d.cam_partial, coeff, d.U, d.g,
+                                                                   d.uvdiag); note_launch(1);
+}
+
+// ---------------------------------------------------------------------------
+// V_i^-1 of the damped V_i + mu I by cofactors (compute_Vinv.cl:29-86); the
+// near-singular branch (|T| < 1e-16, :31-73) restates the reference's pivoted
+// elimination on the symmetric matrix.
+__device__ __forceinline__ void vinv_one(const double *Vi, double mu, double *out)
+{
+    const double a11 = Vi[0] + mu, a12 = Vi[1], a13 = Vi[2], a22 = Vi[3] + mu, a23 = Vi[4],
+                 a33 = Vi[5] + mu;
+    double T = (a33 * a12 * a12 - 2 * a12 * a13 * a23 + a22 * a13 * a13 + a11 * a23 * a23 -
+                a11 * a22 * a33);
+    if (fabs(T) < 1e-16) {
+        const double a21 = a12, a31 = a13, a32 = a23;
+        double m[3][3] = {{a11, a12, a13}, {a21, a22, a23}, {a31, a32, a33}}, tmp;
+        int mx = 0;
+        if (m[0][0] < m[1][0]) mx = 1;
+        if (m[mx][0] < m[2][0]) mx = 2;
+        if (mx != 0)
+            for (int c = 0; c < 3; ++c) { tmp = m[0][c]; m[0][c] = m[mx][c]; m[mx][c] = tmp; }
+        m[1][0] = m[1][0] / m[0][0];
+        m[2][0] = m[2][0] / m[0][0];
+        m[1][1] = m[1][1] - m[1][0] * m[0][1];
+        m[1][2] = m[1][2] - m[1][0] * m[0][2];
+        m[2][1] = m[2][1] - m[2][0] * m[0][1];
+        m[2][2] = m[2][2] - m[2][0] * m[0][2];
+        if (m[1][1] < m[2][1])
+            for (int c = 0; c < 3; ++c) { tmp = m[1][c]; m[1][c] = m[2][c]; m[2][c] = tmp; }
+        if (m[1][1] != 0.0) {
+            m[2][1] = m[2][1] / m[1][1];
+            m[2][2] = m[2][2] - m[2][1] * m[1][2];
+        }
+        T = m[0][0] * m[1][1] * m[2][2];
+        out[0] = (a22 * a33 - a23 * a32) / T;
+        out[1] = -(a21 * a33 - a23 * a31) / T;
+        out[2] = (a21 * a32 - a22 * a31) / T;
+        out[3] = (a11 * a33 - a13 * a31) / T;
+        out[4] = -(a11 * a32 - a12 * a31) / T;
+        out[5] = (a11 * a22 - a12 * a21) / T;
+        return;
+    }
+    out[0] = -(-a23 * a23 + a22 * a33) / T;
+    out[1] = -(a13 * a23 - a12 * a33) / T;
+    out[2] = -(a12 * a23 - a13 * a22) / T;
+    out[3] = -(-a13 * a13 + a11 * a33) / T;
+    out[4] = -(a12 * a13 - a11 * a23) / T;
+    out[5] = -(-a12 * a12 + a11 * a22) / T;
+}
+
+__global__ void k_vinv(int np, const double *__restrict__ V, double mu, double *__restrict__ Vinv)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    double vi[6], out[6];
+    for (int e = 0; e < 6; ++e) vi[e] = V[6 * (size_t)i + e];
+    vinv_one(vi, mu, out);
+    for (int e = 0; e < 6; ++e) Vinv[6 * (size_t)i + e] = out[e];
+}
+
+void launch_vinv(const DeviceProblem &d, double mu, cudaStream_t s)
+{
+    if (d.np == 0) return;
+    k_vinv<<<ceil_div(d.np, 128), 128, 0, s>>>(d.np, d.V, mu, d.Vinv); note_launch(1);
+}
+
+// Y = W V^-1 (compute_Yblks.cl:26-37), one thread per observation.
+__global__ void __launch_bounds__(256) k_yblocks(int no, const int *__restrict__ obs_pt,
+                                                 const double *__restrict__ W,
+                                                 const double *__restrict__ Vinv,
+                                                 double *__restrict__ Y)
+{
+    int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= no) return;
+    const double *vi = Vinv + 6 * (size_t)__ldg(obs_pt + o);
+    const double s00 = __ldg(vi), s01 = __ldg(vi + 1), s02 = __ldg(vi + 2), s11 = __ldg(vi + 3),
+                 s12 = __ldg(vi + 4), s22 = __ldg(vi + 5);
+    const double2 *Wo = reinterpret_cast<const double2 *>(W + 18 * (size_t)o);
+    double w[18];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) {
+        const double2 x = Wo[e];
+        w[2 * e] = x.x;
+        w[2 * e + 1] = x.y;
+    }
+    double y[18];
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+        const double w0 = w[3 * r], w1 = w[3 * r + 1], w2 = w[3 * r + 2];
+        y[3 * r + 0] = w0 * s00 + w1 * s01 + w2 * s02;
+        y[3 * r + 1] = w0 * s01 + w1 * s11 + w2 * s12;
+        y[3 * r + 2] = w0 * s02 + w1 * s12 + w2 * s22;
+    }
+    double2 *Yo = reinterpret_cast<double2 *>(Y + 18 * (size_t)o);
+#pragma unroll
+    for (int e = 0; e < 9; ++e) Yo[e] = make_double2(y[2 * e], y[2 * e + 1]);
+}
+
+void launch_yblocks(const DeviceProblem &d, cudaStream_t s)
+{
+    if (d.no == 0) return;
+    k_yblocks<<<ceil_div(d.no, 256), 256, 0, s>>>(d.no, d.obs_pt, d.W, d.Vinv, d.Y); note_launch(1);
+}
+
+// ---------------------------------------------------------------------------
+// Schur complement S = U + mu I - sum_i Y_ik W_il^T (compute_S.cl:39-77) and
+// ea = ga - sum_i Y_ij gb_i (compute_ea.cl:21-36).
+// Off-diagonal blocks (k > l): one thread per unit of <= SCHUR_CHUNK common
+// points of a camera pair, all 36 entries of the 6x6 product.
+// Diagonal blocks: one thread per unit of a camera's observations, the 21
+// lower entries plus the 6 ea sums.  Units are then summed in order.
+__global__ void __launch_bounds__(128) k_schur_off(int n_units, const SchurUnit *__restrict__ units,
+                                                   const int *__restrict__ pa,
+                                                   const int *__restrict__ pb,
+                                                   const double *__restrict__ Y,
+                                                   const double *__restrict__ W,
+                                                   double *__restrict__ partial)
+{
+    const int uid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (uid >= n_units) return;
+    const SchurUnit u = units[uid];
+    double acc[36];
+#pragma unroll
+    for (int e = 0; e < 36; ++e) acc[e] = 0.0;
+    for (int t = 0; t < u.count; ++t) {
+        const int a = __ldg(pa + u.begin + t), b = __ldg(pb + u.begin + t);
+        const double2 *Wb = reinterpret_cast<const double2 *>(W + 18 * (size_t)b);
+        const double2 *Ya = reinterpret_cast<const double2 *>(Y + 18 * (size_t)a);
+        double w[18], y[18];
+#pragma unroll
+        for (int e = 0; e < 9; ++e) {
+            const double2 x = __ldg(Wb + e);
+            w[2 * e] = x.x;
+            w[2 * e + 1] = x.y;
+            const double2 z = __ldg(Ya + e);
+            y[2 * e] = z.x;
+            y[2 * e + 1] = z.y;
+        }
+#pragma unroll
+        for (int r = 0; r < 6; ++r)
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                double s = acc[r * 6 + c];
+                s = fma(y[3 * r], w[3 * c], s);
+                s = fma(y[3 * r + 1], w[3 * c + 1], s);
+                s = fma(y[3 * r + 2], w[3 * c + 2], s);
+                acc[r * 6 + c] = s;
+            }
+    }
+    double *p = partial + (size_t)u.out * 36;
+#pragma unroll
+    for (int e = 0; e < 36; ++e) p[e] = acc[e];
+}
+
+constexpr int DIAG_NV = 27;  // 21 lower entries + 6 ea sums
+
+__global__ void __launch_bounds__(128) k_schur_diag(int n_units, const SchurUnit *__restrict__ units,
+                                                    const int *__restrict__ cam_obs,
+                                                    const int *__restrict__ obs_pt,
+                                                    const double *__restrict__ Y,
+                                                    const double *__restrict__ W,
+                                                    const double *__restrict__ gb,
+                                                    double *__restrict__ partial)
+{
+    const int uid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (uid >= n_units) return;
+    const SchurUnit u = units[uid];
+    double acc[DIAG_NV];
+#pragma unroll
+    for (int e = 0; e < DIAG_NV; ++e) acc[e] = 0.0;
+    for (int t = 0; t < u.count; ++t) {
+        const int a = __ldg(cam_obs + u.begin + t);
+        const int i = __ldg(obs_pt + a);
+        const double2 *Wa = reinterpret_cast<const double2 *>(W + 18 * (size_t)a);
+        const double2 *Ya = reinterpret_cast<const double2 *>(Y + 18 * (size_t)a);
+        double w[18], y[18];
+#pragma unroll
+        for (int e = 0; e < 9; ++e) {
+            const double2 x = __ldg(Wa + e);
+            w[2 * e] = x.x;
+            w[2 * e + 1] = x.y;
+            const double2 z = __ldg(Ya + e);
+            y[2 * e] = z.x;
+            y[2 * e + 1] = z.y;
+        }
+        const double g0 = __ldg(gb + 3 * (size_t)i), g1 = __ldg(gb + 3 * (size_t)i + 1),
+                     g2 = __ldg(gb + 3 * (size_t)i + 2);
+        int v = 0;
+#pragma unroll
+        for (int r = 0; r < 6; ++r)
+#pragma unroll
+            for (int c = 0; c <= r; ++c, ++v) {
+                double s = acc[v];
+                s = fma(y[3 * r], w[3 * c], s);
+                s = fma(y[3 * r + 1], w[3 * c + 1], s);
+                s = fma(y[3 * r + 2], w[3 * c + 2], s);
+                acc[v] = s;
+            }
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+            double s = acc[21 + r];
+            s = fma(y[3 * r], g0, s);
+            s = fma(y[3 * r + 1], g1, s);
+            s = fma(y[3 * r + 2], g2, s);
+            acc[21 + r] = s;
+        }
+    }
+    double *p = partial + (size_t)u.out * DIAG_NV;
+#pragma unroll
+    for (int e = 0; e < DIAG_NV; ++e) p[e] = acc[e];
+}
+
+// Sum unit partials into S (lower) and rhs = ea.
+__global__ void k_schur_reduce(int n_pairs, int nc, int Np, const int *__restrict__ pair_kl,
+                               const int *__restrict__ off_start, const double *__restrict__ off_partial,
+                               const int *__restrict__ diag_start,
+                               const double *__restrict__ diag_partial,
+                               const double *__restrict__ U, const double *__restrict__ g, double mu,
+                               double *__restrict__ S, double *__restrict__ rhs)
+{
+    const int id = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n_off = n_pairs * 36;
+    if (id < n_off) {
+        const int p = id / 36, v = id % 36;
+        double sum = 0.0;
+        for (int u = off_start[p]; u < off_start[p + 1]; ++u) sum += off_partial[(size_t)u * 36 + v];
+        const int k = pair_kl[2 * p], l = pair_kl[2 * p + 1];
+        const int r = v / 6, c = v % 6;
+        S[(size_t)(6 * k + r) * Np + 6 * l + c] = -sum;
+        return;
+    }
+    const int id2 = id - n_off;
+    if (id2 >= nc * DIAG_NV) return;
+    const int k = id2 / DIAG_NV, v = id2 % DIAG_NV;
+    double sum = 0.0;
+    for (int u = diag_start[k]; u < diag_start[k + 1]; ++u) sum += diag_partial[(size_t)u * DIAG_NV + v];
+    if (v >= 21) {
+        const int r = v - 21;
+        rhs[6 * k + r] = g[6 * k + r] - sum;
+        return;
+    }
+    int r = 0, c = 0, kk = v;
+    for (r = 0; r < 6; ++r) {
+        if (kk <= r) {
+            c = kk;
+            break;
+        }
+        kk -= r + 1;
+    }
+    const double uu = U[36 * (size_t)k + r * 6 + c];
+    S[(size_t)(6 * k + r) * Np + 6 * k + c] = (r == c ? uu + mu : uu) - sum;
+}
+
+__global__ void k_pad_identity(int N, int Np, double *S, double *rhs)
+{
+    const int i = N + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= Np) return;
+    S[(size_t)i * Np + i] = 1.0;
+    rhs[i] = 0.0;
+}
+
+void launch_schur_off(const DeviceProblem &d, cudaStream_t s)
+{
+    if (d.n_off_units > 0)
+        k_schur_off<<<ceil_div(d.n_off_units, 128), 128, 0, s>>>(d.n_off_units, d.off_units, d.pair_a,
+                                                                   d.pair_b, d.Y, d.W, d.schur_partial); note_launch(1);
+}
+
+void launch_schur_diag(const DeviceProblem &d, cudaStream_t s)
+{
+    double *diag_partial = d.schur_partial + (size_t)d.n_off_units * 36;
+    if (d.n_diag_units > 0)
+        k_schur_diag<<<ceil_div(d.n_diag_units, 128), 128, 0, s>>>(
+            d.n_diag_units, d.diag_units, d.cam_obs, d.obs_pt, d.Y, d.W, d.g + d.N, diag_partial); note_launch(1);
+}
+
+void launch_schur_reduce(const DeviceProblem &d, double mu, cudaStream_t s)
+{
+    cudaMemsetAsync(d.S, 0, sizeof(double) * (size_t)d.Np * d.Np, s);
+    double *off_partial = d.schur_partial;
+    double *diag_partial = d.schur_partial + (size_t)d.n_off_units * 36;
+    const int total = d.n_pairs * 36 + d.nc * DIAG_NV;
+    k_schur_reduce<<<ceil_div(total, 128), 128, 0, s>>>(d.n_pairs, d.nc, d.Np, d.pair_kl,
+                                                          d.off_unit_start, off_partial,
+                                                          d.diag_unit_start, diag_partial, d.U, d.g,
+                                                          mu, d.S, d.rhs); note_launch(1);
+    if (d.Np > d.N) k_pad_identity<<<1, TILE, 0, s>>>(d.N, d.Np, d.S, d.rhs); note_launch(1);
+}
+
+void launch_schur(const DeviceProblem &d, double mu, cudaStream_t s)
+{
+    launch_schur_off(d, s);
+    launch_schur_diag(d, s);
+    launch_schur_reduce(d, mu, s);
+}
+
+// ---------------------------------------------------------------------------
+// eb = gb - sum_j W_ij^T dpa_j (compute_eb.cl:25-39), dpb = V^-1 eb
+// (compute_dpb.cl:19-34), one thread per point; block partials of |dpb|^2
+// and dpb (mu dpb + gb) for the gain ratio (levmar.cpp:271-280).
+__global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int *__restrict__ pt_start,
+                                                const int *__restrict__ obs_cam,
+                                                const double *__restrict__ W,
+                                                const double *__restrict__ Vinv,
+                                                const double *__restrict__ g, double mu,
+                                                double *__restrict__ dp, double *__restrict__ eb,
+                                                double *__restrict__ partial)
+{
+    __shared__ double r0[256], r1[256];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double s_sq = 0.0, s_rho = 0.0;
+    if (i < np) {
+        double e0 = 0, e1 = 0, e2 = 0;
+        const int end = pt_start[i + 1];
+        for (int o = pt_start[i]; o < end; ++o) {
+            const double *w = W + 18 * (size_t)o;
+            const double *da = dp + 6 * (size_t)__ldg(obs_cam + o);
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                const double dk = da[k];
+                e0 = e0 + w[3 * k] * dk;
+                e1 = e1 + w[3 * k + 1] * dk;
+                e2 = e2 + w[3 * k + 2] * dk;
+            }
+        }
+        const double *gb = g + ncp + 3 * (size_t)i;
+        e0 = gb[0] - e0;
+        e1 = gb[1] - e1;
+        e2 = gb[2] - e2;
+        eb[3 * (size_t)i] = e0;
+        eb[3 * (size_t)i + 1] = e1;
+        eb[3 * (size_t)i + 2] = e2;
+        const double *vi = Vinv + 6 * (size_t)i;
+        const double d0 = vi[0] * e0 + vi[1] * e1 + vi[2] * e2;
+        const double d1 = vi[1] * e0 + vi[3] * e1 + vi[4] * e2;
+        const double d2 = vi[2] * e0 + vi[4] * e1 + vi[5] * e2;
+        double *db = dp + ncp + 3 * (size_t)i;
+        db[0] = d0;
+        db[1] = d1;
+        db[2] = d2;
+        s_sq = d0 * d0 + d1 * d1 + d2 * d2;
+        s_rho = d0 * (mu * d0 + gb[0]) + d1 * (mu * d1 + gb[1]) + d2 * (mu * d2 + gb[2]);
+    }
+    r0[threadIdx.x] = s_sq;
+    r1[threadIdx.x] = s_rho;
+    __syncthreads();
+    for (int st = 128; st > 0; st >>= 1) {
+        if (threadIdx.x < st) {
+            r0[threadIdx.x] += r0[threadIdx.x + st];
+            r1[threadIdx.x] += r1[threadIdx.x + st];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        partial[2 * blockIdx.x] = r0[0];
+        partial[2 * blockIdx.x + 1] = r1[0];
+    }
+}
+
+int eb_blocks(const DeviceProblem &d) { return ceil_div(d.np > 0 ? d.np : 1, 256); }
+
+void launch_eb_dpb(const DeviceProblem &d, double mu, cudaStream_t s)
+{
+    k_eb_dpb<<<eb_blocks(d), 256, 0, s>>>(d.np, d.N, d.pt_start, d.obs_cam, d.W, d.Vinv, d.g, mu,
+                                           d.dp, d.eb, d.red_partial); note_launch(1);
+}
+
+// Sum the dpa part and the per-block partials of the back-substitution in a
+// fixed order; copy the Cholesky status.  One block.
+__global__ void k_finish_trial(int ncp, int nblocks, const double *__restrict__ dp,
+                               const double *__restrict__ g, double mu,
+                               const double *__restrict__ partial, const int *__restrict__ status,
+                               TrialScalars *__restrict__ out)
+{
+    __shared__ double r0[256], r1[256];
+    double a = 0.0, b = 0.0;
+    for (int k = threadIdx.x; k < ncp; k += 256) {
+        const double x = dp[k];
+        a += x * x;
+        b += x * (mu * x + g[k]);
+    }
+    for (int k = threadIdx.x; k < nblocks; k += 256) {
+        a += partial[2 * k];
+        b += partial[2 * k + 1];
+    }
+    r0[threadIdx.x] = a;
+    r1[threadIdx.x] = b;
+    __syncthreads();
+    for (int st = 128; st > 0; st >>= 1) {
+        if (threadIdx.x < st) {
+            r0[threadIdx.x] += r0[threadIdx.x + st];
+            r1[threadIdx.x] += r1[threadIdx.x + st];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out->dp_L2 = r0[0];
+        out->rho_den = r1[0];
+        out->chol_status = *status;
+    }
+}
+
+void launch_finish_trial(const DeviceProblem &d, double mu, cudaStream_t s)
+{
+    k_finish_trial<<<1, 256, 0, s>>>(d.N, eb_blocks(d), d.dp, d.g, mu, d.red_partial, d.status,
+                                     d.scal); note_launch(1);
+}
+
+// Fixed-order sum of n partials into *dst (one block).
+__global__ void k_sum_partials(const double *__restrict__ partial, int n, double *__restrict__ dst)
+{
+    __shared__ double r[256];
+    double a = 0.0;
+    for (int k = threadIdx.x; k < n; k += 256) a += partial[k];
+    r[threadIdx.x] = a;
+    __syncthreads();
+    for (int st = 128; st > 0; st >>= 1) {
+        if (threadIdx.x < st) r[threadIdx.x] += r[threadIdx.x + st];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *dst = r[0];
+}
+
+void launch_sum_partials(const double *partial, int n, double *dst, cudaStream_t s)
+{
+    k_sum_partials<<<1, 256, 0, s>>>(partial, n, dst); note_launch(1);
+}
+
+__global__ void k_max_uvdiag(const double *__restrict__ x, int n, double *__restrict__ dst)
+{
+    __shared__ double r[256];
+    double m = 0.0;  // maxElmOfUV starts from 0 (sba_func.cpp:433-440)
+    for (int k = threadIdx.x; k < n; k += 256) m = fmax(m, x[k]);
+    r[threadIdx.x] = m;
+    __syncthreads();
+    for (int st = 128; st > 0; st >>= 1) {
+        if (threadIdx.x < st) r[threadIdx.x] = fmax(r[threadIdx.x], r[threadIdx.x + st]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *dst = r[0];
+}
+
+void launch_max_uvdiag(const DeviceProblem &d, double *dst, cudaStream_t s)
+{
+    k_max_uvdiag<<<1, 256, 0, s>>>(d.uvdiag, d.N + 3 * d.np, dst); note_launch(1);
+}
+
+// Two-pass fixed-order reductions over long vectors.
+__global__ void k_sumsq_partial(const double *__restrict__ x, const double *__restrict__ y, long long n,
+                                double *__restrict__ partial)
+{
+    __shared__ double r[256];
+    double a = 0.0;
+    const long long stride = (long long)gridDim.x * 256;
+    for (long long k = (long long)blockIdx.x * 256 + threadIdx.x; k < n; k += stride)
+        a += y ? x[k] * y[k] : x[k] * x[k];
+    r[threadIdx.x] = a;
+    __syncthreads();
+    for (int st = 128; st > 0; st >>= 1) {
+        if (threadIdx.x < st) r[threadIdx.x] += r[threadIdx.x + st];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = r[0];
+}
+
+void launch_sumsq(const double *x, long long n, double *partial, int nblocks, double *dst,
+                  cudaStream_t s)
+{
+    k_sumsq_partial<<<nblocks, 256, 0, s>>>(x, nullptr, n, partial); note_launch(1);
+    k_sum_partials<<<1, 256, 0, s>>>(partial, nblocks, dst); note_launch(1);
+}
+
+void launch_dot(const double *x, const double *y, long long n, double *partial, int nblocks,
+                double *dst, cudaStream_t s)
+{
+    k_sumsq_partial<<<nblocks, 256, 0, s>>>(x, y, n, partial); note_launch(1);
+    k_sum_partials<<<1, 256, 0, s>>>(partial, nblocks, dst); note_launch(1);
+}
+
+// Accept a step: cams += dpa, pts += dpb (compute_newp.cl + update_p.cl).
+__global__ void k_update_params(int ncp, int npp, double *cams, double *pts, const double *dp)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < ncp)
+        cams[k] = cams[k] + dp[k];
+    else if (k < ncp + npp)
+        pts[k - ncp] = pts[k - ncp] + dp[k];
+}
+
+void launch_update_params(const DeviceProblem &d, cudaStream_t s)
+{
+    const int n = d.N + 3 * d.np;
+    k_update_params<<<ceil_div(n, 256), 256, 0, s>>>(d.N, 3 * d.np, d.cams, d.pts, d.dp); note_launch(1);
+}
+
+// J x per observation (compute_Jmultiply.cl:28-44), 2 outputs each.
+__global__ void k_jmultiply(int no, int ncp, const int *__restrict__ obs_pt,
+                            const int *__restrict__ obs_cam, const double *__restrict__ A,
+                            const double *__restrict__ B, const double *__restrict__ x,
+                            double *__restrict__ out)
+{
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= no) return;
+    const double *xa = x + 6 * (size_t)obs_cam[o];
+    const double *xb = x + ncp + 3 * (size_t)obs_pt[o];
+    const double *a = A + 12 * (size_t)o;
+    const double *b = B + 6 * (size_t)o;
+    for (int k = 0; k < 2; ++k) {
+        double s = 0.0;
+        for (int m = 0; m < 6; ++m) s += a[6 * k + m] * xa[m];
+        for (int m = 0; m < 3; ++m) s += b[3 * k + m] * xb[m];
+        out[2 * (size_t)o + k] = s;
+    }
+}
+
+void launch_jmultiply(const DeviceProblem &d, const double *x, double *out, cudaStream_t s)
+{
+    if (d.no == 0) return;
+    k_jmultiply<<<ceil_div(d.no, 256), 256, 0, s>>>(d.no, d.N, d.obs_pt, d.obs_cam, d.A, d.B, x, out); note_launch(1);
+}
+
+__global__ void k_axpby(double *out, const double *x, double a, const double *y, double b, long long n)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) out[k] = y ? a * x[k] + b * y[k] : a * x[k];
+}
+
+void launch_axpby(double *out, const double *x, double a, const double *y, double b, long long n,
+                  cudaStream_t s)
+{
+    k_axpby<<<ceil_div(n, 256), 256, 0, s>>>(out, x, a, y, b, n); note_launch(1);
+}
+
+// out = sign * (x * num) / (den_scale * den) with num, den on the device.
+__global__ void k_scale(double *out, const double *x, const double *num, const double *den,
+                        double den_scale, double sign, long long n)
+{
+    const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) out[k] = sign * (x[k] * (*num)) / (den_scale * (*den));
+}
+
+void launch_scale(double *out, const double *x, const double *num, const double *den,
+                  double den_scale, double sign, long long n, cudaStream_t s)
+{
+    k_scale<<<ceil_div(n, 256), 256, 0, s>>>(out, x, num, den, den_scale, sign, n); note_launch(1);
+}
+
+__global__ void k_expand_V(int np, const double *V6, double *V9)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= np) return;
+    const double *v = V6 + 6 * (size_t)i;
+    double *o = V9 + 9 * (size_t)i;
+    o[0] = v[0]; o[1] = v[1]; o[2] = v[2];
+    o[3] = v[1]; o[4] = v[3]; o[5] = v[4];
+    o[6] = v[2]; o[7] = v[4]; o[8] = v[5];
+}
+
+void launch_expand_V(const DeviceProblem &d, const double *V6, double *V9, cudaStream_t s)
+{
+    if (d.np == 0) return;
+    k_expand_V<<<ceil_div(d.np, 128), 128, 0, s>>>(d.np, V6, V9); note_launch(1);
+}
+
+}  // namespace psba

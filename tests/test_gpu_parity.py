@@ -1,0 +1,185 @@
+"""GPU parity: every stage and the drivers of the sm_103a library against the
+FP64 oracle and the reference-kernel fixtures, called through the C ABI.
+
+FP64 tolerances: stage outputs agree with the reference's arithmetic to
+1e-10 of the array's largest magnitude (the kernels use FMA and a different
+but exact formulation of the rotation and its derivative, so they differ in
+the last few bits, not more).  Driver runs must reproduce the oracle's LM
+accept/reject sequence over the first 10 iterations with final cost within
+1e-9 relative.
+"""
+import numpy as np
+import pytest
+
+import oracle
+import psba_gb300 as P
+from psba_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    P.build()
+
+
+def close(a, b, tol=TOL):
+    scale = max(np.abs(b).max(), 1e-300)
+    err = np.abs(np.asarray(a) - np.asarray(b)).max() / scale
+    assert err <= tol, "relative error %.3e > %.1e" % (err, tol)
+
+
+def test_residual_and_jacobian(golden):
+    sc, z = golden
+    with P.Solver(sc) as s:
+        ex, cost = s.eval_residual()
+        close(ex, z["ex"], 1e-12 * np.abs(sc.meas).max() / np.abs(z["ex"]).max())
+        assert abs(cost - oracle.sumsq(z["ex"])) <= 1e-10 * cost
+        JA, JB = s.eval_jacobian()
+        close(JA, z["JA"])
+        close(JB, z["JB"])
+
+
+@pytest.mark.parametrize("tag,coeff", [("c1", 1.0), ("c2", 2.0), ("cm2", -2.0)])
+def test_normal_blocks(golden, tag, coeff):
+    sc, z = golden
+    with P.Solver(sc) as s:
+        U, V, W, g = s.eval_normal(coeff)
+        close(U, z["U_" + tag])
+        close(V, z["V_" + tag])
+        close(W, z["W_" + tag])
+        close(g, z["g_" + tag])
+
+
+def test_reduced_system_and_step(golden):
+    sc, z = golden
+    mu = float(z["mu"])
+    with P.Solver(sc) as s:
+        s.eval_normal(1.0)
+        Vinv, Y, S, ea = s.eval_reduced(mu)
+        close(Vinv, z["Vinv"])
+        close(Y, z["Y"])
+        close(S, np.tril(z["S"]))
+        assert np.all(np.triu(S, 1) == 0)
+        close(ea, z["ea"])
+        st, dp = s.eval_step()
+        assert st == 0
+        N = 6 * sc.n_cams
+        close(dp[:N], z["dpa"], 1e-8)
+        close(dp[N:], z["dpb"], 1e-8)
+        # the reduced system is solved: |S dpa - ea| small
+        Sf = np.tril(S) + np.tril(S, -1).T
+        assert np.abs(Sf @ dp[:N] - ea).max() <= 1e-9 * np.abs(ea).max()
+
+
+def test_step_reports_non_spd(golden):
+    sc, z = golden
+    with P.Solver(sc) as s:
+        s.eval_normal(1.0)
+        s.eval_reduced(-1e12)  # damping that makes S indefinite
+        st, _ = s.eval_step()
+        assert st == 1
+
+
+def test_jmultiply(golden):
+    sc, z = golden
+    with P.Solver(sc) as s:
+        s.eval_jacobian()
+        jx = s.eval_jmultiply(z["jx_in"])
+        dense = z["jx_dense"].reshape(sc.n_pts, sc.n_cams, 2)[sc.obs_pt, sc.obs_cam].ravel()
+        close(jx, dense)
+
+
+def test_cholmod_matches_oracle():
+    rng = np.random.default_rng(0)
+    n = 30
+    Q = rng.normal(size=(n, n))
+    A = Q @ np.diag(np.linspace(-1, 3, n)) @ Q.T
+    Lo, Eo = oracle.cholmod(np.tril(A))
+    Lg, Eg = P.cholmod(np.tril(A))
+    close(np.tril(Lg), np.tril(Lo), 1e-9)
+    close(Eg, Eo, 1e-9)
+
+
+def test_cholmod_on_singular_schur(golden):
+    # lambda = 0 trust-region system: S of 2 J^T J has the 7-dimensional gauge null space
+    sc, z = golden
+    with P.Solver(sc) as s:
+        s.eval_normal(2.0)
+        _, _, S, _ = s.eval_reduced(0.0)
+    Lo, Eo = oracle.cholmod(S)
+    Lg, Eg = P.cholmod(S)
+    assert abs(Eg.sum() - Eo.sum()) <= 1e-6 * max(abs(Eo.sum()), 1.0)
+
+
+def _lm(sc, max_iter=20, **kw):
+    o = oracle.levmar(sc, allow_switch=0, max_iter=max_iter, **kw)
+    with P.Solver(sc) as s:
+        g = s.levmar(allow_switch=0, max_iter=max_iter)
+    return o, g
+
+
+def _first_iters(trace, n):
+    t = trace[trace["itno"] < n]
+    return t["kind"], t["accepted"]
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_levmar_matches_oracle(seed):
+    sc = scenes.small_lm_scene(seed)
+    o, g = _lm(sc)
+    ko, ao = _first_iters(o.trace, 10)
+    kg, ag = _first_iters(g.trace, 10)
+    assert np.array_equal(ko, kg) and np.array_equal(ao, ag)
+    assert g.status == o.status and g.iterations == o.iterations
+    assert abs(g.initial_cost - o.initial_cost) <= 1e-12 * o.initial_cost
+    assert abs(g.final_cost - o.final_cost) <= 1e-9 * o.final_cost
+    n = min(len(o.trace), len(g.trace))
+    close(g.trace["damping"][:n], o.trace["damping"][:n], 1e-6)
+    close(g.cams, o.cams, 1e-6)
+    close(g.pts, o.pts, 1e-6)
+
+
+def test_levmar_matches_oracle_solve_mode():
+    # the oracle with Cholesky + triangular solves (as the GPU) instead of S^-1
+    sc = scenes.small_lm_scene(3)
+    o, g = _lm(sc, solve_mode=1)
+    assert np.array_equal(o.trace["accepted"], g.trace["accepted"])
+    assert abs(g.final_cost - o.final_cost) <= 1e-9 * o.final_cost
+
+
+def test_levmar_is_deterministic():
+    sc = scenes.small_lm_scene(4)
+    with P.Solver(sc) as s:
+        a = s.levmar(allow_switch=0, max_iter=12)
+        s.set_params(sc.cams, sc.pts)
+        b = s.levmar(allow_switch=0, max_iter=12)
+    assert np.array_equal(a.trace, b.trace)
+    assert np.array_equal(a.cams, b.cams) and np.array_equal(a.pts, b.pts)
+
+
+def test_levmar_power_law_scene():
+    sc = scenes.circle_scene(seed=1, n_cams=24, n_pts=3000, name="circle24")
+    o, g = _lm(sc, max_iter=10)
+    assert np.array_equal(o.trace["accepted"], g.trace["accepted"])
+    assert abs(g.final_cost - o.final_cost) <= 1e-9 * o.final_cost
+
+
+def test_trust_region_matched_final_cost():
+    sc = scenes.small_lm_scene(5)
+    o = oracle.trust_region(sc, max_iter=30)
+    with P.Solver(sc) as s:
+        g = s.trust_region(max_iter=30)
+    assert g.final_cost <= o.initial_cost
+    assert abs(g.final_cost - o.final_cost) <= 1e-6 * o.final_cost
+
+
+def test_hybrid_matched_final_cost():
+    sc = scenes.small_lm_scene(6)
+    o = oracle.solve_hybrid(sc)
+    with P.Solver(sc) as s:
+        g = s.solve_hybrid()
+    assert g.status == o.status
+    assert abs(g.final_cost - o.final_cost) <= 1e-6 * o.final_cost

@@ -270,6 +270,27 @@ def main():
         iters_all = iters
     value = iters_all / total_dev_s
 
+    # ---- the mixed FP32/FP64 form on the same workload (same protocol)
+    mopts = P.default_opts(allow_switch=0, max_iter=args.max_iter, precision=P.PREC_MIXED)
+    for _ in range(max(1, args.warmup // 2)):
+        solver.reset_params()
+        solver.levmar(mopts, fetch=False, trace_cap=0)
+    solver.set_stage_timing(True)
+    m_ms, m_iters, m_costs = [], 0, []
+    for _ in range(args.steps):
+        solver.reset_params()
+        flush_l2(torch, flush)
+        r = solver.levmar(mopts, fetch=False, trace_cap=0)
+        m_ms.append(r.device_ms)
+        m_iters += r.iterations
+        m_costs.append(r.final_cost)
+    m_stages = solver.stage_timing()
+    solver.set_stage_timing(False)
+    mixed = {"value": m_iters / (sum(m_ms) / 1e3), "unit": UNIT, "ms_per_step": sum(m_ms) / len(m_ms),
+             "final_cost": m_costs[-1], "final_cost_rel_vs_fp64": abs(m_costs[-1] - costs[-1]) / costs[-1],
+             "speedup_vs_fp64": (m_iters / sum(m_ms)) / (iters / sum(dev_ms)),
+             "stage_ms": {k: (v[0] / v[1] if v[1] else 0.0) for k, v in m_stages.items()}}
+
     # ---- end to end through the C ABI from host buffers
     e2e_s, e2e_iters, h2d, d2h = 0.0, 0, 0, 0
     for _ in range(args.e2e_steps):
@@ -312,7 +333,7 @@ def main():
                      "fp64": {"achieved_tflops": fp64_achieved, "peak_tflops": fp64_peak,
                               "frac": fp64_achieved / fp64_peak, "flops": schur_flops(cfg),
                               "peak_source": "measured FP64 FMA kernel (psba_measure_peak)"}},
-        "stage_ms": stage_ms,
+        "stage_ms": stage_ms, "mixed": mixed,
         "stage_share": {k: (v[0] / total_stage if total_stage else 0.0) for k, v in stages.items()},
         "clocks": clk, "gpu_launches": int(launches),
     }

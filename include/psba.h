@@ -156,6 +156,11 @@ int psba_solve_hybrid(psba_handle *h, const psba_opts *opts, psba_result *res);
 
 /* ---- stage evaluation (parity checks; reference layouts, host buffers) -- */
 
+/* Precision used by the psba_eval_* calls (PSBA_PREC_*); the drivers take it
+ * from their options.  No reference counterpart: the reference is FP64 only
+ * (CL_files/PSBA.cl:2). */
+int psba_set_precision(psba_handle *h, int precision);
+
 /* compute_exQT (sba_func.cpp:81-145): ex = meas - projection; *cost = sum ex^2. */
 int psba_eval_residual(psba_handle *h, double *ex, double *cost);
 

@@ -63,7 +63,7 @@ TRACE_DTYPE = np.dtype([("itno", np.int32), ("kind", np.int32), ("accepted", np.
 
 # every entry point declared in include/psba.h
 EXPORTS = ("psba_default_opts", "psba_create", "psba_destroy", "psba_get_params", "psba_set_params",
-           "psba_reset_params",
+           "psba_reset_params", "psba_set_precision",
            "psba_levmar", "psba_trust_region", "psba_solve_hybrid", "psba_eval_residual",
            "psba_eval_jacobian", "psba_eval_normal", "psba_eval_reduced", "psba_eval_step",
            "psba_eval_jmultiply", "psba_eval_cholmod", "psba_last_error", "psba_stream",
@@ -98,6 +98,7 @@ def lib():
         L.psba_get_params.argtypes = [C.c_void_p, _dp, _dp]
         L.psba_set_params.argtypes = [C.c_void_p, _dp, _dp]
         L.psba_reset_params.argtypes = [C.c_void_p]
+        L.psba_set_precision.argtypes = [C.c_void_p, C.c_int]
         for f in ("psba_levmar", "psba_trust_region"):
             getattr(L, f).argtypes = [C.c_void_p, C.POINTER(Opts), _ip, C.POINTER(Result)]
         L.psba_solve_hybrid.argtypes = [C.c_void_p, C.POINTER(Opts), C.POINTER(Result)]
@@ -238,6 +239,10 @@ class Solver:
 
     def set_params(self, cams, pts):
         _check(lib().psba_set_params(self.h, _d(_f64(cams)), _d(_f64(pts))))
+
+    def set_precision(self, precision):
+        """Precision of the eval_* stages: PREC_FP64 or PREC_MIXED."""
+        _check(lib().psba_set_precision(self.h, int(precision)))
 
     def reset_params(self):
         """Back to the initial estimate given at creation (device-side copy)."""

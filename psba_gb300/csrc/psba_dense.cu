@@ -1,217 +1,335 @@
-// Dense FP64 reduced-camera solve on sm_103a: blocked right-looking
-// Cholesky of S (Np x Np, lower triangle, Np a multiple of TILE) with the
-// forward solve L y = ea carried along as an extra column, then the back
-// solve L^T x = y.
+// Dense FP64 reduced-camera solve on sm_103a.
+//
+// S (Np x Np, lower triangle, Np a multiple of TILE) is factored S = L L^T
+// by one cooperative persistent kernel that runs a tile dataflow: every
+// TILE x TILE lower tile is a task; tasks are numbered column by column and
+// each CTA takes tasks c, c + G, c + 2G, ... in increasing order.  A task
+// waits (bounded spin on per-task flags in global memory, acquire/release)
+// only for tasks with smaller numbers, so with all CTAs resident (cooperative
+// launch) the smallest unfinished task can always run: no deadlock.
+//   tile (I,I):  A_II -= sum_J L_IJ L_IJ^T, then a warp-level Cholesky in
+//                registers, its inverse, and y_I = L_II^-1 (b_I - sum_J L_IJ y_J)
+//                (the forward solve of L y = ea rides along)
+//   tile (I,K):  A_IK -= sum_{J<K} L_IJ L_KJ^T, then L_IK = A_IK L_KK^-T
+// After the factor, back-substitution tasks B_K (K descending) solve
+// L^T x = y:  x_K = L_KK^-T (y_K - sum_{I>K} L_IK^T x_I).
 //
 // This replaces the reference's explicit inverse (SPD_inv.cl: 3x3-block
-// Cholesky, kern_trigMat_inv, kern_trigMat_mul, then matVec_mul) with two
-// triangular solves: fewer flops and no N^2 inverse in memory.  The failure
-// test is the reference's: a non-positive or non-finite pivot sets the status
-// word (SPD_inv.cl:66-107) and every later kernel of the sweep returns early.
-//
-// Per step J: trsm(J) computes the panel L_IJ = A_IJ L_JJ^-T (one block per
-// tile), update(J) applies A_IK -= L_IJ L_KJ^T to the trailing tiles and the
-// block that owns tile (J+1, J+1) factors it right away.
+// Cholesky chain, kern_trigMat_inv, kern_trigMat_mul, then matVec_mul) with
+// two triangular solves.  The failure test is the reference's: a non-positive
+// or non-finite pivot (SPD_inv.cl:66-107) sets status 1; every task still
+// raises its flag, so nothing waits forever.  A spin that runs out of its
+// iteration budget sets status 2 and the kernel completes.
 #include "psba_internal.h"
 
 namespace psba {
 
 constexpr int T = TILE;
 constexpr int TT = TILE * TILE;
+constexpr int CF_THREADS = 128;
+constexpr long long SPIN_LIMIT = 1LL << 22;  // ~0.5 s of polling with 64 ns sleeps
 
-// Factor the tile in shared memory a[T][T+1] (lower), compute its inverse
-// linv and y = linv * b.  Returns false (and sets *status) on a bad pivot.
-__device__ bool tile_potrf(double (*a)[T + 1], double (*linv)[T + 1], const double *b, double *y,
-                           int *status)
+__device__ __forceinline__ int ld_acquire(const int *p)
 {
-    __shared__ int bad;
-    const int tid = threadIdx.x;
-    if (tid == 0) bad = 0;
-    __syncthreads();
-    for (int k = 0; k < T; ++k) {
-        if (tid == 0) {
-            const double d = a[k][k];
-            if (!(d > 0.0) || !isfinite(d)) {
-                bad = 1;
-            } else {
-                a[k][k] = sqrt(d);
+    int v;
+    asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release(int *p, int v)
+{
+    asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Thread 0 waits for flag == epoch; the block then proceeds.  Returns false
+// when the budget ran out or another task already reported a timeout.
+__device__ bool block_wait(const int *flag, int epoch, int *status)
+{
+    __shared__ int ok;
+    if (threadIdx.x == 0) {
+        int good = 0;
+        for (long long it = 0; it < SPIN_LIMIT; ++it) {
+            if (ld_acquire(flag) == epoch) {
+                good = 1;
+                break;
             }
+            if (ld_acquire(status) == 2) break;
+            __nanosleep(64);
         }
-        __syncthreads();
-        if (bad) break;
-        const double piv = a[k][k];
-        for (int i = k + 1 + tid; i < T; i += blockDim.x) a[i][k] = a[i][k] / piv;
-        __syncthreads();
-        const int m = T - k - 1;  // trailing size
-        for (int e = tid; e < m * m; e += blockDim.x) {
-            const int i = k + 1 + e / m, j = k + 1 + e % m;
-            if (j <= i) a[i][j] = a[i][j] - a[i][k] * a[j][k];
+        if (!good) atomicExch(status, 2);
+        ok = good;
+    }
+    __syncthreads();
+    const bool r = ok != 0;
+    __syncthreads();
+    return r;
+}
+
+__device__ __forceinline__ int tile_task(int I, int K, int nb)
+{
+    return K * nb - (K * (K - 1)) / 2 + (I - K);  // column-major over the lower triangle
+}
+
+__device__ __forceinline__ void load_tile(double (*dst)[T + 1], const double *S, int Np, int I, int K)
+{
+    for (int e = threadIdx.x; e < TT; e += CF_THREADS) {
+        const int r = e / T, c = e % T;
+        dst[r][c] = __ldcg(S + (size_t)(I * T + r) * Np + K * T + c);
+    }
+}
+
+// Warp 0: Cholesky of the lower triangle of a (in registers), inverse of
+// the factor into linv, y = linv * b.  Returns false on a bad pivot.
+__device__ bool warp_potrf(double (*a)[T + 1], double (*linv)[T + 1], double *invd, const double *b,
+                           double *y)
+{
+    const unsigned FULL = 0xffffffffu;
+    const int r = threadIdx.x;  // < 32
+    double row[T];
+#pragma unroll
+    for (int c = 0; c < T; ++c) row[c] = r < T ? a[r][c] : 0.0;
+    bool bad = false;
+#pragma unroll
+    for (int k = 0; k < T; ++k) {
+        const double d = __shfl_sync(FULL, row[k], k);
+        bad = bad || !(d > 0.0) || !isfinite(d);
+        const double inv = rsqrt(d);
+        if (r == k) row[k] = d * inv;
+        if (r > k) row[k] *= inv;
+        if (r == 0) invd[k] = inv;
+#pragma unroll
+        for (int j = k + 1; j < T; ++j) {
+            const double ljk = __shfl_sync(FULL, row[k], j);
+            if (r >= j) row[j] = fma(-row[k], ljk, row[j]);
         }
-        __syncthreads();
     }
-    if (bad) {
-        if (tid == 0) *status = 1;
-        return false;
+    if (r < T) {
+#pragma unroll
+        for (int c = 0; c < T; ++c) a[r][c] = c <= r ? row[c] : 0.0;
     }
-    // inverse of the lower-triangular factor, one column per thread
-    if (tid < T) {
-        const int c = tid;
+    __syncwarp();
+    if (r < T) {  // column r of L^-1
+        const int c = r;
         for (int i = 0; i < c; ++i) linv[i][c] = 0.0;
-        linv[c][c] = 1.0 / a[c][c];
+        linv[c][c] = invd[c];
         for (int i = c + 1; i < T; ++i) {
             double s = 0.0;
             for (int k = c; k < i; ++k) s = fma(a[i][k], linv[k][c], s);
-            linv[i][c] = -s / a[i][i];
+            linv[i][c] = -s * invd[i];
         }
     }
-    __syncthreads();
-    if (tid < T) {
+    __syncwarp();
+    if (r < T) {
         double s = 0.0;
-        for (int k = 0; k <= tid; ++k) s = fma(linv[tid][k], b[k], s);
-        y[tid] = s;
+        for (int k = 0; k <= r; ++k) s = fma(linv[r][k], b[k], s);
+        y[r] = s;
     }
-    __syncthreads();
-    return true;
+    __syncwarp();
+    return !bad;
 }
 
-// Store a factored diagonal tile, its inverse and y.
-__device__ void tile_store_diag(double (*a)[T + 1], double (*linv)[T + 1], const double *y, int J,
-                                int Np, double *S, double *Linv, double *rhs)
+// mode 0: factor + forward solve + back solve; mode 1: forward + back solve
+// with an existing factor (S lower = L, Linv) for the right-hand side rhs.
+__global__ void __launch_bounds__(CF_THREADS) k_chol_dataflow(int mode, int Np, int nb,
+                                                              const int2 *__restrict__ tasks,
+                                                              double *__restrict__ S,
+                                                              double *__restrict__ Linv,
+                                                              double *__restrict__ rhs,
+                                                              double *__restrict__ x,
+                                                              int *__restrict__ flags, int epoch,
+                                                              int *__restrict__ status)
 {
-    for (int e = threadIdx.x; e < TT; e += blockDim.x) {
-        const int r = e / T, c = e % T;
-        S[(size_t)(J * T + r) * Np + J * T + c] = c <= r ? a[r][c] : 0.0;
-        Linv[(size_t)J * TT + e] = linv[r][c];
-    }
-    if (threadIdx.x < T) rhs[J * T + threadIdx.x] = y[threadIdx.x];
-}
-
-__global__ void __launch_bounds__(TT) k_chol_first(int Np, double *S, double *Linv, double *rhs,
-                                                   int *status)
-{
-    __shared__ double a[T][T + 1], linv[T][T + 1], b[T], y[T];
-    for (int e = threadIdx.x; e < TT; e += blockDim.x) {
-        const int r = e / T, c = e % T;
-        a[r][c] = S[(size_t)r * Np + c];
-    }
-    if (threadIdx.x < T) b[threadIdx.x] = rhs[threadIdx.x];
-    if (threadIdx.x == 0) *status = 0;
-    __syncthreads();
-    if (!tile_potrf(a, linv, b, y, status)) return;
-    tile_store_diag(a, linv, y, 0, Np, S, Linv, rhs);
-}
-
-// L_IJ = A_IJ Linv_J^T for I = J+1 .. nb-1 (one block per tile).
-__global__ void __launch_bounds__(TT) k_chol_trsm(int J, int Np, double *S, const double *Linv,
-                                                  const int *status)
-{
-    if (*status) return;
-    __shared__ double a[T][T + 1], li[T][T + 1];
-    const int I = J + 1 + blockIdx.x;
-    for (int e = threadIdx.x; e < TT; e += blockDim.x) {
-        const int r = e / T, c = e % T;
-        a[r][c] = S[(size_t)(I * T + r) * Np + J * T + c];
-        li[r][c] = Linv[(size_t)J * TT + e];
-    }
-    __syncthreads();
-    for (int e = threadIdx.x; e < TT; e += blockDim.x) {
-        const int r = e / T, c = e % T;
-        double s = 0.0;
-        for (int k = 0; k <= c; ++k) s = fma(a[r][k], li[c][k], s);
-        S[(size_t)(I * T + r) * Np + J * T + c] = s;
-    }
-}
-
-// Trailing update after step J: tiles (I, K), J < K <= I < nb, plus the
-// right-hand side; the block of tile (J+1, J+1) then factors it.
-__global__ void __launch_bounds__(TT) k_chol_update(int J, int nb, int Np, double *S, double *Linv,
-                                                    double *rhs, int *status)
-{
-    if (*status) return;
-    __shared__ double li[T][T + 1], lk[T][T + 1], a[T][T + 1], linv[T][T + 1], b[T], y[T];
-    // tile index -> (I, K) over the lower triangle of the trailing matrix
-    const int m = nb - J - 1;
-    int t = blockIdx.x, I = 0, K = 0;
-    {
-        int row = 0;
-        while (t >= row + 1) {
-            t -= row + 1;
-            ++row;
+    __shared__ double a[T][T + 1], li[T][T + 1], lk[T][T + 1], linv[T][T + 1];
+    __shared__ double bvec[T], yvec[T], invd[T], red[CF_THREADS / T][T];
+    const int n_fact = mode == 0 ? nb * (nb + 1) / 2 : nb;  // mode 1: forward tasks F_K
+    const int n_tasks = n_fact + nb;
+    const int tid = threadIdx.x;
+    for (int t = blockIdx.x; t < n_tasks; t += gridDim.x) {
+        if (t < n_fact && mode == 0) {
+            const int I = tasks[t].x, K = tasks[t].y;
+            load_tile(a, S, Np, I, K);
+            if (I == K && tid < T) bvec[tid] = __ldcg(rhs + I * T + tid);
+            __syncthreads();
+            for (int J = 0; J < K; ++J) {
+                block_wait(flags + tile_task(I, J, nb), epoch, status);
+                if (I != K) block_wait(flags + tile_task(K, J, nb), epoch, status);
+                load_tile(li, S, Np, I, J);
+                if (I != K) load_tile(lk, S, Np, K, J);
+                if (I == K && tid < T) yvec[tid] = __ldcg(rhs + J * T + tid);
+                __syncthreads();
+                double(*lkp)[T + 1] = I == K ? li : lk;
+                for (int e = tid; e < TT; e += CF_THREADS) {
+                    const int r = e / T, c = e % T;
+                    double s = a[r][c];
+#pragma unroll
+                    for (int k = 0; k < T; ++k) s = fma(-li[r][k], lkp[c][k], s);
+                    a[r][c] = s;
+                }
+                if (I == K && tid < T) {
+                    double s = bvec[tid];
+#pragma unroll
+                    for (int k = 0; k < T; ++k) s = fma(-li[tid][k], yvec[k], s);
+                    bvec[tid] = s;
+                }
+                __syncthreads();
+            }
+            const bool failed = ld_acquire(status) != 0;
+            if (I == K) {
+                if (!failed) {
+                    bool good = true;
+                    if (tid < 32) good = warp_potrf(a, linv, invd, bvec, yvec);
+                    if (tid == 0 && !good) atomicCAS(status, 0, 1);
+                    __syncthreads();
+                    for (int e = tid; e < TT; e += CF_THREADS) {
+                        const int r = e / T, c = e % T;
+                        S[(size_t)(I * T + r) * Np + I * T + c] = a[r][c];
+                        Linv[(size_t)I * TT + e] = linv[r][c];
+                    }
+                    if (tid < T) rhs[I * T + tid] = yvec[tid];
+                }
+            } else {
+                block_wait(flags + tile_task(K, K, nb), epoch, status);
+                for (int e = tid; e < TT; e += CF_THREADS) linv[e / T][e % T] = __ldcg(Linv + (size_t)K * TT + e);
+                __syncthreads();
+                if (ld_acquire(status) == 0) {
+                    for (int e = tid; e < TT; e += CF_THREADS) {
+                        const int r = e / T, c = e % T;
+                        double s = 0.0;
+                        for (int k = 0; k <= c; ++k) s = fma(a[r][k], linv[c][k], s);
+                        S[(size_t)(I * T + r) * Np + K * T + c] = s;
+                    }
+                }
+            }
+            __syncthreads();
+            if (tid == 0) {
+                __threadfence();
+                st_release(flags + t, epoch);
+            }
+        } else if (t < n_fact) {
+            // mode 1 forward task F_K: y_K = Linv_K (b_K - sum_{J<K} L_KJ y_J)
+            const int K = t;
+            if (K > 0) block_wait(flags + (K - 1), epoch, status);
+            const int g = tid / T, r = tid % T;
+            double s = 0.0;
+            for (int J = g; J < K; J += CF_THREADS / T) {
+                const double *L = S + (size_t)(K * T + r) * Np + J * T;
+                for (int c = 0; c < T; ++c) s = fma(__ldcg(L + c), __ldcg(rhs + J * T + c), s);
+            }
+            red[g][r] = s;
+            __syncthreads();
+            if (tid < T) {
+                double bb = __ldcg(rhs + K * T + tid);
+                for (int q = 0; q < CF_THREADS / T; ++q) bb -= red[q][tid];
+                bvec[tid] = bb;
+            }
+            for (int e = tid; e < TT; e += CF_THREADS) linv[e / T][e % T] = __ldcg(Linv + (size_t)K * TT + e);
+            __syncthreads();
+            if (tid < T) {
+                double yy = 0.0;
+                for (int k = 0; k <= tid; ++k) yy = fma(linv[tid][k], bvec[k], yy);
+                rhs[K * T + tid] = yy;
+            }
+            __syncthreads();
+            if (tid == 0) {
+                __threadfence();
+                st_release(flags + t, epoch);
+            }
+        } else {
+            // back-substitution task B_K
+            const int K = nb - 1 - (t - n_fact);
+            const int last_fact = mode == 0 ? tile_task(nb - 1, nb - 1, nb) : nb - 1;
+            block_wait(flags + last_fact, epoch, status);  // whole factor and y ready
+            if (K < nb - 1) block_wait(flags + t - 1, epoch, status);  // x_{K+1..} ready
+            const int g = tid / T, r = tid % T;
+            double s = 0.0;
+            for (int I = K + 1 + g; I < nb; I += CF_THREADS / T) {
+                const double *L = S + (size_t)(I * T) * Np + K * T + r;  // L_IK[c][r], c = 0..T-1
+                for (int c = 0; c < T; ++c) s = fma(__ldcg(L + (size_t)c * Np), __ldcg(x + I * T + c), s);
+            }
+            red[g][r] = s;
+            for (int e = tid; e < TT; e += CF_THREADS) linv[e / T][e % T] = __ldcg(Linv + (size_t)K * TT + e);
+            __syncthreads();
+            if (tid < T) {
+                double yy = __ldcg(rhs + K * T + tid);
+                for (int q = 0; q < CF_THREADS / T; ++q) yy -= red[q][tid];
+                bvec[tid] = yy;
+            }
+            __syncthreads();
+            if (tid < T) {
+                double xx = 0.0;
+                for (int k = tid; k < T; ++k) xx = fma(linv[k][tid], bvec[k], xx);
+                x[K * T + tid] = xx;
+            }
+            __syncthreads();
+            if (tid == 0) {
+                __threadfence();
+                st_release(flags + t, epoch);
+            }
         }
-        I = J + 1 + row;
-        K = J + 1 + t;
+        __syncthreads();
     }
-    (void)m;
-    for (int e = threadIdx.x; e < TT; e += blockDim.x) {
-        const int r = e / T, c = e % T;
-        li[r][c] = S[(size_t)(I * T + r) * Np + J * T + c];
-        lk[r][c] = S[(size_t)(K * T + r) * Np + J * T + c];
-        a[r][c] = S[(size_t)(I * T + r) * Np + K * T + c];
-    }
-    __syncthreads();
-    for (int e = threadIdx.x; e < TT; e += blockDim.x) {
-        const int r = e / T, c = e % T;
-        double s = a[r][c];
-        for (int k = 0; k < T; ++k) s = fma(-li[r][k], lk[c][k], s);
-        a[r][c] = s;
-    }
-    if (I == K && threadIdx.x < T) {
-        const int r = threadIdx.x;
-        double s = rhs[I * T + r];
-        for (int k = 0; k < T; ++k) s = fma(-li[r][k], rhs[J * T + k], s);
-        b[r] = s;
-    }
-    __syncthreads();
-    if (I == K && I == J + 1) {
-        if (!tile_potrf(a, linv, b, y, status)) return;
-        tile_store_diag(a, linv, y, I, Np, S, Linv, rhs);
-        return;
-    }
-    for (int e = threadIdx.x; e < TT; e += blockDim.x) {
-        const int r = e / T, c = e % T;
-        S[(size_t)(I * T + r) * Np + K * T + c] = a[r][c];
-    }
-    if (I == K && threadIdx.x < T) rhs[I * T + threadIdx.x] = b[threadIdx.x];
 }
 
-// Back solve step J (descending): x_J = Linv_J^T y_J; tiles I < J update
-// y_I -= L_JI^T x_J.  One block per I in [0, J].
-__global__ void __launch_bounds__(TT) k_chol_back(int J, int Np, const double *S, const double *Linv,
-                                                  double *rhs, double *x, const int *status)
+int chol_grid(int n_tasks)
 {
-    if (*status) return;
-    __shared__ double xj[T];
-    const int I = blockIdx.x;
-    if (threadIdx.x < T) {
-        const int c = threadIdx.x;
-        double s = 0.0;
-        for (int k = c; k < T; ++k) s = fma(Linv[(size_t)J * TT + k * T + c], rhs[J * T + k], s);
-        xj[c] = s;
+    static int per_sm = -1, sms = 0;
+    if (per_sm < 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_chol_dataflow, CF_THREADS, 0);
+        if (per_sm < 1) per_sm = 1;
     }
-    __syncthreads();
-    if (I == J) {
-        if (threadIdx.x < T) x[J * T + threadIdx.x] = xj[threadIdx.x];
-        return;
-    }
-    if (threadIdx.x < T) {
-        const int r = threadIdx.x;
-        double s = rhs[I * T + r];
-        for (int c = 0; c < T; ++c) s = fma(-S[(size_t)(J * T + c) * Np + I * T + r], xj[c], s);
-        rhs[I * T + r] = s;
-    }
+    const int cap = per_sm * sms;
+    return n_tasks < cap ? n_tasks : cap;
 }
 
-void launch_cholesky_solve(const DeviceProblem &d, cudaStream_t s)
+void launch_chol_dataflow(const DeviceProblem &d, int mode, int epoch, double *x_out, cudaStream_t s)
 {
     const int nb = d.Np / T;
-    k_chol_first<<<1, TT, 0, s>>>(d.Np, d.S, d.Linv, d.rhs, d.status); note_launch(1);
-    for (int J = 0; J + 1 < nb; ++J) {
-        k_chol_trsm<<<nb - J - 1, TT, 0, s>>>(J, d.Np, d.S, d.Linv, d.status); note_launch(1);
-        const int m = nb - J - 1;
-        k_chol_update<<<m * (m + 1) / 2, TT, 0, s>>>(J, nb, d.Np, d.S, d.Linv, d.rhs, d.status); note_launch(1);
+    const int n_tasks = (mode == 0 ? nb * (nb + 1) / 2 : nb) + nb;
+    const int grid = chol_grid(n_tasks);
+    int Np = d.Np;
+    const int2 *tasks = d.chol_tasks;
+    double *S = d.S, *Linv = d.Linv, *rhs = d.rhs, *x = x_out;
+    int *flags = d.chol_flags, *status = d.status;
+    void *args[] = {&mode, &Np, (void *)&nb, (void *)&tasks, &S, &Linv, &rhs, &x, &flags, &epoch, &status};
+    if (mode == 0) cudaMemsetAsync(d.status, 0, sizeof(int), s);
+    cudaLaunchCooperativeKernel((const void *)k_chol_dataflow, dim3(grid), dim3(CF_THREADS), args, 0, s);
+    note_launch(1);
+}
+
+// Iterative refinement residual r = b - S x with the symmetric S given by its
+// lower triangle (one warp per row, lanes over columns, fixed-order warp sum).
+__global__ void k_refine_residual(int Np, const double *__restrict__ S, const double *__restrict__ x,
+                                  const double *__restrict__ b, double *__restrict__ r)
+{
+    const int row = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x % 32;
+    if (row >= Np) return;
+    double s = 0.0;
+    for (int c = lane; c < Np; c += 32) {
+        const double v = c <= row ? S[(size_t)row * Np + c] : S[(size_t)c * Np + row];
+        s = fma(v, x[c], s);
     }
-    for (int J = nb - 1; J >= 0; --J)
-        k_chol_back<<<J + 1, TT, 0, s>>>(J, d.Np, d.S, d.Linv, d.rhs, d.xsol, d.status); note_launch(1);
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    if (lane == 0) r[row] = b[row] - s;
+}
+
+__global__ void k_add_inplace(int n, double *x, const double *dx)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] = x[i] + dx[i];
+}
+
+void launch_refine(const DeviceProblem &d, int epoch, cudaStream_t s)
+{
+    // r = rhs_save - Ssave x  (into rhs), solve with the existing factor into xref, x += xref
+    k_refine_residual<<<(d.Np + 7) / 8, 256, 0, s>>>(d.Np, d.Ssave, d.xsol, d.rhs_save, d.rhs);
+    note_launch(1);
+    launch_chol_dataflow(d, 1, epoch, d.xref, s);
+    k_add_inplace<<<(d.Np + 255) / 256, 256, 0, s>>>(d.Np, d.xsol, d.xref);
+    note_launch(1);
 }
 
 // ---------------------------------------------------------------------------

@@ -17,8 +17,9 @@ constexpr int CNP = 6;   // camera parameters (rotation vector part + translatio
 constexpr int PNP = 3;   // point parameters
 constexpr int MNP = 2;   // image coordinates
 constexpr int CAMTAB = 48;  // doubles per camera table entry (CamTab)
-constexpr int TILE = 32;    // dense Cholesky block size
-constexpr int SCHUR_CHUNK = 64;  // pair-list entries per Schur work unit
+constexpr int TILE = 16;    // dense Cholesky tile size
+constexpr int SCHUR_CHUNK = 32;  // pair-list entries per off-diagonal Schur work unit
+constexpr int DIAG_CHUNK = 16;   // observations per diagonal Schur work unit
 constexpr int CAM_CHUNK = 512;   // observations per camera-reduction work unit
 constexpr int RED_THREADS = 256; // threads of the reduction kernels
 
@@ -72,6 +73,7 @@ long long launch_count();
 
 struct DeviceProblem {
     int nc = 0, np = 0, no = 0, N = 0, Np = 0;  // N = 6 nc, Np = N padded to TILE
+    int prec = PSBA_PREC_FP64;  // storage of the per-observation / per-point arrays (double or float)
     // problem (immutable)
     double *K = nullptr, *q0 = nullptr, *meas = nullptr;
     int *obs_pt = nullptr, *obs_cam = nullptr;
@@ -115,8 +117,13 @@ struct DeviceProblem {
     double *Ssave = nullptr;      // copy of S (TR fallback, refinement)
     double *rhs = nullptr;        // Np (ea on entry, y after the forward solve)
     double *xsol = nullptr;       // Np
+    double *rhs_save = nullptr;   // Np: ea before the solve (refinement)
+    double *xref = nullptr;       // Np: refinement correction
     double *Linv = nullptr;       // (Np / TILE) * TILE * TILE inverses of the diagonal blocks
-    int *status = nullptr;        // Cholesky status word
+    int *status = nullptr;        // Cholesky status word (0 ok, 1 not SPD, 2 wait budget exhausted)
+    int2 *chol_tasks = nullptr;   // (I, K) of every lower tile, column-major
+    int *chol_flags = nullptr;    // one flag per dataflow task (value = epoch when done)
+    int chol_n_flags = 0;
     double *dp = nullptr;         // N + 3 np
     double *eb = nullptr;         // 3 np
     double *red_partial = nullptr;  // reduction partials
@@ -168,9 +175,14 @@ void launch_axpby(double *out, const double *x, double a, const double *y, doubl
 void launch_scale(double *out, const double *x, const double *num, const double *den,
                   double den_scale, double sign, long long n, cudaStream_t s);
 
-// Dense reduced-camera solve (psba_dense.cu): Cholesky of S (Np x Np, lower),
-// forward solve of rhs in the same sweep, back solve into xsol.
-void launch_cholesky_solve(const DeviceProblem &d, cudaStream_t s);
+// Dense reduced-camera solve (psba_dense.cu): mode 0 factors S (Np x Np,
+// lower) in place with the forward solve of rhs carried along and the back
+// solve into xsol; mode 1 solves again with the existing factor.  One
+// cooperative launch; epoch must increase from launch to launch.
+void launch_chol_dataflow(const DeviceProblem &d, int mode, int epoch, double *x_out, cudaStream_t s);
+// One step of iterative refinement of S x = rhs_save with the factor in S/Linv
+// and the original matrix in Ssave (mixed precision); updates xsol.
+void launch_refine(const DeviceProblem &d, int epoch, cudaStream_t s);
 // Modified Cholesky (trust-region lambda fallback) and its diagonal correction.
 void launch_cholmod(double *S, int n, int ld, double *E, double *work, cudaStream_t s);
 

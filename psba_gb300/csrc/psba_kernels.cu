@@ -14,6 +14,50 @@ namespace psba {
 
 static inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
+// Per-observation arrays are stored in R = double (PSBA_PREC_FP64) or
+// R = float (PSBA_PREC_MIXED).  Every per-observation array has an even
+// number of entries, so pairs are loaded and stored as double2 / float2.
+template <typename R> struct Pair;
+template <> struct Pair<double> { using T = double2; };
+template <> struct Pair<float> { using T = float2; };
+
+template <typename R>
+__device__ __forceinline__ void st2(R *p, R a, R b)
+{
+    typename Pair<R>::T v;
+    v.x = a;
+    v.y = b;
+    *reinterpret_cast<typename Pair<R>::T *>(p) = v;
+}
+
+template <typename R>
+__device__ __forceinline__ void ld2(const R *p, R &a, R &b)
+{
+    const typename Pair<R>::T v = __ldg(reinterpret_cast<const typename Pair<R>::T *>(p));
+    a = v.x;
+    b = v.y;
+}
+
+template <typename R, int N>
+__device__ __forceinline__ void ldn(const R *p, R *out)
+{
+#pragma unroll
+    for (int e = 0; e < N / 2; ++e) ld2(p + 2 * e, out[2 * e], out[2 * e + 1]);
+}
+
+template <typename R, int N>
+__device__ __forceinline__ void stn(R *p, const R *in)
+{
+#pragma unroll
+    for (int e = 0; e < N / 2; ++e) st2(p + 2 * e, in[2 * e], in[2 * e + 1]);
+}
+
+template <typename R> __host__ __device__ constexpr bool is_fp64() { return sizeof(R) == 8; }
+
+// Mixed precision: FP32 products summed in FP32 over FLUSH consecutive
+// terms, then added into the FP64 accumulator.
+constexpr int FLUSH = 8;
+
 // ---------------------------------------------------------------------------
 // Camera tables.  q = q(v) (x) q0 (compute_exQT.cl:82-87), M = matrix of
 // X -> q (0,X) conj(q), D[m] = dM/dv_m through q(v) with s = sqrt(1-|v|^2).
@@ -78,80 +122,78 @@ void launch_cam_tables(const DeviceProblem &d, const double *cams, const double 
 // Jacobian blocks A = d(x,y)/d(v,t), B = d(x,y)/dX (compute_jacobiQT.cl) by
 // the chain rule through the camera table, and W = coeff A^T B
 // (compute_Wblks.cl:28-33).
+template <typename R>
 __global__ void __launch_bounds__(256) k_linearize(int no, const int *__restrict__ obs_pt,
                                                    const int *__restrict__ obs_cam,
                                                    const double *__restrict__ meas,
                                                    const double *__restrict__ pts,
-                                                   const double *__restrict__ tab, double coeff,
-                                                   double *__restrict__ ex, double *__restrict__ A,
-                                                   double *__restrict__ B, double *__restrict__ W)
+                                                   const double *__restrict__ tab, R coeff,
+                                                   R *__restrict__ ex, R *__restrict__ A,
+                                                   R *__restrict__ B, R *__restrict__ W)
 {
     int o = blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= no) return;
     const int i = __ldg(obs_pt + o), j = __ldg(obs_cam + o);
-    const double X0 = __ldg(pts + 3 * i), X1 = __ldg(pts + 3 * i + 1), X2 = __ldg(pts + 3 * i + 2);
+    const R X0 = (R)__ldg(pts + 3 * i), X1 = (R)__ldg(pts + 3 * i + 1), X2 = (R)__ldg(pts + 3 * i + 2);
     const double *T = tab + (size_t)CAMTAB * j;
-    double M[9];
+    R M[9];
 #pragma unroll
-    for (int e = 0; e < 9; ++e) M[e] = __ldg(T + e);
-    const double xc = M[0] * X0 + M[1] * X1 + M[2] * X2 + __ldg(T + 36);
-    const double yc = M[3] * X0 + M[4] * X1 + M[5] * X2 + __ldg(T + 37);
-    const double zc = M[6] * X0 + M[7] * X1 + M[8] * X2 + __ldg(T + 38);
-    const double fx = __ldg(T + 39), sk = __ldg(T + 40), cx = __ldg(T + 41), fy = __ldg(T + 42),
-                 cy = __ldg(T + 43);
-    const double iz = 1.0 / zc;
-    const double2 m2 = *reinterpret_cast<const double2 *>(meas + 2 * (size_t)o);
-    const double nu = fx * xc + sk * yc;
-    const double u = (nu + cx * zc) * iz;
-    const double v = (fy * yc + cy * zc) * iz;
-    double2 e2;
-    e2.x = m2.x - u;
-    e2.y = m2.y - v;
-    *reinterpret_cast<double2 *>(ex + 2 * (size_t)o) = e2;
+    for (int e = 0; e < 9; ++e) M[e] = (R)__ldg(T + e);
+    const R xc = M[0] * X0 + M[1] * X1 + M[2] * X2 + (R)__ldg(T + 36);
+    const R yc = M[3] * X0 + M[4] * X1 + M[5] * X2 + (R)__ldg(T + 37);
+    const R zc = M[6] * X0 + M[7] * X1 + M[8] * X2 + (R)__ldg(T + 38);
+    const R fx = (R)__ldg(T + 39), sk = (R)__ldg(T + 40), cx = (R)__ldg(T + 41), fy = (R)__ldg(T + 42),
+            cy = (R)__ldg(T + 43);
+    const R iz = (R)1 / zc;
+    const double2 m2 = __ldg(reinterpret_cast<const double2 *>(meas + 2 * (size_t)o));
+    const R nu = fx * xc + sk * yc;
+    const R u = (nu + cx * zc) * iz;
+    const R v = (fy * yc + cy * zc) * iz;
+    st2<R>(ex + 2 * (size_t)o, (R)m2.x - u, (R)m2.y - v);
     // d(x,y)/dXc
-    const double p00 = fx * iz, p01 = sk * iz, p02 = -nu * iz * iz;
-    const double p11 = fy * iz, p12 = -fy * yc * iz * iz;
+    const R p00 = fx * iz, p01 = sk * iz, p02 = -nu * iz * iz;
+    const R p11 = fy * iz, p12 = -fy * yc * iz * iz;
     // dXc/dv = D[m] X
-    double a0[6], a1[6];
+    R a[12];
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
         const double *Dm = T + 9 + 9 * m;
-        const double g0 = __ldg(Dm + 0) * X0 + __ldg(Dm + 1) * X1 + __ldg(Dm + 2) * X2;
-        const double g1 = __ldg(Dm + 3) * X0 + __ldg(Dm + 4) * X1 + __ldg(Dm + 5) * X2;
-        const double g2 = __ldg(Dm + 6) * X0 + __ldg(Dm + 7) * X1 + __ldg(Dm + 8) * X2;
-        a0[m] = p00 * g0 + p01 * g1 + p02 * g2;
-        a1[m] = p11 * g1 + p12 * g2;
+        const R g0 = (R)__ldg(Dm + 0) * X0 + (R)__ldg(Dm + 1) * X1 + (R)__ldg(Dm + 2) * X2;
+        const R g1 = (R)__ldg(Dm + 3) * X0 + (R)__ldg(Dm + 4) * X1 + (R)__ldg(Dm + 5) * X2;
+        const R g2 = (R)__ldg(Dm + 6) * X0 + (R)__ldg(Dm + 7) * X1 + (R)__ldg(Dm + 8) * X2;
+        a[m] = p00 * g0 + p01 * g1 + p02 * g2;
+        a[6 + m] = p11 * g1 + p12 * g2;
     }
-    a0[3] = p00; a0[4] = p01; a0[5] = p02;
-    a1[3] = 0.0; a1[4] = p11; a1[5] = p12;
-    double b0[3], b1[3];
+    a[3] = p00; a[4] = p01; a[5] = p02;
+    a[9] = (R)0; a[10] = p11; a[11] = p12;
+    R bb[6];
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
-        b0[m] = p00 * M[m] + p01 * M[3 + m] + p02 * M[6 + m];
-        b1[m] = p11 * M[3 + m] + p12 * M[6 + m];
+        bb[m] = p00 * M[m] + p01 * M[3 + m] + p02 * M[6 + m];
+        bb[3 + m] = p11 * M[3 + m] + p12 * M[6 + m];
     }
-    double2 *Ao = reinterpret_cast<double2 *>(A + 12 * (size_t)o);
-    Ao[0] = make_double2(a0[0], a0[1]); Ao[1] = make_double2(a0[2], a0[3]);
-    Ao[2] = make_double2(a0[4], a0[5]); Ao[3] = make_double2(a1[0], a1[1]);
-    Ao[4] = make_double2(a1[2], a1[3]); Ao[5] = make_double2(a1[4], a1[5]);
-    double2 *Bo = reinterpret_cast<double2 *>(B + 6 * (size_t)o);
-    Bo[0] = make_double2(b0[0], b0[1]); Bo[1] = make_double2(b0[2], b1[0]);
-    Bo[2] = make_double2(b1[1], b1[2]);
-    double w[18];
+    stn<R, 12>(A + 12 * (size_t)o, a);
+    stn<R, 6>(B + 6 * (size_t)o, bb);
+    R w[18];
 #pragma unroll
     for (int r = 0; r < 6; ++r)
 #pragma unroll
-        for (int c = 0; c < 3; ++c) w[r * 3 + c] = coeff * (a0[r] * b0[c] + a1[r] * b1[c]);
-    double2 *Wo = reinterpret_cast<double2 *>(W + 18 * (size_t)o);
-#pragma unroll
-    for (int e = 0; e < 9; ++e) Wo[e] = make_double2(w[2 * e], w[2 * e + 1]);
+        for (int c = 0; c < 3; ++c) w[r * 3 + c] = coeff * (a[r] * bb[c] + a[6 + r] * bb[3 + c]);
+    stn<R, 18>(W + 18 * (size_t)o, w);
 }
 
 void launch_linearize(const DeviceProblem &d, double coeff, cudaStream_t s)
 {
     if (d.no == 0) return;
-    k_linearize<<<ceil_div(d.no, 256), 256, 0, s>>>(d.no, d.obs_pt, d.obs_cam, d.meas, d.pts,
-                                                      d.camtab, coeff, d.ex, d.A, d.B, d.W); note_launch(1);
+    if (d.prec == PSBA_PREC_FP64) {
+        k_linearize<double><<<ceil_div(d.no, 256), 256, 0, s>>>(d.no, d.obs_pt, d.obs_cam, d.meas, d.pts,
+                                                                  d.camtab, coeff, d.ex, d.A, d.B, d.W);
+    } else {
+        k_linearize<float><<<ceil_div(d.no, 256), 256, 0, s>>>(
+            d.no, d.obs_pt, d.obs_cam, d.meas, d.pts, d.camtab, (float)coeff, (float *)d.ex, (float *)d.A,
+            (float *)d.B, (float *)d.W);
+    }
+    note_launch(1);
 }
 
 // ---------------------------------------------------------------------------
@@ -207,19 +249,22 @@ void launch_residual(const DeviceProblem &d, const double *tab, const double *pt
 // ---------------------------------------------------------------------------
 // Per-point sums: V_i = coeff sum B^T B (compute_V.cl:24-37) and
 // gb_i = coeff sum B^T e (compute_g.cl:42-57), ascending camera order.
+template <typename R>
 __global__ void k_point_blocks(int np, int ncp, const int *__restrict__ pt_start,
-                               const double *__restrict__ B, const double *__restrict__ ex,
-                               double coeff, double *__restrict__ V, double *__restrict__ g,
-                               double *__restrict__ uvdiag)
+                               const R *__restrict__ B, const R *__restrict__ ex, R coeff,
+                               R *__restrict__ V, double *__restrict__ g, double *__restrict__ uvdiag)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= np) return;
-    double v00 = 0, v01 = 0, v02 = 0, v11 = 0, v12 = 0, v22 = 0, g0 = 0, g1 = 0, g2 = 0;
+    R v00 = 0, v01 = 0, v02 = 0, v11 = 0, v12 = 0, v22 = 0, g0 = 0, g1 = 0, g2 = 0;
     const int e = pt_start[i + 1];
+#pragma unroll 4
     for (int o = pt_start[i]; o < e; ++o) {
-        const double *b = B + 6 * (size_t)o;
-        const double b0 = b[0], b1 = b[1], b2 = b[2], c0 = b[3], c1 = b[4], c2 = b[5];
-        const double e0 = ex[2 * (size_t)o], e1 = ex[2 * (size_t)o + 1];
+        R b[6], ee[2];
+        ldn<R, 6>(B + 6 * (size_t)o, b);
+        ld2<R>(ex + 2 * (size_t)o, ee[0], ee[1]);
+        const R b0 = b[0], b1 = b[1], b2 = b[2], c0 = b[3], c1 = b[4], c2 = b[5];
+        const R e0 = ee[0], e1 = ee[1];
         v00 = v00 + b0 * b0 + c0 * c0;
         v01 = v01 + b0 * b1 + c0 * c1;
         v02 = v02 + b0 * b2 + c0 * c2;
@@ -230,22 +275,28 @@ __global__ void k_point_blocks(int np, int ncp, const int *__restrict__ pt_start
         g1 = g1 + b1 * e0 + c1 * e1;
         g2 = g2 + b2 * e0 + c2 * e1;
     }
-    double *Vi = V + 6 * (size_t)i;
+    R *Vi = V + 6 * (size_t)i;
     Vi[0] = coeff * v00; Vi[1] = coeff * v01; Vi[2] = coeff * v02;
     Vi[3] = coeff * v11; Vi[4] = coeff * v12; Vi[5] = coeff * v22;
-    uvdiag[ncp + 3 * (size_t)i] = Vi[0];
-    uvdiag[ncp + 3 * (size_t)i + 1] = Vi[3];
-    uvdiag[ncp + 3 * (size_t)i + 2] = Vi[5];
-    g[ncp + 3 * (size_t)i] = coeff * g0;
-    g[ncp + 3 * (size_t)i + 1] = coeff * g1;
-    g[ncp + 3 * (size_t)i + 2] = coeff * g2;
+    uvdiag[ncp + 3 * (size_t)i] = (double)Vi[0];
+    uvdiag[ncp + 3 * (size_t)i + 1] = (double)Vi[3];
+    uvdiag[ncp + 3 * (size_t)i + 2] = (double)Vi[5];
+    g[ncp + 3 * (size_t)i] = (double)(coeff * g0);
+    g[ncp + 3 * (size_t)i + 1] = (double)(coeff * g1);
+    g[ncp + 3 * (size_t)i + 2] = (double)(coeff * g2);
 }
 
 void launch_point_blocks(const DeviceProblem &d, double coeff, cudaStream_t s)
 {
     if (d.np == 0) return;
-    k_point_blocks<<<ceil_div(d.np, 128), 128, 0, s>>>(d.np, d.N, d.pt_start, d.B, d.ex, coeff, d.V,
-                                                         d.g, d.uvdiag); note_launch(1);
+    if (d.prec == PSBA_PREC_FP64)
+        k_point_blocks<double><<<ceil_div(d.np, 128), 128, 0, s>>>(d.np, d.N, d.pt_start, d.B, d.ex, coeff,
+                                                                     d.V, d.g, d.uvdiag);
+    else
+        k_point_blocks<float><<<ceil_div(d.np, 128), 128, 0, s>>>(
+            d.np, d.N, d.pt_start, (const float *)d.B, (const float *)d.ex, (float)coeff, (float *)d.V, d.g,
+            d.uvdiag);
+    note_launch(1);
 }
 
 // ---------------------------------------------------------------------------
@@ -256,10 +307,11 @@ void launch_point_blocks(const DeviceProblem &d, double coeff, cudaStream_t s)
 constexpr int CAM_THREADS = 128;
 constexpr int CAM_NV = 27;  // 21 upper-triangle entries of A^T A + 6 of A^T e
 
+template <typename R>
 __global__ void __launch_bounds__(CAM_THREADS) k_camera_partial(const CamUnit *__restrict__ units,
                                                                 const int *__restrict__ cam_obs,
-                                                                const double *__restrict__ A,
-                                                                const double *__restrict__ ex,
+                                                                const R *__restrict__ A,
+                                                                const R *__restrict__ ex,
                                                                 double *__restrict__ partial)
 {
     __shared__ double red[CAM_NV][CAM_THREADS];
@@ -267,24 +319,27 @@ __global__ void __launch_bounds__(CAM_THREADS) k_camera_partial(const CamUnit *_
     double acc[CAM_NV];
 #pragma unroll
     for (int v = 0; v < CAM_NV; ++v) acc[v] = 0.0;
-    for (int t = threadIdx.x; t < u.count; t += CAM_THREADS) {
-        const int o = cam_obs[u.begin + t];
-        double a[12];
-        const double2 *Ao = reinterpret_cast<const double2 *>(A + 12 * (size_t)o);
+    for (int t0 = threadIdx.x; t0 < u.count; t0 += CAM_THREADS * FLUSH) {
+        // FP64: accumulate directly; FP32: FLUSH products per FP64 addition
+        R part[CAM_NV];
 #pragma unroll
-        for (int e = 0; e < 6; ++e) {
-            const double2 x = Ao[e];
-            a[2 * e] = x.x;
-            a[2 * e + 1] = x.y;
+        for (int v = 0; v < CAM_NV; ++v) part[v] = (R)0;
+        const int tend = min(u.count, t0 + CAM_THREADS * FLUSH);
+        for (int t = t0; t < tend; t += CAM_THREADS) {
+            const int o = cam_obs[u.begin + t];
+            R a[12], e2[2];
+            ldn<R, 12>(A + 12 * (size_t)o, a);
+            ld2<R>(ex + 2 * (size_t)o, e2[0], e2[1]);
+            int v = 0;
+#pragma unroll
+            for (int r = 0; r < 6; ++r)
+#pragma unroll
+                for (int c = r; c < 6; ++c, ++v) part[v] = part[v] + a[r] * a[c] + a[6 + r] * a[6 + c];
+#pragma unroll
+            for (int k = 0; k < 6; ++k) part[21 + k] = part[21 + k] + a[k] * e2[0] + a[6 + k] * e2[1];
         }
-        const double2 e2 = *reinterpret_cast<const double2 *>(ex + 2 * (size_t)o);
-        int v = 0;
 #pragma unroll
-        for (int r = 0; r < 6; ++r)
-#pragma unroll
-            for (int c = r; c < 6; ++c, ++v) acc[v] = acc[v] + a[r] * a[c] + a[6 + r] * a[6 + c];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) acc[21 + k] = acc[21 + k] + a[k] * e2.x + a[6 + k] * e2.y;
+        for (int v = 0; v < CAM_NV; ++v) acc[v] += (double)part[v];
     }
 #pragma unroll
     for (int v = 0; v < CAM_NV; ++v) red[v][threadIdx.x] = acc[v];
@@ -328,9 +383,15 @@ __global__ void k_camera_finish(int nc, const int *__restrict__ unit_start,
 
 void launch_camera_blocks(const DeviceProblem &d, double coeff, cudaStream_t s)
 {
-    if (d.n_cam_units > 0)
-        k_camera_partial<<<d.n_cam_units, CAM_THREADS, 0, s>>>(d.cam_units, d.cam_obs, d.A, d.ex,
-                                                                 d.cam_partial); note_launch(1);
+    if (d.n_cam_units > 0) {
+        if (d.prec == PSBA_PREC_FP64)
+            k_camera_partial<double><<<d.n_cam_units, CAM_THREADS, 0, s>>>(d.cam_units, d.cam_obs, d.A, d.ex,
+                                                                             d.cam_partial);
+        else
+            k_camera_partial<float><<<d.n_cam_units, CAM_THREADS, 0, s>>>(
+                d.cam_units, d.cam_obs, (const float *)d.A, (const float *)d.ex, d.cam_partial);
+        note_launch(1);
+    }
     k_camera_finish<<<ceil_div(d.nc * CAM_NV, 128), 128, 0, s>>>(d.nc, d.cam_unit_start,
                                                                    d.cam_partial, coeff, d.U, d.g,
                                                                    d.uvdiag); note_launch(1);
@@ -340,15 +401,16 @@ void launch_camera_blocks(const DeviceProblem &d, double coeff, cudaStream_t s)
 // V_i^-1 of the damped V_i + mu I by cofactors (compute_Vinv.cl:29-86); the
 // near-singular branch (|T| < 1e-16, :31-73) restates the reference's pivoted
 // elimination on the symmetric matrix.
-__device__ __forceinline__ void vinv_one(const double *Vi, double mu, double *out)
+template <typename R>
+__device__ __forceinline__ void vinv_one(const R *Vi, R mu, R *out)
 {
-    const double a11 = Vi[0] + mu, a12 = Vi[1], a13 = Vi[2], a22 = Vi[3] + mu, a23 = Vi[4],
-                 a33 = Vi[5] + mu;
-    double T = (a33 * a12 * a12 - 2 * a12 * a13 * a23 + a22 * a13 * a13 + a11 * a23 * a23 -
+    const R a11 = Vi[0] + mu, a12 = Vi[1], a13 = Vi[2], a22 = Vi[3] + mu, a23 = Vi[4],
+            a33 = Vi[5] + mu;
+    R T = (a33 * a12 * a12 - 2 * a12 * a13 * a23 + a22 * a13 * a13 + a11 * a23 * a23 -
                 a11 * a22 * a33);
-    if (fabs(T) < 1e-16) {
-        const double a21 = a12, a31 = a13, a32 = a23;
-        double m[3][3] = {{a11, a12, a13}, {a21, a22, a23}, {a31, a32, a33}}, tmp;
+    if (fabs(T) < (R)1e-16) {
+        const R a21 = a12, a31 = a13, a32 = a23;
+        R m[3][3] = {{a11, a12, a13}, {a21, a22, a23}, {a31, a32, a33}}, tmp;
         int mx = 0;
         if (m[0][0] < m[1][0]) mx = 1;
         if (m[mx][0] < m[2][0]) mx = 2;
@@ -362,7 +424,7 @@ __device__ __forceinline__ void vinv_one(const double *Vi, double mu, double *ou
         m[2][2] = m[2][2] - m[2][0] * m[0][2];
         if (m[1][1] < m[2][1])
             for (int c = 0; c < 3; ++c) { tmp = m[1][c]; m[1][c] = m[2][c]; m[2][c] = tmp; }
-        if (m[1][1] != 0.0) {
+        if (m[1][1] != (R)0) {
             m[2][1] = m[2][1] / m[1][1];
             m[2][2] = m[2][2] - m[2][1] * m[1][2];
         }
@@ -383,58 +445,59 @@ __device__ __forceinline__ void vinv_one(const double *Vi, double mu, double *ou
     out[5] = -(-a12 * a12 + a11 * a22) / T;
 }
 
-__global__ void k_vinv(int np, const double *__restrict__ V, double mu, double *__restrict__ Vinv)
+template <typename R>
+__global__ void k_vinv(int np, const R *__restrict__ V, R mu, R *__restrict__ Vinv)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= np) return;
-    double vi[6], out[6];
+    R vi[6], out[6];
     for (int e = 0; e < 6; ++e) vi[e] = V[6 * (size_t)i + e];
-    vinv_one(vi, mu, out);
+    vinv_one<R>(vi, mu, out);
     for (int e = 0; e < 6; ++e) Vinv[6 * (size_t)i + e] = out[e];
 }
 
 void launch_vinv(const DeviceProblem &d, double mu, cudaStream_t s)
 {
     if (d.np == 0) return;
-    k_vinv<<<ceil_div(d.np, 128), 128, 0, s>>>(d.np, d.V, mu, d.Vinv); note_launch(1);
+    if (d.prec == PSBA_PREC_FP64)
+        k_vinv<double><<<ceil_div(d.np, 128), 128, 0, s>>>(d.np, d.V, mu, d.Vinv);
+    else
+        k_vinv<float><<<ceil_div(d.np, 128), 128, 0, s>>>(d.np, (const float *)d.V, (float)mu, (float *)d.Vinv);
+    note_launch(1);
 }
 
 // Y = W V^-1 (compute_Yblks.cl:26-37), one thread per observation.
+template <typename R>
 __global__ void __launch_bounds__(256) k_yblocks(int no, const int *__restrict__ obs_pt,
-                                                 const double *__restrict__ W,
-                                                 const double *__restrict__ Vinv,
-                                                 double *__restrict__ Y)
+                                                 const R *__restrict__ W, const R *__restrict__ Vinv,
+                                                 R *__restrict__ Y)
 {
     int o = blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= no) return;
-    const double *vi = Vinv + 6 * (size_t)__ldg(obs_pt + o);
-    const double s00 = __ldg(vi), s01 = __ldg(vi + 1), s02 = __ldg(vi + 2), s11 = __ldg(vi + 3),
-                 s12 = __ldg(vi + 4), s22 = __ldg(vi + 5);
-    const double2 *Wo = reinterpret_cast<const double2 *>(W + 18 * (size_t)o);
-    double w[18];
-#pragma unroll
-    for (int e = 0; e < 9; ++e) {
-        const double2 x = Wo[e];
-        w[2 * e] = x.x;
-        w[2 * e + 1] = x.y;
-    }
-    double y[18];
+    const R *vi = Vinv + 6 * (size_t)__ldg(obs_pt + o);
+    const R s00 = __ldg(vi), s01 = __ldg(vi + 1), s02 = __ldg(vi + 2), s11 = __ldg(vi + 3),
+            s12 = __ldg(vi + 4), s22 = __ldg(vi + 5);
+    R w[18], y[18];
+    ldn<R, 18>(W + 18 * (size_t)o, w);
 #pragma unroll
     for (int r = 0; r < 6; ++r) {
-        const double w0 = w[3 * r], w1 = w[3 * r + 1], w2 = w[3 * r + 2];
+        const R w0 = w[3 * r], w1 = w[3 * r + 1], w2 = w[3 * r + 2];
         y[3 * r + 0] = w0 * s00 + w1 * s01 + w2 * s02;
         y[3 * r + 1] = w0 * s01 + w1 * s11 + w2 * s12;
         y[3 * r + 2] = w0 * s02 + w1 * s12 + w2 * s22;
     }
-    double2 *Yo = reinterpret_cast<double2 *>(Y + 18 * (size_t)o);
-#pragma unroll
-    for (int e = 0; e < 9; ++e) Yo[e] = make_double2(y[2 * e], y[2 * e + 1]);
+    stn<R, 18>(Y + 18 * (size_t)o, y);
 }
 
 void launch_yblocks(const DeviceProblem &d, cudaStream_t s)
 {
     if (d.no == 0) return;
-    k_yblocks<<<ceil_div(d.no, 256), 256, 0, s>>>(d.no, d.obs_pt, d.W, d.Vinv, d.Y); note_launch(1);
+    if (d.prec == PSBA_PREC_FP64)
+        k_yblocks<double><<<ceil_div(d.no, 256), 256, 0, s>>>(d.no, d.obs_pt, d.W, d.Vinv, d.Y);
+    else
+        k_yblocks<float><<<ceil_div(d.no, 256), 256, 0, s>>>(d.no, d.obs_pt, (const float *)d.W,
+                                                               (const float *)d.Vinv, (float *)d.Y);
+    note_launch(1);
 }
 
 // ---------------------------------------------------------------------------
@@ -444,11 +507,12 @@ void launch_yblocks(const DeviceProblem &d, cudaStream_t s)
 // points of a camera pair, all 36 entries of the 6x6 product.
 // Diagonal blocks: one thread per unit of a camera's observations, the 21
 // lower entries plus the 6 ea sums.  Units are then summed in order.
+template <typename R>
 __global__ void __launch_bounds__(128) k_schur_off(int n_units, const SchurUnit *__restrict__ units,
                                                    const int *__restrict__ pa,
                                                    const int *__restrict__ pb,
-                                                   const double *__restrict__ Y,
-                                                   const double *__restrict__ W,
+                                                   const R *__restrict__ Y,
+                                                   const R *__restrict__ W,
                                                    double *__restrict__ partial)
 {
     const int uid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -457,30 +521,48 @@ __global__ void __launch_bounds__(128) k_schur_off(int n_units, const SchurUnit 
     double acc[36];
 #pragma unroll
     for (int e = 0; e < 36; ++e) acc[e] = 0.0;
-    for (int t = 0; t < u.count; ++t) {
-        const int a = __ldg(pa + u.begin + t), b = __ldg(pb + u.begin + t);
-        const double2 *Wb = reinterpret_cast<const double2 *>(W + 18 * (size_t)b);
-        const double2 *Ya = reinterpret_cast<const double2 *>(Y + 18 * (size_t)a);
-        double w[18], y[18];
+    if constexpr (is_fp64<R>()) {
+        for (int t = 0; t < u.count; ++t) {
+            const int a = __ldg(pa + u.begin + t), b = __ldg(pb + u.begin + t);
+            R w[18], y[18];
+            ldn<R, 18>(W + 18 * (size_t)b, w);
+            ldn<R, 18>(Y + 18 * (size_t)a, y);
 #pragma unroll
-        for (int e = 0; e < 9; ++e) {
-            const double2 x = __ldg(Wb + e);
-            w[2 * e] = x.x;
-            w[2 * e + 1] = x.y;
-            const double2 z = __ldg(Ya + e);
-            y[2 * e] = z.x;
-            y[2 * e + 1] = z.y;
+            for (int r = 0; r < 6; ++r)
+#pragma unroll
+                for (int c = 0; c < 6; ++c) {
+                    double s = acc[r * 6 + c];
+                    s = fma((double)y[3 * r], (double)w[3 * c], s);
+                    s = fma((double)y[3 * r + 1], (double)w[3 * c + 1], s);
+                    s = fma((double)y[3 * r + 2], (double)w[3 * c + 2], s);
+                    acc[r * 6 + c] = s;
+                }
         }
+    } else {
+        for (int t0 = 0; t0 < u.count; t0 += FLUSH) {
+            R part[36];
 #pragma unroll
-        for (int r = 0; r < 6; ++r)
+            for (int e = 0; e < 36; ++e) part[e] = (R)0;
+            const int tend = min(u.count, t0 + FLUSH);
+            for (int t = t0; t < tend; ++t) {
+                const int a = __ldg(pa + u.begin + t), b = __ldg(pb + u.begin + t);
+                R w[18], y[18];
+                ldn<R, 18>(W + 18 * (size_t)b, w);
+                ldn<R, 18>(Y + 18 * (size_t)a, y);
 #pragma unroll
-            for (int c = 0; c < 6; ++c) {
-                double s = acc[r * 6 + c];
-                s = fma(y[3 * r], w[3 * c], s);
-                s = fma(y[3 * r + 1], w[3 * c + 1], s);
-                s = fma(y[3 * r + 2], w[3 * c + 2], s);
-                acc[r * 6 + c] = s;
+                for (int r = 0; r < 6; ++r)
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) {
+                        R s = part[r * 6 + c];
+                        s = fma(y[3 * r], w[3 * c], s);
+                        s = fma(y[3 * r + 1], w[3 * c + 1], s);
+                        s = fma(y[3 * r + 2], w[3 * c + 2], s);
+                        part[r * 6 + c] = s;
+                    }
             }
+#pragma unroll
+            for (int e = 0; e < 36; ++e) acc[e] += (double)part[e];
+        }
     }
     double *p = partial + (size_t)u.out * 36;
 #pragma unroll
@@ -489,11 +571,36 @@ __global__ void __launch_bounds__(128) k_schur_off(int n_units, const SchurUnit 
 
 constexpr int DIAG_NV = 27;  // 21 lower entries + 6 ea sums
 
+template <typename R>
+__device__ __forceinline__ void diag_products(const R *y, const R *w, R g0, R g1, R g2, R *acc)
+{
+    int v = 0;
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int c = 0; c <= r; ++c, ++v) {
+            R s = acc[v];
+            s = fma(y[3 * r], w[3 * c], s);
+            s = fma(y[3 * r + 1], w[3 * c + 1], s);
+            s = fma(y[3 * r + 2], w[3 * c + 2], s);
+            acc[v] = s;
+        }
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+        R s = acc[21 + r];
+        s = fma(y[3 * r], g0, s);
+        s = fma(y[3 * r + 1], g1, s);
+        s = fma(y[3 * r + 2], g2, s);
+        acc[21 + r] = s;
+    }
+}
+
+template <typename R>
 __global__ void __launch_bounds__(128) k_schur_diag(int n_units, const SchurUnit *__restrict__ units,
                                                     const int *__restrict__ cam_obs,
                                                     const int *__restrict__ obs_pt,
-                                                    const double *__restrict__ Y,
-                                                    const double *__restrict__ W,
+                                                    const R *__restrict__ Y,
+                                                    const R *__restrict__ W,
                                                     const double *__restrict__ gb,
                                                     double *__restrict__ partial)
 {
@@ -503,42 +610,23 @@ __global__ void __launch_bounds__(128) k_schur_diag(int n_units, const SchurUnit
     double acc[DIAG_NV];
 #pragma unroll
     for (int e = 0; e < DIAG_NV; ++e) acc[e] = 0.0;
-    for (int t = 0; t < u.count; ++t) {
-        const int a = __ldg(cam_obs + u.begin + t);
-        const int i = __ldg(obs_pt + a);
-        const double2 *Wa = reinterpret_cast<const double2 *>(W + 18 * (size_t)a);
-        const double2 *Ya = reinterpret_cast<const double2 *>(Y + 18 * (size_t)a);
-        double w[18], y[18];
+    for (int t0 = 0; t0 < u.count; t0 += FLUSH) {
+        R part[DIAG_NV];
 #pragma unroll
-        for (int e = 0; e < 9; ++e) {
-            const double2 x = __ldg(Wa + e);
-            w[2 * e] = x.x;
-            w[2 * e + 1] = x.y;
-            const double2 z = __ldg(Ya + e);
-            y[2 * e] = z.x;
-            y[2 * e + 1] = z.y;
+        for (int e = 0; e < DIAG_NV; ++e) part[e] = (R)0;
+        const int tend = min(u.count, t0 + FLUSH);
+        for (int t = t0; t < tend; ++t) {
+            const int a = __ldg(cam_obs + u.begin + t);
+            const int i = __ldg(obs_pt + a);
+            R w[18], y[18];
+            ldn<R, 18>(W + 18 * (size_t)a, w);
+            ldn<R, 18>(Y + 18 * (size_t)a, y);
+            const R g0 = (R)__ldg(gb + 3 * (size_t)i), g1 = (R)__ldg(gb + 3 * (size_t)i + 1),
+                    g2 = (R)__ldg(gb + 3 * (size_t)i + 2);
+            diag_products<R>(y, w, g0, g1, g2, part);
         }
-        const double g0 = __ldg(gb + 3 * (size_t)i), g1 = __ldg(gb + 3 * (size_t)i + 1),
-                     g2 = __ldg(gb + 3 * (size_t)i + 2);
-        int v = 0;
 #pragma unroll
-        for (int r = 0; r < 6; ++r)
-#pragma unroll
-            for (int c = 0; c <= r; ++c, ++v) {
-                double s = acc[v];
-                s = fma(y[3 * r], w[3 * c], s);
-                s = fma(y[3 * r + 1], w[3 * c + 1], s);
-                s = fma(y[3 * r + 2], w[3 * c + 2], s);
-                acc[v] = s;
-            }
-#pragma unroll
-        for (int r = 0; r < 6; ++r) {
-            double s = acc[21 + r];
-            s = fma(y[3 * r], g0, s);
-            s = fma(y[3 * r + 1], g1, s);
-            s = fma(y[3 * r + 2], g2, s);
-            acc[21 + r] = s;
-        }
+        for (int e = 0; e < DIAG_NV; ++e) acc[e] += (double)part[e];
     }
     double *p = partial + (size_t)u.out * DIAG_NV;
 #pragma unroll
@@ -596,17 +684,29 @@ __global__ void k_pad_identity(int N, int Np, double *S, double *rhs)
 
 void launch_schur_off(const DeviceProblem &d, cudaStream_t s)
 {
-    if (d.n_off_units > 0)
-        k_schur_off<<<ceil_div(d.n_off_units, 128), 128, 0, s>>>(d.n_off_units, d.off_units, d.pair_a,
-                                                                   d.pair_b, d.Y, d.W, d.schur_partial); note_launch(1);
+    if (d.n_off_units == 0) return;
+    if (d.prec == PSBA_PREC_FP64)
+        k_schur_off<double><<<ceil_div(d.n_off_units, 128), 128, 0, s>>>(d.n_off_units, d.off_units, d.pair_a,
+                                                                           d.pair_b, d.Y, d.W, d.schur_partial);
+    else
+        k_schur_off<float><<<ceil_div(d.n_off_units, 128), 128, 0, s>>>(
+            d.n_off_units, d.off_units, d.pair_a, d.pair_b, (const float *)d.Y, (const float *)d.W,
+            d.schur_partial);
+    note_launch(1);
 }
 
 void launch_schur_diag(const DeviceProblem &d, cudaStream_t s)
 {
     double *diag_partial = d.schur_partial + (size_t)d.n_off_units * 36;
-    if (d.n_diag_units > 0)
-        k_schur_diag<<<ceil_div(d.n_diag_units, 128), 128, 0, s>>>(
-            d.n_diag_units, d.diag_units, d.cam_obs, d.obs_pt, d.Y, d.W, d.g + d.N, diag_partial); note_launch(1);
+    if (d.n_diag_units == 0) return;
+    if (d.prec == PSBA_PREC_FP64)
+        k_schur_diag<double><<<ceil_div(d.n_diag_units, 128), 128, 0, s>>>(
+            d.n_diag_units, d.diag_units, d.cam_obs, d.obs_pt, d.Y, d.W, d.g + d.N, diag_partial);
+    else
+        k_schur_diag<float><<<ceil_div(d.n_diag_units, 128), 128, 0, s>>>(
+            d.n_diag_units, d.diag_units, d.cam_obs, d.obs_pt, (const float *)d.Y, (const float *)d.W,
+            d.g + d.N, diag_partial);
+    note_launch(1);
 }
 
 void launch_schur_reduce(const DeviceProblem &d, double mu, cudaStream_t s)
@@ -633,10 +733,10 @@ void launch_schur(const DeviceProblem &d, double mu, cudaStream_t s)
 // eb = gb - sum_j W_ij^T dpa_j (compute_eb.cl:25-39), dpb = V^-1 eb
 // (compute_dpb.cl:19-34), one thread per point; block partials of |dpb|^2
 // and dpb (mu dpb + gb) for the gain ratio (levmar.cpp:271-280).
+template <typename R>
 __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int *__restrict__ pt_start,
                                                 const int *__restrict__ obs_cam,
-                                                const double *__restrict__ W,
-                                                const double *__restrict__ Vinv,
+                                                const R *__restrict__ W, const R *__restrict__ Vinv,
                                                 const double *__restrict__ g, double mu,
                                                 double *__restrict__ dp, double *__restrict__ eb,
                                                 double *__restrict__ partial)
@@ -647,15 +747,17 @@ __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int *__re
     if (i < np) {
         double e0 = 0, e1 = 0, e2 = 0;
         const int end = pt_start[i + 1];
+#pragma unroll 4
         for (int o = pt_start[i]; o < end; ++o) {
-            const double *w = W + 18 * (size_t)o;
+            R w[18];
+            ldn<R, 18>(W + 18 * (size_t)o, w);
             const double *da = dp + 6 * (size_t)__ldg(obs_cam + o);
 #pragma unroll
             for (int k = 0; k < 6; ++k) {
                 const double dk = da[k];
-                e0 = e0 + w[3 * k] * dk;
-                e1 = e1 + w[3 * k + 1] * dk;
-                e2 = e2 + w[3 * k + 2] * dk;
+                e0 = e0 + (double)w[3 * k] * dk;
+                e1 = e1 + (double)w[3 * k + 1] * dk;
+                e2 = e2 + (double)w[3 * k + 2] * dk;
             }
         }
         const double *gb = g + ncp + 3 * (size_t)i;
@@ -665,10 +767,11 @@ __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int *__re
         eb[3 * (size_t)i] = e0;
         eb[3 * (size_t)i + 1] = e1;
         eb[3 * (size_t)i + 2] = e2;
-        const double *vi = Vinv + 6 * (size_t)i;
-        const double d0 = vi[0] * e0 + vi[1] * e1 + vi[2] * e2;
-        const double d1 = vi[1] * e0 + vi[3] * e1 + vi[4] * e2;
-        const double d2 = vi[2] * e0 + vi[4] * e1 + vi[5] * e2;
+        const R *vi = Vinv + 6 * (size_t)i;
+        const double v0 = vi[0], v1 = vi[1], v2 = vi[2], v3 = vi[3], v4 = vi[4], v5 = vi[5];
+        const double d0 = v0 * e0 + v1 * e1 + v2 * e2;
+        const double d1 = v1 * e0 + v3 * e1 + v4 * e2;
+        const double d2 = v2 * e0 + v4 * e1 + v5 * e2;
         double *db = dp + ncp + 3 * (size_t)i;
         db[0] = d0;
         db[1] = d1;
@@ -696,8 +799,14 @@ int eb_blocks(const DeviceProblem &d) { return ceil_div(d.np > 0 ? d.np : 1, 256
 
 void launch_eb_dpb(const DeviceProblem &d, double mu, cudaStream_t s)
 {
-    k_eb_dpb<<<eb_blocks(d), 256, 0, s>>>(d.np, d.N, d.pt_start, d.obs_cam, d.W, d.Vinv, d.g, mu,
-                                           d.dp, d.eb, d.red_partial); note_launch(1);
+    if (d.prec == PSBA_PREC_FP64)
+        k_eb_dpb<double><<<eb_blocks(d), 256, 0, s>>>(d.np, d.N, d.pt_start, d.obs_cam, d.W, d.Vinv, d.g, mu,
+                                                        d.dp, d.eb, d.red_partial);
+    else
+        k_eb_dpb<float><<<eb_blocks(d), 256, 0, s>>>(d.np, d.N, d.pt_start, d.obs_cam, (const float *)d.W,
+                                                       (const float *)d.Vinv, d.g, mu, d.dp, d.eb,
+                                                       d.red_partial);
+    note_launch(1);
 }
 
 // Sum the dpa part and the per-block partials of the back-substitution in a
@@ -829,21 +938,22 @@ void launch_update_params(const DeviceProblem &d, cudaStream_t s)
 }
 
 // J x per observation (compute_Jmultiply.cl:28-44), 2 outputs each.
+template <typename R>
 __global__ void k_jmultiply(int no, int ncp, const int *__restrict__ obs_pt,
-                            const int *__restrict__ obs_cam, const double *__restrict__ A,
-                            const double *__restrict__ B, const double *__restrict__ x,
+                            const int *__restrict__ obs_cam, const R *__restrict__ A,
+                            const R *__restrict__ B, const double *__restrict__ x,
                             double *__restrict__ out)
 {
     const int o = blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= no) return;
     const double *xa = x + 6 * (size_t)obs_cam[o];
     const double *xb = x + ncp + 3 * (size_t)obs_pt[o];
-    const double *a = A + 12 * (size_t)o;
-    const double *b = B + 6 * (size_t)o;
+    const R *a = A + 12 * (size_t)o;
+    const R *b = B + 6 * (size_t)o;
     for (int k = 0; k < 2; ++k) {
         double s = 0.0;
-        for (int m = 0; m < 6; ++m) s += a[6 * k + m] * xa[m];
-        for (int m = 0; m < 3; ++m) s += b[3 * k + m] * xb[m];
+        for (int m = 0; m < 6; ++m) s += (double)a[6 * k + m] * xa[m];
+        for (int m = 0; m < 3; ++m) s += (double)b[3 * k + m] * xb[m];
         out[2 * (size_t)o + k] = s;
     }
 }
@@ -851,7 +961,12 @@ __global__ void k_jmultiply(int no, int ncp, const int *__restrict__ obs_pt,
 void launch_jmultiply(const DeviceProblem &d, const double *x, double *out, cudaStream_t s)
 {
     if (d.no == 0) return;
-    k_jmultiply<<<ceil_div(d.no, 256), 256, 0, s>>>(d.no, d.N, d.obs_pt, d.obs_cam, d.A, d.B, x, out); note_launch(1);
+    if (d.prec == PSBA_PREC_FP64)
+        k_jmultiply<double><<<ceil_div(d.no, 256), 256, 0, s>>>(d.no, d.N, d.obs_pt, d.obs_cam, d.A, d.B, x, out);
+    else
+        k_jmultiply<float><<<ceil_div(d.no, 256), 256, 0, s>>>(d.no, d.N, d.obs_pt, d.obs_cam,
+                                                                 (const float *)d.A, (const float *)d.B, x, out);
+    note_launch(1);
 }
 
 __global__ void k_axpby(double *out, const double *x, double a, const double *y, double b, long long n)
@@ -880,11 +995,12 @@ void launch_scale(double *out, const double *x, const double *num, const double 
     k_scale<<<ceil_div(n, 256), 256, 0, s>>>(out, x, num, den, den_scale, sign, n); note_launch(1);
 }
 
-__global__ void k_expand_V(int np, const double *V6, double *V9)
+template <typename R>
+__global__ void k_expand_V(int np, const R *V6, double *V9)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= np) return;
-    const double *v = V6 + 6 * (size_t)i;
+    const R *v = V6 + 6 * (size_t)i;
     double *o = V9 + 9 * (size_t)i;
     o[0] = v[0]; o[1] = v[1]; o[2] = v[2];
     o[3] = v[1]; o[4] = v[3]; o[5] = v[4];
@@ -894,7 +1010,11 @@ __global__ void k_expand_V(int np, const double *V6, double *V9)
 void launch_expand_V(const DeviceProblem &d, const double *V6, double *V9, cudaStream_t s)
 {
     if (d.np == 0) return;
-    k_expand_V<<<ceil_div(d.np, 128), 128, 0, s>>>(d.np, V6, V9); note_launch(1);
+    if (d.prec == PSBA_PREC_FP64)
+        k_expand_V<double><<<ceil_div(d.np, 128), 128, 0, s>>>(d.np, V6, V9);
+    else
+        k_expand_V<float><<<ceil_div(d.np, 128), 128, 0, s>>>(d.np, (const float *)V6, V9);
+    note_launch(1);
 }
 
 }  // namespace psba

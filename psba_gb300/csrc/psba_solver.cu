@@ -75,6 +75,7 @@ struct psba_handle {
     int linearized = 0;          // 1 after eval_normal / a linearization
     double last_mu = 0.0;
     double *host_scalars = nullptr;  // pinned, 64 doubles
+    int chol_epoch = 0;              // increases with every dense-solver launch
 };
 
 namespace {
@@ -292,7 +293,13 @@ void enqueue_step(psba_handle *h, double mu)
     DeviceProblem &d = h->d;
     {
         StageScope sc(h, ST_CHOL);
-        launch_cholesky_solve(d, h->stream);
+        if (d.prec == PSBA_PREC_MIXED) {
+            cudaMemcpyAsync(d.Ssave, d.S, sizeof(double) * (size_t)d.Np * d.Np, cudaMemcpyDeviceToDevice,
+                            h->stream);
+            cudaMemcpyAsync(d.rhs_save, d.rhs, sizeof(double) * d.Np, cudaMemcpyDeviceToDevice, h->stream);
+        }
+        launch_chol_dataflow(d, 0, ++h->chol_epoch, d.xsol, h->stream);
+        if (d.prec == PSBA_PREC_MIXED) launch_refine(d, ++h->chol_epoch, h->stream);
         cudaMemcpyAsync(d.dp, d.xsol, sizeof(double) * d.N, cudaMemcpyDeviceToDevice, h->stream);
     }
     {
@@ -367,6 +374,8 @@ int levmar_impl(psba_handle *h, const psba_opts *o, int *itno, psba_result *res,
             TRY(check_launch());
             TrialScalars ts;
             TRY(read_trial(h, &ts));
+            if (ts.chol_status == 2)
+                return set_error("dense solver wait budget exhausted (device dataflow stalled)"), PSBA_ERR_STATE;
             if (res) res->n_trials++;
             if (have_pl2_pending) {
                 p_L2 = h->host_scalars[SC_PL2A] + h->host_scalars[SC_PL2B];
@@ -455,6 +464,8 @@ int compute_pb(psba_handle *h, double *lambda, int *solved)
     TRY(check_launch());
     TrialScalars ts;
     TRY(read_trial(h, &ts));
+    if (ts.chol_status == 2)
+        return set_error("dense solver wait budget exhausted (device dataflow stalled)"), PSBA_ERR_STATE;
     if (ts.chol_status != 0) {
         if (*lambda == 0.0) {
             // modified Cholesky of the saved S (lower, N x N inside the padded Np)
@@ -776,8 +787,8 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
         off_start[q + 1] = (int)off_units.size();
     }
     for (int j = 0; j < nc; ++j) {
-        for (int b = cam_start[j]; b < cam_start[j + 1]; b += SCHUR_CHUNK) {
-            const int cnt = std::min(SCHUR_CHUNK, cam_start[j + 1] - b);
+        for (int b = cam_start[j]; b < cam_start[j + 1]; b += DIAG_CHUNK) {
+            const int cnt = std::min(DIAG_CHUNK, cam_start[j + 1] - b);
             diag_units.push_back({j, b, cnt, (int)diag_units.size()});
         }
         diag_start[j + 1] = (int)diag_units.size();
@@ -838,8 +849,21 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     TRY(dalloc(h, &d.Ssave, (size_t)d.Np * d.Np));
     TRY(dalloc(h, &d.rhs, (size_t)d.Np));
     TRY(dalloc(h, &d.xsol, (size_t)d.Np));
+    TRY(dalloc(h, &d.rhs_save, (size_t)d.Np));
+    TRY(dalloc(h, &d.xref, (size_t)d.Np));
     TRY(dalloc(h, &d.Linv, (size_t)d.Np * TILE));
     TRY(dalloc(h, &d.status, 4));
+    {
+        const int nb = d.Np / TILE;
+        std::vector<int2> tasks;
+        for (int K = 0; K < nb; ++K)
+            for (int I = K; I < nb; ++I) tasks.push_back(make_int2(I, K));
+        d.chol_n_flags = nb * (nb + 1) / 2 + 2 * nb;
+        TRY(dalloc(h, &d.chol_tasks, tasks.size()));
+        TRY(dalloc(h, &d.chol_flags, (size_t)d.chol_n_flags));
+        TRY(upload(h, d.chol_tasks, tasks.data(), tasks.size()));
+        PSBA_CUDA_TRY(cudaMemsetAsync(d.chol_flags, 0, sizeof(int) * d.chol_n_flags, h->stream));
+    }
     TRY(dalloc(h, &d.dp, nt));
     TRY(dalloc(h, &d.eb, 3 * (size_t)np));
     h->nred = 512;
@@ -931,13 +955,26 @@ int timed_end(psba_handle *h, psba_result *res)
     return PSBA_OK;
 }
 
+// Device array of the per-observation / per-point storage type -> host doubles.
+int copy_out(psba_handle *h, double *dst, const double *src, size_t count)
+{
+    if (count == 0 || !dst) return PSBA_OK;
+    if (h->d.prec == PSBA_PREC_FP64) {
+        PSBA_CUDA_TRY(cudaMemcpyAsync(dst, src, sizeof(double) * count, cudaMemcpyDeviceToHost, h->stream));
+        return PSBA_OK;
+    }
+    std::vector<float> tmp(count);
+    PSBA_CUDA_TRY(cudaMemcpyAsync(tmp.data(), src, sizeof(float) * count, cudaMemcpyDeviceToHost, h->stream));
+    TRY(sync(h));
+    for (size_t k = 0; k < count; ++k) dst[k] = tmp[k];
+    return PSBA_OK;
+}
+
 int check_opts(const psba_opts *o)
 {
     if (!o) return set_error("null options"), PSBA_ERR_ARG;
     if (o->precision != PSBA_PREC_FP64 && o->precision != PSBA_PREC_MIXED)
         return set_error("unknown precision"), PSBA_ERR_ARG;
-    if (o->precision == PSBA_PREC_MIXED)
-        return set_error("mixed precision is not available in this build"), PSBA_ERR_ARG;
     return PSBA_OK;
 }
 
@@ -1032,6 +1069,7 @@ int psba_levmar(psba_handle *h, const psba_opts *opts, int *itno, psba_result *r
 {
     if (!h || !itno) return set_error("null argument"), PSBA_ERR_ARG;
     TRY(check_opts(opts));
+    h->d.prec = opts->precision;
     reset_result(res);
     TRY(timed_begin(h));
     int flag = 0;
@@ -1044,6 +1082,7 @@ int psba_trust_region(psba_handle *h, const psba_opts *opts, int *itno, psba_res
 {
     if (!h || !itno) return set_error("null argument"), PSBA_ERR_ARG;
     TRY(check_opts(opts));
+    h->d.prec = opts->precision;
     reset_result(res);
     TRY(timed_begin(h));
     int flag = 0;
@@ -1056,6 +1095,7 @@ int psba_solve_hybrid(psba_handle *h, const psba_opts *opts, psba_result *res)
 {
     if (!h) return set_error("null argument"), PSBA_ERR_ARG;
     TRY(check_opts(opts));
+    h->d.prec = opts->precision;
     reset_result(res);
     TRY(timed_begin(h));
     int itno = 0, flag = 0;
@@ -1093,8 +1133,8 @@ int psba_eval_jacobian(psba_handle *h, double *JA, double *JB)
     h->linearized = 1;
     TRY(check_launch());
     const size_t no = (size_t)h->d.no;
-    if (JA && no) PSBA_CUDA_TRY(cudaMemcpyAsync(JA, h->d.A, sizeof(double) * 12 * no, cudaMemcpyDeviceToHost, h->stream));
-    if (JB && no) PSBA_CUDA_TRY(cudaMemcpyAsync(JB, h->d.B, sizeof(double) * 6 * no, cudaMemcpyDeviceToHost, h->stream));
+    TRY(copy_out(h, JA, h->d.A, 12 * no));
+    TRY(copy_out(h, JB, h->d.B, 6 * no));
     return sync(h);
 }
 
@@ -1111,7 +1151,7 @@ int psba_eval_normal(psba_handle *h, double coeff, double *U, double *V, double 
         launch_expand_V(d, d.V, d.tmp9, h->stream);
         PSBA_CUDA_TRY(cudaMemcpyAsync(V, d.tmp9, sizeof(double) * 9 * np, cudaMemcpyDeviceToHost, h->stream));
     }
-    if (W && no) PSBA_CUDA_TRY(cudaMemcpyAsync(W, d.W, sizeof(double) * 18 * no, cudaMemcpyDeviceToHost, h->stream));
+    TRY(copy_out(h, W, d.W, 18 * no));
     if (g) PSBA_CUDA_TRY(cudaMemcpyAsync(g, d.g, sizeof(double) * (d.N + 3 * np), cudaMemcpyDeviceToHost, h->stream));
     return sync(h);
 }
@@ -1125,7 +1165,7 @@ int psba_eval_reduced(psba_handle *h, double mu, double *Vinv, double *Y, double
     h->last_mu = mu;
     TRY(check_launch());
     const size_t no = (size_t)d.no, np = (size_t)d.np;
-    if (Y && no) PSBA_CUDA_TRY(cudaMemcpyAsync(Y, d.Y, sizeof(double) * 18 * no, cudaMemcpyDeviceToHost, h->stream));
+    TRY(copy_out(h, Y, d.Y, 18 * no));
     if (Vinv && np) {
         launch_expand_V(d, d.Vinv, d.tmp9, h->stream);
         PSBA_CUDA_TRY(cudaMemcpyAsync(Vinv, d.tmp9, sizeof(double) * 9 * np, cudaMemcpyDeviceToHost, h->stream));
@@ -1150,6 +1190,8 @@ int psba_eval_step(psba_handle *h, double *dp, int *chol_status)
     TRY(check_launch());
     TrialScalars ts;
     TRY(read_trial(h, &ts));
+    if (ts.chol_status == 2)
+        return set_error("dense solver wait budget exhausted (device dataflow stalled)"), PSBA_ERR_STATE;
     if (chol_status) *chol_status = ts.chol_status;
     if (dp && ts.chol_status == 0)
         PSBA_CUDA_TRY(cudaMemcpyAsync(dp, d.dp, sizeof(double) * (d.N + 3 * (size_t)d.np),
@@ -1223,6 +1265,17 @@ int psba_transfer_bytes(psba_handle *h, size_t *h2d, size_t *d2h)
     if (!h) return set_error("null handle"), PSBA_ERR_ARG;
     if (h2d) *h2d = h->h2d_bytes;
     if (d2h) *d2h = h->d2h_bytes;
+    return PSBA_OK;
+}
+
+int psba_set_precision(psba_handle *h, int precision)
+{
+    if (!h) return set_error("null handle"), PSBA_ERR_ARG;
+    if (precision != PSBA_PREC_FP64 && precision != PSBA_PREC_MIXED)
+        return set_error("unknown precision"), PSBA_ERR_ARG;
+    TRY(sync(h));
+    h->d.prec = precision;
+    h->linearized = 0;
     return PSBA_OK;
 }
 

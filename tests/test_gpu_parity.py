@@ -183,3 +183,53 @@ def test_hybrid_matched_final_cost():
         g = s.solve_hybrid()
     assert g.status == o.status
     assert abs(g.final_cost - o.final_cost) <= 1e-6 * o.final_cost
+
+
+# ---------------------------------------------------------------- mixed precision
+# Jacobian, residual, W, V^-1 and Y in FP32; U, S, ea accumulated in FP64;
+# Cholesky, refinement, step, cost and gain ratio in FP64.  Stage tolerance:
+# 1e-5 of the array's largest magnitude (FP32 rounding of quantities built
+# from a handful of FP32 operations); solves: final cost within 1e-6 of the
+# FP64 oracle's.
+MIXED_TOL = 1e-5
+
+
+def test_mixed_stages(golden):
+    sc, z = golden
+    with P.Solver(sc) as s:
+        s.set_precision(P.PREC_MIXED)
+        JA, JB = s.eval_jacobian()
+        close(JA, z["JA"], MIXED_TOL)
+        close(JB, z["JB"], MIXED_TOL)
+        U, V, W, g = s.eval_normal(1.0)
+        close(U, z["U_c1"], MIXED_TOL)
+        close(V, z["V_c1"], MIXED_TOL)
+        close(W, z["W_c1"], MIXED_TOL)
+        close(g, z["g_c1"], 1e-4)
+        Vinv, Y, S, ea = s.eval_reduced(float(z["mu"]))
+        close(Vinv, z["Vinv"], 1e-4)
+        close(Y, z["Y"], 1e-4)
+        close(S, np.tril(z["S"]), 1e-4)
+        st, dp = s.eval_step()
+        assert st == 0
+        N = 6 * sc.n_cams
+        Sf = np.tril(S) + np.tril(S, -1).T
+        # refined solve of the (mixed-precision) reduced system
+        assert np.abs(Sf @ dp[:N] - ea).max() <= 1e-9 * np.abs(ea).max()
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_mixed_levmar_matched_final_cost(seed):
+    sc = scenes.small_lm_scene(seed)
+    o = oracle.levmar(sc, allow_switch=0, max_iter=30)
+    with P.Solver(sc) as s:
+        g = s.levmar(allow_switch=0, max_iter=30, precision=P.PREC_MIXED)
+    assert abs(g.final_cost - o.final_cost) <= 1e-6 * o.final_cost
+
+
+def test_mixed_power_law_matched_final_cost():
+    sc = scenes.circle_scene(seed=2, n_cams=24, n_pts=3000, name="circle24")
+    o = oracle.levmar(sc, allow_switch=0, max_iter=40)
+    with P.Solver(sc) as s:
+        g = s.levmar(allow_switch=0, max_iter=40, precision=P.PREC_MIXED)
+    assert abs(g.final_cost - o.final_cost) <= 1e-6 * o.final_cost

@@ -249,14 +249,19 @@ void launch_residual(const DeviceProblem &d, const double *tab, const double *pt
 // ---------------------------------------------------------------------------
 // Per-point sums: V_i = coeff sum B^T B (compute_V.cl:24-37) and
 // gb_i = coeff sum B^T e (compute_g.cl:42-57), ascending camera order.
+// V is accumulated in FP64 in both forms (in the mixed form from FP32
+// products): an FP32 running sum of B^T B can turn the nearly singular V of a
+// point seen from two close cameras indefinite, which moved the mixed form's
+// LM fixed point by 7e-3 of the cost on a 24-camera power-law scene.
 template <typename R>
 __global__ void k_point_blocks(int np, int ncp, const int *__restrict__ pt_start,
                                const R *__restrict__ B, const R *__restrict__ ex, R coeff,
-                               R *__restrict__ V, double *__restrict__ g, double *__restrict__ uvdiag)
+                               double *__restrict__ V, double *__restrict__ g, double *__restrict__ uvdiag)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= np) return;
-    R v00 = 0, v01 = 0, v02 = 0, v11 = 0, v12 = 0, v22 = 0, g0 = 0, g1 = 0, g2 = 0;
+    double v00 = 0, v01 = 0, v02 = 0, v11 = 0, v12 = 0, v22 = 0;
+    R g0 = 0, g1 = 0, g2 = 0;
     const int e = pt_start[i + 1];
 #pragma unroll 4
     for (int o = pt_start[i]; o < e; ++o) {
@@ -265,22 +270,32 @@ __global__ void k_point_blocks(int np, int ncp, const int *__restrict__ pt_start
         ld2<R>(ex + 2 * (size_t)o, ee[0], ee[1]);
         const R b0 = b[0], b1 = b[1], b2 = b[2], c0 = b[3], c1 = b[4], c2 = b[5];
         const R e0 = ee[0], e1 = ee[1];
-        v00 = v00 + b0 * b0 + c0 * c0;
-        v01 = v01 + b0 * b1 + c0 * c1;
-        v02 = v02 + b0 * b2 + c0 * c2;
-        v11 = v11 + b1 * b1 + c1 * c1;
-        v12 = v12 + b1 * b2 + c1 * c2;
-        v22 = v22 + b2 * b2 + c2 * c2;
+        if constexpr (is_fp64<R>()) {
+            v00 = v00 + b0 * b0 + c0 * c0;
+            v01 = v01 + b0 * b1 + c0 * c1;
+            v02 = v02 + b0 * b2 + c0 * c2;
+            v11 = v11 + b1 * b1 + c1 * c1;
+            v12 = v12 + b1 * b2 + c1 * c2;
+            v22 = v22 + b2 * b2 + c2 * c2;
+        } else {
+            v00 += (double)(b0 * b0 + c0 * c0);
+            v01 += (double)(b0 * b1 + c0 * c1);
+            v02 += (double)(b0 * b2 + c0 * c2);
+            v11 += (double)(b1 * b1 + c1 * c1);
+            v12 += (double)(b1 * b2 + c1 * c2);
+            v22 += (double)(b2 * b2 + c2 * c2);
+        }
         g0 = g0 + b0 * e0 + c0 * e1;
         g1 = g1 + b1 * e0 + c1 * e1;
         g2 = g2 + b2 * e0 + c2 * e1;
     }
-    R *Vi = V + 6 * (size_t)i;
-    Vi[0] = coeff * v00; Vi[1] = coeff * v01; Vi[2] = coeff * v02;
-    Vi[3] = coeff * v11; Vi[4] = coeff * v12; Vi[5] = coeff * v22;
-    uvdiag[ncp + 3 * (size_t)i] = (double)Vi[0];
-    uvdiag[ncp + 3 * (size_t)i + 1] = (double)Vi[3];
-    uvdiag[ncp + 3 * (size_t)i + 2] = (double)Vi[5];
+    const double cf = (double)coeff;
+    double *Vi = V + 6 * (size_t)i;
+    Vi[0] = cf * v00; Vi[1] = cf * v01; Vi[2] = cf * v02;
+    Vi[3] = cf * v11; Vi[4] = cf * v12; Vi[5] = cf * v22;
+    uvdiag[ncp + 3 * (size_t)i] = Vi[0];
+    uvdiag[ncp + 3 * (size_t)i + 1] = Vi[3];
+    uvdiag[ncp + 3 * (size_t)i + 2] = Vi[5];
     g[ncp + 3 * (size_t)i] = (double)(coeff * g0);
     g[ncp + 3 * (size_t)i + 1] = (double)(coeff * g1);
     g[ncp + 3 * (size_t)i + 2] = (double)(coeff * g2);
@@ -294,8 +309,7 @@ void launch_point_blocks(const DeviceProblem &d, double coeff, cudaStream_t s)
                                                                      d.V, d.g, d.uvdiag);
     else
         k_point_blocks<float><<<ceil_div(d.np, 128), 128, 0, s>>>(
-            d.np, d.N, d.pt_start, (const float *)d.B, (const float *)d.ex, (float)coeff, (float *)d.V, d.g,
-            d.uvdiag);
+            d.np, d.N, d.pt_start, (const float *)d.B, (const float *)d.ex, (float)coeff, d.V, d.g, d.uvdiag);
     note_launch(1);
 }
 
@@ -445,46 +459,47 @@ __device__ __forceinline__ void vinv_one(const R *Vi, R mu, R *out)
     out[5] = -(-a12 * a12 + a11 * a22) / T;
 }
 
-template <typename R>
-__global__ void k_vinv(int np, const R *__restrict__ V, R mu, R *__restrict__ Vinv)
+// The damping is added and the inverse taken in FP64 in both forms, and V^-1
+// is kept in FP64: for a point seen from two nearby cameras V_i is nearly
+// singular, and an FP32 V_i + mu I (which drops mu) or an FP32 V^-1 moves the
+// LM fixed point by ~1e-2 of the cost.
+__global__ void k_vinv(int np, const double *__restrict__ V, double mu, double *__restrict__ Vinv)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= np) return;
-    R vi[6], out[6];
+    double vi[6], out[6];
     for (int e = 0; e < 6; ++e) vi[e] = V[6 * (size_t)i + e];
-    vinv_one<R>(vi, mu, out);
+    vinv_one<double>(vi, mu, out);
     for (int e = 0; e < 6; ++e) Vinv[6 * (size_t)i + e] = out[e];
 }
 
 void launch_vinv(const DeviceProblem &d, double mu, cudaStream_t s)
 {
     if (d.np == 0) return;
-    if (d.prec == PSBA_PREC_FP64)
-        k_vinv<double><<<ceil_div(d.np, 128), 128, 0, s>>>(d.np, d.V, mu, d.Vinv);
-    else
-        k_vinv<float><<<ceil_div(d.np, 128), 128, 0, s>>>(d.np, (const float *)d.V, (float)mu, (float *)d.Vinv);
+    k_vinv<<<ceil_div(d.np, 128), 128, 0, s>>>(d.np, d.V, mu, d.Vinv);
     note_launch(1);
 }
 
 // Y = W V^-1 (compute_Yblks.cl:26-37), one thread per observation.
+// Y = W V^-1 evaluated in FP64 (V^-1 is FP64), stored in R.
 template <typename R>
 __global__ void __launch_bounds__(256) k_yblocks(int no, const int *__restrict__ obs_pt,
-                                                 const R *__restrict__ W, const R *__restrict__ Vinv,
+                                                 const R *__restrict__ W, const double *__restrict__ Vinv,
                                                  R *__restrict__ Y)
 {
     int o = blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= no) return;
-    const R *vi = Vinv + 6 * (size_t)__ldg(obs_pt + o);
-    const R s00 = __ldg(vi), s01 = __ldg(vi + 1), s02 = __ldg(vi + 2), s11 = __ldg(vi + 3),
-            s12 = __ldg(vi + 4), s22 = __ldg(vi + 5);
+    const double *vi = Vinv + 6 * (size_t)__ldg(obs_pt + o);
+    const double s00 = __ldg(vi), s01 = __ldg(vi + 1), s02 = __ldg(vi + 2), s11 = __ldg(vi + 3),
+                 s12 = __ldg(vi + 4), s22 = __ldg(vi + 5);
     R w[18], y[18];
     ldn<R, 18>(W + 18 * (size_t)o, w);
 #pragma unroll
     for (int r = 0; r < 6; ++r) {
-        const R w0 = w[3 * r], w1 = w[3 * r + 1], w2 = w[3 * r + 2];
-        y[3 * r + 0] = w0 * s00 + w1 * s01 + w2 * s02;
-        y[3 * r + 1] = w0 * s01 + w1 * s11 + w2 * s12;
-        y[3 * r + 2] = w0 * s02 + w1 * s12 + w2 * s22;
+        const double w0 = w[3 * r], w1 = w[3 * r + 1], w2 = w[3 * r + 2];
+        y[3 * r + 0] = (R)(w0 * s00 + w1 * s01 + w2 * s02);
+        y[3 * r + 1] = (R)(w0 * s01 + w1 * s11 + w2 * s12);
+        y[3 * r + 2] = (R)(w0 * s02 + w1 * s12 + w2 * s22);
     }
     stn<R, 18>(Y + 18 * (size_t)o, y);
 }
@@ -495,8 +510,8 @@ void launch_yblocks(const DeviceProblem &d, cudaStream_t s)
     if (d.prec == PSBA_PREC_FP64)
         k_yblocks<double><<<ceil_div(d.no, 256), 256, 0, s>>>(d.no, d.obs_pt, d.W, d.Vinv, d.Y);
     else
-        k_yblocks<float><<<ceil_div(d.no, 256), 256, 0, s>>>(d.no, d.obs_pt, (const float *)d.W,
-                                                               (const float *)d.Vinv, (float *)d.Y);
+        k_yblocks<float><<<ceil_div(d.no, 256), 256, 0, s>>>(d.no, d.obs_pt, (const float *)d.W, d.Vinv,
+                                                               (float *)d.Y);
     note_launch(1);
 }
 
@@ -736,7 +751,7 @@ void launch_schur(const DeviceProblem &d, double mu, cudaStream_t s)
 template <typename R>
 __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int *__restrict__ pt_start,
                                                 const int *__restrict__ obs_cam,
-                                                const R *__restrict__ W, const R *__restrict__ Vinv,
+                                                const R *__restrict__ W, const double *__restrict__ Vinv,
                                                 const double *__restrict__ g, double mu,
                                                 double *__restrict__ dp, double *__restrict__ eb,
                                                 double *__restrict__ partial)
@@ -767,7 +782,7 @@ __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int *__re
         eb[3 * (size_t)i] = e0;
         eb[3 * (size_t)i + 1] = e1;
         eb[3 * (size_t)i + 2] = e2;
-        const R *vi = Vinv + 6 * (size_t)i;
+        const double *vi = Vinv + 6 * (size_t)i;
         const double v0 = vi[0], v1 = vi[1], v2 = vi[2], v3 = vi[3], v4 = vi[4], v5 = vi[5];
         const double d0 = v0 * e0 + v1 * e1 + v2 * e2;
         const double d1 = v1 * e0 + v3 * e1 + v4 * e2;
@@ -804,8 +819,7 @@ void launch_eb_dpb(const DeviceProblem &d, double mu, cudaStream_t s)
                                                         d.dp, d.eb, d.red_partial);
     else
         k_eb_dpb<float><<<eb_blocks(d), 256, 0, s>>>(d.np, d.N, d.pt_start, d.obs_cam, (const float *)d.W,
-                                                       (const float *)d.Vinv, d.g, mu, d.dp, d.eb,
-                                                       d.red_partial);
+                                                       d.Vinv, d.g, mu, d.dp, d.eb, d.red_partial);
     note_launch(1);
 }
 

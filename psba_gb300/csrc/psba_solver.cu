@@ -1148,7 +1148,10 @@ int psba_eval_normal(psba_handle *h, double coeff, double *U, double *V, double 
     const size_t no = (size_t)d.no, np = (size_t)d.np;
     if (U) PSBA_CUDA_TRY(cudaMemcpyAsync(U, d.U, sizeof(double) * 36 * (size_t)d.nc, cudaMemcpyDeviceToHost, h->stream));
     if (V && np) {
+        const int prec = d.prec;
+        d.prec = PSBA_PREC_FP64;  // V is FP64 in both forms
         launch_expand_V(d, d.V, d.tmp9, h->stream);
+        d.prec = prec;
         PSBA_CUDA_TRY(cudaMemcpyAsync(V, d.tmp9, sizeof(double) * 9 * np, cudaMemcpyDeviceToHost, h->stream));
     }
     TRY(copy_out(h, W, d.W, 18 * no));
@@ -1167,7 +1170,10 @@ int psba_eval_reduced(psba_handle *h, double mu, double *Vinv, double *Y, double
     const size_t no = (size_t)d.no, np = (size_t)d.np;
     TRY(copy_out(h, Y, d.Y, 18 * no));
     if (Vinv && np) {
+        const int prec = d.prec;
+        d.prec = PSBA_PREC_FP64;  // V^-1 is FP64 in both forms
         launch_expand_V(d, d.Vinv, d.tmp9, h->stream);
+        d.prec = prec;
         PSBA_CUDA_TRY(cudaMemcpyAsync(Vinv, d.tmp9, sizeof(double) * 9 * np, cudaMemcpyDeviceToHost, h->stream));
     }
     if (S)

@@ -186,8 +186,9 @@ def test_hybrid_matched_final_cost():
 
 
 # ---------------------------------------------------------------- mixed precision
-# Jacobian, residual, W, V^-1 and Y in FP32; U, S, ea accumulated in FP64;
-# Cholesky, refinement, step, cost and gain ratio in FP64.  Stage tolerance:
+# Jacobian, residual, W, V and Y in FP32; U, S, ea accumulated in FP64; the
+# damped V^-1, Y's products, Cholesky, refinement, step, cost and gain ratio
+# in FP64.  Stage tolerance:
 # 1e-5 of the array's largest magnitude (FP32 rounding of quantities built
 # from a handful of FP32 operations); solves: final cost within 1e-6 of the
 # FP64 oracle's.
@@ -203,11 +204,11 @@ def test_mixed_stages(golden):
         close(JB, z["JB"], MIXED_TOL)
         U, V, W, g = s.eval_normal(1.0)
         close(U, z["U_c1"], MIXED_TOL)
-        close(V, z["V_c1"], MIXED_TOL)
+        close(V, z["V_c1"], MIXED_TOL)  # FP64 sum of FP32 products
         close(W, z["W_c1"], MIXED_TOL)
         close(g, z["g_c1"], 1e-4)
         Vinv, Y, S, ea = s.eval_reduced(float(z["mu"]))
-        close(Vinv, z["Vinv"], 1e-4)
+        close(Vinv, z["Vinv"], 1e-5)  # FP64 inverse of the FP32-accumulated V
         close(Y, z["Y"], 1e-4)
         close(S, np.tril(z["S"]), 1e-4)
         st, dp = s.eval_step()
@@ -228,8 +229,9 @@ def test_mixed_levmar_matched_final_cost(seed):
 
 
 def test_mixed_power_law_matched_final_cost():
+    # both forms run to convergence (the FP64 cost settles after ~60 iterations)
     sc = scenes.circle_scene(seed=2, n_cams=24, n_pts=3000, name="circle24")
-    o = oracle.levmar(sc, allow_switch=0, max_iter=40)
+    o = oracle.levmar(sc, allow_switch=0, max_iter=100)
     with P.Solver(sc) as s:
-        g = s.levmar(allow_switch=0, max_iter=40, precision=P.PREC_MIXED)
+        g = s.levmar(allow_switch=0, max_iter=100, precision=P.PREC_MIXED)
     assert abs(g.final_cost - o.final_cost) <= 1e-6 * o.final_cost

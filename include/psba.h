@@ -214,6 +214,29 @@ long long psba_kernel_launches(void);
 /* FMA throughput of the current device in TFLOP/s: which = 0 FP64, 1 FP32. */
 int psba_measure_peak(int which, double *tflops);
 
+/* ---- cost evaluation without device allocation ------------------------ */
+
+/* Sum of squared reprojection residuals (what psba_eval_residual returns in
+ * *cost) for callers that cannot allocate device memory when they need it:
+ * code running while a CUDA stream is being captured into a graph (cudaMalloc
+ * is not allowed then), a serving loop held to a fixed HBM budget, or a host
+ * framework that owns all device memory.  No counterpart in the reference.
+ *
+ * Every pointer is a device pointer the caller owns, in this header's layout
+ * (K 5, q0 4, cams 6 per camera; pts 3 per point; meas 2 per observation;
+ * obs_pt, obs_cam per observation); *cost (device) receives the result on
+ * `stream` (a cudaStream_t, NULL for the default stream).  Nothing is
+ * allocated: the scratch (camera tables and block sums) is a fixed 1 MiB
+ * array inside the library, held by every GPU that loads it until the
+ * process exits.  Limits: n_cams <= 1024, n_obs <= 16,777,216; larger sizes
+ * return PSBA_ERR_ARG.  The first call on a device looks up the array's
+ * device address (no allocation); make that first call before any stream
+ * capture begins.  All calls on a device share the array and keep the last
+ * call's contents, so calls that overlap on the GPU race: order them. */
+int psba_cost_noalloc(int n_cams, int n_obs, const double *K, const double *q0, const double *cams,
+                      const double *pts, const double *meas, const int *obs_pt, const int *obs_cam,
+                      double *cost, void *stream);
+
 /* ---- misc -------------------------------------------------------------- */
 
 /* Message of the last error on the calling thread. */

@@ -53,6 +53,14 @@ def parse():
     ap.add_argument("--cpu-iters", type=int, default=2, help="oracle LM iterations in the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--batch", type=int, default=1024, help="problems in the batched leg (0: skip)")
+    ap.add_argument("--batch-steps", type=int, default=3)
+    ap.add_argument("--pbp-sample", type=int, default=64,
+                    help="problems solved one by one by the plain FP64 form for the batched comparison")
+    ap.add_argument("--serve-rates", default="50,200,1000,2000", help="Poisson rates, req/s ('none' to skip)")
+    ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per rate")
+    ap.add_argument("--serve-max", type=int, default=400, help="requests per rate at most")
+    ap.add_argument("--serve-pool", type=int, default=32, help="distinct request scenes (cycled)")
     return ap.parse_args()
 
 
@@ -200,6 +208,108 @@ def run_reference(args):
     }
     print(json.dumps(line))
     return 0
+
+
+def batched_leg(P, args):
+    """1,024 independent problems (5-30 cameras, 200-3,000 points, 3-8 views)
+    in one persistent launch under a CUDA graph, 15 LM iterations each: the
+    mixed form with the autotuned shape, the FP64 form in the same launch
+    shape, and the plain FP64 single-problem solver one problem at a time on
+    a sample of the same problems."""
+    from psba_gb300 import batch as B
+    from psba_gb300 import scenes
+    probs = scenes.batch_scenes(args.batch, seed=1000)
+    iters = 15
+    mo = P.default_opts(allow_switch=0, max_iter=iters, precision=P.PREC_MIXED)
+    fo = P.default_opts(allow_switch=0, max_iter=iters)
+    with B.Batch(probs) as b:
+        choice, table = B.autotune(b, P.PREC_MIXED, iters=1, repeats=1)
+        b.reset()
+        b.levmar(mo)
+        m_ms = []
+        for _ in range(args.batch_steps):
+            b.reset()
+            res_m, ms = b.levmar(mo)
+            m_ms.append(ms)
+        b.reset()
+        b.levmar(fo)
+        f_ms = []
+        for _ in range(args.batch_steps):
+            b.reset()
+            res_f, ms = b.levmar(fo)
+            f_ms.append(ms)
+        dev_bytes = b.device_bytes()
+    # the plain FP64 form, problem by problem (create outside the timing)
+    sample = probs[: args.pbp_sample]
+    pbp_ms, pbp_cost = [], []
+    for sc in sample:
+        with P.Solver(sc) as s:
+            r = s.levmar(fo, fetch=False, trace_cap=0)
+        pbp_ms.append(r.device_ms)
+        pbp_cost.append(r.final_cost)
+    rel = np.abs(res_m["final_cost"] - res_f["final_cost"]) / res_f["final_cost"]
+    pbp_rel = np.abs(res_f["final_cost"][: len(sample)] - np.array(pbp_cost)) / np.array(pbp_cost)
+    m_sps = args.batch / (min(m_ms) / 1e3)
+    f_sps = args.batch / (min(f_ms) / 1e3)
+    pbp_sps = len(sample) / (sum(pbp_ms) / 1e3)
+    return {
+        "workload": "%d problems, 5-30 cameras, 200-3,000 points, 3-8 views per point, %d LM iterations each, "
+                    "one persistent launch under a CUDA graph" % (args.batch, iters),
+        "observations": int(sum(sc.n_obs for sc in probs)), "device_bytes": int(dev_bytes),
+        "mixed_solves_per_s": m_sps, "mixed_ms": min(m_ms),
+        "fp64_batched_solves_per_s": f_sps, "fp64_batched_ms": min(f_ms),
+        "fp64_problem_by_problem_solves_per_s": pbp_sps,
+        "fp64_problem_by_problem_sample": len(sample),
+        "speedup_mixed_batched_vs_fp64_problem_by_problem": m_sps / pbp_sps,
+        "mixed_final_cost_rel_vs_fp64": {"max": float(rel.max()), "median": float(np.median(rel)),
+                                          "frac_within_1e-6": float((rel <= 1e-6).mean())},
+        "fp64_batched_vs_single_max_rel": float(pbp_rel.max()),
+        "autotune": choice, "autotune_candidates": len(table),
+    }
+
+
+def serving_leg(P, args):
+    """Poisson arrivals of requests (cameras log-uniform 5-138, points
+    500-60,000, 4-6 views, 6-parameter cameras) into the serving engine
+    (mixed form, 15 LM iterations, 120 GB HBM budget); p50/p99 latency from
+    submission to result on the host clock."""
+    from psba_gb300 import scenes
+    from psba_gb300 import serve as S
+    rates = [float(x) for x in args.serve_rates.split(",") if x.strip()]
+    pool = scenes.serving_scenes(args.serve_pool, seed=2000)
+    iters = 15
+    out = {"workload": "Poisson arrivals; %d distinct request scenes cycled: cameras log-U[5,138], points "
+                       "log-U[500,60000], 4-6 views/point, 6-param cameras, mixed form, %d LM iterations, "
+                       "120 GB HBM budget" % (len(pool), iters),
+           "mean_observations": float(np.mean([sc.n_obs for sc in pool])), "rates": []}
+    with S.Server(precision=P.PREC_MIXED, max_iter=iters, hbm_budget_bytes=120e9) as srv:
+        S.run_poisson(srv, pool[:4], rate=1000.0, n_requests=4, seed=1)
+        first = {}
+        for rate in rates:
+            n = int(min(max(rate * args.serve_seconds, 20), args.serve_max))
+            got, wall = S.run_poisson(srv, pool, rate, n, seed=int(rate))
+            lat = np.array([r.latency_ms for r in got])
+            qd = np.array([r.queued_ms for r in got])
+            for q, r in enumerate(got):
+                first.setdefault(q % len(pool), r.final_cost)
+            out["rates"].append({"rate_req_s": rate, "requests": n, "solves_per_s": n / wall,
+                                 "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                                 "queued_p50_ms": float(np.percentile(qd, 50)),
+                                 "queued_p99_ms": float(np.percentile(qd, 99))})
+        st = srv.stats()
+    out["launches"] = st["launches"]
+    out["peak_bytes"] = st["peak_bytes"]
+    # final cost against the plain FP64 single-problem solver on the same scenes
+    rel = []
+    fo = P.default_opts(allow_switch=0, max_iter=iters)
+    for q, c in sorted(first.items()):
+        with P.Solver(pool[q]) as s:
+            r = s.levmar(fo, fetch=False, trace_cap=0)
+        rel.append(abs(c - r.final_cost) / r.final_cost)
+    rel = np.array(rel)
+    out["final_cost_rel_vs_fp64"] = {"max": float(rel.max()), "median": float(np.median(rel)),
+                                     "frac_within_1e-6": float((rel <= 1e-6).mean())}
+    return out
 
 
 def main():
@@ -350,6 +460,10 @@ def main():
             "cost_after_sample": r.final_cost, "gpu_cost_after_sample": g.final_cost,
             "cost_rel_diff": abs(g.final_cost - r.final_cost) / r.final_cost,
         }
+    if rank == 0 and args.batch > 0:
+        line["batched"] = batched_leg(P, args)
+    if rank == 0 and args.serve_rates.strip() not in ("", "none"):
+        line["serving"] = serving_leg(P, args)
     if rank == 0:
         print(json.dumps(line))
     if dist:

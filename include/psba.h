@@ -214,6 +214,101 @@ long long psba_kernel_launches(void);
 /* FMA throughput of the current device in TFLOP/s: which = 0 FP64, 1 FP32. */
 int psba_measure_peak(int which, double *tflops);
 
+/* ---- batches of independent problems ------------------------------------ */
+
+/* Many independent small problems solved in one persistent launch (a CUDA
+ * graph of [queue reset, kernel]): each CTA takes a problem from a device
+ * queue and runs levmar() (PSBA/levmar.cpp:45-256) for it with every stage
+ * done by the CTA.  A problem's result does not depend on the batch it is in.
+ * The reference solves one problem per process; it has no counterpart. */
+typedef struct psba_batch psba_batch;
+typedef struct {
+    int status;      /* PSBA_ITER_* */
+    int iterations;
+    int n_trials;
+    int n_linearizations;
+    double initial_cost;
+    double final_cost;
+} psba_batch_result;
+
+int psba_batch_create(const psba_problem_desc *problems, int n_problems, psba_batch **out);
+int psba_batch_destroy(psba_batch *b);
+/* Runs LM on every problem (opts->precision selects the form); results has
+ * n_problems entries; *device_ms = GPU time of the launch. */
+int psba_batch_levmar(psba_batch *b, const psba_opts *opts, psba_batch_result *results, double *device_ms);
+int psba_batch_get_params(psba_batch *b, int problem, double *cams, double *pts);
+int psba_batch_reset_params(psba_batch *b);
+/* Tile/segment shape knobs set by the autotuner (psba_gb300.batch.autotune):
+ * threads per CTA (128, 256, 512) and, per problem, lanes per camera pair in
+ * the Schur stage (8, 16, 32). */
+int psba_batch_set_threads(psba_batch *b, int threads);
+int psba_batch_set_lanes_per_pair(psba_batch *b, const int *lanes);
+size_t psba_batch_device_bytes(psba_batch *b);
+
+/* ---- serving: continuous batching of solve requests -------------------- */
+
+/* A server owns one HBM pool of hbm_budget_bytes and a worker thread.
+ * psba_batch_submit lays a request out on the calling thread and queues it;
+ * the worker admits queued requests in arrival order while a resident slot is
+ * free and the request fits the pool, and advances all resident problems
+ * together, a time slice of LM iterations per persistent launch (the
+ * heaviest problem runs slice_iters iterations, lighter ones proportionally
+ * more).  Parameters, linearisation and LM state stay on the device between
+ * slices; a request arriving while others run joins the next launch, and a
+ * finished one leaves at the end of its launch and frees its memory.  A
+ * request's result is bit-identical alone and in any mix.
+ *
+ * Reference: none -- the reference solves one problem per process
+ * (PSBA/main.cpp:193-208); each request is solved by levmar()
+ * (PSBA/levmar.cpp:45-256) with the LM-to-TR hand-over off. */
+typedef struct psba_server psba_server;
+
+typedef struct psba_server_opts {
+    double hbm_budget_bytes; /* pool for resident problems (default 120e9) */
+    int max_active;          /* resident problems at once (default 1024) */
+    int slice_iters;         /* outer LM iterations of the heaviest problem per launch (default 1) */
+    int threads;             /* CTA size of the persistent launch: 128, 256, 512 (default 256) */
+    int lanes_per_pair;      /* lanes per camera pair in the Schur stage: 8, 16, 32 (default 32) */
+    int reserved[4];
+} psba_server_opts;
+
+typedef struct psba_request_result {
+    int status; /* PSBA_ITER_* */
+    int iterations;
+    int n_trials;
+    int n_linearizations;
+    double initial_cost;
+    double final_cost;
+    double queued_ms;    /* submit to admission (host clock) */
+    double latency_ms;   /* submit to result ready (host clock) */
+    double device_bytes; /* pool bytes held while resident */
+} psba_request_result;
+
+typedef struct psba_server_stats {
+    long long submitted, admitted, finished, launches;
+    int active, queued;
+    double bytes_in_use, peak_bytes;
+    double busy_ms; /* GPU time of all slice launches */
+} psba_server_stats;
+
+#define PSBA_PENDING 1 /* psba_batch_poll: not finished yet */
+
+void psba_server_default_opts(psba_server_opts *o);
+/* lm: tau, thresholds, max_iter and precision for every request. */
+int psba_server_create(const psba_server_opts *so, const psba_opts *lm, psba_server **out);
+/* Never waits for the GPU.  PSBA_ERR_NOMEM if the problem alone exceeds the
+ * budget, PSBA_ERR_ARG if it is malformed. */
+int psba_batch_submit(psba_server *s, const psba_problem_desc *desc, long long *ticket);
+/* PSBA_OK: finished; *res, and cams (6 per camera) / pts (3 per point) when
+ * not NULL, are written and the ticket is released.  PSBA_PENDING: not
+ * finished within timeout_ms (0: return at once).  PSBA_ERR_ARG: unknown
+ * ticket.  PSBA_ERR_CUDA: the server stopped on a device error. */
+int psba_batch_poll(psba_server *s, long long ticket, int timeout_ms, psba_request_result *res, double *cams,
+                    double *pts);
+int psba_server_stats_get(psba_server *s, psba_server_stats *st);
+/* Stops after the launch in flight; unfinished requests are dropped. */
+int psba_server_destroy(psba_server *s);
+
 /* ---- cost evaluation without device allocation ------------------------ */
 
 /* Sum of squared reprojection residuals (what psba_eval_residual returns in

@@ -21,7 +21,7 @@ _ip = C.POINTER(C.c_int)
 
 class Problem(C.Structure):
     _fields_ = [("nc", C.c_int), ("np", C.c_int), ("no", C.c_int), ("K", _dp), ("q0", _dp),
-                ("meas", _dp), ("obs_pt", _ip), ("obs_cam", _ip)]
+                ("meas", _dp), ("obs_pt", _ip), ("obs_cam", _ip), ("cnp", C.c_int)]
 
 
 class Opts(C.Structure):
@@ -110,8 +110,9 @@ class OracleProblem:
         self.obs_pt = np.ascontiguousarray(scene.obs_pt, dtype=np.int32)
         self.obs_cam = np.ascontiguousarray(scene.obs_cam, dtype=np.int32)
         self.nc, self.np_, self.no = scene.n_cams, scene.n_pts, scene.n_obs
+        self.cnp = int(getattr(scene, "cnp", 6))
         self.c = Problem(self.nc, self.np_, self.no, _d(self.K), _d(self.q0), _d(self.meas),
-                         _i(self.obs_pt), _i(self.obs_cam))
+                         _i(self.obs_pt), _i(self.obs_cam), self.cnp)
 
     @property
     def ref(self):
@@ -140,18 +141,19 @@ def sumsq(x):
 
 
 def jacobian(pr, cams, pts):
-    JA = np.empty((pr.no, 2, 6))
+    JA = np.empty((pr.no, 2, pr.cnp))
     JB = np.empty((pr.no, 2, 3))
     lib().orc_jacobian(pr.ref, _d(_f64(cams)), _d(_f64(pts)), _d(JA), _d(JB))
     return JA, JB
 
 
 def normal_blocks(pr, JA, JB, ex, coeff=1.0):
-    U = np.empty((pr.nc, 6, 6))
+    c = pr.cnp
+    U = np.empty((pr.nc, c, c))
     V = np.empty((pr.np_, 3, 3))
-    W = np.empty((pr.no, 6, 3))
-    g = np.empty(6 * pr.nc + 3 * pr.np_)
-    d = np.empty(6 * pr.nc + 3 * pr.np_)
+    W = np.empty((pr.no, c, 3))
+    g = np.empty(c * pr.nc + 3 * pr.np_)
+    d = np.empty(c * pr.nc + 3 * pr.np_)
     lib().orc_normal_blocks(pr.ref, _d(_f64(JA)), _d(_f64(JB)), _d(_f64(ex)), float(coeff), _d(U),
                             _d(V), _d(W), _d(g), _d(d))
     return U, V, W, g, d
@@ -165,20 +167,20 @@ def vinv(V, mu):
 
 
 def yblocks(pr, W, Vinv):
-    Y = np.empty((pr.no, 6, 3))
+    Y = np.empty((pr.no, pr.cnp, 3))
     lib().orc_yblocks(pr.ref, _d(_f64(W)), _d(_f64(Vinv)), _d(Y))
     return Y
 
 
 def schur(pr, U, mu, Y, W):
-    N = 6 * pr.nc
+    N = pr.cnp * pr.nc
     S = np.zeros((N, N))
     lib().orc_schur(pr.ref, _d(_f64(U)), float(mu), _d(_f64(Y)), _d(_f64(W)), _d(S))
     return np.tril(S)
 
 
 def ea(pr, Y, g):
-    out = np.empty(6 * pr.nc)
+    out = np.empty(pr.cnp * pr.nc)
     lib().orc_ea(pr.ref, _d(_f64(Y)), _d(_f64(g)), _d(out))
     return out
 

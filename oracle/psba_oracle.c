@@ -158,6 +158,44 @@ static void quat_rotate_t(const double q[4], const double X[3], const double *t,
     out[2] = -m0 * c + s * m3 - b * m1 + a * m2 + t[2];
 }
 
+static int cnp_of(const orc_problem *p) { return p->cnp > 0 ? p->cnp : CNP; }
+
+/* Variable intrinsics (cnp 11 / 16; no reference counterpart).  Camera j's
+ * parameters: v (3), t (3), K = fx, cx, cy, ar, skew (5), and for cnp 16
+ * distortion kc = k1, k2, p1, p2, k3 (5).  With x = Xc/Zc, y = Yc/Zc,
+ * r2 = x^2 + y^2:
+ *   radial = 1 + k1 r2 + k2 r2^2 + k3 r2^3,
+ *   xd = radial x + 2 p1 x y + p2 (r2 + 2 x^2),
+ *   yd = radial y + p1 (r2 + 2 y^2) + 2 p2 x y,
+ *   u = fx xd + skew yd + cx,   v = fx ar yd + cy.
+ * Without distortion (cnp 11) the projection is evaluated exactly as for
+ * fixed K: u = (fx Xc + skew Yc + cx Zc) / Zc, v = (fx ar Yc + cy Zc) / Zc. */
+static void distort(const double *kc, double x, double y, double *xd, double *yd)
+{
+    double r2 = x * x + y * y;
+    double radial = 1.0 + r2 * (kc[0] + r2 * (kc[1] + r2 * kc[4]));
+    *xd = radial * x + 2.0 * kc[2] * x * y + kc[3] * (r2 + 2.0 * x * x);
+    *yd = radial * y + kc[2] * (r2 + 2.0 * y * y) + 2.0 * kc[3] * x * y;
+}
+
+static void project_v(const double *q0, const double *cam, int cnp, const double *X, double *xy)
+{
+    double q[4], Xc[3];
+    compose_quat(q0, cam, q);
+    quat_rotate_t(q, X, cam + 3, Xc);
+    const double *K = cam + 6;
+    double iz = 1 / Xc[2];
+    if (cnp == 11) {
+        xy[0] = (K[0] * Xc[0] + K[4] * Xc[1] + K[1] * Xc[2]) * iz;
+        xy[1] = (K[0] * K[3] * Xc[1] + K[2] * Xc[2]) * iz;
+        return;
+    }
+    double xd, yd;
+    distort(cam + 11, Xc[0] * iz, Xc[1] * iz, &xd, &yd);
+    xy[0] = K[0] * xd + K[4] * yd + K[1];
+    xy[1] = K[0] * K[3] * yd + K[2];
+}
+
 static void project(const double *K, const double q[4], const double *t, const double *X,
                     double *xy, double Xc[3])
 {
@@ -169,12 +207,17 @@ static void project(const double *K, const double q[4], const double *t, const d
 
 void orc_residual(const orc_problem *p, const double *cams, const double *pts, double *ex)
 {
+    const int cnp = cnp_of(p);
 #pragma omp parallel for schedule(static)
     for (int o = 0; o < p->no; ++o) {
         int i = p->obs_pt[o], j = p->obs_cam[o];
         double q[4], xy[2], Xc[3];
-        compose_quat(p->q0 + 4 * j, cams + CNP * j, q);
-        project(p->K + 5 * j, q, cams + CNP * j + 3, pts + PNP * i, xy, Xc);
+        if (cnp > 6) {
+            project_v(p->q0 + 4 * j, cams + (size_t)cnp * j, cnp, pts + PNP * i, xy);
+        } else {
+            compose_quat(p->q0 + 4 * j, cams + CNP * j, q);
+            project(p->K + 5 * j, q, cams + CNP * j + 3, pts + PNP * i, xy, Xc);
+        }
         ex[2 * o] = p->meas[2 * o] - xy[0];
         ex[2 * o + 1] = p->meas[2 * o + 1] - xy[1];
     }
@@ -274,13 +317,119 @@ static void jac_one(const double *K, const double *q0, const double *cam, const 
     }
 }
 
+/* Jacobian of the variable-intrinsics model, 2 x cnp (camera) and 2 x 3
+ * (point).  With P = d(u,v)/d(xd,yd) = [[fx, skew], [0, fx ar]],
+ * Dd = d(xd,yd)/d(x,y) (identity without distortion) and
+ * N = d(x,y)/dXc = [[1/Zc, 0, -x/Zc], [0, 1/Zc, -y/Zc]], the chain
+ * H = P Dd N replaces d(x,y)/dXc of jac_one; the pose and point columns are
+ * then H dXc/dv_l, H, H dXc/dX as there.  Intrinsics columns:
+ * du/dfx = xd, dv/dfx = ar yd; du/dcx = 1; dv/dcy = 1; dv/dar = fx yd;
+ * du/dskew = yd.  Distortion columns: P d(xd,yd)/dkc.                       */
+static void jac_one_v(const double *q0, const double *cam, int cnp, const double *X, double *A, double *B)
+{
+    const double *vl = cam, *K = cam + 6;
+    double q[4], Xc[3];
+    compose_quat(q0, vl, q);
+    quat_rotate_t(q, X, cam + 3, Xc);
+    double iz = 1.0 / Xc[2], x = Xc[0] * iz, y = Xc[1] * iz;
+    double fx = K[0], sk = K[4], ar = K[3], fy = K[0] * K[3];
+    double Dd[2][2] = {{1.0, 0.0}, {0.0, 1.0}}, xd = x, yd = y, r2 = x * x + y * y;
+    const double *kc = cam + 11;
+    if (cnp == 16) {
+        distort(kc, x, y, &xd, &yd);
+        double radial = 1.0 + r2 * (kc[0] + r2 * (kc[1] + r2 * kc[4]));
+        double dr = kc[0] + r2 * (2.0 * kc[1] + 3.0 * kc[4] * r2); /* d radial / d r2 */
+        Dd[0][0] = radial + 2.0 * x * x * dr + 2.0 * kc[2] * y + 6.0 * kc[3] * x;
+        Dd[0][1] = 2.0 * x * y * dr + 2.0 * kc[2] * x + 2.0 * kc[3] * y;
+        Dd[1][0] = 2.0 * x * y * dr + 2.0 * kc[2] * x + 2.0 * kc[3] * y;
+        Dd[1][1] = radial + 2.0 * y * y * dr + 6.0 * kc[2] * y + 2.0 * kc[3] * x;
+    }
+    double PD[2][2] = {{fx * Dd[0][0] + sk * Dd[1][0], fx * Dd[0][1] + sk * Dd[1][1]},
+                       {fy * Dd[1][0], fy * Dd[1][1]}};
+    double H[2][3];
+    for (int r = 0; r < 2; ++r) {
+        H[r][0] = PD[r][0] * iz;
+        H[r][1] = PD[r][1] * iz;
+        H[r][2] = -(PD[r][0] * x + PD[r][1] * y) * iz;
+    }
+    /* dXc/dv_l and dXc/dX as in jac_one */
+    double s = q[0], v[3] = {q[1], q[2], q[3]};
+    double vX = v[0] * X[0] + v[1] * X[1] + v[2] * X[2];
+    double vv = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    double vxX[3] = {v[1] * X[2] - v[2] * X[1], v[2] * X[0] - v[0] * X[2], v[0] * X[1] - v[1] * X[0]};
+    double F[3][4];
+    for (int r = 0; r < 3; ++r) F[r][0] = 2.0 * s * X[r] + 2.0 * vxX[r];
+    for (int m = 0; m < 3; ++m) {
+        double em_x_X[3] = {0, 0, 0};
+        if (m == 0) { em_x_X[1] = -X[2]; em_x_X[2] = X[1]; }
+        if (m == 1) { em_x_X[0] = X[2]; em_x_X[2] = -X[0]; }
+        if (m == 2) { em_x_X[0] = -X[1]; em_x_X[1] = X[0]; }
+        for (int r = 0; r < 3; ++r)
+            F[r][m + 1] = -2.0 * v[m] * X[r] + 2.0 * X[m] * v[r] + (r == m ? 2.0 * vX : 0.0) +
+                          2.0 * s * em_x_X[r];
+    }
+    double sl = sqrt(1.0 - vl[0] * vl[0] - vl[1] * vl[1] - vl[2] * vl[2]);
+    double s0 = q0[0], a[3] = {q0[1], q0[2], q0[3]};
+    double D[4][3];
+    for (int m = 0; m < 3; ++m) {
+        double ds = -vl[m] / sl;
+        double em_x_a[3] = {0, 0, 0};
+        if (m == 0) { em_x_a[1] = -a[2]; em_x_a[2] = a[1]; }
+        if (m == 1) { em_x_a[0] = a[2]; em_x_a[2] = -a[0]; }
+        if (m == 2) { em_x_a[0] = -a[1]; em_x_a[1] = a[0]; }
+        D[0][m] = s0 * ds - a[m];
+        for (int r = 0; r < 3; ++r) D[r + 1][m] = a[r] * ds + (r == m ? s0 : 0.0) + em_x_a[r];
+    }
+    double G[3][3];
+    for (int r = 0; r < 3; ++r)
+        for (int m = 0; m < 3; ++m)
+            G[r][m] = F[r][0] * D[0][m] + F[r][1] * D[1][m] + F[r][2] * D[2][m] + F[r][3] * D[3][m];
+    double R[3][3];
+    double d = s * s - vv;
+    R[0][0] = d + 2 * v[0] * v[0];
+    R[0][1] = 2 * v[0] * v[1] - 2 * s * v[2];
+    R[0][2] = 2 * v[0] * v[2] + 2 * s * v[1];
+    R[1][0] = 2 * v[1] * v[0] + 2 * s * v[2];
+    R[1][1] = d + 2 * v[1] * v[1];
+    R[1][2] = 2 * v[1] * v[2] - 2 * s * v[0];
+    R[2][0] = 2 * v[2] * v[0] - 2 * s * v[1];
+    R[2][1] = 2 * v[2] * v[1] + 2 * s * v[0];
+    R[2][2] = d + 2 * v[2] * v[2];
+    for (int r = 0; r < 2; ++r)
+        for (int m = 0; m < 3; ++m) {
+            A[r * cnp + m] = H[r][0] * G[0][m] + H[r][1] * G[1][m] + H[r][2] * G[2][m];
+            A[r * cnp + 3 + m] = H[r][m];
+            B[r * 3 + m] = H[r][0] * R[0][m] + H[r][1] * R[1][m] + H[r][2] * R[2][m];
+        }
+    /* intrinsics fx, cx, cy, ar, skew */
+    A[6] = xd;       A[cnp + 6] = ar * yd;
+    A[7] = 1.0;      A[cnp + 7] = 0.0;
+    A[8] = 0.0;      A[cnp + 8] = 1.0;
+    A[9] = 0.0;      A[cnp + 9] = fx * yd;
+    A[10] = yd;      A[cnp + 10] = 0.0;
+    if (cnp == 16) {
+        double r4 = r2 * r2, r6 = r4 * r2;
+        double dxd[5] = {x * r2, x * r4, 2.0 * x * y, r2 + 2.0 * x * x, x * r6};
+        double dyd[5] = {y * r2, y * r4, r2 + 2.0 * y * y, 2.0 * x * y, y * r6};
+        for (int k = 0; k < 5; ++k) {
+            A[11 + k] = fx * dxd[k] + sk * dyd[k];
+            A[cnp + 11 + k] = fy * dyd[k];
+        }
+    }
+}
+
 void orc_jacobian(const orc_problem *p, const double *cams, const double *pts, double *JA, double *JB)
 {
+    const int cnp = cnp_of(p);
 #pragma omp parallel for schedule(static)
     for (int o = 0; o < p->no; ++o) {
         int i = p->obs_pt[o], j = p->obs_cam[o];
-        jac_one(p->K + 5 * j, p->q0 + 4 * j, cams + CNP * j, pts + PNP * i, JA + 12 * (size_t)o,
-                JB + 6 * (size_t)o);
+        if (cnp > 6)
+            jac_one_v(p->q0 + 4 * j, cams + (size_t)cnp * j, cnp, pts + PNP * i, JA + 2 * (size_t)cnp * o,
+                      JB + 6 * (size_t)o);
+        else
+            jac_one(p->K + 5 * j, p->q0 + 4 * j, cams + CNP * j, pts + PNP * i, JA + 12 * (size_t)o,
+                    JB + 6 * (size_t)o);
     }
 }
 
@@ -292,27 +441,28 @@ static void normal_blocks_ix(const orc_problem *p, const orc_index *ix, const do
                              double *W, double *g, double *UVdiag)
 {
     int nc = p->nc, np = p->np;
+    const int cnp = cnp_of(p);
 #pragma omp parallel for schedule(dynamic, 1)
     for (int j = 0; j < nc; ++j) {
-        for (int r = 0; r < CNP; ++r)
-            for (int c = 0; c < CNP; ++c) {
+        for (int r = 0; r < cnp; ++r)
+            for (int c = 0; c < cnp; ++c) {
                 double sum = 0;
                 for (int e = ix->cam_start[j]; e < ix->cam_start[j + 1]; ++e) {
-                    const double *A = JA + 12 * (size_t)ix->cam_obs[e];
-                    sum = sum + A[r] * A[c] + A[CNP + r] * A[CNP + c];
+                    const double *A = JA + 2 * (size_t)cnp * ix->cam_obs[e];
+                    sum = sum + A[r] * A[c] + A[cnp + r] * A[cnp + c];
                 }
                 sum = coeff * sum;
-                U[(size_t)j * 36 + r * 6 + c] = sum;
-                if (r == c) UVdiag[j * CNP + r] = sum;
+                U[(size_t)j * cnp * cnp + r * cnp + c] = sum;
+                if (r == c) UVdiag[j * cnp + r] = sum;
             }
-        for (int k = 0; k < CNP; ++k) {
+        for (int k = 0; k < cnp; ++k) {
             double sum = 0;
             for (int e = ix->cam_start[j]; e < ix->cam_start[j + 1]; ++e) {
                 int o = ix->cam_obs[e];
-                const double *A = JA + 12 * (size_t)o;
-                sum = sum + A[k] * ex[2 * (size_t)o] + A[k + CNP] * ex[2 * (size_t)o + 1];
+                const double *A = JA + 2 * (size_t)cnp * o;
+                sum = sum + A[k] * ex[2 * (size_t)o] + A[k + cnp] * ex[2 * (size_t)o + 1];
             }
-            g[j * CNP + k] = coeff * sum;
+            g[j * cnp + k] = coeff * sum;
         }
     }
 #pragma omp parallel for schedule(static)
@@ -326,7 +476,7 @@ static void normal_blocks_ix(const orc_problem *p, const orc_index *ix, const do
                 }
                 sum = coeff * sum;
                 V[(size_t)i * 9 + r * 3 + c] = sum;
-                if (r == c) UVdiag[(size_t)nc * CNP + i * PNP + r] = sum;
+                if (r == c) UVdiag[(size_t)nc * cnp + i * PNP + r] = sum;
             }
         for (int k = 0; k < PNP; ++k) {
             double sum = 0;
@@ -334,16 +484,16 @@ static void normal_blocks_ix(const orc_problem *p, const orc_index *ix, const do
                 const double *B = JB + 6 * (size_t)o;
                 sum = sum + B[k] * ex[2 * (size_t)o] + B[k + PNP] * ex[2 * (size_t)o + 1];
             }
-            g[(size_t)nc * CNP + i * PNP + k] = coeff * sum;
+            g[(size_t)nc * cnp + i * PNP + k] = coeff * sum;
         }
     }
 #pragma omp parallel for schedule(static)
     for (int o = 0; o < p->no; ++o) {
-        const double *A = JA + 12 * (size_t)o, *B = JB + 6 * (size_t)o;
-        for (int r = 0; r < CNP; ++r)
+        const double *A = JA + 2 * (size_t)cnp * o, *B = JB + 6 * (size_t)o;
+        for (int r = 0; r < cnp; ++r)
             for (int c = 0; c < PNP; ++c) {
-                double sum = A[r] * B[c] + A[CNP + r] * B[PNP + c];
-                W[(size_t)o * 18 + r * 3 + c] = coeff * sum;
+                double sum = A[r] * B[c] + A[cnp + r] * B[PNP + c];
+                W[(size_t)o * 3 * cnp + r * 3 + c] = coeff * sum;
             }
     }
 }
@@ -421,11 +571,12 @@ void orc_vinv(int np, const double *V, double mu, double *Vinv)
 /* a12: Y_ij = W_ij V_i^-1, compute_Yblks.cl:26-37 */
 void orc_yblocks(const orc_problem *p, const double *W, const double *Vinv, double *Y)
 {
+    const int cnp = cnp_of(p);
 #pragma omp parallel for schedule(static)
     for (int o = 0; o < p->no; ++o) {
-        const double *Wo = W + 18 * (size_t)o, *Vi = Vinv + 9 * (size_t)p->obs_pt[o];
-        double *Yo = Y + 18 * (size_t)o;
-        for (int r = 0; r < CNP; ++r)
+        const double *Wo = W + 3 * (size_t)cnp * o, *Vi = Vinv + 9 * (size_t)p->obs_pt[o];
+        double *Yo = Y + 3 * (size_t)cnp * o;
+        for (int r = 0; r < cnp; ++r)
             for (int c = 0; c < PNP; ++c)
                 Yo[r * 3 + c] = Wo[r * 3] * Vi[0 * 3 + c] + Wo[r * 3 + 1] * Vi[1 * 3 + c] +
                                 Wo[r * 3 + 2] * Vi[2 * 3 + c];
@@ -439,7 +590,8 @@ static void schur_ix(const orc_problem *p, const orc_index *ix, const double *U,
                      const double *Y, const double *W, double *S)
 {
     int nc = p->nc;
-    size_t N = (size_t)nc * CNP;
+    const int cnp = cnp_of(p);
+    size_t N = (size_t)nc * cnp;
     long long npair = (long long)nc * (nc + 1) / 2;
 #pragma omp parallel for schedule(dynamic, 4)
     for (long long s = 0; s < npair; ++s) {
@@ -448,21 +600,21 @@ static void schur_ix(const orc_problem *p, const orc_index *ix, const double *U,
         while ((long long)(k + 1) * (k + 2) / 2 <= s) ++k;
         int l = (int)(s - (long long)k * (k + 1) / 2);
         long long b = ix->pair_start[s], e = ix->pair_start[s + 1];
-        for (int r = 0; r < CNP; ++r)
-            for (int c = 0; c < CNP; ++c) {
+        for (int r = 0; r < cnp; ++r)
+            for (int c = 0; c < cnp; ++c) {
                 if (k == l && c > r) continue;
                 double sum = 0;
                 for (long long t = b; t < e; ++t) {
-                    const double *y = Y + 18 * (size_t)ix->pair_a[t] + r * 3;
-                    const double *w = W + 18 * (size_t)ix->pair_b[t] + c * 3;
+                    const double *y = Y + 3 * (size_t)cnp * ix->pair_a[t] + r * 3;
+                    const double *w = W + 3 * (size_t)cnp * ix->pair_b[t] + c * 3;
                     sum += (y[0] * w[0] + y[1] * w[1] + y[2] * w[2]);
                 }
                 double val;
                 if (k == l)
-                    val = (r == c ? U[(size_t)k * 36 + r * 6 + c] + mu : U[(size_t)k * 36 + r * 6 + c]) - sum;
+                    val = (r == c ? U[(size_t)k * cnp * cnp + r * cnp + c] + mu : U[(size_t)k * cnp * cnp + r * cnp + c]) - sum;
                 else
                     val = -sum;
-                S[((size_t)k * CNP + r) * N + (size_t)l * CNP + c] = val;
+                S[((size_t)k * cnp + r) * N + (size_t)l * cnp + c] = val;
             }
     }
 }
@@ -481,17 +633,18 @@ static void ea_ix(const orc_problem *p, const orc_index *ix, const double *Y, co
                   double *ea)
 {
     int nc = p->nc;
-    const double *gb = g + (size_t)nc * CNP;
+    const int cnp = cnp_of(p);
+    const double *gb = g + (size_t)nc * cnp;
     for (int j = 0; j < nc; ++j)
-        for (int r = 0; r < CNP; ++r) {
+        for (int r = 0; r < cnp; ++r) {
             double sum = 0;
             for (int e = ix->cam_start[j]; e < ix->cam_start[j + 1]; ++e) {
                 int o = ix->cam_obs[e];
-                const double *y = Y + 18 * (size_t)o + r * 3;
+                const double *y = Y + 3 * (size_t)cnp * o + r * 3;
                 const double *b = gb + 3 * (size_t)p->obs_pt[o];
                 sum = sum + y[0] * b[0] + y[1] * b[1] + y[2] * b[2];
             }
-            ea[j * CNP + r] = g[j * CNP + r] - sum;
+            ea[j * cnp + r] = g[j * cnp + r] - sum;
         }
 }
 
@@ -595,8 +748,28 @@ static int blk_cholesky(int n, double *S, double *dinv)
     return 0;
 }
 
+/* Plain column Cholesky of the lower triangle (used where n % 3 != 0). */
+static int col_cholesky(int n, double *S)
+{
+    for (int j = 0; j < n; ++j) {
+        double d = S[(size_t)j * n + j];
+        for (int k = 0; k < j; ++k) d -= S[(size_t)j * n + k] * S[(size_t)j * n + k];
+        if (!(d > 0) || !isfinite(d)) return 1;
+        double l = sqrt(d);
+        S[(size_t)j * n + j] = l;
+        for (int i = j + 1; i < n; ++i) {
+            double s = S[(size_t)i * n + j];
+            for (int k = 0; k < j; ++k) s -= S[(size_t)i * n + k] * S[(size_t)j * n + k];
+            S[(size_t)i * n + j] = s / l;
+            S[(size_t)j * n + i] = 0.0;
+        }
+    }
+    return 0;
+}
+
 int orc_cholesky(int n, double *S)
 {
+    if (n % 3 != 0) return col_cholesky(n, S);
     double *dinv = (double *)malloc(sizeof(double) * 3 * (size_t)n);
     int r = blk_cholesky(n, S, dinv);
     free(dinv);
@@ -690,6 +863,7 @@ static void eb_dpb_ix(const orc_problem *p, const orc_index *ix, const double *W
                       const double *Vinv, const double *g, const double *dpa, double *eb, double *dpb)
 {
     int nc = p->nc;
+    const int cnp = cnp_of(p);
     (void)ix;
 #pragma omp parallel for schedule(static)
     for (int i = 0; i < p->np; ++i) {
@@ -697,11 +871,11 @@ static void eb_dpb_ix(const orc_problem *p, const orc_index *ix, const double *W
         for (int c = 0; c < PNP; ++c) {
             double sum = 0;
             for (int o = ix->pt_start[i]; o < ix->pt_start[i + 1]; ++o) {
-                const double *Wo = W + 18 * (size_t)o;
-                const double *d = dpa + CNP * (size_t)p->obs_cam[o];
-                for (int k = 0; k < CNP; ++k) sum = sum + Wo[k * 3 + c] * d[k];
+                const double *Wo = W + 3 * (size_t)cnp * o;
+                const double *d = dpa + cnp * (size_t)p->obs_cam[o];
+                for (int k = 0; k < cnp; ++k) sum = sum + Wo[k * 3 + c] * d[k];
             }
-            e3[c] = g[(size_t)nc * CNP + i * PNP + c] - sum;
+            e3[c] = g[(size_t)nc * cnp + i * PNP + c] - sum;
             eb[i * PNP + c] = e3[c];
         }
         const double *Vi = Vinv + 9 * (size_t)i;
@@ -725,14 +899,15 @@ void orc_eb_dpb(const orc_problem *p, const double *W, const double *Vinv, const
 void orc_jmultiply(const orc_problem *p, const double *JA, const double *JB, const double *x,
                    double *out)
 {
-    size_t ncp = (size_t)p->nc * CNP;
+    const int cnp = cnp_of(p);
+    size_t ncp = (size_t)p->nc * cnp;
 #pragma omp parallel for schedule(static)
     for (int o = 0; o < p->no; ++o) {
         int i = p->obs_pt[o], j = p->obs_cam[o];
         for (int k = 0; k < MNP; ++k) {
-            const double *a = JA + 12 * (size_t)o + k * CNP;
+            const double *a = JA + 2 * (size_t)cnp * o + k * cnp;
             const double *b = JB + 6 * (size_t)o + k * PNP;
-            const double *xa = x + (size_t)j * CNP;
+            const double *xa = x + (size_t)j * cnp;
             const double *xb = x + ncp + (size_t)i * PNP;
             double sum = 0;
             sum += a[0] * xa[0];
@@ -898,7 +1073,7 @@ void orc_cholmod(int n, double *S, double *E)
 typedef struct {
     const orc_problem *p;
     orc_index ix;
-    int nc, np, no, ncp, ntot;
+    int nc, np, no, cnp, ncp, ntot;
     double *ex, *JA, *JB, *U, *V, *W, *g, *UVdiag, *Vinv, *Y, *S, *Saux, *ea, *dp, *eb;
     double *ncams, *npts, *Jx1, *Jx2, *PU, *PB, *P, *E, *tmpn;
 } orc_ws;
@@ -910,17 +1085,18 @@ static void ws_init(orc_ws *w, const orc_problem *p)
     w->nc = p->nc;
     w->np = p->np;
     w->no = p->no;
-    w->ncp = p->nc * CNP;
+    w->cnp = cnp_of(p);
+    w->ncp = p->nc * w->cnp;
     w->ntot = w->ncp + p->np * PNP;
     idx_build(p, &w->ix, 1);
     size_t no = (size_t)p->no, nt = (size_t)w->ntot, N = (size_t)w->ncp;
     w->ex = malloc(sizeof(double) * 2 * no + 8);
-    w->JA = malloc(sizeof(double) * 12 * no + 8);
+    w->JA = malloc(sizeof(double) * 2 * w->cnp * no + 8);
     w->JB = malloc(sizeof(double) * 6 * no + 8);
-    w->U = malloc(sizeof(double) * 36 * (size_t)p->nc + 8);
+    w->U = malloc(sizeof(double) * w->cnp * w->cnp * (size_t)p->nc + 8);
     w->V = malloc(sizeof(double) * 9 * (size_t)p->np + 8);
-    w->W = malloc(sizeof(double) * 18 * no + 8);
-    w->Y = malloc(sizeof(double) * 18 * no + 8);
+    w->W = malloc(sizeof(double) * 3 * w->cnp * no + 8);
+    w->Y = malloc(sizeof(double) * 3 * w->cnp * no + 8);
     w->g = malloc(sizeof(double) * nt + 8);
     w->UVdiag = malloc(sizeof(double) * nt + 8);
     w->Vinv = malloc(sizeof(double) * 9 * (size_t)p->np + 8);
@@ -976,6 +1152,11 @@ static void trace_push(orc_result *res, int itno, int kind, int acc, double damp
 static int reduced_solve(orc_ws *w, int mode, double *dpa)
 {
     int N = w->ncp;
+    if (N % 3 != 0) {  /* variable intrinsics: no 3x3-block form; column Cholesky + solves */
+        if (col_cholesky(N, w->S)) return 1;
+        orc_chol_solve(N, w->S, w->ea, dpa);
+        return 0;
+    }
     if (mode == 0) {
         if (orc_spd_inverse(N, w->S)) return 1;
         orc_matvec(N, w->S, w->ea, dpa);
@@ -1194,7 +1375,7 @@ static int trust_region_ws(orc_ws *w, double *cams, double *pts, const orc_opts 
         /* g = -2 J^T e (compute_g with coeff -2), U, V, W with coeff 2 */
         normal_blocks_ix(p, &w->ix, w->JA, w->JB, w->ex, -2.0, w->U, w->V, w->W, w->g, w->UVdiag);
         /* the U/V/W of coeff 2 are the negatives of coeff -2 */
-        for (int k = 0; k < 36 * w->nc; ++k) w->U[k] = -w->U[k];
+        for (int k = 0; k < w->cnp * w->cnp * w->nc; ++k) w->U[k] = -w->U[k];
         for (int k = 0; k < 9 * w->np; ++k) w->V[k] = -w->V[k];
         for (long long k = 0; k < 18LL * w->no; ++k) w->W[k] = -w->W[k];
         for (int k = 0; k < nt; ++k) w->UVdiag[k] = -w->UVdiag[k];

@@ -17,6 +17,13 @@
  *   meas   2 per observation, observations sorted (point asc, camera asc)
  *   JA 2x6, JB 2x3, W/Y 6x3 per observation; U 6x6 per camera; V 3x3 per point
  *   g = [ga (6C) | gb (3P)];  S dense N x N, N = 6C (only the lower triangle is defined)
+ *
+ * Variable intrinsics (no counterpart in the reference, whose kernels fix
+ * cnp = 6, CL_files/PSBA.cl:5): cnp = 11 appends the intrinsics in the
+ * reference's K layout (fx, cx, cy, ar, skew) to each camera's 6 pose
+ * parameters, cnp = 16 further appends distortion (k1, k2, p1, p2, k3) in
+ * the Bouguet order of the sba camera files (data/54camsvarKD.txt); the
+ * 6-wide blocks above become cnp-wide (JA 2 x cnp, W/Y cnp x 3, U cnp x cnp).
  */
 #ifndef PSBA_ORACLE_H
 #define PSBA_ORACLE_H
@@ -53,11 +60,12 @@ typedef struct {
 
 typedef struct {
     int nc, np, no;
-    const double *K;
+    const double *K;      /* 5 per camera; read only when cnp == 6 */
     const double *q0;
     const double *meas;
     const int *obs_pt;
     const int *obs_cam;
+    int cnp;              /* parameters per camera: 6 (0 means 6), 11, 16 */
 } orc_problem;
 
 typedef struct {

@@ -68,7 +68,11 @@ EXPORTS = ("psba_default_opts", "psba_create", "psba_destroy", "psba_get_params"
            "psba_eval_jacobian", "psba_eval_normal", "psba_eval_reduced", "psba_eval_step",
            "psba_eval_jmultiply", "psba_eval_cholmod", "psba_last_error", "psba_stream",
            "psba_device_bytes", "psba_version", "psba_set_stage_timing", "psba_get_stage_timing",
-           "psba_transfer_bytes", "psba_kernel_launches", "psba_measure_peak", "psba_cost_noalloc")
+           "psba_transfer_bytes", "psba_kernel_launches", "psba_measure_peak", "psba_cost_noalloc",
+           "psba_batch_create", "psba_batch_destroy", "psba_batch_levmar", "psba_batch_get_params",
+           "psba_batch_reset_params", "psba_batch_set_threads", "psba_batch_set_lanes_per_pair",
+           "psba_batch_device_bytes", "psba_server_default_opts", "psba_server_create", "psba_batch_submit",
+           "psba_batch_poll", "psba_server_stats_get", "psba_server_destroy")
 STAGES = ("linearize", "point_blocks", "camera_blocks", "vinv", "yblocks", "schur_off", "schur_diag",
           "schur_reduce", "cholesky", "eb_dpb", "trial_cost")
 

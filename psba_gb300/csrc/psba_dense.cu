@@ -11,8 +11,9 @@
 //                registers, its inverse, and y_I = L_II^-1 (b_I - sum_J L_IJ y_J)
 //                (the forward solve of L y = ea rides along)
 //   tile (I,K):  A_IK -= sum_{J<K} L_IJ L_KJ^T, then L_IK = A_IK L_KK^-T
-// After the factor, back-substitution tasks B_K (K descending) solve
-// L^T x = y:  x_K = L_KK^-T (y_K - sum_{I>K} L_IK^T x_I).
+// After the factor, one CTA solves L^T x = y with y in shared memory; the
+// refinement solve of the mixed form (mode 1) runs both triangular solves in
+// one CTA the same way.
 //
 // This replaces the reference's explicit inverse (SPD_inv.cl: 3x3-block
 // Cholesky chain, kern_trigMat_inv, kern_trigMat_mul, then matVec_mul) with
@@ -28,6 +29,7 @@ constexpr int T = TILE;
 constexpr int TT = TILE * TILE;
 constexpr int CF_THREADS = 128;
 constexpr long long SPIN_LIMIT = 1LL << 22;  // ~0.5 s of polling with 64 ns sleeps
+constexpr int MAX_NP = 4096;                 // largest reduced system (dynamic shared memory of the solve)
 
 __device__ __forceinline__ int ld_acquire(const int *p)
 {
@@ -128,8 +130,73 @@ __device__ bool warp_potrf(double (*a)[T + 1], double (*linv)[T + 1], double *in
     return !bad;
 }
 
-// mode 0: factor + forward solve + back solve; mode 1: forward + back solve
-// with an existing factor (S lower = L, Linv) for the right-hand side rhs.
+// Single-CTA triangular solves over the factor (S lower = L, Linv = diagonal
+// tile inverses) with the right-hand side in shared memory.  Each column step
+// reads one row panel of L with coalesced loads (16 independent loads per
+// thread), so a step costs about one L2 round trip.
+// forward: b <- L^-1 b (right-looking: y_K = Linv_K b_K, then b_I -= L_IK y_K)
+__device__ void cta_forward(int Np, int nb, const double *__restrict__ S, const double *__restrict__ Linv,
+                            double *bs, double *tmp)
+{
+    const int tid = threadIdx.x;
+    for (int K = 0; K < nb; ++K) {
+        if (tid < T) {
+            const double *Li = Linv + (size_t)K * TT + tid * T;
+            double y = 0.0;
+#pragma unroll
+            for (int k = 0; k < T; ++k) y = fma(k <= tid ? __ldcg(Li + k) : 0.0, bs[K * T + k], y);
+            tmp[tid] = y;
+        }
+        __syncthreads();
+        if (tid < T) bs[K * T + tid] = tmp[tid];
+        for (int i = (K + 1) * T + tid; i < Np; i += CF_THREADS) {
+            const double2 *row = reinterpret_cast<const double2 *>(S + (size_t)i * Np + K * T);
+            double s = 0.0;
+#pragma unroll
+            for (int c = 0; c < T / 2; ++c) {
+                const double2 v = __ldcg(row + c);
+                s = fma(v.x, tmp[2 * c], s);
+                s = fma(v.y, tmp[2 * c + 1], s);
+            }
+            bs[i] -= s;
+        }
+        __syncthreads();
+    }
+}
+
+// back: x <- L^-T y (right-looking over the columns of L^T: x_K = Linv_K^T y_K,
+// then y_I -= L_KI^T x_K for I < K, reading rows K*T..K*T+T-1 of L).
+__device__ void cta_back(int Np, int nb, const double *__restrict__ S, const double *__restrict__ Linv,
+                         double *ys, double *xs, double *__restrict__ x)
+{
+    const int tid = threadIdx.x;
+    for (int K = nb - 1; K >= 0; --K) {
+        if (tid < T) {
+            const double *Li = Linv + (size_t)K * TT;
+            double v = 0.0;
+#pragma unroll
+            for (int k = 0; k < T; ++k) v = fma(k >= tid ? __ldcg(Li + k * T + tid) : 0.0, ys[K * T + k], v);
+            xs[tid] = v;
+            x[K * T + tid] = v;
+        }
+        __syncthreads();
+        for (int col = tid; col < K * T; col += CF_THREADS) {
+            const double *base = S + (size_t)(K * T) * Np + col;
+            double v[T];
+#pragma unroll
+            for (int c = 0; c < T; ++c) v[c] = __ldcg(base + (size_t)c * Np);
+            double s = 0.0;
+#pragma unroll
+            for (int c = 0; c < T; ++c) s = fma(v[c], xs[c], s);
+            ys[col] -= s;
+        }
+        __syncthreads();
+    }
+}
+
+// mode 0: factor (tile dataflow) with the forward solve of rhs carried along,
+// then one CTA runs the back solve into x.  mode 1: one CTA runs the forward
+// and back solves of rhs with the existing factor.
 __global__ void __launch_bounds__(CF_THREADS) k_chol_dataflow(int mode, int Np, int nb,
                                                               const int2 *__restrict__ tasks,
                                                               double *__restrict__ S,
@@ -140,12 +207,13 @@ __global__ void __launch_bounds__(CF_THREADS) k_chol_dataflow(int mode, int Np, 
                                                               int *__restrict__ status)
 {
     __shared__ double a[T][T + 1], li[T][T + 1], lk[T][T + 1], linv[T][T + 1];
-    __shared__ double bvec[T], yvec[T], invd[T], red[CF_THREADS / T][T];
-    const int n_fact = mode == 0 ? nb * (nb + 1) / 2 : nb;  // mode 1: forward tasks F_K
-    const int n_tasks = n_fact + nb;
+    __shared__ double bvec[T], yvec[T], invd[T];
+    extern __shared__ double vec[];  // Np: right-hand side of the single-CTA solves
+    const int n_fact = mode == 0 ? nb * (nb + 1) / 2 : 0;
+    const int n_tasks = n_fact + 1;
     const int tid = threadIdx.x;
     for (int t = blockIdx.x; t < n_tasks; t += gridDim.x) {
-        if (t < n_fact && mode == 0) {
+        if (t < n_fact) {
             const int I = tasks[t].x, K = tasks[t].y;
             load_tile(a, S, Np, I, K);
             if (I == K && tid < T) bvec[tid] = __ldcg(rhs + I * T + tid);
@@ -205,65 +273,14 @@ __global__ void __launch_bounds__(CF_THREADS) k_chol_dataflow(int mode, int Np, 
                 __threadfence();
                 st_release(flags + t, epoch);
             }
-        } else if (t < n_fact) {
-            // mode 1 forward task F_K: y_K = Linv_K (b_K - sum_{J<K} L_KJ y_J)
-            const int K = t;
-            if (K > 0) block_wait(flags + (K - 1), epoch, status);
-            const int g = tid / T, r = tid % T;
-            double s = 0.0;
-            for (int J = g; J < K; J += CF_THREADS / T) {
-                const double *L = S + (size_t)(K * T + r) * Np + J * T;
-                for (int c = 0; c < T; ++c) s = fma(__ldcg(L + c), __ldcg(rhs + J * T + c), s);
-            }
-            red[g][r] = s;
-            __syncthreads();
-            if (tid < T) {
-                double bb = __ldcg(rhs + K * T + tid);
-                for (int q = 0; q < CF_THREADS / T; ++q) bb -= red[q][tid];
-                bvec[tid] = bb;
-            }
-            for (int e = tid; e < TT; e += CF_THREADS) linv[e / T][e % T] = __ldcg(Linv + (size_t)K * TT + e);
-            __syncthreads();
-            if (tid < T) {
-                double yy = 0.0;
-                for (int k = 0; k <= tid; ++k) yy = fma(linv[tid][k], bvec[k], yy);
-                rhs[K * T + tid] = yy;
-            }
-            __syncthreads();
-            if (tid == 0) {
-                __threadfence();
-                st_release(flags + t, epoch);
-            }
         } else {
-            // back-substitution task B_K
-            const int K = nb - 1 - (t - n_fact);
-            const int last_fact = mode == 0 ? tile_task(nb - 1, nb - 1, nb) : nb - 1;
-            block_wait(flags + last_fact, epoch, status);  // whole factor and y ready
-            if (K < nb - 1) block_wait(flags + t - 1, epoch, status);  // x_{K+1..} ready
-            const int g = tid / T, r = tid % T;
-            double s = 0.0;
-            for (int I = K + 1 + g; I < nb; I += CF_THREADS / T) {
-                const double *L = S + (size_t)(I * T) * Np + K * T + r;  // L_IK[c][r], c = 0..T-1
-                for (int c = 0; c < T; ++c) s = fma(__ldcg(L + (size_t)c * Np), __ldcg(x + I * T + c), s);
-            }
-            red[g][r] = s;
-            for (int e = tid; e < TT; e += CF_THREADS) linv[e / T][e % T] = __ldcg(Linv + (size_t)K * TT + e);
+            // the solve task: waits for the whole factor (mode 0), then one CTA
+            if (mode == 0) block_wait(flags + (n_fact - 1), epoch, status);
+            for (int i = tid; i < Np; i += CF_THREADS) vec[i] = __ldcg(rhs + i);
             __syncthreads();
-            if (tid < T) {
-                double yy = __ldcg(rhs + K * T + tid);
-                for (int q = 0; q < CF_THREADS / T; ++q) yy -= red[q][tid];
-                bvec[tid] = yy;
-            }
-            __syncthreads();
-            if (tid < T) {
-                double xx = 0.0;
-                for (int k = tid; k < T; ++k) xx = fma(linv[k][tid], bvec[k], xx);
-                x[K * T + tid] = xx;
-            }
-            __syncthreads();
-            if (tid == 0) {
-                __threadfence();
-                st_release(flags + t, epoch);
+            if (ld_acquire(status) == 0) {
+                if (mode == 1) cta_forward(Np, nb, S, Linv, vec, yvec);
+                cta_back(Np, nb, S, Linv, vec, yvec, x);
             }
         }
         __syncthreads();
@@ -277,7 +294,8 @@ int chol_grid(int n_tasks)
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_chol_dataflow, CF_THREADS, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_chol_dataflow, CF_THREADS,
+                                                      sizeof(double) * MAX_NP);
         if (per_sm < 1) per_sm = 1;
     }
     const int cap = per_sm * sms;
@@ -287,7 +305,7 @@ int chol_grid(int n_tasks)
 void launch_chol_dataflow(const DeviceProblem &d, int mode, int epoch, double *x_out, cudaStream_t s)
 {
     const int nb = d.Np / T;
-    const int n_tasks = (mode == 0 ? nb * (nb + 1) / 2 : nb) + nb;
+    const int n_tasks = (mode == 0 ? nb * (nb + 1) / 2 : 0) + 1;
     const int grid = chol_grid(n_tasks);
     int Np = d.Np;
     const int2 *tasks = d.chol_tasks;
@@ -295,7 +313,8 @@ void launch_chol_dataflow(const DeviceProblem &d, int mode, int epoch, double *x
     int *flags = d.chol_flags, *status = d.status;
     void *args[] = {&mode, &Np, (void *)&nb, (void *)&tasks, &S, &Linv, &rhs, &x, &flags, &epoch, &status};
     if (mode == 0) cudaMemsetAsync(d.status, 0, sizeof(int), s);
-    cudaLaunchCooperativeKernel((const void *)k_chol_dataflow, dim3(grid), dim3(CF_THREADS), args, 0, s);
+    cudaLaunchCooperativeKernel((const void *)k_chol_dataflow, dim3(grid), dim3(CF_THREADS), args,
+                                sizeof(double) * d.Np, s);
     note_launch(1);
 }
 

@@ -134,22 +134,31 @@ __global__ void __launch_bounds__(256) k_linearize(int no, const int *__restrict
     int o = blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= no) return;
     const int i = __ldg(obs_pt + o), j = __ldg(obs_cam + o);
-    const R X0 = (R)__ldg(pts + 3 * i), X1 = (R)__ldg(pts + 3 * i + 1), X2 = (R)__ldg(pts + 3 * i + 2);
     const double *T = tab + (size_t)CAMTAB * j;
+    // The projection and the residual are FP64 in both forms: e = m - pi(X) is
+    // a small difference of ~1e3 px quantities, and its error moves the
+    // gradient and with it the LM fixed point.  Only the stored e, J and W are
+    // rounded to R.
+    const double Xd0 = __ldg(pts + 3 * i), Xd1 = __ldg(pts + 3 * i + 1), Xd2 = __ldg(pts + 3 * i + 2);
+    double Md[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) Md[e] = __ldg(T + e);
+    const double xcd = Md[0] * Xd0 + Md[1] * Xd1 + Md[2] * Xd2 + __ldg(T + 36);
+    const double ycd = Md[3] * Xd0 + Md[4] * Xd1 + Md[5] * Xd2 + __ldg(T + 37);
+    const double zcd = Md[6] * Xd0 + Md[7] * Xd1 + Md[8] * Xd2 + __ldg(T + 38);
+    const double fxd = __ldg(T + 39), skd = __ldg(T + 40), cxd = __ldg(T + 41), fyd = __ldg(T + 42),
+                 cyd = __ldg(T + 43);
+    const double izd = 1.0 / zcd;
+    const double2 m2 = __ldg(reinterpret_cast<const double2 *>(meas + 2 * (size_t)o));
+    const double nud = fxd * xcd + skd * ycd;
+    const double u = (nud + cxd * zcd) * izd;
+    const double v = (fyd * ycd + cyd * zcd) * izd;
+    st2<R>(ex + 2 * (size_t)o, (R)(m2.x - u), (R)(m2.y - v));
+    const R X0 = (R)Xd0, X1 = (R)Xd1, X2 = (R)Xd2;
     R M[9];
 #pragma unroll
-    for (int e = 0; e < 9; ++e) M[e] = (R)__ldg(T + e);
-    const R xc = M[0] * X0 + M[1] * X1 + M[2] * X2 + (R)__ldg(T + 36);
-    const R yc = M[3] * X0 + M[4] * X1 + M[5] * X2 + (R)__ldg(T + 37);
-    const R zc = M[6] * X0 + M[7] * X1 + M[8] * X2 + (R)__ldg(T + 38);
-    const R fx = (R)__ldg(T + 39), sk = (R)__ldg(T + 40), cx = (R)__ldg(T + 41), fy = (R)__ldg(T + 42),
-            cy = (R)__ldg(T + 43);
-    const R iz = (R)1 / zc;
-    const double2 m2 = __ldg(reinterpret_cast<const double2 *>(meas + 2 * (size_t)o));
-    const R nu = fx * xc + sk * yc;
-    const R u = (nu + cx * zc) * iz;
-    const R v = (fy * yc + cy * zc) * iz;
-    st2<R>(ex + 2 * (size_t)o, (R)m2.x - u, (R)m2.y - v);
+    for (int e = 0; e < 9; ++e) M[e] = (R)Md[e];
+    const R yc = (R)ycd, iz = (R)izd, nu = (R)nud, fx = (R)fxd, sk = (R)skd, fy = (R)fyd;
     // d(x,y)/dXc
     const R p00 = fx * iz, p01 = sk * iz, p02 = -nu * iz * iz;
     const R p11 = fy * iz, p12 = -fy * yc * iz * iz;
@@ -261,7 +270,7 @@ __global__ void k_point_blocks(int np, int ncp, const int *__restrict__ pt_start
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= np) return;
     double v00 = 0, v01 = 0, v02 = 0, v11 = 0, v12 = 0, v22 = 0;
-    R g0 = 0, g1 = 0, g2 = 0;
+    double g0 = 0, g1 = 0, g2 = 0;  // gradient: FP64 sums of exact products in both forms
     const int e = pt_start[i + 1];
 #pragma unroll 4
     for (int o = pt_start[i]; o < e; ++o) {
@@ -285,9 +294,9 @@ __global__ void k_point_blocks(int np, int ncp, const int *__restrict__ pt_start
             v12 += (double)(b1 * b2 + c1 * c2);
             v22 += (double)(b2 * b2 + c2 * c2);
         }
-        g0 = g0 + b0 * e0 + c0 * e1;
-        g1 = g1 + b1 * e0 + c1 * e1;
-        g2 = g2 + b2 * e0 + c2 * e1;
+        g0 = g0 + (double)b0 * (double)e0 + (double)c0 * (double)e1;
+        g1 = g1 + (double)b1 * (double)e0 + (double)c1 * (double)e1;
+        g2 = g2 + (double)b2 * (double)e0 + (double)c2 * (double)e1;
     }
     const double cf = (double)coeff;
     double *Vi = V + 6 * (size_t)i;
@@ -296,9 +305,9 @@ __global__ void k_point_blocks(int np, int ncp, const int *__restrict__ pt_start
     uvdiag[ncp + 3 * (size_t)i] = Vi[0];
     uvdiag[ncp + 3 * (size_t)i + 1] = Vi[3];
     uvdiag[ncp + 3 * (size_t)i + 2] = Vi[5];
-    g[ncp + 3 * (size_t)i] = (double)(coeff * g0);
-    g[ncp + 3 * (size_t)i + 1] = (double)(coeff * g1);
-    g[ncp + 3 * (size_t)i + 2] = (double)(coeff * g2);
+    g[ncp + 3 * (size_t)i] = cf * g0;
+    g[ncp + 3 * (size_t)i + 1] = cf * g1;
+    g[ncp + 3 * (size_t)i + 2] = cf * g2;
 }
 
 void launch_point_blocks(const DeviceProblem &d, double coeff, cudaStream_t s)
@@ -349,11 +358,14 @@ __global__ void __launch_bounds__(CAM_THREADS) k_camera_partial(const CamUnit *_
             for (int r = 0; r < 6; ++r)
 #pragma unroll
                 for (int c = r; c < 6; ++c, ++v) part[v] = part[v] + a[r] * a[c] + a[6 + r] * a[6 + c];
+            // the gradient sets the LM fixed point: FP64 sums of the exact
+            // products of the stored values in both forms
 #pragma unroll
-            for (int k = 0; k < 6; ++k) part[21 + k] = part[21 + k] + a[k] * e2[0] + a[6 + k] * e2[1];
+            for (int k = 0; k < 6; ++k)
+                acc[21 + k] = acc[21 + k] + (double)a[k] * (double)e2[0] + (double)a[6 + k] * (double)e2[1];
         }
 #pragma unroll
-        for (int v = 0; v < CAM_NV; ++v) acc[v] += (double)part[v];
+        for (int v = 0; v < 21; ++v) acc[v] += (double)part[v];
     }
 #pragma unroll
     for (int v = 0; v < CAM_NV; ++v) red[v][threadIdx.x] = acc[v];

@@ -1,0 +1,465 @@
+// Serving engine: continuous (iteration-level) batching of independent
+// bundle-adjustment requests on one GPU.
+//
+// A request is laid out on the submitting thread (index lists, Schur pair
+// lists) and queued.  A worker thread admits queued requests in arrival order
+// while a resident slot is free and the request's footprint fits the HBM
+// pool (one cudaMalloc of the budget at creation, carved by a first-fit
+// allocator, so admission is exactly "fits the budget").  Admitted problems
+// keep parameters, linearisation and LM state (BatchResult) on the device and
+// advance together in time slices: each slice is one persistent launch of the
+// batched LM kernel in which every resident problem runs a number of outer LM
+// iterations scaled so that all of them take about as long as the heaviest
+// one's slice.  Between slices the worker retires finished problems (copies
+// their parameters out, frees their memory and slot) and admits new ones,
+// which join the next launch.  A problem's arithmetic depends only on its own
+// data and on outer-iteration boundaries, which are where slices cut, so its
+// result is the same bits alone and in any mix.
+//
+// The per-request solve is levmar() (PSBA/levmar.cpp:45-256); the reference
+// has no serving layer (one problem per process, PSBA/main.cpp:193-208).
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "psba_batch_internal.h"
+
+using namespace psba;
+using namespace psba::batch;
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+double ms_between(Clock::time_point a, Clock::time_point b)
+{
+    return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+struct Request {
+    long long ticket = 0;
+    ProblemLayout L;
+    size_t bytes = 0;
+    int slot = -1;
+    size_t off = 0;
+    int state = 0;  // 0 queued, 1 resident, 2 finished
+    Clock::time_point t_submit, t_admit, t_done;
+    BatchResult st{};
+    std::vector<double> cams, pts;
+};
+
+// First-fit allocator over [0, size) in 256-byte units, coalescing on free.
+class PoolAllocator {
+  public:
+    void reset(size_t size)
+    {
+        free_.clear();
+        if (size) free_[0] = size;
+        used_ = 0;
+    }
+    bool alloc(size_t bytes, size_t &off)
+    {
+        bytes = (bytes + 255) & ~(size_t)255;
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= bytes) {
+                off = it->first;
+                const size_t rest = it->second - bytes;
+                free_.erase(it);
+                if (rest) free_[off + bytes] = rest;
+                used_ += bytes;
+                return true;
+            }
+        }
+        return false;
+    }
+    void release(size_t off, size_t bytes)
+    {
+        bytes = (bytes + 255) & ~(size_t)255;
+        used_ -= bytes;
+        auto it = free_.emplace(off, bytes).first;
+        auto nx = std::next(it);
+        if (nx != free_.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free_.erase(nx);
+        }
+        if (it != free_.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+    size_t used() const { return used_; }
+
+  private:
+    std::map<size_t, size_t> free_;
+    size_t used_ = 0;
+};
+
+}  // namespace
+
+struct psba_server {
+    psba_server_opts so{};
+    BatchOpts bo{};
+    int precision = PSBA_PREC_FP64;
+    size_t rsize = sizeof(double);
+    // device
+    char *pool = nullptr;
+    size_t pool_size = 0;
+    BatchProblem *d_probs = nullptr;
+    int *d_order = nullptr, *d_queue = nullptr;
+    BatchResult *d_state = nullptr;
+    BatchOpts *d_opts = nullptr;
+    // pinned host mirrors
+    BatchProblem *h_probs = nullptr;
+    BatchResult *h_state = nullptr;
+    int *h_order = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int device = 0, grid_cap = 1;
+    // scheduling state (guarded by mu)
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    PoolAllocator alloc;
+    std::deque<Request *> queue;
+    std::vector<Request *> slots;
+    std::unordered_map<long long, std::unique_ptr<Request>> reqs;
+    long long next_ticket = 1;
+    int n_active = 0;
+    bool stop = false;
+    int failed = 0;
+    std::string fail_msg;
+    psba_server_stats stats{};
+    std::thread worker;
+};
+
+namespace {
+
+void server_fail(psba_server *s, cudaError_t e, const char *what)
+{
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (!s->failed) {
+        s->failed = 1;
+        s->fail_msg = std::string("psba server: ") + what + ": " + cudaGetErrorString(e);
+    }
+    s->cv_done.notify_all();
+}
+
+// Upload a newly admitted request into its pool region and slot.
+cudaError_t upload(psba_server *s, Request *r)
+{
+    const ProblemLayout &L = r->L;
+    const size_t d_bytes = (sizeof(double) * L.dA.size() + 255) & ~(size_t)255;
+    const size_t i_bytes = (sizeof(int) * L.iA.size() + 255) & ~(size_t)255;
+    BatchProblem bp = L.bp;
+    rebase_problem(bp, (long long)(r->off / sizeof(double)), (long long)((r->off + d_bytes) / sizeof(int)),
+                   (long long)((r->off + d_bytes + i_bytes) / s->rsize));
+    bp.flags = (bp.flags & ~0xff) | (s->so.lanes_per_pair & 0xff);
+    s->h_probs[r->slot] = bp;
+    cudaError_t e = cudaSuccess;
+    if (!L.dA.empty())
+        e = cudaMemcpyAsync(s->pool + r->off, L.dA.data(), sizeof(double) * L.dA.size(), cudaMemcpyHostToDevice,
+                            s->stream);
+    if (e == cudaSuccess && !L.iA.empty())
+        e = cudaMemcpyAsync(s->pool + r->off + d_bytes, L.iA.data(), sizeof(int) * L.iA.size(),
+                            cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s->d_state + r->slot, 0, sizeof(BatchResult), s->stream);
+    return e;
+}
+
+void worker_main(psba_server *s)
+{
+    cudaSetDevice(s->device);
+    std::vector<Request *> admitted, active, done;
+    while (true) {
+        admitted.clear();
+        active.clear();
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            s->cv_work.wait(lk, [&] { return s->stop || !s->queue.empty() || s->n_active > 0; });
+            if (s->stop || s->failed) break;
+            while (!s->queue.empty() && s->n_active < s->so.max_active) {
+                Request *r = s->queue.front();
+                size_t off = 0;
+                if (!s->alloc.alloc(r->bytes, off)) break;  // arrival order: wait for memory
+                int slot = 0;
+                while (s->slots[slot]) ++slot;
+                r->slot = slot;
+                r->off = off;
+                r->state = 1;
+                r->t_admit = Clock::now();
+                s->slots[slot] = r;
+                s->n_active++;
+                s->queue.pop_front();
+                admitted.push_back(r);
+                s->stats.admitted++;
+            }
+            s->stats.bytes_in_use = (double)s->alloc.used();
+            s->stats.peak_bytes = std::max(s->stats.peak_bytes, s->stats.bytes_in_use);
+            for (Request *r : s->slots)
+                if (r) active.push_back(r);
+        }
+        if (active.empty()) continue;
+        cudaError_t e = cudaSuccess;
+        for (Request *r : admitted)
+            if (e == cudaSuccess) e = upload(s, r);
+        if (e != cudaSuccess) {
+            server_fail(s, e, "upload");
+            break;
+        }
+        // time-balanced slice: the heaviest resident problem runs slice_iters
+        // outer iterations, lighter ones proportionally more
+        double wmax = 0.0;
+        for (Request *r : active) wmax = std::max(wmax, r->L.work);
+        int max_slot = 0;
+        for (Request *r : active) {
+            const double k = std::floor(s->so.slice_iters * wmax / std::max(r->L.work, 1.0));
+            s->h_probs[r->slot].slice = (int)std::min<double>(std::max<double>(k, s->so.slice_iters), s->bo.max_iter);
+            max_slot = std::max(max_slot, r->slot + 1);
+        }
+        std::sort(active.begin(), active.end(), [](const Request *a, const Request *b) {
+            return a->L.work > b->L.work;
+        });
+        for (size_t q = 0; q < active.size(); ++q) s->h_order[q] = active[q]->slot;
+        const int n = (int)active.size();
+        e = cudaMemcpyAsync(s->d_probs, s->h_probs, sizeof(BatchProblem) * max_slot, cudaMemcpyHostToDevice,
+                            s->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(s->d_order, s->h_order, sizeof(int) * n, cudaMemcpyHostToDevice, s->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(s->d_queue, 0, sizeof(int), s->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(s->ev0, s->stream);
+        if (e == cudaSuccess)
+            e = launch_batch_lm(s->precision, std::min(n, s->grid_cap), s->so.threads, s->stream, s->d_probs,
+                                s->d_order, n, s->d_queue, (double *)s->pool, (int *)s->pool, (void *)s->pool,
+                                s->d_opts, s->d_state);
+        note_launch(1);
+        if (e == cudaSuccess) e = cudaEventRecord(s->ev1, s->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(s->h_state, s->d_state, sizeof(BatchResult) * max_slot, cudaMemcpyDeviceToHost,
+                                s->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) {
+            server_fail(s, e, "slice");
+            break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, s->ev0, s->ev1);
+        // retire finished problems
+        done.clear();
+        for (Request *r : active) {
+            const BatchResult &st = s->h_state[r->slot];
+            if (st.status != PSBA_ITER_CONTINUE || st.iterations >= s->bo.max_iter) {
+                r->st = st;
+                const BatchProblem &bp = s->h_probs[r->slot];
+                r->cams.resize(6 * (size_t)bp.nc);
+                r->pts.resize(3 * (size_t)bp.np);
+                e = cudaMemcpyAsync(r->cams.data(), (double *)s->pool + bp.d_cams, sizeof(double) * r->cams.size(),
+                                    cudaMemcpyDeviceToHost, s->stream);
+                if (e == cudaSuccess && bp.np)
+                    e = cudaMemcpyAsync(r->pts.data(), (double *)s->pool + bp.d_pts, sizeof(double) * r->pts.size(),
+                                        cudaMemcpyDeviceToHost, s->stream);
+                if (e != cudaSuccess) break;
+                done.push_back(r);
+            }
+        }
+        if (e == cudaSuccess && !done.empty()) e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) {
+            server_fail(s, e, "retire");
+            break;
+        }
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->stats.launches++;
+            s->stats.busy_ms += ms;
+            const auto now = Clock::now();
+            for (Request *r : done) {
+                s->alloc.release(r->off, r->bytes);
+                s->slots[r->slot] = nullptr;
+                s->n_active--;
+                r->slot = -1;
+                r->state = 2;
+                r->t_done = now;
+                s->stats.finished++;
+                r->L.dA.clear();
+                r->L.dA.shrink_to_fit();
+                r->L.iA.clear();
+                r->L.iA.shrink_to_fit();
+            }
+            s->stats.bytes_in_use = (double)s->alloc.used();
+        }
+        if (!done.empty()) s->cv_done.notify_all();
+    }
+}
+
+void server_free(psba_server *s)
+{
+    if (!s) return;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+    }
+    s->cv_work.notify_all();
+    if (s->worker.joinable()) s->worker.join();
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    cudaFree(s->pool);
+    cudaFree(s->d_probs);
+    cudaFree(s->d_order);
+    cudaFree(s->d_queue);
+    cudaFree(s->d_state);
+    cudaFree(s->d_opts);
+    cudaFreeHost(s->h_probs);
+    cudaFreeHost(s->h_state);
+    cudaFreeHost(s->h_order);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+}  // namespace
+
+extern "C" {
+
+void psba_server_default_opts(psba_server_opts *o)
+{
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->hbm_budget_bytes = 120e9;
+    o->max_active = 1024;
+    o->slice_iters = 1;
+    o->threads = 256;
+    o->lanes_per_pair = 32;
+}
+
+int psba_server_create(const psba_server_opts *so, const psba_opts *lm, psba_server **out)
+{
+    if (!so || !lm || !out) return set_error("psba_server_create: null argument"), PSBA_ERR_ARG;
+    *out = nullptr;
+    if (so->hbm_budget_bytes < 1e6 || so->max_active < 1 || so->max_active > 65536 || so->slice_iters < 1 ||
+        (so->threads != 128 && so->threads != 256 && so->threads != 512) ||
+        (so->lanes_per_pair != 8 && so->lanes_per_pair != 16 && so->lanes_per_pair != 32) ||
+        (lm->precision != PSBA_PREC_FP64 && lm->precision != PSBA_PREC_MIXED) || lm->max_iter < 0)
+        return set_error("psba_server_create: bad options"), PSBA_ERR_ARG;
+    psba_server *s = new psba_server();
+    s->so = *so;
+    s->precision = lm->precision;
+    s->rsize = lm->precision == PSBA_PREC_MIXED ? sizeof(float) : sizeof(double);
+    s->bo.tau = lm->tau;
+    s->bo.stop_thresh = lm->stop_thresh;
+    s->bo.eps = lm->eps;
+    s->bo.max_iter = lm->max_iter;
+    s->bo.allow_switch = 0;  // the batched driver is LM only
+    s->bo.precision = lm->precision;
+    s->pool_size = (size_t)so->hbm_budget_bytes & ~(size_t)255;
+    const int M = so->max_active;
+    cudaError_t e = cudaGetDevice(&s->device);
+    int sms = 1;
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&s->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&s->ev1);
+    if (e == cudaSuccess) e = cudaMalloc(&s->pool, s->pool_size);
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_probs, sizeof(BatchProblem) * M);
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_order, sizeof(int) * M);
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_queue, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_state, sizeof(BatchResult) * M);
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_opts, sizeof(BatchOpts));
+    if (e == cudaSuccess) e = cudaMallocHost(&s->h_probs, sizeof(BatchProblem) * M);
+    if (e == cudaSuccess) e = cudaMallocHost(&s->h_state, sizeof(BatchResult) * M);
+    if (e == cudaSuccess) e = cudaMallocHost(&s->h_order, sizeof(int) * M);
+    if (e == cudaSuccess) e = cudaMemcpy(s->d_opts, &s->bo, sizeof(BatchOpts), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        set_error(std::string("psba_server_create: ") + cudaGetErrorString(e));
+        server_free(s);
+        return e == cudaErrorMemoryAllocation ? PSBA_ERR_NOMEM : PSBA_ERR_CUDA;
+    }
+    std::memset(s->h_probs, 0, sizeof(BatchProblem) * M);
+    s->grid_cap = batch_blocks_per_sm(s->precision, so->threads) * sms;
+    s->alloc.reset(s->pool_size);
+    s->slots.assign(M, nullptr);
+    s->worker = std::thread(worker_main, s);
+    *out = s;
+    return PSBA_OK;
+}
+
+int psba_batch_submit(psba_server *s, const psba_problem_desc *desc, long long *ticket)
+{
+    if (!s || !desc || !ticket) return set_error("psba_batch_submit: null argument"), PSBA_ERR_ARG;
+    auto r = std::make_unique<Request>();
+    r->t_submit = Clock::now();
+    std::string err;
+    if (!build_problem_layout(*desc, r->L, err)) return set_error("psba_batch_submit: " + err), PSBA_ERR_ARG;
+    r->bytes = pool_bytes(r->L, s->precision);
+    if (r->bytes > s->pool_size)
+        return set_error("psba_batch_submit: the problem alone exceeds the HBM budget"), PSBA_ERR_NOMEM;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (s->failed) return set_error(s->fail_msg), PSBA_ERR_CUDA;
+        r->ticket = s->next_ticket++;
+        *ticket = r->ticket;
+        s->queue.push_back(r.get());
+        s->reqs.emplace(r->ticket, std::move(r));
+        s->stats.submitted++;
+    }
+    s->cv_work.notify_one();
+    return PSBA_OK;
+}
+
+int psba_batch_poll(psba_server *s, long long ticket, int timeout_ms, psba_request_result *res, double *cams,
+                    double *pts)
+{
+    if (!s || timeout_ms < 0) return set_error("psba_batch_poll: bad arguments"), PSBA_ERR_ARG;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(ticket);
+    if (it == s->reqs.end()) return set_error("psba_batch_poll: unknown ticket"), PSBA_ERR_ARG;
+    Request *r = it->second.get();
+    const auto ready = [&] { return r->state == 2 || s->failed; };
+    if (!ready() && timeout_ms > 0) s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), ready);
+    if (r->state != 2) {
+        if (s->failed) return set_error(s->fail_msg), PSBA_ERR_CUDA;
+        return PSBA_PENDING;
+    }
+    if (res) {
+        res->status = r->st.status;
+        res->iterations = r->st.iterations;
+        res->n_trials = r->st.trials;
+        res->n_linearizations = r->st.linearizations;
+        res->initial_cost = r->st.initial_cost;
+        res->final_cost = r->st.final_cost;
+        res->queued_ms = ms_between(r->t_submit, r->t_admit);
+        res->latency_ms = ms_between(r->t_submit, r->t_done);
+        res->device_bytes = (double)r->bytes;
+    }
+    if (cams) std::memcpy(cams, r->cams.data(), sizeof(double) * r->cams.size());
+    if (pts && !r->pts.empty()) std::memcpy(pts, r->pts.data(), sizeof(double) * r->pts.size());
+    s->reqs.erase(it);
+    return PSBA_OK;
+}
+
+int psba_server_stats_get(psba_server *s, psba_server_stats *st)
+{
+    if (!s || !st) return set_error("psba_server_stats_get: null argument"), PSBA_ERR_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    *st = s->stats;
+    st->active = s->n_active;
+    st->queued = (int)s->queue.size();
+    return s->failed ? (set_error(s->fail_msg), PSBA_ERR_CUDA) : PSBA_OK;
+}
+
+int psba_server_destroy(psba_server *s)
+{
+    server_free(s);
+    return PSBA_OK;
+}
+
+}  // extern "C"

@@ -742,6 +742,7 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     const bool dense_tab = (long long)nc * nc <= (1LL << 24);
     std::vector<std::pair<long long, int>> sparse_ids;
     if (!dense_tab) return set_error("more than 4096 cameras is not supported"), PSBA_ERR_ARG;
+    if (d.Np > 4096) return set_error("more than 682 cameras is not supported (reduced system > 4096)"), PSBA_ERR_ARG;
     pair_of.assign((size_t)nc * nc, -1);
     std::vector<int> pair_kl;
     std::vector<long long> pair_cnt;

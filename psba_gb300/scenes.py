@@ -217,30 +217,32 @@ def arc_scene(seed=0, n_cams=7, n_pts=500, arc_deg=30.0, k_range=None, noise_px=
     q_true = quat_from_matrix(R)
     t_true = -np.einsum("nij,nj->ni", quat_to_matrix(q_true), centers)
     need = max(min_views, k_range[0] if k_range else min_views)
-    pts, opt, ocam = [], [], []
+    Xs, opt, ocam = [], [], []
     got = 0
+    R_all = quat_to_matrix(q_true)
     while got < P:
-        m = 4 * (P - got) + 16
+        m = min(4 * (P - got) + 16, max(4096, 4_000_000 // C))  # bounded candidate chunk
         X = np.stack([rng.uniform(-1.0, 1.0, m), rng.uniform(-1.0, 1.0, m), rng.uniform(5.0, 7.0, m)], 1)
-        xy, z = project(np.repeat(K[:1], m * C, 0), np.tile(q_true, (m, 1)), np.tile(t_true, (m, 1)),
-                        np.repeat(X, C, 0))
-        vis = ((z > 0.1) & (xy[:, 0] >= 0) & (xy[:, 0] < W) & (xy[:, 1] >= 0) & (xy[:, 1] < H)).reshape(m, C)
-        for r in range(m):
-            cams_r = np.nonzero(vis[r])[0]
-            if len(cams_r) < need:
-                continue
-            if k_range is not None:
-                k = int(rng.integers(k_range[0], k_range[1] + 1))
-                k = min(k, len(cams_r))
-                start = int(rng.integers(0, len(cams_r) - k + 1))
-                cams_r = cams_r[start:start + k]
-            pts.append(X[r])
-            opt.append(np.full(len(cams_r), got))
-            ocam.append(cams_r)
-            got += 1
-            if got == P:
-                break
-    X_true = np.array(pts)
+        Xc = np.einsum("cij,mj->mci", R_all, X) + t_true[None]
+        z = Xc[..., 2]
+        with np.errstate(divide="ignore", invalid="ignore"):
+            u = K[0, 0] * Xc[..., 0] / z + K[0, 1]
+            v = K[0, 0] * K[0, 3] * Xc[..., 1] / z + K[0, 2]
+        vis = (z > 0.1) & (u >= 0) & (u < W) & (v >= 0) & (v < H)
+        cnt = vis.sum(1)
+        keep = np.nonzero(cnt >= need)[0][: P - got]
+        vis, cnt, X = vis[keep], cnt[keep], X[keep]
+        if k_range is not None:
+            k = np.minimum(rng.integers(k_range[0], k_range[1] + 1, size=len(keep)), cnt)
+            start = (rng.random(len(keep)) * (cnt - k + 1)).astype(np.int64)
+            pos = np.cumsum(vis, axis=1) - 1
+            vis = vis & (pos >= start[:, None]) & (pos < (start + k)[:, None])
+        rows, cols = np.nonzero(vis)
+        Xs.append(X)
+        opt.append(rows + got)
+        ocam.append(cols)
+        got += len(keep)
+    X_true = np.concatenate(Xs)
     return _finish(name, rng, K, q_true, t_true, X_true, np.concatenate(opt), np.concatenate(ocam),
                    noise_px, outlier_frac, rot_sigma, trans_frac, pt_frac, W, H,
                    {"seed": seed, "generator": "arc", "k_range": k_range})
@@ -319,4 +321,19 @@ def batch_scenes(n_problems=1024, seed=0, cams=(5, 30), pts=(200, 3000), views=(
         out.append(arc_scene(seed=int(rng.integers(0, 2**31 - 1)), n_cams=C, n_pts=P,
                              arc_deg=max(30.0, 4.0 * C), k_range=views,
                              name="batch%d_%dx%d" % (b, C, P)))
+    return out
+
+
+def serving_scenes(n_problems=32, seed=0, cams=(5, 138), pts=(500, 60000), views=(4, 6)):
+    """Requests of the serving workload: cameras and points log-uniform on the
+    given ranges, 4-6 views per point, the small-scene generator with a
+    per-request seed (the arc widens with the camera count, up to 160 deg)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for b in range(n_problems):
+        C = int(round(np.exp(rng.uniform(np.log(cams[0]), np.log(cams[1])))))
+        P = int(round(np.exp(rng.uniform(np.log(pts[0]), np.log(pts[1])))))
+        out.append(arc_scene(seed=int(rng.integers(0, 2**31 - 1)), n_cams=C, n_pts=P,
+                             arc_deg=float(min(max(30.0, 2.0 * C), 160.0)), k_range=views,
+                             name="serve%d_%dx%d" % (b, C, P)))
     return out

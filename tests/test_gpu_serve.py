@@ -1,0 +1,113 @@
+"""The serving engine (psba_server_*, psba_batch_submit/poll): continuous
+batching with HBM-budget admission.  Results against the FP64 oracle, and the
+same bits for a request alone and inside a stream of other requests."""
+import time
+
+import numpy as np
+import pytest
+
+import oracle
+import psba_gb300 as P
+from psba_gb300 import scenes
+from psba_gb300 import serve as S
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    P.build()
+
+
+def probs(n, seed):
+    return scenes.batch_scenes(n, seed=seed, cams=(5, 16), pts=(200, 900), views=(3, 8))
+
+
+def test_serve_fp64_matches_oracle():
+    ps = probs(5, seed=11)
+    with S.Server(precision=P.PREC_FP64, max_iter=12, hbm_budget_bytes=2e9) as srv:
+        tickets = [srv.submit(sc) for sc in ps]
+        res = [srv.wait(t) for t in tickets]
+    for sc, r in zip(ps, res):
+        o = oracle.levmar(sc, allow_switch=0, max_iter=12)
+        assert r.status == o.status
+        assert r.iterations == o.iterations
+        assert abs(r.final_cost - o.final_cost) <= 1e-9 * o.final_cost
+        assert np.abs(r.cams - o.cams).max() <= 1e-6 * max(1.0, np.abs(o.cams).max())
+
+
+@pytest.mark.parametrize("precision", [P.PREC_FP64, P.PREC_MIXED])
+def test_serve_same_bits_alone_and_in_mix(precision):
+    ps = probs(9, seed=12)
+    target = ps[4]
+    with S.Server(precision=precision, max_iter=15, hbm_budget_bytes=2e9) as srv:
+        alone = srv.wait(srv.submit(target))
+    with S.Server(precision=precision, max_iter=15, hbm_budget_bytes=2e9, slice_iters=1) as srv:
+        early = [srv.submit(sc) for sc in ps[:4]]
+        time.sleep(0.02)  # the target arrives while the others are resident
+        t = srv.submit(target)
+        late = [srv.submit(sc) for sc in ps[5:]]
+        mixed = srv.wait(t)
+        for q in early + late:
+            srv.wait(q)
+        st = srv.stats()
+    assert st["launches"] > 1
+    assert mixed.final_cost == alone.final_cost
+    assert mixed.iterations == alone.iterations and mixed.status == alone.status
+    assert np.array_equal(mixed.cams, alone.cams) and np.array_equal(mixed.pts, alone.pts)
+
+
+def test_serve_slice_length_does_not_change_results():
+    ps = probs(4, seed=13)
+    out = []
+    for sl in (1, 4):
+        with S.Server(precision=P.PREC_MIXED, max_iter=10, hbm_budget_bytes=2e9, slice_iters=sl) as srv:
+            ts = [srv.submit(sc) for sc in ps]
+            out.append([srv.wait(t) for t in ts])
+    for a, b in zip(*out):
+        assert a.final_cost == b.final_cost and np.array_equal(a.cams, b.cams)
+
+
+def test_serve_admission_respects_budget():
+    ps = probs(6, seed=14)
+    # the pool holds the two largest problems at most
+    with S.Server(precision=P.PREC_FP64, max_iter=6, hbm_budget_bytes=1e9) as probe:
+        sizes = [probe.wait(probe.submit(sc)).device_bytes for sc in ps]
+    budget = sorted(sizes)[-1] + sorted(sizes)[-2] + 4096
+    with S.Server(precision=P.PREC_FP64, max_iter=6, hbm_budget_bytes=budget) as srv:
+        ts = [srv.submit(sc) for sc in ps]
+        res = [srv.wait(t) for t in ts]
+        st = srv.stats()
+    assert st["finished"] == len(ps)
+    assert st["peak_bytes"] <= budget
+    assert max(r.queued_ms for r in res) > 0.0
+    for sc, r in zip(ps, res):
+        o = oracle.levmar(sc, allow_switch=0, max_iter=6)
+        assert abs(r.final_cost - o.final_cost) <= 1e-9 * o.final_cost
+
+
+def test_serve_rejects_and_reports():
+    big = scenes.batch_scenes(1, seed=15, cams=(20, 21), pts=(2000, 2001), views=(4, 6))[0]
+    with S.Server(precision=P.PREC_FP64, max_iter=30, hbm_budget_bytes=2e6) as srv:
+        with pytest.raises(P.PSBAError):
+            srv.submit(big)  # alone larger than the pool: PSBA_ERR_NOMEM, nothing queued
+        small = scenes.batch_scenes(1, seed=16, cams=(5, 5), pts=(200, 200), views=(3, 5))[0]
+        t = srv.submit(small)
+        r = srv.wait(t)
+        assert r.status in (P.ITER_CONTINUE, P.ITER_DP_NO_CHANGE, P.ITER_ERR_SMALL_ENOUGH)
+        with pytest.raises(KeyError):
+            srv.poll(t)  # released by the successful poll
+
+
+def test_serve_poisson_small():
+    ps = probs(6, seed=17)
+    with S.Server(precision=P.PREC_MIXED, max_iter=10, hbm_budget_bytes=2e9) as srv:
+        out, wall = S.run_poisson(srv, ps, rate=200.0, n_requests=24, seed=3)
+    assert all(r is not None for r in out)
+    # the same scene gives the same bits whenever it arrived
+    by_scene = {}
+    for q, r in enumerate(out):
+        by_scene.setdefault(q % len(ps), []).append(r.final_cost)
+    for costs in by_scene.values():
+        assert len(set(costs)) == 1
+    assert wall > 0

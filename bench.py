@@ -16,8 +16,13 @@ estimate.  The metric is LM iterations per second.
   than L2 anyway).
 * e2e: the same metric through the C ABI from host buffers: psba_create
   (upload, index lists) + psba_levmar + psba_get_params per step, host clock.
-* roofline: the Schur-complement stage (k_schur_off + k_schur_diag +
-  k_schur_reduce), timed live with CUDA events inside the timed solves.
+* roofline: the dominant kernel, the dense solve of the reduced camera
+  system (k_chol_dataflow, one launch per LM trial), timed live with CUDA
+  events inside the timed solves; FP64-bound, so its peak is the measured
+  FP64 FMA rate.  roofline_schur: the same for the Schur-complement stage.
+* batched: 1,024 small problems in one persistent launch (mixed form,
+  autotuned shape) against the plain FP64 single-problem solver.
+* serving: Poisson arrivals into the continuous-batching server, p50/p99.
 * cpu_baseline: the FP64 CPU oracle (a C restatement of the reference's
   path) on the host cores, on a bounded sample of the same problem.
 * --impl reference: the CPU oracle alone (the reference's OpenCL/MSVC path
@@ -40,6 +45,12 @@ sys.path.insert(0, ROOT)
 METRIC = "LM iterations/s (plain FP64 Levenberg-Marquardt, 88 cams x 64,298 pts)"
 UNIT = "iterations/s"
 
+# DRAM bytes (read + write) per launch from one ncu capture of this workload
+# (profiles/k_schur_off_circle88.md); None where no capture of the current
+# kernel exists yet.
+SCHUR_OFF_TRAFFIC = 164.0e6
+CHOL_TRAFFIC = None  # S (2.2 MB) is L2-resident: ncu reads ~1.5 MB of DRAM per launch, 0.1% of peak
+
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -53,6 +64,8 @@ def parse():
     ap.add_argument("--cpu-iters", type=int, default=2, help="oracle LM iterations in the CPU sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-form leg")
+    ap.add_argument("--varcam-iters", type=int, default=30, help="LM iterations of the variable-intrinsics leg (0: skip)")
     ap.add_argument("--batch", type=int, default=1024, help="problems in the batched leg (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--pbp-sample", type=int, default=64,
@@ -268,6 +281,32 @@ def batched_leg(P, args):
     }
 
 
+def varcam_leg(P, args):
+    """Variable intrinsics: 52 cameras x 64,053 points (power-law views,
+    mean 5.42), 11- and 16-parameter cameras, intrinsics 5% off, LM for
+    --varcam-iters iterations in the mixed and the FP64 form."""
+    from psba_gb300 import scenes
+    out = {}
+    for cnp in (11, 16):
+        sc = scenes.varcam_scene(cnp, seed=0)
+        res = {"cameras": sc.n_cams, "points": sc.n_pts, "observations": sc.n_obs, "N": cnp * sc.n_cams}
+        with P.Solver(sc) as s:
+            for tag, prec in (("mixed", P.PREC_MIXED), ("fp64", P.PREC_FP64)):
+                o = P.default_opts(allow_switch=0, max_iter=args.varcam_iters, precision=prec)
+                s.reset_params()
+                s.levmar(o, fetch=False, trace_cap=0)  # warm-up
+                s.reset_params()
+                r = s.levmar(o, fetch=False, trace_cap=0)
+                res[tag] = {"iterations_per_s": r.iterations / (r.device_ms / 1e3), "ms_per_solve": r.device_ms,
+                            "iterations": r.iterations, "trials": r.n_trials, "initial_cost": r.initial_cost,
+                            "final_cost": r.final_cost}
+        res["mixed_final_cost_rel_vs_fp64"] = abs(res["mixed"]["final_cost"] - res["fp64"]["final_cost"]) / \
+            res["fp64"]["final_cost"]
+        res["speedup_mixed_vs_fp64"] = res["mixed"]["iterations_per_s"] / res["fp64"]["iterations_per_s"]
+        out["cnp%d" % cnp] = res
+    return out
+
+
 def serving_leg(P, args):
     """Poisson arrivals of requests (cameras log-uniform 5-138, points
     500-60,000, 4-6 views, 6-parameter cameras) into the serving engine
@@ -381,25 +420,27 @@ def main():
     value = iters_all / total_dev_s
 
     # ---- the mixed FP32/FP64 form on the same workload (same protocol)
-    mopts = P.default_opts(allow_switch=0, max_iter=args.max_iter, precision=P.PREC_MIXED)
-    for _ in range(min(1, args.warmup)):
-        solver.reset_params()
-        solver.levmar(mopts, fetch=False, trace_cap=0)
-    solver.set_stage_timing(True)
-    m_ms, m_iters, m_costs = [], 0, []
-    for _ in range(args.steps):
-        solver.reset_params()
-        flush_l2(torch, flush)
-        r = solver.levmar(mopts, fetch=False, trace_cap=0)
-        m_ms.append(r.device_ms)
-        m_iters += r.iterations
-        m_costs.append(r.final_cost)
-    m_stages = solver.stage_timing()
-    solver.set_stage_timing(False)
-    mixed = {"value": m_iters / (sum(m_ms) / 1e3), "unit": UNIT, "ms_per_step": sum(m_ms) / len(m_ms),
-             "final_cost": m_costs[-1], "final_cost_rel_vs_fp64": abs(m_costs[-1] - costs[-1]) / costs[-1],
-             "speedup_vs_fp64": (m_iters / sum(m_ms)) / (iters / sum(dev_ms)),
-             "stage_ms": {k: (v[0] / v[1] if v[1] else 0.0) for k, v in m_stages.items()}}
+    mixed = None
+    if not args.no_mixed:
+        mopts = P.default_opts(allow_switch=0, max_iter=args.max_iter, precision=P.PREC_MIXED)
+        for _ in range(min(1, args.warmup)):
+            solver.reset_params()
+            solver.levmar(mopts, fetch=False, trace_cap=0)
+        solver.set_stage_timing(True)
+        m_ms, m_iters, m_costs = [], 0, []
+        for _ in range(args.steps):
+            solver.reset_params()
+            flush_l2(torch, flush)
+            r = solver.levmar(mopts, fetch=False, trace_cap=0)
+            m_ms.append(r.device_ms)
+            m_iters += r.iterations
+            m_costs.append(r.final_cost)
+        m_stages = solver.stage_timing()
+        solver.set_stage_timing(False)
+        mixed = {"value": m_iters / (sum(m_ms) / 1e3), "unit": UNIT, "ms_per_step": sum(m_ms) / len(m_ms),
+                 "final_cost": m_costs[-1], "final_cost_rel_vs_fp64": abs(m_costs[-1] - costs[-1]) / costs[-1],
+                 "speedup_vs_fp64": (m_iters / sum(m_ms)) / (iters / sum(dev_ms)),
+                 "stage_ms": {k: (v[0] / v[1] if v[1] else 0.0) for k, v in m_stages.items()}}
 
     # ---- end to end through the C ABI from host buffers
     e2e_s, e2e_iters, h2d, d2h = 0.0, 0, 0, 0
@@ -414,14 +455,18 @@ def main():
         h2d, d2h = a, b
     e2e_value = e2e_iters / e2e_s if e2e_s > 0 else None
 
-    # ---- roofline of the dominant stage (Schur complement)
+    # ---- rooflines: the dominant kernel (dense solve) and the Schur stage
+    peak_gbs, peak_kind = measured_peaks()
+    fp64_peak = P.measure_peak("fp64")
     schur_ms = sum(stages[k][0] for k in ("schur_off", "schur_diag", "schur_reduce"))
     schur_n = max(stages["schur_off"][1], 1)
     schur_avg_s = schur_ms / schur_n / 1e3
-    peak_gbs, peak_kind = measured_peaks()
     achieved_gbs = schur_bytes(sc) / schur_avg_s / 1e9
-    fp64_peak = P.measure_peak("fp64")
     fp64_achieved = schur_flops(cfg) / schur_avg_s / 1e12
+    chol_avg_s = stages["cholesky"][0] / max(stages["cholesky"][1], 1) / 1e3
+    Np = -(-6 * sc.n_cams // 16) * 16
+    chol_flops = Np ** 3 / 3 + 2 * Np ** 2
+    chol_bytes = Np * Np * 8 + 2 * Np * 8
     stage_ms = {k: (v[0] / v[1] if v[1] else 0.0) for k, v in stages.items()}
     total_stage = sum(v[0] for v in stages.values())
 
@@ -436,13 +481,24 @@ def main():
         "final_cost": costs[-1], "wall_ms_per_step": 1e3 * wall / args.steps,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "steps": args.e2e_steps},
-        "roofline": {"kernel": "schur (k_schur_off + k_schur_diag + k_schur_reduce), per trial",
-                     "bound": "hbm", "achieved": achieved_gbs, "peak": peak_gbs, "unit": "GB/s",
-                     "frac": achieved_gbs / peak_gbs, "peak_source": peak_kind, "traffic": None,
-                     "algorithmic_bytes": schur_bytes(sc), "avg_ms": schur_avg_s * 1e3,
-                     "fp64": {"achieved_tflops": fp64_achieved, "peak_tflops": fp64_peak,
-                              "frac": fp64_achieved / fp64_peak, "flops": schur_flops(cfg),
-                              "peak_source": "measured FP64 FMA kernel (psba_measure_peak)"}},
+        "roofline": {"kernel": "k_chol_dataflow: Cholesky of S + mu I and both triangular solves, "
+                               "one launch per LM trial, N = %d" % Np,
+                     "bound": "fp64", "achieved": chol_flops / chol_avg_s / 1e12, "peak": fp64_peak,
+                     "unit": "TFLOP/s", "frac": chol_flops / chol_avg_s / 1e12 / fp64_peak,
+                     "peak_source": "measured FP64 FMA rate (psba_measure_peak); MEASURED_PEAKS.json "
+                                    "carries no FP64 figure",
+                     "traffic": CHOL_TRAFFIC, "algorithmic_flops": chol_flops, "avg_ms": chol_avg_s * 1e3,
+                     "hbm": {"achieved": chol_bytes / chol_avg_s / 1e9, "peak": peak_gbs, "unit": "GB/s",
+                             "frac": chol_bytes / chol_avg_s / 1e9 / peak_gbs, "algorithmic_bytes": chol_bytes,
+                             "peak_source": peak_kind}},
+        "roofline_schur": {"kernel": "schur (k_schur_off + k_schur_diag + k_schur_reduce), per trial",
+                           "bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                           "frac": fp64_achieved / fp64_peak, "flops": schur_flops(cfg),
+                           "traffic": SCHUR_OFF_TRAFFIC, "traffic_kernel": "k_schur_off",
+                           "avg_ms": schur_avg_s * 1e3,
+                           "hbm": {"achieved": achieved_gbs, "peak": peak_gbs, "unit": "GB/s",
+                                   "frac": achieved_gbs / peak_gbs, "algorithmic_bytes": schur_bytes(sc),
+                                   "peak_source": peak_kind}},
         "stage_ms": stage_ms, "mixed": mixed,
         "stage_share": {k: (v[0] / total_stage if total_stage else 0.0) for k, v in stages.items()},
         "clocks": clk, "gpu_launches": int(launches),
@@ -460,6 +516,8 @@ def main():
             "cost_after_sample": r.final_cost, "gpu_cost_after_sample": g.final_cost,
             "cost_rel_diff": abs(g.final_cost - r.final_cost) / r.final_cost,
         }
+    if rank == 0 and args.varcam_iters > 0:
+        line["variable_intrinsics"] = varcam_leg(P, args)
     if rank == 0 and args.batch > 0:
         line["batched"] = batched_leg(P, args)
     if rank == 0 and args.serve_rates.strip() not in ("", "none"):

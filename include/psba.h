@@ -65,8 +65,9 @@ extern "C" {
 
 /* precision of the per-observation stages */
 #define PSBA_PREC_FP64 0  /* every stage in FP64 */
-#define PSBA_PREC_MIXED 1 /* Jacobian, residual, W, V^-1, Y in FP32; Schur accumulation,
-                             Cholesky, damping and gain ratio in FP64 */
+#define PSBA_PREC_MIXED 1 /* Jacobian, residual, W, Y stored in FP32 (the projection itself
+                             is evaluated in FP64); V, V^-1, the gradient, the Schur
+                             accumulation, Cholesky, damping and gain ratio in FP64 */
 
 typedef struct psba_handle psba_handle;
 
@@ -74,13 +75,30 @@ typedef struct {
     int n_cams;
     int n_pts;
     int n_obs;
-    const double *K;    /* 5 * n_cams */
+    const double *K;    /* 5 * n_cams: fx, cx, cy, aspect, skew; unused (may be NULL) when cnp > 6 */
     const double *q0;   /* 4 * n_cams */
-    const double *cams; /* 6 * n_cams */
+    const double *cams; /* cnp * n_cams */
     const double *pts;  /* 3 * n_pts */
     const double *meas; /* 2 * n_obs */
     const int *obs_pt;  /* n_obs, non-decreasing */
     const int *obs_cam; /* n_obs, increasing within a point */
+    /* Parameters per camera.  0 or 6: quaternion vector part and translation,
+     * intrinsics fixed from K (the reference's only model, CL_files/PSBA.cl:5).
+     * 11: followed by the intrinsics fx, cx, cy, aspect, skew (the sba
+     * variable-K camera files, data/7camsvarK.txt).  16: followed further by
+     * the distortion k1, k2, p1, p2, k3 (data/54camsvarKD.txt).  The 11- and
+     * 16-parameter models have no reference kernels; the trust-region entry
+     * points and the batched / serving engines take 6-parameter cameras. */
+    int cnp;
+    /* Optional (NULL: unweighted): per observation the 2x2 covariance of the
+     * image measurement, row-major (4 values, symmetric positive definite),
+     * as the reference's reader parses it (PSBA/readparams.cpp:272-282,
+     * 380-412) and its solver ignores (PSBA/main.cpp:112-113).  Residuals and
+     * Jacobian rows are whitened by the upper Cholesky factor L of the
+     * inverse covariance (L^T L = cov^-1), so the cost is sum e^T cov^-1 e.
+     * psba_create only; the batched / serving engines take unweighted
+     * problems. */
+    const double *cov;
 } psba_problem_desc;
 
 typedef struct {
@@ -247,7 +265,13 @@ size_t psba_batch_device_bytes(psba_batch *b);
 
 /* ---- serving: continuous batching of solve requests -------------------- */
 
-/* A server owns one HBM pool of hbm_budget_bytes and a worker thread.
+/* A server owns one HBM pool and a worker thread (the batch lane), plus
+ * large_lanes threads (the large lane).  Requests with more than large_cams
+ * cameras go to the large lane: each is solved by the single-problem engine
+ * (psba_create / psba_levmar: multi-CTA kernels and the dataflow Cholesky
+ * over the whole GPU) on its own stream, concurrently with the batch lane;
+ * its device memory counts against large_share of the budget.  The rest of
+ * the budget is the batch lane's pool.
  * psba_batch_submit lays a request out on the calling thread and queues it;
  * the worker admits queued requests in arrival order while a resident slot is
  * free and the request fits the pool, and advances all resident problems
@@ -264,12 +288,14 @@ size_t psba_batch_device_bytes(psba_batch *b);
 typedef struct psba_server psba_server;
 
 typedef struct psba_server_opts {
-    double hbm_budget_bytes; /* pool for resident problems (default 120e9) */
-    int max_active;          /* resident problems at once (default 1024) */
+    double hbm_budget_bytes; /* all device memory the server may hold for requests (default 120e9) */
+    int max_active;          /* resident problems of the batch lane at once (default 1024) */
     int slice_iters;         /* outer LM iterations of the heaviest problem per launch (default 1) */
     int threads;             /* CTA size of the persistent launch: 128, 256, 512 (default 256) */
     int lanes_per_pair;      /* lanes per camera pair in the Schur stage: 8, 16, 32 (default 32) */
-    int reserved[4];
+    int large_cams;          /* requests with more cameras run on the large lane (default 40; 0: no large lane) */
+    int large_lanes;         /* large-lane host threads, each solving one request at a time (default 2) */
+    double large_share;      /* share of hbm_budget_bytes reserved for the large lane (default 0.25) */
 } psba_server_opts;
 
 typedef struct psba_request_result {

@@ -21,7 +21,7 @@ _ip = C.POINTER(C.c_int)
 
 class Problem(C.Structure):
     _fields_ = [("nc", C.c_int), ("np", C.c_int), ("no", C.c_int), ("K", _dp), ("q0", _dp),
-                ("meas", _dp), ("obs_pt", _ip), ("obs_cam", _ip), ("cnp", C.c_int)]
+                ("meas", _dp), ("obs_pt", _ip), ("obs_cam", _ip), ("cnp", C.c_int), ("wt", _dp)]
 
 
 class Opts(C.Structure):
@@ -100,6 +100,17 @@ def _f64(a):
     return np.ascontiguousarray(a, dtype=np.float64)
 
 
+def whitening(cov):
+    """Per observation (a, b, c) of the upper factor L = [[a, b], [0, c]]
+    with L^T L = cov^-1, for (O, 2, 2) covariances."""
+    cov = np.asarray(cov, dtype=np.float64).reshape(-1, 2, 2)
+    det = cov[:, 0, 0] * cov[:, 1, 1] - cov[:, 0, 1] * cov[:, 1, 0]
+    p, q, r = cov[:, 1, 1] / det, -cov[:, 0, 1] / det, cov[:, 0, 0] / det
+    a = np.sqrt(p)
+    b = q / a
+    return np.ascontiguousarray(np.stack([a, b, np.sqrt(r - b * b)], axis=1))
+
+
 class OracleProblem:
     """Keeps the scene arrays alive for the C problem struct."""
 
@@ -111,8 +122,11 @@ class OracleProblem:
         self.obs_cam = np.ascontiguousarray(scene.obs_cam, dtype=np.int32)
         self.nc, self.np_, self.no = scene.n_cams, scene.n_pts, scene.n_obs
         self.cnp = int(getattr(scene, "cnp", 6))
+        cov = getattr(scene, "cov", None)
+        self.wt = None if cov is None else whitening(cov)
         self.c = Problem(self.nc, self.np_, self.no, _d(self.K), _d(self.q0), _d(self.meas),
-                         _i(self.obs_pt), _i(self.obs_cam), self.cnp)
+                         _i(self.obs_pt), _i(self.obs_cam), self.cnp,
+                         None if self.wt is None else _d(self.wt))
 
     @property
     def ref(self):

@@ -218,8 +218,15 @@ void orc_residual(const orc_problem *p, const double *cams, const double *pts, d
             compose_quat(p->q0 + 4 * j, cams + CNP * j, q);
             project(p->K + 5 * j, q, cams + CNP * j + 3, pts + PNP * i, xy, Xc);
         }
-        ex[2 * o] = p->meas[2 * o] - xy[0];
-        ex[2 * o + 1] = p->meas[2 * o + 1] - xy[1];
+        double e0 = p->meas[2 * o] - xy[0], e1 = p->meas[2 * o + 1] - xy[1];
+        if (p->wt) {
+            const double *w = p->wt + 3 * (size_t)o;
+            double t0 = w[0] * e0 + w[1] * e1;
+            e1 = w[2] * e1;
+            e0 = t0;
+        }
+        ex[2 * o] = e0;
+        ex[2 * o + 1] = e1;
     }
 }
 
@@ -424,12 +431,24 @@ void orc_jacobian(const orc_problem *p, const double *cams, const double *pts, d
 #pragma omp parallel for schedule(static)
     for (int o = 0; o < p->no; ++o) {
         int i = p->obs_pt[o], j = p->obs_cam[o];
+        double *A = JA + 2 * (size_t)cnp * o, *B = JB + 6 * (size_t)o;
         if (cnp > 6)
-            jac_one_v(p->q0 + 4 * j, cams + (size_t)cnp * j, cnp, pts + PNP * i, JA + 2 * (size_t)cnp * o,
-                      JB + 6 * (size_t)o);
+            jac_one_v(p->q0 + 4 * j, cams + (size_t)cnp * j, cnp, pts + PNP * i, A, B);
         else
-            jac_one(p->K + 5 * j, p->q0 + 4 * j, cams + CNP * j, pts + PNP * i, JA + 12 * (size_t)o,
-                    JB + 6 * (size_t)o);
+            jac_one(p->K + 5 * j, p->q0 + 4 * j, cams + CNP * j, pts + PNP * i, A, B);
+        if (p->wt) {  /* rows <- L rows */
+            const double *w = p->wt + 3 * (size_t)o;
+            for (int m = 0; m < cnp; ++m) {
+                double a0 = A[m], a1 = A[cnp + m];
+                A[m] = w[0] * a0 + w[1] * a1;
+                A[cnp + m] = w[2] * a1;
+            }
+            for (int m = 0; m < PNP; ++m) {
+                double b0 = B[m], b1 = B[PNP + m];
+                B[m] = w[0] * b0 + w[1] * b1;
+                B[PNP + m] = w[2] * b1;
+            }
+        }
     }
 }
 
@@ -910,12 +929,7 @@ void orc_jmultiply(const orc_problem *p, const double *JA, const double *JB, con
             const double *xa = x + (size_t)j * cnp;
             const double *xb = x + ncp + (size_t)i * PNP;
             double sum = 0;
-            sum += a[0] * xa[0];
-            sum += a[1] * xa[1];
-            sum += a[2] * xa[2];
-            sum += a[3] * xa[3];
-            sum += a[4] * xa[4];
-            sum += a[5] * xa[5];
+            for (int m = 0; m < cnp; ++m) sum += a[m] * xa[m];
             sum += b[0] * xb[0];
             sum += b[1] * xb[1];
             sum += b[2] * xb[2];

@@ -66,6 +66,9 @@ typedef struct {
     const int *obs_pt;
     const int *obs_cam;
     int cnp;              /* parameters per camera: 6 (0 means 6), 11, 16 */
+    const double *wt;     /* NULL, or per observation a, b, c of the upper factor
+                             L = [[a, b], [0, c]] with L^T L = cov^-1: residual and
+                             Jacobian rows are whitened, e <- L e, J <- L J */
 } orc_problem;
 
 typedef struct {

@@ -35,7 +35,8 @@ _ip = C.POINTER(C.c_int)
 
 class ProblemDesc(C.Structure):
     _fields_ = [("n_cams", C.c_int), ("n_pts", C.c_int), ("n_obs", C.c_int), ("K", _dp), ("q0", _dp),
-                ("cams", _dp), ("pts", _dp), ("meas", _dp), ("obs_pt", _ip), ("obs_cam", _ip)]
+                ("cams", _dp), ("pts", _dp), ("meas", _dp), ("obs_pt", _ip), ("obs_cam", _ip),
+                ("cnp", C.c_int), ("cov", _dp)]
 
 
 class Opts(C.Structure):
@@ -177,12 +178,17 @@ class Solver:
     def __init__(self, scene):
         L = lib()
         self.nc, self.np_, self.no = scene.n_cams, scene.n_pts, scene.n_obs
+        self.cnp = int(getattr(scene, "cnp", 6))
         self._keep = [_f64(scene.K), _f64(scene.q0), _f64(scene.cams), _f64(scene.pts), _f64(scene.meas),
                       np.ascontiguousarray(scene.obs_pt, dtype=np.int32),
                       np.ascontiguousarray(scene.obs_cam, dtype=np.int32)]
         K, q0, cams, pts, meas, opt, ocam = self._keep
+        cov = getattr(scene, "cov", None)
+        cov = None if cov is None else _f64(cov).reshape(-1, 2, 2)
+        self._keep.append(cov)
         desc = ProblemDesc(self.nc, self.np_, self.no, _d(K), _d(q0), _d(cams), _d(pts), _d(meas),
-                           opt.ctypes.data_as(_ip), ocam.ctypes.data_as(_ip))
+                           opt.ctypes.data_as(_ip), ocam.ctypes.data_as(_ip), self.cnp,
+                           None if cov is None else _d(cov))
         h = C.c_void_p()
         _check(L.psba_create(C.byref(desc), C.byref(h)))
         self.h = h
@@ -207,11 +213,11 @@ class Solver:
 
     @property
     def N(self):
-        return 6 * self.nc
+        return self.cnp * self.nc
 
     @property
     def n_params(self):
-        return 6 * self.nc + 3 * self.np_
+        return self.cnp * self.nc + 3 * self.np_
 
     def device_bytes(self):
         return lib().psba_device_bytes(self.h)
@@ -236,7 +242,7 @@ class Solver:
         return lib().psba_stream(self.h)
 
     def get_params(self):
-        cams = np.empty((self.nc, 6))
+        cams = np.empty((self.nc, self.cnp))
         pts = np.empty((self.np_, 3))
         _check(lib().psba_get_params(self.h, _d(cams), _d(pts)))
         return cams, pts
@@ -283,22 +289,22 @@ class Solver:
         return ex, cost.value
 
     def eval_jacobian(self):
-        JA = np.empty((self.no, 2, 6))
+        JA = np.empty((self.no, 2, self.cnp))
         JB = np.empty((self.no, 2, 3))
         _check(lib().psba_eval_jacobian(self.h, _d(JA), _d(JB)))
         return JA, JB
 
     def eval_normal(self, coeff=1.0):
-        U = np.empty((self.nc, 6, 6))
+        U = np.empty((self.nc, self.cnp, self.cnp))
         V = np.empty((self.np_, 3, 3))
-        W = np.empty((self.no, 6, 3))
+        W = np.empty((self.no, self.cnp, 3))
         g = np.empty(self.n_params)
         _check(lib().psba_eval_normal(self.h, float(coeff), _d(U), _d(V), _d(W), _d(g)))
         return U, V, W, g
 
     def eval_reduced(self, mu):
         Vinv = np.empty((self.np_, 3, 3))
-        Y = np.empty((self.no, 6, 3))
+        Y = np.empty((self.no, self.cnp, 3))
         S = np.empty((self.N, self.N))
         ea = np.empty(self.N)
         _check(lib().psba_eval_reduced(self.h, float(mu), _d(Vinv), _d(Y), _d(S), _d(ea)))

@@ -698,6 +698,14 @@ __global__ void __launch_bounds__(MAX_THREADS) k_batch_lm(const BatchProblem *__
 
 bool build_problem_layout(const psba_problem_desc &p, ProblemLayout &L, std::string &err)
 {
+    if (p.cnp != 0 && p.cnp != 6) {
+        err = "the batched engine takes 6-parameter cameras (cnp 0 or 6)";
+        return false;
+    }
+    if (p.cov) {
+        err = "the batched engine takes unweighted problems (cov must be NULL)";
+        return false;
+    }
     if (p.n_cams <= 0 || p.n_pts < 0 || p.n_obs < 0 || !p.K || !p.q0 || !p.cams || (p.n_pts && !p.pts) ||
         (p.n_obs && (!p.meas || !p.obs_pt || !p.obs_cam))) {
         err = "problem is malformed";

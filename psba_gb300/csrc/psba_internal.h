@@ -16,7 +16,7 @@ namespace psba {
 constexpr int CNP = 6;   // camera parameters (rotation vector part + translation)
 constexpr int PNP = 3;   // point parameters
 constexpr int MNP = 2;   // image coordinates
-constexpr int CAMTAB = 48;  // doubles per camera table entry (CamTab)
+constexpr int CAMTAB = 56;  // doubles per camera table entry (CamTab)
 constexpr int TILE = 16;    // dense Cholesky tile size
 constexpr int SCHUR_CHUNK = 32;  // pair-list entries per off-diagonal Schur work unit
 constexpr int DIAG_CHUNK = 16;   // observations per diagonal Schur work unit
@@ -31,7 +31,9 @@ struct CamTab {
     double D[27];
     double t[3];
     double fx, sk, cx, fy, cy;  // fy = fx * aspect
-    double pad[4];
+    double ar;                  // aspect (variable intrinsics)
+    double kc[5];               // k1, k2, p1, p2, k3 (16-parameter cameras; zero otherwise)
+    double pad[6];
 };
 static_assert(sizeof(CamTab) == CAMTAB * sizeof(double), "CamTab layout");
 
@@ -72,10 +74,12 @@ long long launch_count();
 // ---- kernel launchers (psba_kernels.cu) ---------------------------------
 
 struct DeviceProblem {
-    int nc = 0, np = 0, no = 0, N = 0, Np = 0;  // N = 6 nc, Np = N padded to TILE
+    int nc = 0, np = 0, no = 0, N = 0, Np = 0;  // N = cnp nc, Np = N padded to TILE
+    int cnp = 6;                // parameters per camera: 6, 11 or 16
     int prec = PSBA_PREC_FP64;  // storage of the per-observation / per-point arrays (double or float)
     // problem (immutable)
     double *K = nullptr, *q0 = nullptr, *meas = nullptr;
+    double *wt = nullptr;      // 3 per obs (a, b, c of L = [[a, b], [0, c]]), or null: unweighted
     int *obs_pt = nullptr, *obs_cam = nullptr;
     int *pt_start = nullptr;   // np + 1
     int *cam_obs = nullptr;    // observations sorted by (camera, point)
@@ -180,6 +184,20 @@ void launch_scale(double *out, const double *x, const double *num, const double 
 // solve into xsol; mode 1 solves again with the existing factor.  One
 // cooperative launch; epoch must increase from launch to launch.
 void launch_chol_dataflow(const DeviceProblem &d, int mode, int epoch, double *x_out, cudaStream_t s);
+
+// variable intrinsics (cnp 11 / 16), psba_varcam.cu
+size_t varcam_cam_partial(int cnp);   // doubles per camera-unit partial
+size_t varcam_diag_partial(int cnp);  // doubles per diagonal Schur-unit partial
+void launch_linearize_v(const DeviceProblem &d, double coeff, cudaStream_t s);
+void launch_camera_blocks_v(const DeviceProblem &d, double coeff, cudaStream_t s);
+void launch_yblocks_v(const DeviceProblem &d, cudaStream_t s);
+void launch_schur_off_v(const DeviceProblem &d, cudaStream_t s);
+void launch_schur_diag_v(const DeviceProblem &d, cudaStream_t s);
+void launch_schur_reduce_v(const DeviceProblem &d, double mu, cudaStream_t s);
+void launch_eb_dpb_v(const DeviceProblem &d, double mu, int nblocks, cudaStream_t s);
+void launch_jmultiply_v(const DeviceProblem &d, const double *x, double *out, cudaStream_t s);
+void launch_residual_dist(const DeviceProblem &d, const double *tab, const double *pts, const double *dpb,
+                          double *ex_out, double *partial, int nblocks, cudaStream_t s);
 // One step of iterative refinement of S x = rhs_save with the factor in S/Linv
 // and the original matrix in Ssave (mixed precision); updates xsol.
 void launch_refine(const DeviceProblem &d, int epoch, cudaStream_t s);

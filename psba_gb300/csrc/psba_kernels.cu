@@ -61,16 +61,21 @@ constexpr int FLUSH = 8;
 // ---------------------------------------------------------------------------
 // Camera tables.  q = q(v) (x) q0 (compute_exQT.cl:82-87), M = matrix of
 // X -> q (0,X) conj(q), D[m] = dM/dv_m through q(v) with s = sqrt(1-|v|^2).
-__global__ void k_cam_tables(int nc, const double *__restrict__ K, const double *__restrict__ q0,
+// With cnp > 6 the intrinsics (fx, cx, cy, ar, skew) and, for cnp 16, the
+// distortion (k1, k2, p1, p2, k3) are parameters 6.. of the camera, moved by
+// dpa like the pose; with cnp 6 they come from the fixed K array.
+__global__ void k_cam_tables(int nc, int cnp, const double *__restrict__ K, const double *__restrict__ q0,
                              const double *__restrict__ cams, const double *__restrict__ dpa,
                              double *__restrict__ tab)
 {
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= nc) return;
+    const double *cj = cams + (size_t)cnp * j;
+    const double *dj = dpa ? dpa + (size_t)cnp * j : nullptr;
     double vl[3], t[3];
     for (int m = 0; m < 3; ++m) {
-        vl[m] = dpa ? cams[6 * j + m] + dpa[6 * j + m] : cams[6 * j + m];
-        t[m] = dpa ? cams[6 * j + 3 + m] + dpa[6 * j + 3 + m] : cams[6 * j + 3 + m];
+        vl[m] = dj ? cj[m] + dj[m] : cj[m];
+        t[m] = dj ? cj[3 + m] + dj[3 + m] : cj[3 + m];
     }
     const double s0 = q0[4 * j], a1 = q0[4 * j + 1], a2 = q0[4 * j + 2], a3 = q0[4 * j + 3];
     const double sl = sqrt(1.0 - vl[0] * vl[0] - vl[1] * vl[1] - vl[2] * vl[2]);
@@ -103,9 +108,18 @@ __global__ void k_cam_tables(int nc, const double *__restrict__ K, const double 
             T.D[9 * m + e] = dS[e] * dq0 + dA[e] * dqv[0] + dB[e] * dqv[1] + dC[e] * dqv[2];
     }
     T.t[0] = t[0]; T.t[1] = t[1]; T.t[2] = t[2];
-    const double *k = K + 5 * j;
-    T.fx = k[0]; T.cx = k[1]; T.cy = k[2]; T.fy = k[0] * k[3]; T.sk = k[4];
-    T.pad[0] = T.pad[1] = T.pad[2] = T.pad[3] = 0.0;
+    double kk[5], kc[5] = {0, 0, 0, 0, 0};
+    if (cnp > 6) {
+        for (int m = 0; m < 5; ++m) kk[m] = dj ? cj[6 + m] + dj[6 + m] : cj[6 + m];
+        if (cnp == 16)
+            for (int m = 0; m < 5; ++m) kc[m] = dj ? cj[11 + m] + dj[11 + m] : cj[11 + m];
+    } else {
+        for (int m = 0; m < 5; ++m) kk[m] = K[5 * j + m];
+    }
+    T.fx = kk[0]; T.cx = kk[1]; T.cy = kk[2]; T.fy = kk[0] * kk[3]; T.sk = kk[4];
+    T.ar = kk[3];
+    for (int m = 0; m < 5; ++m) T.kc[m] = kc[m];
+    for (int m = 0; m < 6; ++m) T.pad[m] = 0.0;
     double *o = tab + (size_t)CAMTAB * j;
     const double *src = reinterpret_cast<const double *>(&T);
     for (int e = 0; e < CAMTAB; ++e) o[e] = src[e];
@@ -114,7 +128,7 @@ __global__ void k_cam_tables(int nc, const double *__restrict__ K, const double 
 void launch_cam_tables(const DeviceProblem &d, const double *cams, const double *dpa, double *tab,
                        cudaStream_t s)
 {
-    k_cam_tables<<<ceil_div(d.nc, 128), 128, 0, s>>>(d.nc, d.K, d.q0, cams, dpa, tab); note_launch(1);
+    k_cam_tables<<<ceil_div(d.nc, 128), 128, 0, s>>>(d.nc, d.cnp, d.K, d.q0, cams, dpa, tab); note_launch(1);
 }
 
 // ---------------------------------------------------------------------------
@@ -128,6 +142,7 @@ __global__ void __launch_bounds__(256) k_linearize(int no, const int *__restrict
                                                    const double *__restrict__ meas,
                                                    const double *__restrict__ pts,
                                                    const double *__restrict__ tab, R coeff,
+                                                   const double *__restrict__ wt,
                                                    R *__restrict__ ex, R *__restrict__ A,
                                                    R *__restrict__ B, R *__restrict__ W)
 {
@@ -153,7 +168,16 @@ __global__ void __launch_bounds__(256) k_linearize(int no, const int *__restrict
     const double nud = fxd * xcd + skd * ycd;
     const double u = (nud + cxd * zcd) * izd;
     const double v = (fyd * ycd + cyd * zcd) * izd;
-    st2<R>(ex + 2 * (size_t)o, (R)(m2.x - u), (R)(m2.y - v));
+    double e0 = m2.x - u, e1 = m2.y - v, wa = 1.0, wb = 0.0, wc = 1.0;
+    if (wt) {  // whitening: e <- L e, J rows <- L J
+        wa = __ldg(wt + 3 * (size_t)o);
+        wb = __ldg(wt + 3 * (size_t)o + 1);
+        wc = __ldg(wt + 3 * (size_t)o + 2);
+        const double t0 = wa * e0 + wb * e1;
+        e1 = wc * e1;
+        e0 = t0;
+    }
+    st2<R>(ex + 2 * (size_t)o, (R)e0, (R)e1);
     const R X0 = (R)Xd0, X1 = (R)Xd1, X2 = (R)Xd2;
     R M[9];
 #pragma unroll
@@ -181,6 +205,21 @@ __global__ void __launch_bounds__(256) k_linearize(int no, const int *__restrict
         bb[m] = p00 * M[m] + p01 * M[3 + m] + p02 * M[6 + m];
         bb[3 + m] = p11 * M[3 + m] + p12 * M[6 + m];
     }
+    if (wt) {
+        const R ra = (R)wa, rb = (R)wb, rc = (R)wc;
+#pragma unroll
+        for (int m = 0; m < 6; ++m) {
+            const R a0 = a[m], a1 = a[6 + m];
+            a[m] = ra * a0 + rb * a1;
+            a[6 + m] = rc * a1;
+        }
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+            const R b0 = bb[m], b1 = bb[3 + m];
+            bb[m] = ra * b0 + rb * b1;
+            bb[3 + m] = rc * b1;
+        }
+    }
     stn<R, 12>(A + 12 * (size_t)o, a);
     stn<R, 6>(B + 6 * (size_t)o, bb);
     R w[18];
@@ -193,13 +232,14 @@ __global__ void __launch_bounds__(256) k_linearize(int no, const int *__restrict
 
 void launch_linearize(const DeviceProblem &d, double coeff, cudaStream_t s)
 {
+    if (d.cnp != 6) return launch_linearize_v(d, coeff, s);
     if (d.no == 0) return;
     if (d.prec == PSBA_PREC_FP64) {
         k_linearize<double><<<ceil_div(d.no, 256), 256, 0, s>>>(d.no, d.obs_pt, d.obs_cam, d.meas, d.pts,
-                                                                  d.camtab, coeff, d.ex, d.A, d.B, d.W);
+                                                                  d.camtab, coeff, d.wt, d.ex, d.A, d.B, d.W);
     } else {
         k_linearize<float><<<ceil_div(d.no, 256), 256, 0, s>>>(
-            d.no, d.obs_pt, d.obs_cam, d.meas, d.pts, d.camtab, (float)coeff, (float *)d.ex, (float *)d.A,
+            d.no, d.obs_pt, d.obs_cam, d.meas, d.pts, d.camtab, (float)coeff, d.wt, (float *)d.ex, (float *)d.A,
             (float *)d.B, (float *)d.W);
     }
     note_launch(1);
@@ -213,6 +253,7 @@ __global__ void __launch_bounds__(256) k_residual(int no, const int *__restrict_
                                                   const double *__restrict__ pts,
                                                   const double *__restrict__ dpb,
                                                   const double *__restrict__ tab,
+                                                  const double *__restrict__ wt,
                                                   double *__restrict__ ex_out,
                                                   double *__restrict__ partial)
 {
@@ -233,7 +274,12 @@ __global__ void __launch_bounds__(256) k_residual(int no, const int *__restrict_
         const double u = (__ldg(T + 39) * xc + __ldg(T + 40) * yc + __ldg(T + 41) * zc) * iz;
         const double v = (__ldg(T + 42) * yc + __ldg(T + 43) * zc) * iz;
         const double2 m2 = *reinterpret_cast<const double2 *>(meas + 2 * (size_t)o);
-        const double e0 = m2.x - u, e1 = m2.y - v;
+        double e0 = m2.x - u, e1 = m2.y - v;
+        if (wt) {
+            const double t0 = wt[3 * (size_t)o] * e0 + wt[3 * (size_t)o + 1] * e1;
+            e1 = wt[3 * (size_t)o + 2] * e1;
+            e0 = t0;
+        }
         if (ex_out) *reinterpret_cast<double2 *>(ex_out + 2 * (size_t)o) = make_double2(e0, e1);
         sq = e0 * e0 + e1 * e1;
     }
@@ -251,7 +297,8 @@ int residual_blocks(const DeviceProblem &d) { return ceil_div(d.no > 0 ? d.no : 
 void launch_residual(const DeviceProblem &d, const double *tab, const double *pts, const double *dpb,
                      double *ex_out, double *partial, int nblocks, cudaStream_t s)
 {
-    k_residual<<<nblocks, 256, 0, s>>>(d.no, d.obs_pt, d.obs_cam, d.meas, pts, dpb, tab, ex_out,
+    if (d.cnp == 16) return launch_residual_dist(d, tab, pts, dpb, ex_out, partial, nblocks, s);
+    k_residual<<<nblocks, 256, 0, s>>>(d.no, d.obs_pt, d.obs_cam, d.meas, pts, dpb, tab, d.wt, ex_out,
                                         partial); note_launch(1);
 }
 
@@ -409,6 +456,7 @@ __global__ void k_camera_finish(int nc, const int *__restrict__ unit_start,
 
 void launch_camera_blocks(const DeviceProblem &d, double coeff, cudaStream_t s)
 {
+    if (d.cnp != 6) return launch_camera_blocks_v(d, coeff, s);
     if (d.n_cam_units > 0) {
         if (d.prec == PSBA_PREC_FP64)
             k_camera_partial<double><<<d.n_cam_units, CAM_THREADS, 0, s>>>(d.cam_units, d.cam_obs, d.A, d.ex,
@@ -518,6 +566,7 @@ __global__ void __launch_bounds__(256) k_yblocks(int no, const int *__restrict__
 
 void launch_yblocks(const DeviceProblem &d, cudaStream_t s)
 {
+    if (d.cnp != 6) return launch_yblocks_v(d, s);
     if (d.no == 0) return;
     if (d.prec == PSBA_PREC_FP64)
         k_yblocks<double><<<ceil_div(d.no, 256), 256, 0, s>>>(d.no, d.obs_pt, d.W, d.Vinv, d.Y);
@@ -598,8 +647,12 @@ __global__ void __launch_bounds__(128) k_schur_off(int n_units, const SchurUnit 
 
 constexpr int DIAG_NV = 27;  // 21 lower entries + 6 ea sums
 
+// The 21 lower entries of Y W^T into acc (R); the 6 sums of Y gb into eacc
+// in FP64 from the exact products in both forms: ea = ga - sum Y gb cancels
+// near the optimum, where the step is set by it.
 template <typename R>
-__device__ __forceinline__ void diag_products(const R *y, const R *w, R g0, R g1, R g2, R *acc)
+__device__ __forceinline__ void diag_products(const R *y, const R *w, double g0, double g1, double g2, R *acc,
+                                              double *eacc)
 {
     int v = 0;
 #pragma unroll
@@ -614,11 +667,11 @@ __device__ __forceinline__ void diag_products(const R *y, const R *w, R g0, R g1
         }
 #pragma unroll
     for (int r = 0; r < 6; ++r) {
-        R s = acc[21 + r];
-        s = fma(y[3 * r], g0, s);
-        s = fma(y[3 * r + 1], g1, s);
-        s = fma(y[3 * r + 2], g2, s);
-        acc[21 + r] = s;
+        double s = eacc[r];
+        s = fma((double)y[3 * r], g0, s);
+        s = fma((double)y[3 * r + 1], g1, s);
+        s = fma((double)y[3 * r + 2], g2, s);
+        eacc[r] = s;
     }
 }
 
@@ -638,9 +691,9 @@ __global__ void __launch_bounds__(128) k_schur_diag(int n_units, const SchurUnit
 #pragma unroll
     for (int e = 0; e < DIAG_NV; ++e) acc[e] = 0.0;
     for (int t0 = 0; t0 < u.count; t0 += FLUSH) {
-        R part[DIAG_NV];
+        R part[21];
 #pragma unroll
-        for (int e = 0; e < DIAG_NV; ++e) part[e] = (R)0;
+        for (int e = 0; e < 21; ++e) part[e] = (R)0;
         const int tend = min(u.count, t0 + FLUSH);
         for (int t = t0; t < tend; ++t) {
             const int a = __ldg(cam_obs + u.begin + t);
@@ -648,12 +701,12 @@ __global__ void __launch_bounds__(128) k_schur_diag(int n_units, const SchurUnit
             R w[18], y[18];
             ldn<R, 18>(W + 18 * (size_t)a, w);
             ldn<R, 18>(Y + 18 * (size_t)a, y);
-            const R g0 = (R)__ldg(gb + 3 * (size_t)i), g1 = (R)__ldg(gb + 3 * (size_t)i + 1),
-                    g2 = (R)__ldg(gb + 3 * (size_t)i + 2);
-            diag_products<R>(y, w, g0, g1, g2, part);
+            const double g0 = __ldg(gb + 3 * (size_t)i), g1 = __ldg(gb + 3 * (size_t)i + 1),
+                         g2 = __ldg(gb + 3 * (size_t)i + 2);
+            diag_products<R>(y, w, g0, g1, g2, part, acc + 21);
         }
 #pragma unroll
-        for (int e = 0; e < DIAG_NV; ++e) acc[e] += (double)part[e];
+        for (int e = 0; e < 21; ++e) acc[e] += (double)part[e];
     }
     double *p = partial + (size_t)u.out * DIAG_NV;
 #pragma unroll
@@ -711,6 +764,7 @@ __global__ void k_pad_identity(int N, int Np, double *S, double *rhs)
 
 void launch_schur_off(const DeviceProblem &d, cudaStream_t s)
 {
+    if (d.cnp != 6) return launch_schur_off_v(d, s);
     if (d.n_off_units == 0) return;
     if (d.prec == PSBA_PREC_FP64)
         k_schur_off<double><<<ceil_div(d.n_off_units, 128), 128, 0, s>>>(d.n_off_units, d.off_units, d.pair_a,
@@ -724,6 +778,7 @@ void launch_schur_off(const DeviceProblem &d, cudaStream_t s)
 
 void launch_schur_diag(const DeviceProblem &d, cudaStream_t s)
 {
+    if (d.cnp != 6) return launch_schur_diag_v(d, s);
     double *diag_partial = d.schur_partial + (size_t)d.n_off_units * 36;
     if (d.n_diag_units == 0) return;
     if (d.prec == PSBA_PREC_FP64)
@@ -739,6 +794,14 @@ void launch_schur_diag(const DeviceProblem &d, cudaStream_t s)
 void launch_schur_reduce(const DeviceProblem &d, double mu, cudaStream_t s)
 {
     cudaMemsetAsync(d.S, 0, sizeof(double) * (size_t)d.Np * d.Np, s);
+    if (d.cnp != 6) {
+        launch_schur_reduce_v(d, mu, s);
+        if (d.Np > d.N) {
+            k_pad_identity<<<1, TILE, 0, s>>>(d.N, d.Np, d.S, d.rhs);
+            note_launch(1);
+        }
+        return;
+    }
     double *off_partial = d.schur_partial;
     double *diag_partial = d.schur_partial + (size_t)d.n_off_units * 36;
     const int total = d.n_pairs * 36 + d.nc * DIAG_NV;
@@ -826,6 +889,7 @@ int eb_blocks(const DeviceProblem &d) { return ceil_div(d.np > 0 ? d.np : 1, 256
 
 void launch_eb_dpb(const DeviceProblem &d, double mu, cudaStream_t s)
 {
+    if (d.cnp != 6) return launch_eb_dpb_v(d, mu, eb_blocks(d), s);
     if (d.prec == PSBA_PREC_FP64)
         k_eb_dpb<double><<<eb_blocks(d), 256, 0, s>>>(d.np, d.N, d.pt_start, d.obs_cam, d.W, d.Vinv, d.g, mu,
                                                         d.dp, d.eb, d.red_partial);
@@ -986,6 +1050,7 @@ __global__ void k_jmultiply(int no, int ncp, const int *__restrict__ obs_pt,
 
 void launch_jmultiply(const DeviceProblem &d, const double *x, double *out, cudaStream_t s)
 {
+    if (d.cnp != 6) return launch_jmultiply_v(d, x, out, s);
     if (d.no == 0) return;
     if (d.prec == PSBA_PREC_FP64)
         k_jmultiply<double><<<ceil_div(d.no, 256), 256, 0, s>>>(d.no, d.N, d.obs_pt, d.obs_cam, d.A, d.B, x, out);

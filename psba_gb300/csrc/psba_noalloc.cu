@@ -22,14 +22,15 @@
 namespace psba {
 namespace noalloc {
 
-// Limits of the fixed scratch: camera tables (48 doubles per camera) and one
+// Limits of the fixed scratch: camera tables (CAMTAB doubles per camera) and one
 // partial sum per 256 observations.
 constexpr int MAX_CAMS = 1024;
 constexpr long long MAX_OBS = 16LL * 1024 * 1024;
 constexpr int THREADS = 256;
 constexpr size_t TAB_DOUBLES = (size_t)MAX_CAMS * CAMTAB;
 constexpr size_t PARTIAL_DOUBLES = (size_t)(MAX_OBS / THREADS);
-constexpr size_t SCRATCH_DOUBLES = TAB_DOUBLES + PARTIAL_DOUBLES;  // 1 MiB in total
+constexpr size_t SCRATCH_DOUBLES = TAB_DOUBLES + PARTIAL_DOUBLES;  // under 1 MiB in total
+static_assert(SCRATCH_DOUBLES * sizeof(double) <= (1u << 20), "scratch above 1 MiB");
 
 // Every GPU that loads the library holds this array until the process exits.
 static __device__ __align__(256) double g_scratch[SCRATCH_DOUBLES];

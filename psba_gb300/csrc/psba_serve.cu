@@ -16,6 +16,17 @@
 // data and on outer-iteration boundaries, which are where slices cut, so its
 // result is the same bits alone and in any mix.
 //
+// Large requests (more than large_cams cameras) take the large lane instead:
+// large_lanes host threads each solve one request at a time with the
+// single-problem engine (psba_create / psba_levmar on its own stream: kernels
+// over the whole GPU and the cooperative dataflow Cholesky), concurrently
+// with the batch lane's launches, within large_share of the HBM budget; the
+// batch lane's pool is the rest.  One CTA per problem would leave a
+// 138-camera request with an N = 828 FP64 Cholesky on a single SM (~25 ms per
+// trial); the whole GPU factors it in ~2 ms.  A dataflow wait that runs out
+// of budget while the batch lane holds SMs fails that request with an error
+// status (it cannot hang): waits are bounded, and slices end on their own.
+//
 // The per-request solve is levmar() (PSBA/levmar.cpp:45-256); the reference
 // has no serving layer (one problem per process, PSBA/main.cpp:193-208).
 #include <algorithm>
@@ -55,6 +66,13 @@ struct Request {
     Clock::time_point t_submit, t_admit, t_done;
     BatchResult st{};
     std::vector<double> cams, pts;
+    // large lane: a copy of the problem for psba_create, and the outcome
+    bool large = false;
+    int nc = 0, np = 0, no = 0;
+    std::vector<double> hK, hq0, hcams, hpts, hmeas;
+    std::vector<int> hopt, hocam;
+    int err = PSBA_OK;
+    std::string err_msg;
 };
 
 // First-fit allocator over [0, size) in 256-byte units, coalescing on free.
@@ -110,6 +128,7 @@ class PoolAllocator {
 
 struct psba_server {
     psba_server_opts so{};
+    psba_opts lm{};
     BatchOpts bo{};
     int precision = PSBA_PREC_FP64;
     size_t rsize = sizeof(double);
@@ -141,6 +160,12 @@ struct psba_server {
     std::string fail_msg;
     psba_server_stats stats{};
     std::thread worker;
+    // large lane
+    std::condition_variable cv_large;
+    std::deque<Request *> large_queue;
+    size_t large_budget = 0, large_in_use = 0;
+    int n_large = 0;  // large requests being solved
+    std::vector<std::thread> large_workers;
 };
 
 namespace {
@@ -301,6 +326,82 @@ void worker_main(psba_server *s)
     }
 }
 
+// Device bytes of a request on the single-problem engine: the per-observation
+// and per-point arrays in FP64, S and its copy, and the Schur work lists.
+size_t large_bytes(const ProblemLayout &L)
+{
+    const size_t Np = ((size_t)L.bp.N + TILE - 1) / TILE * TILE;
+    return pool_bytes(L, PSBA_PREC_FP64) + 3 * Np * Np * sizeof(double) + ((size_t)16 << 20);
+}
+
+void large_main(psba_server *s)
+{
+    cudaSetDevice(s->device);
+    while (true) {
+        Request *r = nullptr;
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            s->cv_large.wait(lk, [&] {
+                return s->stop ||
+                       (!s->large_queue.empty() && s->large_in_use + s->large_queue.front()->bytes <= s->large_budget);
+            });
+            if (s->stop) break;
+            r = s->large_queue.front();
+            s->large_queue.pop_front();
+            s->large_in_use += r->bytes;
+            r->state = 1;
+            r->t_admit = Clock::now();
+            s->stats.admitted++;
+            s->n_large++;
+        }
+        psba_problem_desc desc{};
+        desc.n_cams = r->nc;
+        desc.n_pts = r->np;
+        desc.n_obs = r->no;
+        desc.K = r->hK.data();
+        desc.q0 = r->hq0.data();
+        desc.cams = r->hcams.data();
+        desc.pts = r->hpts.data();
+        desc.meas = r->hmeas.data();
+        desc.obs_pt = r->hopt.data();
+        desc.obs_cam = r->hocam.data();
+        desc.cnp = 6;
+        psba_handle *h = nullptr;
+        psba_result res{};
+        int itno = 0;
+        int rc = psba_create(&desc, &h);
+        if (rc == PSBA_OK) rc = psba_levmar(h, &s->lm, &itno, &res);
+        r->cams.resize(6 * (size_t)r->nc);
+        r->pts.resize(3 * (size_t)r->np);
+        if (rc == PSBA_OK) rc = psba_get_params(h, r->cams.data(), r->pts.data());
+        const double dev_bytes = h ? (double)psba_device_bytes(h) : 0.0;
+        const std::string msg = rc == PSBA_OK ? std::string() : std::string(psba_last_error());
+        if (h) psba_destroy(h);
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->large_in_use -= r->bytes;
+            s->n_large--;
+            r->st.status = res.status;
+            r->st.iterations = res.iterations;
+            r->st.trials = res.n_trials;
+            r->st.linearizations = res.n_linearizations;
+            r->st.initial_cost = res.initial_cost;
+            r->st.final_cost = res.final_cost;
+            r->err = rc;
+            r->err_msg = msg;
+            if (dev_bytes > 0) r->bytes = (size_t)dev_bytes;
+            r->state = 2;
+            r->t_done = Clock::now();
+            s->stats.finished++;
+            for (std::vector<double> *v : {&r->hK, &r->hq0, &r->hcams, &r->hpts, &r->hmeas}) std::vector<double>().swap(*v);
+            std::vector<int>().swap(r->hopt);
+            std::vector<int>().swap(r->hocam);
+        }
+        s->cv_done.notify_all();
+        s->cv_large.notify_all();
+    }
+}
+
 void server_free(psba_server *s)
 {
     if (!s) return;
@@ -309,7 +410,10 @@ void server_free(psba_server *s)
         s->stop = true;
     }
     s->cv_work.notify_all();
+    s->cv_large.notify_all();
     if (s->worker.joinable()) s->worker.join();
+    for (std::thread &t : s->large_workers)
+        if (t.joinable()) t.join();
     if (s->stream) cudaStreamSynchronize(s->stream);
     cudaFree(s->pool);
     cudaFree(s->d_probs);
@@ -339,6 +443,9 @@ void psba_server_default_opts(psba_server_opts *o)
     o->slice_iters = 1;
     o->threads = 256;
     o->lanes_per_pair = 32;
+    o->large_cams = 40;
+    o->large_lanes = 2;
+    o->large_share = 0.25;
 }
 
 int psba_server_create(const psba_server_opts *so, const psba_opts *lm, psba_server **out)
@@ -347,11 +454,14 @@ int psba_server_create(const psba_server_opts *so, const psba_opts *lm, psba_ser
     *out = nullptr;
     if (so->hbm_budget_bytes < 1e6 || so->max_active < 1 || so->max_active > 65536 || so->slice_iters < 1 ||
         (so->threads != 128 && so->threads != 256 && so->threads != 512) ||
-        (so->lanes_per_pair != 8 && so->lanes_per_pair != 16 && so->lanes_per_pair != 32) ||
+        (so->lanes_per_pair != 8 && so->lanes_per_pair != 16 && so->lanes_per_pair != 32) || so->large_cams < 0 ||
+        so->large_lanes < 0 || so->large_lanes > 16 || !(so->large_share >= 0.0 && so->large_share < 1.0) ||
         (lm->precision != PSBA_PREC_FP64 && lm->precision != PSBA_PREC_MIXED) || lm->max_iter < 0)
         return set_error("psba_server_create: bad options"), PSBA_ERR_ARG;
     psba_server *s = new psba_server();
     s->so = *so;
+    s->lm = *lm;
+    s->lm.allow_switch = 0;
     s->precision = lm->precision;
     s->rsize = lm->precision == PSBA_PREC_MIXED ? sizeof(float) : sizeof(double);
     s->bo.tau = lm->tau;
@@ -360,7 +470,9 @@ int psba_server_create(const psba_server_opts *so, const psba_opts *lm, psba_ser
     s->bo.max_iter = lm->max_iter;
     s->bo.allow_switch = 0;  // the batched driver is LM only
     s->bo.precision = lm->precision;
-    s->pool_size = (size_t)so->hbm_budget_bytes & ~(size_t)255;
+    const bool with_large = so->large_cams > 0 && so->large_lanes > 0;
+    s->large_budget = with_large ? (size_t)(so->hbm_budget_bytes * so->large_share) : 0;
+    s->pool_size = (size_t)(so->hbm_budget_bytes - (double)s->large_budget) & ~(size_t)255;
     const int M = so->max_active;
     cudaError_t e = cudaGetDevice(&s->device);
     int sms = 1;
@@ -388,6 +500,8 @@ int psba_server_create(const psba_server_opts *so, const psba_opts *lm, psba_ser
     s->alloc.reset(s->pool_size);
     s->slots.assign(M, nullptr);
     s->worker = std::thread(worker_main, s);
+    if (with_large)
+        for (int k = 0; k < so->large_lanes; ++k) s->large_workers.emplace_back(large_main, s);
     *out = s;
     return PSBA_OK;
 }
@@ -399,19 +513,49 @@ int psba_batch_submit(psba_server *s, const psba_problem_desc *desc, long long *
     r->t_submit = Clock::now();
     std::string err;
     if (!build_problem_layout(*desc, r->L, err)) return set_error("psba_batch_submit: " + err), PSBA_ERR_ARG;
-    r->bytes = pool_bytes(r->L, s->precision);
-    if (r->bytes > s->pool_size)
-        return set_error("psba_batch_submit: the problem alone exceeds the HBM budget"), PSBA_ERR_NOMEM;
+    r->large = s->large_budget > 0 && desc->n_cams > s->so.large_cams;
+    if (r->large) {
+        r->bytes = large_bytes(r->L);
+        if (r->bytes > s->large_budget)
+            return set_error("psba_batch_submit: the problem alone exceeds the large lane's HBM share"),
+                   PSBA_ERR_NOMEM;
+        // the single-problem engine lays the problem out itself: keep the input
+        r->nc = desc->n_cams;
+        r->np = desc->n_pts;
+        r->no = desc->n_obs;
+        r->hK.assign(desc->K, desc->K + 5 * (size_t)r->nc);
+        r->hq0.assign(desc->q0, desc->q0 + 4 * (size_t)r->nc);
+        r->hcams.assign(desc->cams, desc->cams + 6 * (size_t)r->nc);
+        if (r->np) r->hpts.assign(desc->pts, desc->pts + 3 * (size_t)r->np);
+        if (r->no) {
+            r->hmeas.assign(desc->meas, desc->meas + 2 * (size_t)r->no);
+            r->hopt.assign(desc->obs_pt, desc->obs_pt + r->no);
+            r->hocam.assign(desc->obs_cam, desc->obs_cam + r->no);
+        }
+        std::vector<double>().swap(r->L.dA);
+        std::vector<int>().swap(r->L.iA);
+    } else {
+        r->bytes = pool_bytes(r->L, s->precision);
+        if (r->bytes > s->pool_size)
+            return set_error("psba_batch_submit: the problem alone exceeds the HBM budget"), PSBA_ERR_NOMEM;
+    }
+    const bool large = r->large;
     {
         std::lock_guard<std::mutex> lk(s->mu);
         if (s->failed) return set_error(s->fail_msg), PSBA_ERR_CUDA;
         r->ticket = s->next_ticket++;
         *ticket = r->ticket;
-        s->queue.push_back(r.get());
+        if (large)
+            s->large_queue.push_back(r.get());
+        else
+            s->queue.push_back(r.get());
         s->reqs.emplace(r->ticket, std::move(r));
         s->stats.submitted++;
     }
-    s->cv_work.notify_one();
+    if (large)
+        s->cv_large.notify_all();
+    else
+        s->cv_work.notify_one();
     return PSBA_OK;
 }
 
@@ -428,6 +572,12 @@ int psba_batch_poll(psba_server *s, long long ticket, int timeout_ms, psba_reque
     if (r->state != 2) {
         if (s->failed) return set_error(s->fail_msg), PSBA_ERR_CUDA;
         return PSBA_PENDING;
+    }
+    if (r->err != PSBA_OK) {
+        const int e = r->err;
+        set_error("psba_batch_poll: request failed: " + r->err_msg);
+        s->reqs.erase(it);
+        return e;
     }
     if (res) {
         res->status = r->st.status;
@@ -451,8 +601,8 @@ int psba_server_stats_get(psba_server *s, psba_server_stats *st)
     if (!s || !st) return set_error("psba_server_stats_get: null argument"), PSBA_ERR_ARG;
     std::lock_guard<std::mutex> lk(s->mu);
     *st = s->stats;
-    st->active = s->n_active;
-    st->queued = (int)s->queue.size();
+    st->active = s->n_active + s->n_large;
+    st->queued = (int)(s->queue.size() + s->large_queue.size());
     return s->failed ? (set_error(s->fail_msg), PSBA_ERR_CUDA) : PSBA_OK;
 }
 

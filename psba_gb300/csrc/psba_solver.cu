@@ -409,7 +409,8 @@ int levmar_impl(psba_handle *h, const psba_opts *o, int *itno, psba_result *res,
                     trace_push(res, *itno, PSBA_TRACE_LM_TRIAL, 1, mu_used, rho, new_ex_L2, 0);
                     if (std::fabs(rho - 1) < (1.0 / 5.0)) {
                         gooditer_cnt++;
-                        if (gooditer_cnt >= 5 && o->allow_switch) {
+                        // the trust-region driver takes 6-parameter cameras only
+                        if (gooditer_cnt >= 5 && o->allow_switch && h->d.cnp == 6) {
                             iter_flag = PSBA_ITER_TURN_TO_TR;
                             break;
                         }
@@ -694,11 +695,23 @@ int validate(const psba_problem_desc *p)
     if (!p) return set_error("null problem"), PSBA_ERR_ARG;
     if (p->n_cams <= 0 || p->n_pts < 0 || p->n_obs < 0)
         return set_error("problem sizes must be n_cams > 0, n_pts >= 0, n_obs >= 0"), PSBA_ERR_ARG;
-    if (!p->K || !p->q0 || !p->cams || (p->n_pts && !p->pts) ||
+    if (p->cnp != 0 && p->cnp != 6 && p->cnp != 11 && p->cnp != 16)
+        return set_error("cnp must be 6, 11 or 16 (0 means 6)"), PSBA_ERR_ARG;
+    const bool fixed_k = p->cnp == 0 || p->cnp == 6;
+    if ((fixed_k && !p->K) || !p->q0 || !p->cams || (p->n_pts && !p->pts) ||
         (p->n_obs && (!p->meas || !p->obs_pt || !p->obs_cam)))
         return set_error("null array in problem"), PSBA_ERR_ARG;
-    if ((long long)p->n_cams * 6 > (1LL << 30) || (long long)p->n_obs * 18 > (1LL << 62))
+    if ((long long)p->n_cams * 16 > (1LL << 30) || (long long)p->n_obs * 48 > (1LL << 62))
         return set_error("problem too large"), PSBA_ERR_ARG;
+    if (p->cov)
+        for (int o = 0; o < p->n_obs; ++o) {
+            const double *c = p->cov + 4 * (size_t)o;
+            if (!(c[0] > 0) || !(c[3] > 0) || c[1] != c[2] || !(c[0] * c[3] - c[1] * c[2] > 0) ||
+                !std::isfinite(c[0] * c[3]))
+                return set_error("covariance of observation " + std::to_string(o) +
+                                 " is not symmetric positive definite"),
+                       PSBA_ERR_ARG;
+        }
     for (int o = 0; o < p->n_obs; ++o) {
         const int i = p->obs_pt[o], j = p->obs_cam[o];
         if (i < 0 || i >= p->n_pts || j < 0 || j >= p->n_cams)
@@ -721,7 +734,8 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     d.nc = p->n_cams;
     d.np = p->n_pts;
     d.no = p->n_obs;
-    d.N = 6 * d.nc;
+    d.cnp = p->cnp == 0 ? 6 : p->cnp;
+    d.N = d.cnp * d.nc;
     d.Np = ((d.N + TILE - 1) / TILE) * TILE;
     const int nc = d.nc, np = d.np, no = d.no;
 
@@ -742,7 +756,8 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     const bool dense_tab = (long long)nc * nc <= (1LL << 24);
     std::vector<std::pair<long long, int>> sparse_ids;
     if (!dense_tab) return set_error("more than 4096 cameras is not supported"), PSBA_ERR_ARG;
-    if (d.Np > 4096) return set_error("more than 682 cameras is not supported (reduced system > 4096)"), PSBA_ERR_ARG;
+    if (d.Np > 4096)
+        return set_error("reduced camera system larger than 4096 (cameras x parameters per camera)"), PSBA_ERR_ARG;
     pair_of.assign((size_t)nc * nc, -1);
     std::vector<int> pair_kl;
     std::vector<long long> pair_cnt;
@@ -835,17 +850,20 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     TRY(dalloc(h, &d.camtab, (size_t)CAMTAB * nc));
     TRY(dalloc(h, &d.camtab_new, (size_t)CAMTAB * nc));
     TRY(dalloc(h, &d.ex, 2 * (size_t)no));
-    TRY(dalloc(h, &d.A, 12 * (size_t)no));
+    const size_t cnp = (size_t)d.cnp;
+    const size_t cam_nv = d.cnp == 6 ? 27 : varcam_cam_partial(d.cnp);
+    const size_t diag_nv = d.cnp == 6 ? 27 : varcam_diag_partial(d.cnp);
+    TRY(dalloc(h, &d.A, 2 * cnp * (size_t)no));
     TRY(dalloc(h, &d.B, 6 * (size_t)no));
-    TRY(dalloc(h, &d.W, 18 * (size_t)no));
-    TRY(dalloc(h, &d.U, 36 * (size_t)nc));
+    TRY(dalloc(h, &d.W, 3 * cnp * (size_t)no));
+    TRY(dalloc(h, &d.U, cnp * cnp * (size_t)nc));
     TRY(dalloc(h, &d.V, 6 * (size_t)np));
     TRY(dalloc(h, &d.g, nt));
     TRY(dalloc(h, &d.uvdiag, nt));
-    TRY(dalloc(h, &d.cam_partial, 27 * cam_units.size()));
+    TRY(dalloc(h, &d.cam_partial, cam_nv * cam_units.size()));
     TRY(dalloc(h, &d.Vinv, 6 * (size_t)np));
-    TRY(dalloc(h, &d.Y, 18 * (size_t)no));
-    TRY(dalloc(h, &d.schur_partial, 36 * off_units.size() + 27 * diag_units.size()));
+    TRY(dalloc(h, &d.Y, 3 * cnp * (size_t)no));
+    TRY(dalloc(h, &d.schur_partial, cnp * cnp * off_units.size() + diag_nv * diag_units.size()));
     TRY(dalloc(h, &d.S, (size_t)d.Np * d.Np));
     TRY(dalloc(h, &d.Ssave, (size_t)d.Np * d.Np));
     TRY(dalloc(h, &d.rhs, (size_t)d.Np));
@@ -883,9 +901,24 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     PSBA_CUDA_TRY(cudaMallocHost(&d.scal_host, sizeof(TrialScalars)));
     PSBA_CUDA_TRY(cudaMallocHost(&h->host_scalars, 64 * sizeof(double)));
 
-    TRY(upload(h, d.K, p->K, 5 * (size_t)nc));
+    if (d.cnp == 6) TRY(upload(h, d.K, p->K, 5 * (size_t)nc));
     TRY(upload(h, d.q0, p->q0, 4 * (size_t)nc));
     TRY(upload(h, d.meas, p->meas, 2 * (size_t)no));
+    if (p->cov && no) {
+        // whitening L (upper, L^T L = cov^-1) per observation
+        std::vector<double> w(3 * (size_t)no);
+        for (int o = 0; o < no; ++o) {
+            const double *c = p->cov + 4 * (size_t)o;
+            const double det = c[0] * c[3] - c[1] * c[2];
+            const double pi = c[3] / det, qi = -c[1] / det, ri = c[0] / det;  // cov^-1
+            const double a = std::sqrt(pi), b = qi / a;
+            w[3 * (size_t)o] = a;
+            w[3 * (size_t)o + 1] = b;
+            w[3 * (size_t)o + 2] = std::sqrt(ri - b * b);
+        }
+        TRY(dalloc(h, &d.wt, 3 * (size_t)no));
+        TRY(upload(h, d.wt, w.data(), w.size()));
+    }
     TRY(upload(h, d.obs_pt, p->obs_pt, (size_t)no));
     TRY(upload(h, d.obs_cam, p->obs_cam, (size_t)no));
     TRY(upload(h, d.pt_start, pt_start.data(), (size_t)np + 1));
@@ -1082,6 +1115,10 @@ int psba_levmar(psba_handle *h, const psba_opts *opts, int *itno, psba_result *r
 int psba_trust_region(psba_handle *h, const psba_opts *opts, int *itno, psba_result *res)
 {
     if (!h || !itno) return set_error("null argument"), PSBA_ERR_ARG;
+    if (h->d.cnp != 6)
+        return set_error("psba_trust_region: 6-parameter cameras only (its modified-Cholesky fallback "
+                         "works on 3x3 blocks)"),
+               PSBA_ERR_ARG;
     TRY(check_opts(opts));
     h->d.prec = opts->precision;
     reset_result(res);
@@ -1134,7 +1171,7 @@ int psba_eval_jacobian(psba_handle *h, double *JA, double *JB)
     h->linearized = 1;
     TRY(check_launch());
     const size_t no = (size_t)h->d.no;
-    TRY(copy_out(h, JA, h->d.A, 12 * no));
+    TRY(copy_out(h, JA, h->d.A, 2 * (size_t)h->d.cnp * no));
     TRY(copy_out(h, JB, h->d.B, 6 * no));
     return sync(h);
 }
@@ -1147,7 +1184,9 @@ int psba_eval_normal(psba_handle *h, double coeff, double *U, double *V, double 
     h->linearized = 1;
     TRY(check_launch());
     const size_t no = (size_t)d.no, np = (size_t)d.np;
-    if (U) PSBA_CUDA_TRY(cudaMemcpyAsync(U, d.U, sizeof(double) * 36 * (size_t)d.nc, cudaMemcpyDeviceToHost, h->stream));
+    if (U)
+        PSBA_CUDA_TRY(cudaMemcpyAsync(U, d.U, sizeof(double) * d.cnp * d.cnp * (size_t)d.nc, cudaMemcpyDeviceToHost,
+                                      h->stream));
     if (V && np) {
         const int prec = d.prec;
         d.prec = PSBA_PREC_FP64;  // V is FP64 in both forms
@@ -1155,7 +1194,7 @@ int psba_eval_normal(psba_handle *h, double coeff, double *U, double *V, double 
         d.prec = prec;
         PSBA_CUDA_TRY(cudaMemcpyAsync(V, d.tmp9, sizeof(double) * 9 * np, cudaMemcpyDeviceToHost, h->stream));
     }
-    TRY(copy_out(h, W, d.W, 18 * no));
+    TRY(copy_out(h, W, d.W, 3 * (size_t)d.cnp * no));
     if (g) PSBA_CUDA_TRY(cudaMemcpyAsync(g, d.g, sizeof(double) * (d.N + 3 * np), cudaMemcpyDeviceToHost, h->stream));
     return sync(h);
 }
@@ -1169,7 +1208,7 @@ int psba_eval_reduced(psba_handle *h, double mu, double *Vinv, double *Y, double
     h->last_mu = mu;
     TRY(check_launch());
     const size_t no = (size_t)d.no, np = (size_t)d.np;
-    TRY(copy_out(h, Y, d.Y, 18 * no));
+    TRY(copy_out(h, Y, d.Y, 3 * (size_t)d.cnp * no));
     if (Vinv && np) {
         const int prec = d.prec;
         d.prec = PSBA_PREC_FP64;  // V^-1 is FP64 in both forms

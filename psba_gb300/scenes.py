@@ -37,6 +37,7 @@ class Scene:
     pts_true: Optional[np.ndarray] = None
     q_true: Optional[np.ndarray] = None
     meta: dict = field(default_factory=dict)
+    cnp: int = 6  # parameters per camera: 6 (fixed K), 11 (+ K), 16 (+ K + distortion)
 
     @property
     def n_cams(self):
@@ -51,15 +52,19 @@ class Scene:
         return int(self.meas.shape[0])
 
     def copy(self):
-        return Scene(self.name, self.K.copy(), self.q0.copy(), self.cams.copy(), self.pts.copy(),
-                     self.meas.copy(), self.obs_pt.copy(), self.obs_cam.copy(),
-                     None if self.cams_true is None else self.cams_true.copy(),
-                     None if self.pts_true is None else self.pts_true.copy(),
-                     None if self.q_true is None else self.q_true.copy(), dict(self.meta))
+        sc = Scene(self.name, self.K.copy(), self.q0.copy(), self.cams.copy(), self.pts.copy(),
+                   self.meas.copy(), self.obs_pt.copy(), self.obs_cam.copy(),
+                   None if self.cams_true is None else self.cams_true.copy(),
+                   None if self.pts_true is None else self.pts_true.copy(),
+                   None if self.q_true is None else self.q_true.copy(), dict(self.meta), self.cnp)
+        cov = getattr(self, "cov", None)
+        sc.cov = None if cov is None else cov.copy()
+        return sc
 
     def validate(self):
         C, P, O = self.n_cams, self.n_pts, self.n_obs
-        assert self.K.shape == (C, 5) and self.q0.shape == (C, 4) and self.cams.shape == (C, 6)
+        assert self.K.shape == (C, 5) and self.q0.shape == (C, 4) and self.cams.shape == (C, self.cnp)
+        assert self.cnp in (6, 11, 16)
         assert self.pts.shape == (P, 3) and self.meas.shape == (O, 2)
         assert self.obs_pt.shape == (O,) and self.obs_cam.shape == (O,)
         key = self.obs_pt.astype(np.int64) * C + self.obs_cam
@@ -153,6 +158,28 @@ def project(K, q, t, X):
     return np.stack([x, y], axis=1), Xc[:, 2]
 
 
+def distort(kc, x, y):
+    """Bouguet distortion of normalised coordinates; kc (n, 5) = k1, k2, p1, p2, k3."""
+    r2 = x * x + y * y
+    radial = 1.0 + r2 * (kc[:, 0] + r2 * (kc[:, 1] + r2 * kc[:, 4]))
+    xd = radial * x + 2.0 * kc[:, 2] * x * y + kc[:, 3] * (r2 + 2.0 * x * x)
+    yd = radial * y + kc[:, 2] * (r2 + 2.0 * y * y) + 2.0 * kc[:, 3] * x * y
+    return xd, yd
+
+
+def project_full(K, kc, q, t, X):
+    """Projection with per-row intrinsics K (n, 5) and distortion kc (n, 5) or None."""
+    if kc is None:
+        return project(K, q, t, X)
+    R = quat_to_matrix(q)
+    Xc = np.einsum("nij,nj->ni", R, X) + t
+    x, y = Xc[:, 0] / Xc[:, 2], Xc[:, 1] / Xc[:, 2]
+    xd, yd = distort(kc, x, y)
+    u = K[:, 0] * xd + K[:, 4] * yd + K[:, 1]
+    v = K[:, 0] * K[:, 3] * yd + K[:, 2]
+    return np.stack([u, v], axis=1), Xc[:, 2]
+
+
 def powerlaw_pmf(kmin, kmax, alpha):
     k = np.arange(kmin, kmax + 1)
     w = k.astype(np.float64) ** (-alpha)
@@ -190,6 +217,7 @@ def _finish(name, rng, K, q_true, t_true, X_true, obs_pt, obs_cam, noise_px, out
     cams[:, 3:] = t0
     cams_true = np.zeros((C, 6))
     cams_true[:, 3:] = t_true
+    meta = dict(meta, noise_px=noise_px, outlier_frac=outlier_frac)
     sc = Scene(name, K.copy(), q0, cams, X0, meas, obs_pt, obs_cam, cams_true, X_true.copy(),
                q_true.copy(), meta)
     sc.validate()
@@ -337,3 +365,98 @@ def serving_scenes(n_problems=32, seed=0, cams=(5, 138), pts=(500, 60000), views
                              arc_deg=float(min(max(30.0, 2.0 * C), 160.0)), k_range=views,
                              name="serve%d_%dx%d" % (b, C, P)))
     return out
+
+
+def with_intrinsics(scene, cnp, seed=0, k_off=0.05, k_sigma=0.05, p_sigma=0.001, noise_px=None,
+                    outlier_frac=None):
+    """The same geometry with variable intrinsics: cnp 11 optimises fx, cx, cy,
+    aspect, skew per camera (true values spread around the scene's K, the
+    initial estimate k_off relative off: fx, cx, cy, fy each times
+    1 + N(0, k_off)); cnp 16 adds distortion k1, k2, p1, p2, k3 with true k's
+    from N(0, k_sigma) and p's from N(0, p_sigma), starting at 0.  The
+    observations are re-drawn from the true model with the scene's noise and
+    outlier fractions."""
+    assert cnp in (11, 16) and scene.cams_true is not None
+    rng = np.random.default_rng(seed)
+    C = scene.n_cams
+    Kt = scene.K.copy()
+    Kt[:, 0] *= 1.0 + 0.02 * rng.normal(size=C)
+    Kt[:, 1] += 4.0 * rng.normal(size=C)
+    Kt[:, 2] += 4.0 * rng.normal(size=C)
+    Kt[:, 3] *= 1.0 + 0.005 * rng.normal(size=C)
+    kc_t = None
+    if cnp == 16:
+        kc_t = np.zeros((C, 5))
+        kc_t[:, [0, 1, 4]] = rng.normal(0.0, k_sigma, size=(C, 3))
+        kc_t[:, [2, 3]] = rng.normal(0.0, p_sigma, size=(C, 2))
+    meta = dict(scene.meta)
+    noise = meta.get("noise_px", 1.0) if noise_px is None else noise_px
+    out_frac = meta.get("outlier_frac", 0.0) if outlier_frac is None else outlier_frac
+    j, i = scene.obs_cam, scene.obs_pt
+    xy, _ = project_full(Kt[j], None if kc_t is None else kc_t[j], scene.q_true[j], scene.cams_true[j, 3:],
+                         scene.pts_true[i])
+    meas = xy + rng.normal(0.0, noise, size=xy.shape)
+    if out_frac > 0:
+        m = rng.random(len(meas)) < out_frac
+        meas[m, 0] = rng.uniform(0, 640.0, size=m.sum())
+        meas[m, 1] = rng.uniform(0, 480.0, size=m.sum())
+    fx0 = Kt[:, 0] * (1.0 + k_off * rng.normal(size=C))
+    fy0 = Kt[:, 0] * Kt[:, 3] * (1.0 + k_off * rng.normal(size=C))
+    K0 = np.stack([fx0, Kt[:, 1] * (1.0 + k_off * rng.normal(size=C)),
+                   Kt[:, 2] * (1.0 + k_off * rng.normal(size=C)), fy0 / fx0, Kt[:, 4]], axis=1)
+    cams = np.zeros((C, cnp))
+    cams[:, :6] = scene.cams
+    cams[:, 6:11] = K0
+    cams_true = np.zeros((C, cnp))
+    cams_true[:, :6] = scene.cams_true
+    cams_true[:, 6:11] = Kt
+    if cnp == 16:
+        cams_true[:, 11:16] = kc_t
+    meta.update({"cnp": cnp, "intrinsics_seed": seed})
+    sc = Scene(scene.name + "_cnp%d" % cnp, Kt, scene.q0.copy(), cams, scene.pts.copy(), meas,
+               scene.obs_pt.copy(), scene.obs_cam.copy(), cams_true, scene.pts_true.copy(), scene.q_true.copy(),
+               meta, cnp)
+    sc.validate()
+    return sc
+
+
+def varcam_scene(cnp, seed=0, n_cams=52, n_pts=64053, alpha=None):
+    """The variable-intrinsics workload: 52 cameras on the 200 m circle,
+    64,053 points, power-law views with the exponent re-fitted for a mean of
+    5.42 views per point, cnp 11 or 16."""
+    if alpha is None:
+        alpha = fit_powerlaw_alpha(5.42)
+    base = circle_scene(seed=seed, n_cams=n_cams, n_pts=n_pts, alpha=alpha, name="circle%d" % n_cams)
+    return with_intrinsics(base, cnp, seed=seed + 1000)
+
+
+def fit_powerlaw_alpha(mean, kmin=2, kmax=40):
+    """Exponent of the truncated power law on [kmin, kmax] with the given mean."""
+    lo, hi = 0.5, 4.0
+    for _ in range(60):
+        a = 0.5 * (lo + hi)
+        k, p = powerlaw_pmf(kmin, kmax, a)
+        if (k * p).sum() > mean:
+            lo = a
+        else:
+            hi = a
+    return 0.5 * (lo + hi)
+
+
+def with_covariance(scene, seed=0, sigma=(0.3, 1.5), corr=0.6):
+    """The scene with a random SPD 2x2 measurement covariance per observation
+    (standard deviations uniform on sigma, correlation uniform on [-corr, corr])
+    in ``cov`` (O, 2, 2); the measurements are left as they are."""
+    rng = np.random.default_rng(seed)
+    O = scene.n_obs
+    sx = rng.uniform(*sigma, size=O)
+    sy = rng.uniform(*sigma, size=O)
+    rho = rng.uniform(-corr, corr, size=O)
+    cov = np.empty((O, 2, 2))
+    cov[:, 0, 0] = sx * sx
+    cov[:, 1, 1] = sy * sy
+    cov[:, 0, 1] = cov[:, 1, 0] = rho * sx * sy
+    sc = scene.copy()
+    sc.cov = cov
+    sc.name = scene.name + "_cov"
+    return sc

@@ -53,11 +53,12 @@ def _desc_args(sc):
     return keep
 
 
-def _create(L, sc):
+def _create(L, sc, cnp=6):
     K, q0, cams, pts, meas, opt, ocam = keep = _desc_args(sc)
     d = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
     desc = psba_gb300.ProblemDesc(sc.n_cams, sc.n_pts, sc.n_obs, d(K), d(q0), d(cams), d(pts), d(meas),
-                                  opt.ctypes.data_as(C.POINTER(C.c_int)), ocam.ctypes.data_as(C.POINTER(C.c_int)))
+                                  opt.ctypes.data_as(C.POINTER(C.c_int)), ocam.ctypes.data_as(C.POINTER(C.c_int)),
+                                  cnp)
     h = C.c_void_p()
     rc = L.psba_create(C.byref(desc), C.byref(h))
     del keep
@@ -100,3 +101,11 @@ def test_null_arguments(L):
     h = C.c_void_p()
     assert L.psba_create(None, C.byref(h)) == psba_gb300.PSBA_ERR_ARG
     assert L.psba_eval_cholmod(4, None, None) == psba_gb300.PSBA_ERR_ARG
+
+
+@pytest.mark.parametrize("cnp", [1, 7, 12, -6])
+def test_create_rejects_unknown_camera_model(L, cnp):
+    sc = scenes.arc_scene(seed=0, n_cams=5, n_pts=20)
+    rc, h = _create(L, sc, cnp=cnp)
+    assert rc == psba_gb300.PSBA_ERR_ARG and not h.value
+    assert b"cnp" in L.psba_last_error()

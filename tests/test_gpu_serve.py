@@ -71,10 +71,10 @@ def test_serve_slice_length_does_not_change_results():
 def test_serve_admission_respects_budget():
     ps = probs(6, seed=14)
     # the pool holds the two largest problems at most
-    with S.Server(precision=P.PREC_FP64, max_iter=6, hbm_budget_bytes=1e9) as probe:
+    with S.Server(precision=P.PREC_FP64, max_iter=6, hbm_budget_bytes=1e9, large_cams=0) as probe:
         sizes = [probe.wait(probe.submit(sc)).device_bytes for sc in ps]
     budget = sorted(sizes)[-1] + sorted(sizes)[-2] + 4096
-    with S.Server(precision=P.PREC_FP64, max_iter=6, hbm_budget_bytes=budget) as srv:
+    with S.Server(precision=P.PREC_FP64, max_iter=6, hbm_budget_bytes=budget, large_cams=0) as srv:
         ts = [srv.submit(sc) for sc in ps]
         res = [srv.wait(t) for t in ts]
         st = srv.stats()
@@ -111,3 +111,26 @@ def test_serve_poisson_small():
     for costs in by_scene.values():
         assert len(set(costs)) == 1
     assert wall > 0
+
+
+@pytest.mark.parametrize("precision", [P.PREC_FP64, P.PREC_MIXED])
+def test_serve_large_lane_in_a_mix(precision):
+    # requests above large_cams run on the single-problem engine beside the
+    # batch lane; their results are those of psba_levmar on the same problem
+    small = probs(6, seed=18)
+    large = [scenes.arc_scene(seed=19 + k, n_cams=46, n_pts=700, arc_deg=150.0, k_range=(3, 6),
+                              name="large%d" % k) for k in range(2)]
+    with S.Server(precision=precision, max_iter=12, hbm_budget_bytes=4e9, large_cams=40) as srv:
+        ts = [srv.submit(sc) for sc in small[:3]] + [srv.submit(large[0])] + \
+             [srv.submit(sc) for sc in small[3:]] + [srv.submit(large[1])]
+        res = [srv.wait(t) for t in ts]
+        st = srv.stats()
+    assert st["finished"] == len(ts)
+    for sc, r in zip(large, (res[3], res[-1])):
+        with P.Solver(sc) as s:
+            g = s.levmar(allow_switch=0, max_iter=12, precision=precision)
+        assert r.final_cost == g.final_cost and r.iterations == g.iterations
+        assert np.array_equal(r.cams, g.cams) and np.array_equal(r.pts, g.pts)
+    for sc, r in zip(small, res[:3] + res[4:-1]):
+        o = oracle.levmar(sc, allow_switch=0, max_iter=12)
+        assert abs(r.final_cost - o.final_cost) <= (1e-9 if precision == P.PREC_FP64 else 1e-4) * o.final_cost

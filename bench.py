@@ -46,10 +46,9 @@ METRIC = "LM iterations/s (plain FP64 Levenberg-Marquardt, 88 cams x 64,298 pts)
 UNIT = "iterations/s"
 
 # DRAM bytes (read + write) per launch from one ncu capture of this workload
-# (profiles/k_schur_off_circle88.md); None where no capture of the current
-# kernel exists yet.
+# (profiles/k_schur_off_circle88.md, profiles/k_chol_dataflow_circle88.md).
 SCHUR_OFF_TRAFFIC = 164.0e6
-CHOL_TRAFFIC = None  # S (2.2 MB) is L2-resident: ncu reads ~1.5 MB of DRAM per launch, 0.1% of peak
+CHOL_TRAFFIC = 1.24e6  # profiles/k_chol_dataflow_circle88.md: S (2.2 MB) stays in L2
 
 
 def parse():

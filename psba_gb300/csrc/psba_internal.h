@@ -185,6 +185,15 @@ void launch_scale(double *out, const double *x, const double *num, const double 
 // cooperative launch; epoch must increase from launch to launch.
 void launch_chol_dataflow(const DeviceProblem &d, int mode, int epoch, double *x_out, cudaStream_t s);
 
+// index lists on the GPU, psba_index.cu
+void launch_pt_start(int np, int no, const int *obs_pt, int *pt_start, cudaStream_t s);
+void launch_cam_count(int no, const int *obs_cam, int *cnt, cudaStream_t s);
+void launch_cam_fill(int nc, int no, const int *obs_cam, const int *cam_start, int *cam_obs, cudaStream_t s);
+void launch_pair_count(int nc, const int *cam_start, const int *cam_obs, const int *obs_pt, const int *obs_cam,
+                       const int *pt_start, int *cnt, cudaStream_t s);
+void launch_pair_fill(int nc, const int *cam_start, const int *cam_obs, const int *obs_pt, const int *obs_cam,
+                      const int *pt_start, const int *off, int *pa, int *pb, cudaStream_t s);
+
 // variable intrinsics (cnp 11 / 16), psba_varcam.cu
 size_t varcam_cam_partial(int cnp);   // doubles per camera-unit partial
 size_t varcam_diag_partial(int cnp);  // doubles per diagonal Schur-unit partial

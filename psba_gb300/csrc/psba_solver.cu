@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <memory>
 #include <string>
+#include <mutex>
 #include <vector>
 
 #include "psba_internal.h"
@@ -80,15 +81,64 @@ struct psba_handle {
 
 namespace {
 
+// Device memory comes from the device's stream-ordered pool
+// (cudaMallocAsync / cudaFreeAsync on the handle's stream): creating and
+// destroying a handle then never synchronises the device, so handles come
+// and go (the serving engine's large lane) while other streams run.  The
+// pool keeps freed memory for reuse (release threshold raised once per
+// device, for this process only).
+void keep_pool_memory()
+{
+    static std::mutex mu;
+    static bool done[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return;
+    std::lock_guard<std::mutex> lk(mu);
+    if (done[dev]) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        unsigned long long thr = ~0ULL;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    done[dev] = true;
+}
+
+// Small pinned host buffers (trial scalars), reused across handles: freeing
+// pinned memory can synchronise the device.
+std::mutex g_pinned_mu;
+std::vector<std::pair<size_t, void *>> g_pinned_free;
+
+void *pinned_get(size_t bytes)
+{
+    {
+        std::lock_guard<std::mutex> lk(g_pinned_mu);
+        for (size_t k = 0; k < g_pinned_free.size(); ++k)
+            if (g_pinned_free[k].first == bytes) {
+                void *p = g_pinned_free[k].second;
+                g_pinned_free.erase(g_pinned_free.begin() + (long)k);
+                return p;
+            }
+    }
+    void *p = nullptr;
+    return cudaMallocHost(&p, bytes) == cudaSuccess ? p : nullptr;
+}
+
+void pinned_put(void *p, size_t bytes)
+{
+    if (!p) return;
+    std::lock_guard<std::mutex> lk(g_pinned_mu);
+    g_pinned_free.emplace_back(bytes, p);
+}
+
 template <typename P>
 int dalloc(psba_handle *h, P **ptr, size_t count)
 {
     *ptr = nullptr;
     if (count == 0) count = 1;
     void *p = nullptr;
-    cudaError_t e = cudaMalloc(&p, count * sizeof(P));
+    cudaError_t e = cudaMallocAsync(&p, count * sizeof(P), h->stream);
     if (e != cudaSuccess) {
-        set_error(std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+        set_error(std::string("device allocation failed: ") + cudaGetErrorString(e));
         return PSBA_ERR_NOMEM;
     }
     h->allocs.push_back(p);
@@ -739,59 +789,60 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     d.Np = ((d.N + TILE - 1) / TILE) * TILE;
     const int nc = d.nc, np = d.np, no = d.no;
 
-    // ---- host index lists (replace generate_idxs, misc.cpp:178-218)
-    std::vector<int> pt_start(np + 1, 0), cam_start(nc + 1, 0), cam_obs(no > 0 ? no : 1);
-    for (int o = 0; o < no; ++o) {
-        pt_start[p->obs_pt[o] + 1]++;
-        cam_start[p->obs_cam[o] + 1]++;
-    }
-    for (int i = 0; i < np; ++i) pt_start[i + 1] += pt_start[i];
-    for (int j = 0; j < nc; ++j) cam_start[j + 1] += cam_start[j];
-    {
-        std::vector<int> fill(cam_start.begin(), cam_start.end() - 1);
-        for (int o = 0; o < no; ++o) cam_obs[fill[p->obs_cam[o]]++] = o;
-    }
-    // camera pairs k > l with common points; entries in ascending point order
-    std::vector<int> pair_of;  // dense (k, l) -> pair id, when small enough
-    const bool dense_tab = (long long)nc * nc <= (1LL << 24);
-    std::vector<std::pair<long long, int>> sparse_ids;
-    if (!dense_tab) return set_error("more than 4096 cameras is not supported"), PSBA_ERR_ARG;
+    // ---- index lists, built on the GPU (replace generate_idxs, misc.cpp:178-218)
+    if ((long long)nc * nc > (1LL << 24)) return set_error("more than 4096 cameras is not supported"), PSBA_ERR_ARG;
     if (d.Np > 4096)
         return set_error("reduced camera system larger than 4096 (cameras x parameters per camera)"), PSBA_ERR_ARG;
-    pair_of.assign((size_t)nc * nc, -1);
-    std::vector<int> pair_kl;
-    std::vector<long long> pair_cnt;
-    for (int i = 0; i < np; ++i)
-        for (int a = pt_start[i]; a < pt_start[i + 1]; ++a)
-            for (int b = pt_start[i]; b < a; ++b) {
-                const int k = p->obs_cam[a], l = p->obs_cam[b];
-                int &id = pair_of[(size_t)k * nc + l];
-                if (id < 0) {
-                    id = (int)pair_kl.size() / 2;
-                    pair_kl.push_back(k);
-                    pair_kl.push_back(l);
-                    pair_cnt.push_back(0);
-                }
-                pair_cnt[id]++;
-            }
-    const int n_pairs = (int)pair_cnt.size();
-    std::vector<long long> pair_start(n_pairs + 1, 0);
-    for (int q = 0; q < n_pairs; ++q) pair_start[q + 1] = pair_start[q] + pair_cnt[q];
-    const long long n_entries = pair_start[n_pairs];
-    if (n_entries > (1LL << 31) - 1) return set_error("too many camera-pair entries"), PSBA_ERR_ARG;
-    std::vector<int> pa(n_entries > 0 ? n_entries : 1), pb(n_entries > 0 ? n_entries : 1);
-    {
-        std::vector<long long> fill(pair_start.begin(), pair_start.end() - 1);
-        for (int i = 0; i < np; ++i)
-            for (int a = pt_start[i]; a < pt_start[i + 1]; ++a)
-                for (int b = pt_start[i]; b < a; ++b) {
-                    const int k = p->obs_cam[a], l = p->obs_cam[b];
-                    const int id = pair_of[(size_t)k * nc + l];
-                    const long long at = fill[id]++;
-                    pa[at] = a;
-                    pb[at] = b;
-                }
-    }
+    TRY(dalloc(h, &d.obs_pt, (size_t)no));
+    TRY(dalloc(h, &d.obs_cam, (size_t)no));
+    TRY(dalloc(h, &d.pt_start, (size_t)np + 1));
+    TRY(dalloc(h, &d.cam_obs, (size_t)no));
+    TRY(upload(h, d.obs_pt, p->obs_pt, (size_t)no));
+    TRY(upload(h, d.obs_cam, p->obs_cam, (size_t)no));
+    int *d_cnt = nullptr, *d_cam_start = nullptr, *d_pair_cnt = nullptr, *d_off = nullptr;
+    TRY(dalloc(h, &d_cnt, (size_t)nc));
+    TRY(dalloc(h, &d_cam_start, (size_t)nc + 1));
+    TRY(dalloc(h, &d_pair_cnt, (size_t)nc * nc));
+    TRY(dalloc(h, &d_off, (size_t)nc * nc));
+    PSBA_CUDA_TRY(cudaMemsetAsync(d_cnt, 0, sizeof(int) * nc, h->stream));
+    launch_pt_start(np, no, d.obs_pt, d.pt_start, h->stream);
+    launch_cam_count(no, d.obs_cam, d_cnt, h->stream);
+    std::vector<int> cam_start(nc + 1, 0);
+    PSBA_CUDA_TRY(cudaMemcpyAsync(cam_start.data() + 1, d_cnt, sizeof(int) * nc, cudaMemcpyDeviceToHost, h->stream));
+    TRY(sync(h));
+    for (int j = 0; j < nc; ++j) cam_start[j + 1] += cam_start[j];
+    TRY(upload(h, d_cam_start, cam_start.data(), (size_t)nc + 1));
+    launch_cam_fill(nc, no, d.obs_cam, d_cam_start, d.cam_obs, h->stream);
+    launch_pair_count(nc, d_cam_start, d.cam_obs, d.obs_pt, d.obs_cam, d.pt_start, d_pair_cnt, h->stream);
+    std::vector<int> pair_cnt((size_t)nc * nc);
+    PSBA_CUDA_TRY(cudaMemcpyAsync(pair_cnt.data(), d_pair_cnt, sizeof(int) * pair_cnt.size(), cudaMemcpyDeviceToHost,
+                                  h->stream));
+    TRY(sync(h));
+    // camera pairs k > l with common points, numbered in (k, l) order; the
+    // entries of each pair start at off[k * nc + l]
+    std::vector<int> pair_kl, off((size_t)nc * nc, 0);
+    std::vector<long long> pair_start(1, 0);
+    for (int k = 0; k < nc; ++k)
+        for (int l = 0; l < k; ++l) {
+            const int c = pair_cnt[(size_t)k * nc + l];
+            if (c == 0) continue;
+            if (pair_start.back() + c > (1LL << 31) - 1)
+                return set_error("too many camera-pair entries"), PSBA_ERR_ARG;
+            off[(size_t)k * nc + l] = (int)pair_start.back();
+            pair_kl.push_back(k);
+            pair_kl.push_back(l);
+            pair_start.push_back(pair_start.back() + c);
+        }
+    const int n_pairs = (int)pair_kl.size() / 2;
+    const long long n_entries = pair_start.back();
+    TRY(dalloc(h, &d.pair_kl, 2 * (size_t)n_pairs));
+    TRY(dalloc(h, &d.pair_a, (size_t)n_entries));
+    TRY(dalloc(h, &d.pair_b, (size_t)n_entries));
+    TRY(upload(h, d.pair_kl, pair_kl.data(), pair_kl.size()));
+    TRY(upload(h, d_off, off.data(), off.size()));
+    launch_pair_fill(nc, d_cam_start, d.cam_obs, d.obs_pt, d.obs_cam, d.pt_start, d_off, d.pair_a, d.pair_b,
+                     h->stream);
+    TRY(check_launch());
     // Schur work units; execution order longest first
     std::vector<SchurUnit> off_units, diag_units;
     std::vector<int> off_start(n_pairs + 1, 0), diag_start(nc + 1, 0);
@@ -830,13 +881,6 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     TRY(dalloc(h, &d.K, 5 * (size_t)nc));
     TRY(dalloc(h, &d.q0, 4 * (size_t)nc));
     TRY(dalloc(h, &d.meas, 2 * (size_t)no));
-    TRY(dalloc(h, &d.obs_pt, (size_t)no));
-    TRY(dalloc(h, &d.obs_cam, (size_t)no));
-    TRY(dalloc(h, &d.pt_start, (size_t)np + 1));
-    TRY(dalloc(h, &d.cam_obs, (size_t)no));
-    TRY(dalloc(h, &d.pair_kl, 2 * (size_t)n_pairs));
-    TRY(dalloc(h, &d.pair_a, (size_t)n_entries));
-    TRY(dalloc(h, &d.pair_b, (size_t)n_entries));
     TRY(dalloc(h, &d.off_units, off_units.size()));
     TRY(dalloc(h, &d.off_unit_start, (size_t)n_pairs + 1));
     TRY(dalloc(h, &d.diag_units, diag_units.size()));
@@ -898,8 +942,9 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     TRY(dalloc(h, &d.jx2, 2 * (size_t)no));
     TRY(dalloc(h, &d.E, (size_t)d.Np));
     TRY(dalloc(h, &d.tmp9, 9 * (size_t)np));
-    PSBA_CUDA_TRY(cudaMallocHost(&d.scal_host, sizeof(TrialScalars)));
-    PSBA_CUDA_TRY(cudaMallocHost(&h->host_scalars, 64 * sizeof(double)));
+    d.scal_host = static_cast<TrialScalars *>(pinned_get(sizeof(TrialScalars)));
+    h->host_scalars = static_cast<double *>(pinned_get(64 * sizeof(double)));
+    if (!d.scal_host || !h->host_scalars) return set_error("pinned host allocation failed"), PSBA_ERR_NOMEM;
 
     if (d.cnp == 6) TRY(upload(h, d.K, p->K, 5 * (size_t)nc));
     TRY(upload(h, d.q0, p->q0, 4 * (size_t)nc));
@@ -919,13 +964,6 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
         TRY(dalloc(h, &d.wt, 3 * (size_t)no));
         TRY(upload(h, d.wt, w.data(), w.size()));
     }
-    TRY(upload(h, d.obs_pt, p->obs_pt, (size_t)no));
-    TRY(upload(h, d.obs_cam, p->obs_cam, (size_t)no));
-    TRY(upload(h, d.pt_start, pt_start.data(), (size_t)np + 1));
-    TRY(upload(h, d.cam_obs, cam_obs.data(), (size_t)no));
-    TRY(upload(h, d.pair_kl, pair_kl.data(), pair_kl.size()));
-    TRY(upload(h, d.pair_a, pa.data(), (size_t)n_entries));
-    TRY(upload(h, d.pair_b, pb.data(), (size_t)n_entries));
     TRY(upload(h, d.off_units, off_units.data(), off_units.size()));
     TRY(upload(h, d.off_unit_start, off_start.data(), off_start.size()));
     TRY(upload(h, d.diag_units, diag_units.data(), diag_units.size()));
@@ -946,10 +984,12 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
 void destroy_impl(psba_handle *h)
 {
     if (!h) return;
-    if (h->stream) cudaStreamSynchronize(h->stream);
-    for (void *p : h->allocs) cudaFree(p);
-    if (h->d.scal_host) cudaFreeHost(h->d.scal_host);
-    if (h->host_scalars) cudaFreeHost(h->host_scalars);
+    if (h->stream) {
+        for (void *p : h->allocs) cudaFreeAsync(p, h->stream);
+        cudaStreamSynchronize(h->stream);
+    }
+    pinned_put(h->d.scal_host, sizeof(TrialScalars));
+    pinned_put(h->host_scalars, 64 * sizeof(double));
     for (int k = 0; k < ST_N; ++k) {
         if (h->timers[k].a) cudaEventDestroy(h->timers[k].a);
         if (h->timers[k].b) cudaEventDestroy(h->timers[k].b);
@@ -1036,6 +1076,7 @@ int psba_create(const psba_problem_desc *desc, psba_handle **out)
     TRY(validate(desc));
     psba_handle *h = new (std::nothrow) psba_handle();
     if (!h) return set_error("host allocation failed"), PSBA_ERR_NOMEM;
+    keep_pool_memory();
     cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&h->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&h->ev1);

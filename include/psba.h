@@ -88,7 +88,8 @@ typedef struct {
      * variable-K camera files, data/7camsvarK.txt).  16: followed further by
      * the distortion k1, k2, p1, p2, k3 (data/54camsvarKD.txt).  The 11- and
      * 16-parameter models have no reference kernels; the trust-region entry
-     * points and the batched / serving engines take 6-parameter cameras. */
+     * points and psba_batch_* take 6-parameter cameras (the server runs the
+     * others on its large lane). */
     int cnp;
     /* Optional (NULL: unweighted): per observation the 2x2 covariance of the
      * image measurement, row-major (4 values, symmetric positive definite),
@@ -96,8 +97,8 @@ typedef struct {
      * 380-412) and its solver ignores (PSBA/main.cpp:112-113).  Residuals and
      * Jacobian rows are whitened by the upper Cholesky factor L of the
      * inverse covariance (L^T L = cov^-1), so the cost is sum e^T cov^-1 e.
-     * psba_create only; the batched / serving engines take unweighted
-     * problems. */
+     * psba_batch_* takes unweighted problems (the server runs weighted ones
+     * on its large lane). */
     const double *cov;
 } psba_problem_desc;
 
@@ -271,7 +272,8 @@ size_t psba_batch_device_bytes(psba_batch *b);
  * (psba_create / psba_levmar: multi-CTA kernels and the dataflow Cholesky
  * over the whole GPU) on its own stream, concurrently with the batch lane;
  * its device memory counts against large_share of the budget.  The rest of
- * the budget is the batch lane's pool.
+ * the budget is the batch lane's pool.  Requests with 11- or 16-parameter
+ * cameras or with covariances always take the large lane.
  * psba_batch_submit lays a request out on the calling thread and queues it;
  * the worker admits queued requests in arrival order while a resident slot is
  * free and the request fits the pool, and advances all resident problems

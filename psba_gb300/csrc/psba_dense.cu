@@ -30,6 +30,7 @@ constexpr int TT = TILE * TILE;
 constexpr int CF_THREADS = 128;
 constexpr long long SPIN_LIMIT = 1LL << 22;  // ~0.5 s of polling with 64 ns sleeps
 constexpr int MAX_NP = 4096;                 // largest reduced system (dynamic shared memory of the solve)
+constexpr int BJ = 8;                        // update steps staged per batch in a tile task
 
 __device__ __forceinline__ int ld_acquire(const int *p)
 {
@@ -206,8 +207,10 @@ __global__ void __launch_bounds__(CF_THREADS) k_chol_dataflow(int mode, int Np, 
                                                               int *__restrict__ flags, int epoch,
                                                               int *__restrict__ status)
 {
-    __shared__ double a[T][T + 1], li[T][T + 1], lk[T][T + 1], linv[T][T + 1];
+    __shared__ double a[T][T + 1], linv[T][T + 1];
+    __shared__ double bi[BJ][T][T + 1], bk[BJ][T][T + 1], by[BJ][T];
     __shared__ double bvec[T], yvec[T], invd[T];
+    __shared__ int ready_n;
     extern __shared__ double vec[];  // Np: right-hand side of the single-CTA solves
     const int n_fact = mode == 0 ? nb * (nb + 1) / 2 : 0;
     const int n_tasks = n_fact + 1;
@@ -218,28 +221,56 @@ __global__ void __launch_bounds__(CF_THREADS) k_chol_dataflow(int mode, int Np, 
             load_tile(a, S, Np, I, K);
             if (I == K && tid < T) bvec[tid] = __ldcg(rhs + I * T + tid);
             __syncthreads();
-            for (int J = 0; J < K; ++J) {
-                block_wait(flags + tile_task(I, J, nb), epoch, status);
-                if (I != K) block_wait(flags + tile_task(K, J, nb), epoch, status);
-                load_tile(li, S, Np, I, J);
-                if (I != K) load_tile(lk, S, Np, K, J);
-                if (I == K && tid < T) yvec[tid] = __ldcg(rhs + J * T + tid);
+            // Updates J = 0 .. K-1 in order.  The flags of the next BJ steps are
+            // polled at once (one L2 round trip); the ready ones have all their
+            // tiles loaded together and are applied from shared memory, so an
+            // update costs one round trip per batch instead of two per step.
+            // Each thread updates its own elements in the same order as one
+            // step at a time would: the arithmetic does not depend on batching.
+            int J = 0;
+            while (J < K) {
+                const int nmax = min(BJ, K - J);
+                if (tid == 0) ready_n = nmax;
                 __syncthreads();
-                double(*lkp)[T + 1] = I == K ? li : lk;
-                for (int e = tid; e < TT; e += CF_THREADS) {
-                    const int r = e / T, c = e % T;
-                    double s = a[r][c];
-#pragma unroll
-                    for (int k = 0; k < T; ++k) s = fma(-li[r][k], lkp[c][k], s);
-                    a[r][c] = s;
-                }
-                if (I == K && tid < T) {
-                    double s = bvec[tid];
-#pragma unroll
-                    for (int k = 0; k < T; ++k) s = fma(-li[tid][k], yvec[k], s);
-                    bvec[tid] = s;
+                if (tid < nmax) {
+                    const bool ok = ld_acquire(flags + tile_task(I, J + tid, nb)) == epoch &&
+                                    (I == K || ld_acquire(flags + tile_task(K, J + tid, nb)) == epoch);
+                    if (!ok) atomicMin(&ready_n, tid);
                 }
                 __syncthreads();
+                int n = ready_n;
+                if (n == 0) {  // the next step is not done yet: wait for it alone
+                    block_wait(flags + tile_task(I, J, nb), epoch, status);
+                    if (I != K) block_wait(flags + tile_task(K, J, nb), epoch, status);
+                    n = 1;
+                }
+                for (int e = tid; e < n * TT; e += CF_THREADS) {
+                    const int q = e / TT, r = (e % TT) / T, c = e % T;
+                    bi[q][r][c] = __ldcg(S + (size_t)(I * T + r) * Np + (J + q) * T + c);
+                    if (I != K) bk[q][r][c] = __ldcg(S + (size_t)(K * T + r) * Np + (J + q) * T + c);
+                }
+                if (I == K)
+                    for (int e = tid; e < n * T; e += CF_THREADS) by[e / T][e % T] = __ldcg(rhs + (J + e / T) * T + e % T);
+                __syncthreads();
+                for (int q = 0; q < n; ++q) {
+                    double(*lip)[T + 1] = bi[q];
+                    double(*lkp)[T + 1] = I == K ? bi[q] : bk[q];
+                    for (int e = tid; e < TT; e += CF_THREADS) {
+                        const int r = e / T, c = e % T;
+                        double s = a[r][c];
+#pragma unroll
+                        for (int k = 0; k < T; ++k) s = fma(-lip[r][k], lkp[c][k], s);
+                        a[r][c] = s;
+                    }
+                    if (I == K && tid < T) {
+                        double s = bvec[tid];
+#pragma unroll
+                        for (int k = 0; k < T; ++k) s = fma(-lip[tid][k], by[q][k], s);
+                        bvec[tid] = s;
+                    }
+                }
+                __syncthreads();
+                J += n;
             }
             const bool failed = ld_acquire(status) != 0;
             if (I == K) {

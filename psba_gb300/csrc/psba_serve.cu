@@ -68,8 +68,8 @@ struct Request {
     std::vector<double> cams, pts;
     // large lane: a copy of the problem for psba_create, and the outcome
     bool large = false;
-    int nc = 0, np = 0, no = 0;
-    std::vector<double> hK, hq0, hcams, hpts, hmeas;
+    int nc = 0, np = 0, no = 0, cnp = 6;
+    std::vector<double> hK, hq0, hcams, hpts, hmeas, hcov;
     std::vector<int> hopt, hocam;
     int err = PSBA_OK;
     std::string err_msg;
@@ -326,12 +326,25 @@ void worker_main(psba_server *s)
     }
 }
 
-// Device bytes of a request on the single-problem engine: the per-observation
-// and per-point arrays in FP64, S and its copy, and the Schur work lists.
-size_t large_bytes(const ProblemLayout &L)
+// Device bytes of a request on the single-problem engine (an upper estimate
+// of what psba_create allocates): per observation e, A, B, W, Y, J x
+// buffers and indices; per point V, V^-1, g, dp and trust-region vectors;
+// the camera-pair entries and their Schur partials; S, its copy and the
+// dense-solve work arrays; 16 MB of slack for the small tables.
+size_t large_bytes(const psba_problem_desc &p, int cnp)
 {
-    const size_t Np = ((size_t)L.bp.N + TILE - 1) / TILE * TILE;
-    return pool_bytes(L, PSBA_PREC_FP64) + 3 * Np * Np * sizeof(double) + ((size_t)16 << 20);
+    const size_t no = (size_t)p.n_obs, np = (size_t)p.n_pts, nc = (size_t)p.n_cams, c = (size_t)cnp;
+    size_t entries = 0;
+    for (size_t a = 0, b = 0; a < no; a = b) {
+        while (b < no && p.obs_pt[b] == p.obs_pt[a]) ++b;
+        entries += (b - a) * (b - a - 1) / 2;
+    }
+    const size_t N = c * nc, Np = (N + TILE - 1) / TILE * TILE;
+    const size_t per_obs = 2 + 2 * c + 6 + 2 * 3 * c + 3 * 2 + 3 + 4;
+    const size_t per_pt = 3 * 3 + 6 * 2 + 9 + 3 * 6;
+    const size_t doubles = no * per_obs + np * per_pt + N * 8 + nc * (c * c + 2 * CAMTAB) + 3 * Np * Np +
+                           Np * TILE + (entries / SCHUR_CHUNK + nc * 8) * c * c;
+    return doubles * sizeof(double) + entries * 2 * sizeof(int) + ((size_t)16 << 20);
 }
 
 void large_main(psba_server *s)
@@ -365,13 +378,14 @@ void large_main(psba_server *s)
         desc.meas = r->hmeas.data();
         desc.obs_pt = r->hopt.data();
         desc.obs_cam = r->hocam.data();
-        desc.cnp = 6;
+        desc.cnp = r->cnp;
+        desc.cov = r->hcov.empty() ? nullptr : r->hcov.data();
         psba_handle *h = nullptr;
         psba_result res{};
         int itno = 0;
         int rc = psba_create(&desc, &h);
         if (rc == PSBA_OK) rc = psba_levmar(h, &s->lm, &itno, &res);
-        r->cams.resize(6 * (size_t)r->nc);
+        r->cams.resize((size_t)r->cnp * r->nc);
         r->pts.resize(3 * (size_t)r->np);
         if (rc == PSBA_OK) rc = psba_get_params(h, r->cams.data(), r->pts.data());
         const double dev_bytes = h ? (double)psba_device_bytes(h) : 0.0;
@@ -393,7 +407,8 @@ void large_main(psba_server *s)
             r->state = 2;
             r->t_done = Clock::now();
             s->stats.finished++;
-            for (std::vector<double> *v : {&r->hK, &r->hq0, &r->hcams, &r->hpts, &r->hmeas}) std::vector<double>().swap(*v);
+            for (std::vector<double> *v : {&r->hK, &r->hq0, &r->hcams, &r->hpts, &r->hmeas, &r->hcov})
+                std::vector<double>().swap(*v);
             std::vector<int>().swap(r->hopt);
             std::vector<int>().swap(r->hocam);
         }
@@ -511,11 +526,22 @@ int psba_batch_submit(psba_server *s, const psba_problem_desc *desc, long long *
     if (!s || !desc || !ticket) return set_error("psba_batch_submit: null argument"), PSBA_ERR_ARG;
     auto r = std::make_unique<Request>();
     r->t_submit = Clock::now();
-    std::string err;
-    if (!build_problem_layout(*desc, r->L, err)) return set_error("psba_batch_submit: " + err), PSBA_ERR_ARG;
-    r->large = s->large_budget > 0 && desc->n_cams > s->so.large_cams;
+    const int cnp = desc->cnp == 0 ? 6 : desc->cnp;
+    // the batch lane takes 6-parameter, unweighted problems; the others, and
+    // those above large_cams cameras, go to the single-problem engine
+    const bool special = cnp != 6 || desc->cov != nullptr;
+    if (special && s->large_budget == 0)
+        return set_error("psba_batch_submit: 11/16-parameter cameras and weighted problems need the large lane "
+                         "(large_cams > 0, large_lanes > 0)"),
+               PSBA_ERR_ARG;
+    r->large = s->large_budget > 0 && (special || desc->n_cams > s->so.large_cams);
     if (r->large) {
-        r->bytes = large_bytes(r->L);
+        // checked in full by psba_create on the large lane; enough here to copy safely
+        if ((cnp != 6 && cnp != 11 && cnp != 16) || desc->n_cams <= 0 || desc->n_pts < 0 || desc->n_obs < 0 ||
+            (cnp == 6 && !desc->K) || !desc->q0 || !desc->cams || (desc->n_pts && !desc->pts) ||
+            (desc->n_obs && (!desc->meas || !desc->obs_pt || !desc->obs_cam)))
+            return set_error("psba_batch_submit: problem is malformed"), PSBA_ERR_ARG;
+        r->bytes = large_bytes(*desc, cnp);
         if (r->bytes > s->large_budget)
             return set_error("psba_batch_submit: the problem alone exceeds the large lane's HBM share"),
                    PSBA_ERR_NOMEM;
@@ -523,18 +549,21 @@ int psba_batch_submit(psba_server *s, const psba_problem_desc *desc, long long *
         r->nc = desc->n_cams;
         r->np = desc->n_pts;
         r->no = desc->n_obs;
-        r->hK.assign(desc->K, desc->K + 5 * (size_t)r->nc);
+        r->cnp = cnp;
+        if (desc->K) r->hK.assign(desc->K, desc->K + 5 * (size_t)r->nc);
+        else r->hK.assign(5 * (size_t)r->nc, 0.0);
         r->hq0.assign(desc->q0, desc->q0 + 4 * (size_t)r->nc);
-        r->hcams.assign(desc->cams, desc->cams + 6 * (size_t)r->nc);
+        r->hcams.assign(desc->cams, desc->cams + (size_t)cnp * r->nc);
         if (r->np) r->hpts.assign(desc->pts, desc->pts + 3 * (size_t)r->np);
         if (r->no) {
             r->hmeas.assign(desc->meas, desc->meas + 2 * (size_t)r->no);
             r->hopt.assign(desc->obs_pt, desc->obs_pt + r->no);
             r->hocam.assign(desc->obs_cam, desc->obs_cam + r->no);
+            if (desc->cov) r->hcov.assign(desc->cov, desc->cov + 4 * (size_t)r->no);
         }
-        std::vector<double>().swap(r->L.dA);
-        std::vector<int>().swap(r->L.iA);
     } else {
+        std::string err;
+        if (!build_problem_layout(*desc, r->L, err)) return set_error("psba_batch_submit: " + err), PSBA_ERR_ARG;
         r->bytes = pool_bytes(r->L, s->precision);
         if (r->bytes > s->pool_size)
             return set_error("psba_batch_submit: the problem alone exceeds the HBM budget"), PSBA_ERR_NOMEM;

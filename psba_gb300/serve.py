@@ -101,22 +101,25 @@ class Server:
         self._lock = threading.Lock()
 
     def submit(self, sc):
+        cnp = int(getattr(sc, "cnp", 6))
+        cov = getattr(sc, "cov", None)
         arrs = [_f64(sc.K), _f64(sc.q0), _f64(sc.cams), _f64(sc.pts), _f64(sc.meas),
-                np.ascontiguousarray(sc.obs_pt, dtype=np.int32), np.ascontiguousarray(sc.obs_cam, dtype=np.int32)]
-        K, q0, cams, pts, meas, opt, ocam = arrs
+                np.ascontiguousarray(sc.obs_pt, dtype=np.int32), np.ascontiguousarray(sc.obs_cam, dtype=np.int32),
+                None if cov is None else _f64(cov).reshape(-1, 2, 2)]
+        K, q0, cams, pts, meas, opt, ocam, cv = arrs
         desc = ProblemDesc(sc.n_cams, sc.n_pts, sc.n_obs, _d(K), _d(q0), _d(cams), _d(pts), _d(meas),
-                           opt.ctypes.data_as(_ip), ocam.ctypes.data_as(_ip))
+                           opt.ctypes.data_as(_ip), ocam.ctypes.data_as(_ip), cnp, None if cv is None else _d(cv))
         t = C.c_longlong()
         _check(lib().psba_batch_submit(self.h, C.byref(desc), C.byref(t)))
         with self._lock:
-            self._shapes[t.value] = (sc.n_cams, sc.n_pts)
+            self._shapes[t.value] = (sc.n_cams, sc.n_pts, cnp)
         return t.value
 
     def poll(self, ticket, timeout_ms=0):
         """The finished Request, or None if it is still running."""
         with self._lock:
-            nc, npts = self._shapes[ticket]
-        cams = np.empty((nc, 6))
+            nc, npts, cnp = self._shapes[ticket]
+        cams = np.empty((nc, cnp))
         pts = np.empty((npts, 3))
         r = RequestResult()
         rc = lib().psba_batch_poll(self.h, ticket, int(timeout_ms), C.byref(r), cams.ctypes.data,

@@ -134,3 +134,23 @@ def test_serve_large_lane_in_a_mix(precision):
     for sc, r in zip(small, res[:3] + res[4:-1]):
         o = oracle.levmar(sc, allow_switch=0, max_iter=12)
         assert abs(r.final_cost - o.final_cost) <= (1e-9 if precision == P.PREC_FP64 else 1e-4) * o.final_cost
+
+
+def test_serve_variable_intrinsics_and_weighted_requests():
+    # 11-parameter cameras and covariance-weighted problems take the large
+    # lane; their results are those of psba_levmar on the same problem
+    base = scenes.arc_scene(seed=21, n_cams=8, n_pts=300)
+    var11 = scenes.with_intrinsics(base, 11, seed=22, k_off=0.01)
+    weighted = scenes.with_covariance(scenes.arc_scene(seed=23, n_cams=7, n_pts=250), seed=24)
+    small = probs(3, seed=25)
+    with S.Server(precision=P.PREC_FP64, max_iter=10, hbm_budget_bytes=4e9) as srv:
+        ts = [srv.submit(var11), srv.submit(small[0]), srv.submit(weighted), srv.submit(small[1])]
+        res = [srv.wait(t) for t in ts]
+    for sc, r in ((var11, res[0]), (weighted, res[2])):
+        with P.Solver(sc) as s:
+            g = s.levmar(allow_switch=0, max_iter=10)
+        assert r.final_cost == g.final_cost and np.array_equal(r.cams, g.cams)
+    assert res[0].cams.shape == (8, 11)
+    with S.Server(precision=P.PREC_FP64, max_iter=10, hbm_budget_bytes=4e9, large_cams=0) as srv:
+        with pytest.raises(P.PSBAError):
+            srv.submit(var11)  # no large lane to run it

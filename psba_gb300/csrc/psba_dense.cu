@@ -7,8 +7,8 @@
 // waits (bounded spin on per-task flags in global memory, acquire/release)
 // only for tasks with smaller numbers, so with all CTAs resident (cooperative
 // launch) the smallest unfinished task can always run: no deadlock.
-//   tile (I,I):  A_II -= sum_J L_IJ L_IJ^T, then a warp-level Cholesky in
-//                registers, its inverse, and y_I = L_II^-1 (b_I - sum_J L_IJ y_J)
+//   tile (I,I):  A_II -= sum_J L_IJ L_IJ^T, then a CTA-wide Cholesky of the
+//                tile, its inverse, and y_I = L_II^-1 (b_I - sum_J L_IJ y_J)
 //                (the forward solve of L y = ea rides along)
 //   tile (I,K):  A_IK -= sum_{J<K} L_IJ L_KJ^T, then L_IK = A_IK L_KK^-T
 // After the factor, one CTA solves L^T x = y with y in shared memory; the
@@ -27,10 +27,43 @@ namespace psba {
 
 constexpr int T = TILE;
 constexpr int TT = TILE * TILE;
-constexpr int CF_THREADS = 128;
+// Launch shape (compile-time tuning knobs): threads per CTA, update steps
+// staged per batch, a cap on CTAs per SM (0: as many as fit), and whether
+// CTAs claim tasks through an atomic counter (1) or take every grid-th task (0).
+#ifndef PSBA_CHOL_THREADS
+#define PSBA_CHOL_THREADS 128
+#endif
+#ifndef PSBA_CHOL_BJ
+#define PSBA_CHOL_BJ 8
+#endif
+#ifndef PSBA_CHOL_PER_SM
+#define PSBA_CHOL_PER_SM 0
+#endif
+#ifndef PSBA_CHOL_DYNAMIC
+#define PSBA_CHOL_DYNAMIC 0
+#endif
+constexpr int CF_THREADS = PSBA_CHOL_THREADS;
 constexpr long long SPIN_LIMIT = 1LL << 22;  // ~0.5 s of polling with 64 ns sleeps
 constexpr int MAX_NP = 4096;                 // largest reduced system (dynamic shared memory of the solve)
-constexpr int BJ = 8;                        // update steps staged per batch in a tile task
+constexpr int BJ = PSBA_CHOL_BJ;             // update steps staged per batch in a tile task
+static_assert(BJ >= 2, "the diagonal factor reuses two staging tiles");
+
+#ifdef PSBA_CHOL_TRACE
+// Timing probe (off in the library): per task, the global timer at its
+// start, after its updates, after its factor / triangular solve, at its end.
+__device__ long long g_chol_trace[4 * 65536];
+__device__ __forceinline__ void trace_mark(int t, int k)
+{
+    if (threadIdx.x == 0 && t < 65536) {
+        long long v;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(v));
+        g_chol_trace[4 * t + k] = v;
+    }
+}
+#define CHOL_MARK(t, k) trace_mark(t, k)
+#else
+#define CHOL_MARK(t, k)
+#endif
 
 __device__ __forceinline__ int ld_acquire(const int *p)
 {
@@ -81,54 +114,74 @@ __device__ __forceinline__ void load_tile(double (*dst)[T + 1], const double *S,
     }
 }
 
-// Warp 0: Cholesky of the lower triangle of a (in registers), inverse of
-// the factor into linv, y = linv * b.  Returns false on a bad pivot.
-__device__ bool warp_potrf(double (*a)[T + 1], double (*linv)[T + 1], double *invd, const double *b,
-                           double *y)
+// All threads: Cholesky of the lower triangle of a (T x T, shared memory),
+// the factor into l (zero above the diagonal), its inverse into linv,
+// invd[k] = 1 / L_kk and y = L^-1 b.  Column s: the pivot from a[s][s], column
+// s of L, and the trailing update a[r][j] -= a[r][s] a[j][s] / a[s][s] for
+// s < j <= r; the inverse follows one column behind (right-looking:
+// X[k][.] = acc[k][.] / L_kk, acc[i][.] -= L[i][k] X[k][.] for i > k).  One
+// barrier per column, and each thread does at most two trailing updates and
+// one inverse update per column: on a GPU whose FP64 pipe takes tens of
+// cycles per warp instruction, the chain a single warp would run (~270
+// dependent FP64 operations) is what bounds the whole dense solve.
+// Returns false on a non-positive or non-finite pivot.
+__device__ bool cta_potrf(double (*a)[T + 1], double (*l)[T + 1], double (*acc)[T + 1], double (*linv)[T + 1],
+                          double *invd, const double *b, double *y)
 {
-    const unsigned FULL = 0xffffffffu;
-    const int r = threadIdx.x;  // < 32
-    double row[T];
-#pragma unroll
-    for (int c = 0; c < T; ++c) row[c] = r < T ? a[r][c] : 0.0;
-    bool bad = false;
-#pragma unroll
-    for (int k = 0; k < T; ++k) {
-        const double d = __shfl_sync(FULL, row[k], k);
-        bad = bad || !(d > 0.0) || !isfinite(d);
-        const double inv = rsqrt(d);
-        if (r == k) row[k] = d * inv;
-        if (r > k) row[k] *= inv;
-        if (r == 0) invd[k] = inv;
-#pragma unroll
-        for (int j = k + 1; j < T; ++j) {
-            const double ljk = __shfl_sync(FULL, row[k], j);
-            if (r >= j) row[j] = fma(-row[k], ljk, row[j]);
+    __shared__ int bad;
+    const int tid = threadIdx.x;
+    for (int e = tid; e < TT; e += CF_THREADS) {
+        const int r = e / T, c = e % T;
+        l[r][c] = 0.0;
+        linv[r][c] = 0.0;
+        acc[r][c] = r == c ? 1.0 : 0.0;
+    }
+    if (tid == 0) bad = 0;
+    __syncthreads();
+    for (int s = 0; s <= T; ++s) {
+        if (s < T) {
+            const double d = a[s][s];
+            const double inv = rsqrt(d), inv2 = inv * inv;
+            if (tid == 0) {
+                invd[s] = inv;
+                if (!(d > 0.0) || !isfinite(d)) bad = 1;
+            }
+            // lower-triangle entries (r, j) with j >= s, numbered by column
+            // from the right: column T-1-q holds entries q(q+1)/2 .. (q+1)(q+2)/2 - 1
+            const int m = (T - s) * (T - s + 1) / 2;
+            for (int e = tid; e < m; e += CF_THREADS) {
+                int q = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
+                while ((q + 1) * (q + 2) / 2 <= e) ++q;
+                while (q * (q + 1) / 2 > e) --q;
+                const int j = T - 1 - q, r = j + (e - q * (q + 1) / 2);
+                if (j == s)
+                    l[r][s] = r == s ? d * inv : a[r][s] * inv;
+                else
+                    a[r][j] = fma(-a[r][s], a[j][s] * inv2, a[r][j]);
+            }
         }
-    }
-    if (r < T) {
-#pragma unroll
-        for (int c = 0; c < T; ++c) a[r][c] = c <= r ? row[c] : 0.0;
-    }
-    __syncwarp();
-    if (r < T) {  // column r of L^-1
-        const int c = r;
-        for (int i = 0; i < c; ++i) linv[i][c] = 0.0;
-        linv[c][c] = invd[c];
-        for (int i = c + 1; i < T; ++i) {
-            double s = 0.0;
-            for (int k = c; k < i; ++k) s = fma(a[i][k], linv[k][c], s);
-            linv[i][c] = -s * invd[i];
+        if (s >= 1) {
+            const int k = s - 1;
+            const double ik = invd[k];
+            const int n = (T - k) * (k + 1);
+            for (int e = tid; e < n; e += CF_THREADS) {
+                const int i = k + e / (k + 1), c = e % (k + 1);
+                const double xk = acc[k][c] * ik;
+                if (i == k)
+                    linv[k][c] = xk;
+                else
+                    acc[i][c] = fma(-l[i][k], xk, acc[i][c]);
+            }
         }
+        __syncthreads();
     }
-    __syncwarp();
-    if (r < T) {
-        double s = 0.0;
-        for (int k = 0; k <= r; ++k) s = fma(linv[r][k], b[k], s);
-        y[r] = s;
+    if (tid < T) {
+        double sum = 0.0;
+        for (int k = 0; k <= tid; ++k) sum = fma(linv[tid][k], b[k], sum);
+        y[tid] = sum;
     }
-    __syncwarp();
-    return !bad;
+    __syncthreads();
+    return bad == 0;
 }
 
 // Single-CTA triangular solves over the factor (S lower = L, Linv = diagonal
@@ -215,8 +268,21 @@ __global__ void __launch_bounds__(CF_THREADS) k_chol_dataflow(int mode, int Np, 
     const int n_fact = mode == 0 ? nb * (nb + 1) / 2 : 0;
     const int n_tasks = n_fact + 1;
     const int tid = threadIdx.x;
+#if PSBA_CHOL_DYNAMIC
+    // tasks claimed in increasing order: the smallest unfinished claimed task
+    // has all its (smaller) dependencies claimed, so it can always run
+    __shared__ int claim;
+    while (true) {
+        if (tid == 0) claim = atomicAdd(status + 1, 1);
+        __syncthreads();
+        const int t = claim;
+        __syncthreads();
+        if (t >= n_tasks) break;
+#else
     for (int t = blockIdx.x; t < n_tasks; t += gridDim.x) {
+#endif
         if (t < n_fact) {
+            CHOL_MARK(t, 0);
             const int I = tasks[t].x, K = tasks[t].y;
             load_tile(a, S, Np, I, K);
             if (I == K && tid < T) bvec[tid] = __ldcg(rhs + I * T + tid);
@@ -272,16 +338,16 @@ __global__ void __launch_bounds__(CF_THREADS) k_chol_dataflow(int mode, int Np, 
                 __syncthreads();
                 J += n;
             }
+            CHOL_MARK(t, 1);
             const bool failed = ld_acquire(status) != 0;
             if (I == K) {
                 if (!failed) {
-                    bool good = true;
-                    if (tid < 32) good = warp_potrf(a, linv, invd, bvec, yvec);
+                    // the staging tiles are free now: L in bi[0], the inverse's accumulator in bi[1]
+                    const bool good = cta_potrf(a, bi[0], bi[1], linv, invd, bvec, yvec);
                     if (tid == 0 && !good) atomicCAS(status, 0, 1);
-                    __syncthreads();
                     for (int e = tid; e < TT; e += CF_THREADS) {
                         const int r = e / T, c = e % T;
-                        S[(size_t)(I * T + r) * Np + I * T + c] = a[r][c];
+                        S[(size_t)(I * T + r) * Np + I * T + c] = bi[0][r][c];
                         Linv[(size_t)I * TT + e] = linv[r][c];
                     }
                     if (tid < T) rhs[I * T + tid] = yvec[tid];
@@ -299,20 +365,25 @@ __global__ void __launch_bounds__(CF_THREADS) k_chol_dataflow(int mode, int Np, 
                     }
                 }
             }
+            CHOL_MARK(t, 2);
             __syncthreads();
             if (tid == 0) {
                 __threadfence();
                 st_release(flags + t, epoch);
             }
+            CHOL_MARK(t, 3);
         } else {
+            CHOL_MARK(t, 0);
             // the solve task: waits for the whole factor (mode 0), then one CTA
             if (mode == 0) block_wait(flags + (n_fact - 1), epoch, status);
             for (int i = tid; i < Np; i += CF_THREADS) vec[i] = __ldcg(rhs + i);
             __syncthreads();
             if (ld_acquire(status) == 0) {
+                CHOL_MARK(t, 1);
                 if (mode == 1) cta_forward(Np, nb, S, Linv, vec, yvec);
                 cta_back(Np, nb, S, Linv, vec, yvec, x);
             }
+            CHOL_MARK(t, 3);
         }
         __syncthreads();
     }
@@ -325,9 +396,15 @@ int chol_grid(int n_tasks)
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        // the solve task keeps its right-hand side (up to MAX_NP doubles) in
+        // dynamic shared memory on top of the static tiles: opt in to more
+        // than the default 48 KB per CTA
+        cudaFuncSetAttribute(k_chol_dataflow, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(sizeof(double) * MAX_NP));
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_chol_dataflow, CF_THREADS,
                                                       sizeof(double) * MAX_NP);
         if (per_sm < 1) per_sm = 1;
+        if (PSBA_CHOL_PER_SM > 0 && per_sm > PSBA_CHOL_PER_SM) per_sm = PSBA_CHOL_PER_SM;
     }
     const int cap = per_sm * sms;
     return n_tasks < cap ? n_tasks : cap;
@@ -343,7 +420,10 @@ void launch_chol_dataflow(const DeviceProblem &d, int mode, int epoch, double *x
     double *S = d.S, *Linv = d.Linv, *rhs = d.rhs, *x = x_out;
     int *flags = d.chol_flags, *status = d.status;
     void *args[] = {&mode, &Np, (void *)&nb, (void *)&tasks, &S, &Linv, &rhs, &x, &flags, &epoch, &status};
-    if (mode == 0) cudaMemsetAsync(d.status, 0, sizeof(int), s);
+    if (mode == 0)
+        cudaMemsetAsync(d.status, 0, 2 * sizeof(int), s);  // result word and task claim counter
+    else
+        cudaMemsetAsync(d.status + 1, 0, sizeof(int), s);  // the claim counter; keep the factor's result
     cudaLaunchCooperativeKernel((const void *)k_chol_dataflow, dim3(grid), dim3(CF_THREADS), args,
                                 sizeof(double) * d.Np, s);
     note_launch(1);

@@ -20,9 +20,12 @@ estimate.  The metric is LM iterations per second.
   system (k_chol_dataflow, one launch per LM trial), timed live with CUDA
   events inside the timed solves; FP64-bound, so its peak is the measured
   FP64 FMA rate.  roofline_schur: the same for the Schur-complement stage.
+* variable_intrinsics: 52 cameras x 64,053 points with 11- and
+  16-parameter cameras, mixed and FP64 forms, LM iterations/s.
 * batched: 1,024 small problems in one persistent launch (mixed form,
   autotuned shape) against the plain FP64 single-problem solver.
-* serving: Poisson arrivals into the continuous-batching server, p50/p99.
+* serving: Poisson arrivals into the continuous-batching server (batch lane
+  plus large lane), solves/s, p50/p99 latency per arrival rate.
 * cpu_baseline: the FP64 CPU oracle (a C restatement of the reference's
   path) on the host cores, on a bounded sample of the same problem.
 * --impl reference: the CPU oracle alone (the reference's OpenCL/MSVC path

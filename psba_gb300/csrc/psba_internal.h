@@ -82,6 +82,7 @@ struct DeviceProblem {
     double *wt = nullptr;      // 3 per obs (a, b, c of L = [[a, b], [0, c]]), or null: unweighted
     int *obs_pt = nullptr, *obs_cam = nullptr;
     int *pt_start = nullptr;   // np + 1
+    int *pt_order = nullptr;   // np: points by observation count, descending (per-point kernels' order)
     int *cam_obs = nullptr;    // observations sorted by (camera, point)
     // camera pair lists for the off-diagonal Schur blocks (k > l)
     int n_pairs = 0;           // nonempty pairs

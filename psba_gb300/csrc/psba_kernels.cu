@@ -311,11 +311,13 @@ void launch_residual(const DeviceProblem &d, const double *tab, const double *pt
 // LM fixed point by 7e-3 of the cost on a 24-camera power-law scene.
 template <typename R>
 __global__ void k_point_blocks(int np, int ncp, const int *__restrict__ pt_start,
-                               const R *__restrict__ B, const R *__restrict__ ex, R coeff,
-                               double *__restrict__ V, double *__restrict__ g, double *__restrict__ uvdiag)
+                               const int *__restrict__ pt_order, const R *__restrict__ B,
+                               const R *__restrict__ ex, R coeff, double *__restrict__ V,
+                               double *__restrict__ g, double *__restrict__ uvdiag)
 {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= np) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= np) return;
+    const int i = pt_order[t];  // points by observation count: a warp's points have similar loops
     double v00 = 0, v01 = 0, v02 = 0, v11 = 0, v12 = 0, v22 = 0;
     double g0 = 0, g1 = 0, g2 = 0;  // gradient: FP64 sums of exact products in both forms
     const int e = pt_start[i + 1];
@@ -361,11 +363,12 @@ void launch_point_blocks(const DeviceProblem &d, double coeff, cudaStream_t s)
 {
     if (d.np == 0) return;
     if (d.prec == PSBA_PREC_FP64)
-        k_point_blocks<double><<<ceil_div(d.np, 128), 128, 0, s>>>(d.np, d.N, d.pt_start, d.B, d.ex, coeff,
-                                                                     d.V, d.g, d.uvdiag);
+        k_point_blocks<double><<<ceil_div(d.np, 128), 128, 0, s>>>(d.np, d.N, d.pt_start, d.pt_order, d.B, d.ex,
+                                                                     coeff, d.V, d.g, d.uvdiag);
     else
-        k_point_blocks<float><<<ceil_div(d.np, 128), 128, 0, s>>>(
-            d.np, d.N, d.pt_start, (const float *)d.B, (const float *)d.ex, (float)coeff, d.V, d.g, d.uvdiag);
+        k_point_blocks<float><<<ceil_div(d.np, 128), 128, 0, s>>>(d.np, d.N, d.pt_start, d.pt_order,
+                                                                    (const float *)d.B, (const float *)d.ex,
+                                                                    (float)coeff, d.V, d.g, d.uvdiag);
     note_launch(1);
 }
 
@@ -825,6 +828,7 @@ void launch_schur(const DeviceProblem &d, double mu, cudaStream_t s)
 // and dpb (mu dpb + gb) for the gain ratio (levmar.cpp:271-280).
 template <typename R>
 __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int *__restrict__ pt_start,
+                                                const int *__restrict__ pt_order,
                                                 const int *__restrict__ obs_cam,
                                                 const R *__restrict__ W, const double *__restrict__ Vinv,
                                                 const double *__restrict__ g, double mu,
@@ -832,28 +836,33 @@ __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int *__re
                                                 double *__restrict__ partial)
 {
     __shared__ double r0[256], r1[256];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double s_sq = 0.0, s_rho = 0.0;
-    if (i < np) {
-        double e0 = 0, e1 = 0, e2 = 0;
-        const int end = pt_start[i + 1];
-#pragma unroll 4
-        for (int o = pt_start[i]; o < end; ++o) {
-            R w[18];
-            ldn<R, 18>(W + 18 * (size_t)o, w);
-            const double *da = dp + 6 * (size_t)__ldg(obs_cam + o);
+    // four lanes per point (points in pt_order): lane c < 3 sums component c
+    // of W^T dpa over the point's observations in order, lane 3 only takes
+    // part in the exchange; lane 0 finishes the point
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int slot = t >> 2, c = t & 3;
+    int i = -1;
+    double e = 0.0;
+    if (slot < np) {
+        i = pt_order[slot];
+        if (c < 3) {
+            const int end = pt_start[i + 1];
+#pragma unroll 2
+            for (int o = pt_start[i]; o < end; ++o) {
+                const R *w = W + 18 * (size_t)o;
+                const double *da = dp + 6 * (size_t)__ldg(obs_cam + o);
 #pragma unroll
-            for (int k = 0; k < 6; ++k) {
-                const double dk = da[k];
-                e0 = e0 + (double)w[3 * k] * dk;
-                e1 = e1 + (double)w[3 * k + 1] * dk;
-                e2 = e2 + (double)w[3 * k + 2] * dk;
+                for (int k = 0; k < 6; ++k) e = e + (double)w[3 * k + c] * da[k];
             }
         }
+    }
+    const int base = (threadIdx.x & 31) & ~3;
+    const double w0 = __shfl_sync(0xffffffffu, e, base), w1 = __shfl_sync(0xffffffffu, e, base + 1),
+                 w2 = __shfl_sync(0xffffffffu, e, base + 2);
+    double s_sq = 0.0, s_rho = 0.0;
+    if (slot < np && c == 0) {
         const double *gb = g + ncp + 3 * (size_t)i;
-        e0 = gb[0] - e0;
-        e1 = gb[1] - e1;
-        e2 = gb[2] - e2;
+        const double e0 = gb[0] - w0, e1 = gb[1] - w1, e2 = gb[2] - w2;
         eb[3 * (size_t)i] = e0;
         eb[3 * (size_t)i + 1] = e1;
         eb[3 * (size_t)i + 2] = e2;
@@ -885,16 +894,18 @@ __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int *__re
     }
 }
 
-int eb_blocks(const DeviceProblem &d) { return ceil_div(d.np > 0 ? d.np : 1, 256); }
+// four threads per point in k_eb_dpb (the variable-intrinsics version uses
+// one, and its surplus blocks write zero partials)
+int eb_blocks(const DeviceProblem &d) { return ceil_div(4LL * (d.np > 0 ? d.np : 1), 256); }
 
 void launch_eb_dpb(const DeviceProblem &d, double mu, cudaStream_t s)
 {
     if (d.cnp != 6) return launch_eb_dpb_v(d, mu, eb_blocks(d), s);
     if (d.prec == PSBA_PREC_FP64)
-        k_eb_dpb<double><<<eb_blocks(d), 256, 0, s>>>(d.np, d.N, d.pt_start, d.obs_cam, d.W, d.Vinv, d.g, mu,
+        k_eb_dpb<double><<<eb_blocks(d), 256, 0, s>>>(d.np, d.N, d.pt_start, d.pt_order, d.obs_cam, d.W, d.Vinv, d.g, mu,
                                                         d.dp, d.eb, d.red_partial);
     else
-        k_eb_dpb<float><<<eb_blocks(d), 256, 0, s>>>(d.np, d.N, d.pt_start, d.obs_cam, (const float *)d.W,
+        k_eb_dpb<float><<<eb_blocks(d), 256, 0, s>>>(d.np, d.N, d.pt_start, d.pt_order, d.obs_cam, (const float *)d.W,
                                                        d.Vinv, d.g, mu, d.dp, d.eb, d.red_partial);
     note_launch(1);
 }

@@ -799,6 +799,22 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     TRY(dalloc(h, &d.cam_obs, (size_t)no));
     TRY(upload(h, d.obs_pt, p->obs_pt, (size_t)no));
     TRY(upload(h, d.obs_cam, p->obs_cam, (size_t)no));
+    {
+        // points by observation count, descending (stable): the per-point
+        // kernels give a warp points of similar length (views per point
+        // follow a power law); each point's own sums keep their order
+        std::vector<int> deg(np, 0), order(np > 0 ? np : 1);
+        for (int o = 0; o < no; ++o) deg[p->obs_pt[o]]++;
+        int maxdeg = 0;
+        for (int i = 0; i < np; ++i) maxdeg = std::max(maxdeg, deg[i]);
+        std::vector<int> start(maxdeg + 2, 0);
+        for (int i = 0; i < np; ++i) start[maxdeg - deg[i] + 1]++;
+        for (int k = 0; k <= maxdeg; ++k) start[k + 1] += start[k];
+        for (int i = 0; i < np; ++i) order[start[maxdeg - deg[i]]++] = i;
+        TRY(dalloc(h, &d.pt_order, (size_t)np));
+        TRY(upload(h, d.pt_order, order.data(), (size_t)np));
+        TRY(sync(h));
+    }
     int *d_cnt = nullptr, *d_cam_start = nullptr, *d_pair_cnt = nullptr, *d_off = nullptr;
     TRY(dalloc(h, &d_cnt, (size_t)nc));
     TRY(dalloc(h, &d_cam_start, (size_t)nc + 1));

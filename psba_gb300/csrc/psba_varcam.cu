@@ -479,15 +479,17 @@ __global__ void k_schur_reduce_v(int n_pairs, int nc, int Np, const int *__restr
 // eb = gb - sum_j W_ij^T dpa_j, dpb = V^-1 eb, gain-ratio partials (as k_eb_dpb).
 template <typename R, int CNP>
 __global__ void __launch_bounds__(256) k_eb_dpb_v(int np, int ncp, const int *__restrict__ pt_start,
+                                                  const int *__restrict__ pt_order,
                                                   const int *__restrict__ obs_cam, const R *__restrict__ W,
                                                   const double *__restrict__ Vinv, const double *__restrict__ g,
                                                   double mu, double *__restrict__ dp, double *__restrict__ eb,
                                                   double *__restrict__ partial)
 {
     __shared__ double r0[256], r1[256];
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     double s_sq = 0.0, s_rho = 0.0;
-    if (i < np) {
+    if (t < np) {
+        const int i = pt_order[t];
         double e0 = 0, e1 = 0, e2 = 0;
         for (int o = pt_start[i]; o < pt_start[i + 1]; ++o) {
             const R *w = W + 3 * CNP * (size_t)o;
@@ -664,11 +666,11 @@ void launch_eb_dpb_v(const DeviceProblem &d, double mu, int nblocks, cudaStream_
 {
     const bool f64 = d.prec == PSBA_PREC_FP64;
     if (d.cnp == 11) {
-        if (f64) k_eb_dpb_v<double, 11><<<nblocks, 256, 0, s>>>(d.np, d.N, d.pt_start, d.obs_cam, d.W, d.Vinv, d.g, mu, d.dp, d.eb, d.red_partial);
-        else k_eb_dpb_v<float, 11><<<nblocks, 256, 0, s>>>(d.np, d.N, d.pt_start, d.obs_cam, (const float *)d.W, d.Vinv, d.g, mu, d.dp, d.eb, d.red_partial);
+        if (f64) k_eb_dpb_v<double, 11><<<nblocks, 256, 0, s>>>(d.np, d.N, d.pt_start, d.pt_order, d.obs_cam, d.W, d.Vinv, d.g, mu, d.dp, d.eb, d.red_partial);
+        else k_eb_dpb_v<float, 11><<<nblocks, 256, 0, s>>>(d.np, d.N, d.pt_start, d.pt_order, d.obs_cam, (const float *)d.W, d.Vinv, d.g, mu, d.dp, d.eb, d.red_partial);
     } else {
-        if (f64) k_eb_dpb_v<double, 16><<<nblocks, 256, 0, s>>>(d.np, d.N, d.pt_start, d.obs_cam, d.W, d.Vinv, d.g, mu, d.dp, d.eb, d.red_partial);
-        else k_eb_dpb_v<float, 16><<<nblocks, 256, 0, s>>>(d.np, d.N, d.pt_start, d.obs_cam, (const float *)d.W, d.Vinv, d.g, mu, d.dp, d.eb, d.red_partial);
+        if (f64) k_eb_dpb_v<double, 16><<<nblocks, 256, 0, s>>>(d.np, d.N, d.pt_start, d.pt_order, d.obs_cam, d.W, d.Vinv, d.g, mu, d.dp, d.eb, d.red_partial);
+        else k_eb_dpb_v<float, 16><<<nblocks, 256, 0, s>>>(d.np, d.N, d.pt_start, d.pt_order, d.obs_cam, (const float *)d.W, d.Vinv, d.g, mu, d.dp, d.eb, d.red_partial);
     }
     note_launch(1);
 }

@@ -225,6 +225,20 @@ def run_reference(args):
     return 0
 
 
+def aggregate_replicas(torch, dist, dev_s, wall_s, iters, device):
+    """Replicas only (no data-path collective): each rank solves its own
+    problem; the job's time is the slowest rank's (device and wall clock),
+    its work the sum of the ranks' iterations.  Returns (device seconds, wall
+    seconds, iterations) for the whole job; single-process runs pass through."""
+    if not dist:
+        return dev_s, wall_s, iters
+    t = torch.tensor([dev_s, wall_s], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    it = torch.tensor([float(iters)], dtype=torch.float64, device=device)
+    dist.all_reduce(it, op=dist.ReduceOp.SUM)
+    return float(t[0]), float(t[1]), float(it[0])
+
+
 def batched_leg(P, args):
     """1,024 independent problems (5-30 cameras, 200-3,000 points, 3-8 views)
     in one persistent launch under a CUDA graph, 15 LM iterations each: the
@@ -409,16 +423,7 @@ def main():
     stages = solver.stage_timing()
     solver.set_stage_timing(False)
 
-    total_dev_s = sum(dev_ms) / 1e3
-    if dist:
-        t = torch.tensor([total_dev_s, wall], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        it = torch.tensor([iters], dtype=torch.float64, device="cuda")
-        dist.all_reduce(it, op=dist.ReduceOp.SUM)
-        total_dev_s, wall = float(t[0]), float(t[1])
-        iters_all = float(it[0])
-    else:
-        iters_all = iters
+    total_dev_s, wall, iters_all = aggregate_replicas(torch, dist, sum(dev_ms) / 1e3, wall, iters, "cuda")
     value = iters_all / total_dev_s
 
     # ---- the mixed FP32/FP64 form on the same workload (same protocol)

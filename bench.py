@@ -76,6 +76,8 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=2.0, help="arrival window per rate")
     ap.add_argument("--serve-max", type=int, default=400, help="requests per rate at most")
     ap.add_argument("--serve-pool", type=int, default=32, help="distinct request scenes (cycled)")
+    ap.add_argument("--serve-large-lanes", type=int, default=None, help="server large_lanes (default: library's)")
+    ap.add_argument("--serve-large-obs", type=int, default=None, help="server large_obs (default: library's)")
     return ap.parse_args()
 
 
@@ -337,7 +339,8 @@ def serving_leg(P, args):
                        "log-U[500,60000], 4-6 views/point, 6-param cameras, mixed form, %d LM iterations, "
                        "120 GB HBM budget" % (len(pool), iters),
            "mean_observations": float(np.mean([sc.n_obs for sc in pool])), "rates": []}
-    with S.Server(precision=P.PREC_MIXED, max_iter=iters, hbm_budget_bytes=120e9) as srv:
+    with S.Server(precision=P.PREC_MIXED, max_iter=iters, hbm_budget_bytes=120e9,
+                  large_lanes=args.serve_large_lanes, large_obs=args.serve_large_obs) as srv:
         S.run_poisson(srv, pool[:4], rate=1000.0, n_requests=4, seed=1)
         first = {}
         for rate in rates:

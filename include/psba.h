@@ -272,8 +272,9 @@ size_t psba_batch_device_bytes(psba_batch *b);
  * (psba_create / psba_levmar: multi-CTA kernels and the dataflow Cholesky
  * over the whole GPU) on its own stream, concurrently with the batch lane;
  * its device memory counts against large_share of the budget.  The rest of
- * the budget is the batch lane's pool.  Requests with 11- or 16-parameter
- * cameras or with covariances always take the large lane.
+ * the budget is the batch lane's pool.  Requests with more than large_obs
+ * observations, 11- or 16-parameter cameras, or covariances also take the
+ * large lane.
  * psba_batch_submit lays a request out on the calling thread and queues it;
  * the worker admits queued requests in arrival order while a resident slot is
  * free and the request fits the pool, and advances all resident problems
@@ -298,6 +299,8 @@ typedef struct psba_server_opts {
     int large_cams;          /* requests with more cameras run on the large lane (default 40; 0: no large lane) */
     int large_lanes;         /* large-lane host threads, each solving one request at a time (default 2) */
     double large_share;      /* share of hbm_budget_bytes reserved for the large lane (default 0.25) */
+    int large_obs;           /* ... and so do requests with more observations (default 40000; 0: no limit) */
+    int reserved;
 } psba_server_opts;
 
 typedef struct psba_request_result {

@@ -11,9 +11,10 @@
 //                tile, its inverse, and y_I = L_II^-1 (b_I - sum_J L_IJ y_J)
 //                (the forward solve of L y = ea rides along)
 //   tile (I,K):  A_IK -= sum_{J<K} L_IJ L_KJ^T, then L_IK = A_IK L_KK^-T
-// After the factor, one CTA solves L^T x = y with y in shared memory; the
-// refinement solve of the mixed form (mode 1) runs both triangular solves in
-// one CTA the same way.
+// After the factor, k_tri_solve (one CTA of 512 threads, one column of the
+// update per thread) solves L^T x = y with y in shared memory; the
+// refinement solve of the mixed form (mode 1) runs both triangular solves
+// there the same way.
 //
 // This replaces the reference's explicit inverse (SPD_inv.cl: 3x3-block
 // Cholesky chain, kern_trigMat_inv, kern_trigMat_mul, then matVec_mul) with
@@ -203,7 +204,7 @@ __device__ void cta_forward(int Np, int nb, const double *__restrict__ S, const 
         }
         __syncthreads();
         if (tid < T) bs[K * T + tid] = tmp[tid];
-        for (int i = (K + 1) * T + tid; i < Np; i += CF_THREADS) {
+        for (int i = (K + 1) * T + tid; i < Np; i += blockDim.x) {
             const double2 *row = reinterpret_cast<const double2 *>(S + (size_t)i * Np + K * T);
             double s = 0.0;
 #pragma unroll
@@ -234,7 +235,7 @@ __device__ void cta_back(int Np, int nb, const double *__restrict__ S, const dou
             x[K * T + tid] = v;
         }
         __syncthreads();
-        for (int col = tid; col < K * T; col += CF_THREADS) {
+        for (int col = tid; col < K * T; col += blockDim.x) {
             const double *base = S + (size_t)(K * T) * Np + col;
             double v[T];
 #pragma unroll
@@ -248,15 +249,13 @@ __device__ void cta_back(int Np, int nb, const double *__restrict__ S, const dou
     }
 }
 
-// mode 0: factor (tile dataflow) with the forward solve of rhs carried along,
-// then one CTA runs the back solve into x.  mode 1: one CTA runs the forward
-// and back solves of rhs with the existing factor.
-__global__ void __launch_bounds__(CF_THREADS) k_chol_dataflow(int mode, int Np, int nb,
+// The factor (tile dataflow) with the forward solve of rhs carried along on
+// the diagonal tasks; the back solve runs after it in k_tri_solve.
+__global__ void __launch_bounds__(CF_THREADS) k_chol_dataflow(int Np, int nb,
                                                               const int2 *__restrict__ tasks,
                                                               double *__restrict__ S,
                                                               double *__restrict__ Linv,
                                                               double *__restrict__ rhs,
-                                                              double *__restrict__ x,
                                                               int *__restrict__ flags, int epoch,
                                                               int *__restrict__ status)
 {
@@ -264,9 +263,8 @@ __global__ void __launch_bounds__(CF_THREADS) k_chol_dataflow(int mode, int Np, 
     __shared__ double bi[BJ][T][T + 1], bk[BJ][T][T + 1], by[BJ][T];
     __shared__ double bvec[T], yvec[T], invd[T];
     __shared__ int ready_n;
-    extern __shared__ double vec[];  // Np: right-hand side of the single-CTA solves
-    const int n_fact = mode == 0 ? nb * (nb + 1) / 2 : 0;
-    const int n_tasks = n_fact + 1;
+    const int n_fact = nb * (nb + 1) / 2;
+    const int n_tasks = n_fact;
     const int tid = threadIdx.x;
 #if PSBA_CHOL_DYNAMIC
     // tasks claimed in increasing order: the smallest unfinished claimed task
@@ -372,18 +370,6 @@ __global__ void __launch_bounds__(CF_THREADS) k_chol_dataflow(int mode, int Np, 
                 st_release(flags + t, epoch);
             }
             CHOL_MARK(t, 3);
-        } else {
-            CHOL_MARK(t, 0);
-            // the solve task: waits for the whole factor (mode 0), then one CTA
-            if (mode == 0) block_wait(flags + (n_fact - 1), epoch, status);
-            for (int i = tid; i < Np; i += CF_THREADS) vec[i] = __ldcg(rhs + i);
-            __syncthreads();
-            if (ld_acquire(status) == 0) {
-                CHOL_MARK(t, 1);
-                if (mode == 1) cta_forward(Np, nb, S, Linv, vec, yvec);
-                cta_back(Np, nb, S, Linv, vec, yvec, x);
-            }
-            CHOL_MARK(t, 3);
         }
         __syncthreads();
     }
@@ -396,13 +382,7 @@ int chol_grid(int n_tasks)
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        // the solve task keeps its right-hand side (up to MAX_NP doubles) in
-        // dynamic shared memory on top of the static tiles: opt in to more
-        // than the default 48 KB per CTA
-        cudaFuncSetAttribute(k_chol_dataflow, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)(sizeof(double) * MAX_NP));
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_chol_dataflow, CF_THREADS,
-                                                      sizeof(double) * MAX_NP);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_chol_dataflow, CF_THREADS, 0);
         if (per_sm < 1) per_sm = 1;
         if (PSBA_CHOL_PER_SM > 0 && per_sm > PSBA_CHOL_PER_SM) per_sm = PSBA_CHOL_PER_SM;
     }
@@ -410,22 +390,42 @@ int chol_grid(int n_tasks)
     return n_tasks < cap ? n_tasks : cap;
 }
 
+// Triangular solves in one CTA of TS_THREADS threads with the right-hand side
+// in shared memory: forward = 1 solves L y = rhs then L^T x = y (the
+// refinement solve), forward = 0 only L^T x = rhs (after the factor, whose
+// diagonal tasks already applied L^-1).  A failed factor (status != 0)
+// leaves x untouched.
+constexpr int TS_THREADS = 512;
+
+__global__ void __launch_bounds__(TS_THREADS) k_tri_solve(int forward, int Np, int nb, const double *__restrict__ S,
+                                                           const double *__restrict__ Linv,
+                                                           const double *__restrict__ rhs, double *__restrict__ x,
+                                                           const int *__restrict__ status)
+{
+    extern __shared__ double vec[];  // Np
+    __shared__ double tmp[T];
+    if (*status != 0) return;
+    for (int i = threadIdx.x; i < Np; i += blockDim.x) vec[i] = rhs[i];
+    __syncthreads();
+    if (forward) cta_forward(Np, nb, S, Linv, vec, tmp);
+    cta_back(Np, nb, S, Linv, vec, tmp, x);
+}
+
 void launch_chol_dataflow(const DeviceProblem &d, int mode, int epoch, double *x_out, cudaStream_t s)
 {
-    const int nb = d.Np / T;
-    const int n_tasks = (mode == 0 ? nb * (nb + 1) / 2 : 0) + 1;
-    const int grid = chol_grid(n_tasks);
+    int nb = d.Np / T;
     int Np = d.Np;
-    const int2 *tasks = d.chol_tasks;
-    double *S = d.S, *Linv = d.Linv, *rhs = d.rhs, *x = x_out;
-    int *flags = d.chol_flags, *status = d.status;
-    void *args[] = {&mode, &Np, (void *)&nb, (void *)&tasks, &S, &Linv, &rhs, &x, &flags, &epoch, &status};
-    if (mode == 0)
+    if (mode == 0) {
+        const int grid = chol_grid(nb * (nb + 1) / 2);
+        const int2 *tasks = d.chol_tasks;
+        double *S = d.S, *Linv = d.Linv, *rhs = d.rhs;
+        int *flags = d.chol_flags, *status = d.status;
+        void *args[] = {&Np, &nb, (void *)&tasks, &S, &Linv, &rhs, &flags, &epoch, &status};
         cudaMemsetAsync(d.status, 0, 2 * sizeof(int), s);  // result word and task claim counter
-    else
-        cudaMemsetAsync(d.status + 1, 0, sizeof(int), s);  // the claim counter; keep the factor's result
-    cudaLaunchCooperativeKernel((const void *)k_chol_dataflow, dim3(grid), dim3(CF_THREADS), args,
-                                sizeof(double) * d.Np, s);
+        cudaLaunchCooperativeKernel((const void *)k_chol_dataflow, dim3(grid), dim3(CF_THREADS), args, 0, s);
+        note_launch(1);
+    }
+    k_tri_solve<<<1, TS_THREADS, sizeof(double) * Np, s>>>(mode == 1, Np, nb, d.S, d.Linv, d.rhs, x_out, d.status);
     note_launch(1);
 }
 

@@ -461,6 +461,7 @@ void psba_server_default_opts(psba_server_opts *o)
     o->large_cams = 40;
     o->large_lanes = 2;
     o->large_share = 0.25;
+    o->large_obs = 40000;
 }
 
 int psba_server_create(const psba_server_opts *so, const psba_opts *lm, psba_server **out)
@@ -471,6 +472,7 @@ int psba_server_create(const psba_server_opts *so, const psba_opts *lm, psba_ser
         (so->threads != 128 && so->threads != 256 && so->threads != 512) ||
         (so->lanes_per_pair != 8 && so->lanes_per_pair != 16 && so->lanes_per_pair != 32) || so->large_cams < 0 ||
         so->large_lanes < 0 || so->large_lanes > 16 || !(so->large_share >= 0.0 && so->large_share < 1.0) ||
+        so->large_obs < 0 ||
         (lm->precision != PSBA_PREC_FP64 && lm->precision != PSBA_PREC_MIXED) || lm->max_iter < 0)
         return set_error("psba_server_create: bad options"), PSBA_ERR_ARG;
     psba_server *s = new psba_server();
@@ -534,7 +536,8 @@ int psba_batch_submit(psba_server *s, const psba_problem_desc *desc, long long *
         return set_error("psba_batch_submit: 11/16-parameter cameras and weighted problems need the large lane "
                          "(large_cams > 0, large_lanes > 0)"),
                PSBA_ERR_ARG;
-    r->large = s->large_budget > 0 && (special || desc->n_cams > s->so.large_cams);
+    r->large = s->large_budget > 0 && (special || desc->n_cams > s->so.large_cams ||
+                                       (s->so.large_obs > 0 && desc->n_obs > s->so.large_obs));
     if (r->large) {
         // checked in full by psba_create on the large lane; enough here to copy safely
         if ((cnp != 6 && cnp != 11 && cnp != 16) || desc->n_cams <= 0 || desc->n_pts < 0 || desc->n_obs < 0 ||

@@ -67,6 +67,7 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-form leg")
+    ap.add_argument("--tr-iters", type=int, default=50, help="trust-region leg iterations (0: skip)")
     ap.add_argument("--varcam-iters", type=int, default=30, help="LM iterations of the variable-intrinsics leg (0: skip)")
     ap.add_argument("--batch", type=int, default=1024, help="problems in the batched leg (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=3)
@@ -327,17 +328,20 @@ def varcam_leg(P, args):
 
 def serving_leg(P, args):
     """Poisson arrivals of requests (cameras log-uniform 5-138, points
-    500-60,000, 4-6 views, 6-parameter cameras) into the serving engine
+    500-60,000, 4-6 views, 6- or 11-parameter cameras) into the serving engine
     (mixed form, 15 LM iterations, 120 GB HBM budget); p50/p99 latency from
     submission to result on the host clock."""
     from psba_gb300 import scenes
     from psba_gb300 import serve as S
     rates = [float(x) for x in args.serve_rates.split(",") if x.strip()]
     pool = scenes.serving_scenes(args.serve_pool, seed=2000)
+    # every other request scene with 11-parameter cameras (intrinsics 1% off)
+    pool = [scenes.with_intrinsics(sc, 11, seed=3000 + q, k_off=0.01) if q % 2 else sc
+            for q, sc in enumerate(pool)]
     iters = 15
     out = {"workload": "Poisson arrivals; %d distinct request scenes cycled: cameras log-U[5,138], points "
-                       "log-U[500,60000], 4-6 views/point, 6-param cameras, mixed form, %d LM iterations, "
-                       "120 GB HBM budget" % (len(pool), iters),
+                       "log-U[500,60000], 4-6 views/point, half 6-param and half 11-param cameras, mixed form, "
+                       "%d LM iterations, 120 GB HBM budget" % (len(pool), iters),
            "mean_observations": float(np.mean([sc.n_obs for sc in pool])), "rates": []}
     with S.Server(precision=P.PREC_MIXED, max_iter=iters, hbm_budget_bytes=120e9,
                   large_lanes=args.serve_large_lanes, large_obs=args.serve_large_obs) as srv:
@@ -452,6 +456,24 @@ def main():
                  "speedup_vs_fp64": (m_iters / sum(m_ms)) / (iters / sum(dev_ms)),
                  "stage_ms": {k: (v[0] / v[1] if v[1] else 0.0) for k, v in m_stages.items()}}
 
+    # ---- trust region (dogleg) on the same workload, FP64, same protocol
+    tr = None
+    if args.tr_iters > 0:
+        topts = P.default_opts(allow_switch=0, max_iter=args.tr_iters)
+        solver.reset_params()
+        solver.trust_region(topts, fetch=False, trace_cap=0)  # warm-up
+        t_ms, t_iters, t_cost = [], 0, None
+        for _ in range(max(1, min(args.steps, 3))):
+            solver.reset_params()
+            flush_l2(torch, flush)
+            r = solver.trust_region(topts, fetch=False, trace_cap=0)
+            t_ms.append(r.device_ms)
+            t_iters += r.iterations
+            t_cost = r.final_cost
+        tr = {"value": t_iters / (sum(t_ms) / 1e3), "unit": UNIT, "ms_per_step": sum(t_ms) / len(t_ms),
+              "iterations_per_solve": t_iters / len(t_ms), "final_cost": t_cost,
+              "driver": "trust_region (dogleg / 2-D subspace, modified-Cholesky fallback), FP64"}
+
     # ---- end to end through the C ABI from host buffers
     e2e_s, e2e_iters, h2d, d2h = 0.0, 0, 0, 0
     for _ in range(args.e2e_steps):
@@ -509,7 +531,7 @@ def main():
                            "hbm": {"achieved": achieved_gbs, "peak": peak_gbs, "unit": "GB/s",
                                    "frac": achieved_gbs / peak_gbs, "algorithmic_bytes": schur_bytes(sc),
                                    "peak_source": peak_kind}},
-        "stage_ms": stage_ms, "mixed": mixed,
+        "stage_ms": stage_ms, "mixed": mixed, "trust_region": tr,
         "stage_share": {k: (v[0] / total_stage if total_stage else 0.0) for k, v in stages.items()},
         "clocks": clk, "gpu_launches": int(launches),
     }

@@ -459,9 +459,9 @@ void psba_server_default_opts(psba_server_opts *o)
     o->threads = 256;
     o->lanes_per_pair = 32;
     o->large_cams = 40;
-    o->large_lanes = 2;
+    o->large_lanes = 4;
     o->large_share = 0.25;
-    o->large_obs = 40000;
+    o->large_obs = 20000;
 }
 
 int psba_server_create(const psba_server_opts *so, const psba_opts *lm, psba_server **out)

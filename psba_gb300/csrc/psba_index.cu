@@ -12,6 +12,8 @@
 // Every list is produced in a fixed order (block-wide scans and in-chunk
 // sorts keyed by position, no order-dependent atomics), so it is the same
 // on every run and equal to the host construction entry for entry.
+#include <algorithm>
+
 #include "psba_internal.h"
 
 namespace psba {
@@ -97,24 +99,18 @@ __global__ void k_pt_start(int np, int no, const int *__restrict__ obs_pt, int *
     pt_start[i] = lo;
 }
 
-// observations per camera (integer counts: the order of the additions does
-// not matter)
-__global__ void k_cam_count(int no, const int *__restrict__ obs_cam, int *__restrict__ cnt)
+// CTA (k, s): the observations of camera k in chunk s (observations
+// [s * chunk, (s + 1) * chunk)), in ascending order, from off[k * n_chunks + s]
+// on (a stable block-wide compaction; the host counts the chunks).
+__global__ void __launch_bounds__(IX_THREADS) k_cam_fill(int no, int chunk, const int *__restrict__ obs_cam,
+                                                          const int *__restrict__ off, int *__restrict__ cam_obs)
 {
-    const int o = blockIdx.x * blockDim.x + threadIdx.x;
-    if (o < no) atomicAdd(cnt + obs_cam[o], 1);
-}
-
-// One CTA per camera k: the observations of k in ascending order (a stable
-// block-wide compaction of the observation stream).
-__global__ void __launch_bounds__(IX_THREADS) k_cam_fill(int no, const int *__restrict__ obs_cam,
-                                                          const int *__restrict__ cam_start, int *__restrict__ cam_obs)
-{
-    const int k = blockIdx.x;
-    int base = cam_start[k];
-    for (int o0 = 0; o0 < no; o0 += IX_THREADS) {
-        const int o = o0 + threadIdx.x;
-        const int f = (o < no && obs_cam[o] == k) ? 1 : 0;
+    const int k = blockIdx.x, s = blockIdx.y;
+    const int o0 = s * chunk, o1 = min(no, o0 + chunk);
+    int base = off[(size_t)k * gridDim.y + s];
+    for (int c0 = o0; c0 < o1; c0 += IX_THREADS) {
+        const int o = c0 + threadIdx.x;
+        const int f = (o < o1 && obs_cam[o] == k) ? 1 : 0;
         int total;
         const int pos = block_exscan(f, &total);
         if (f) cam_obs[base + pos] = o;
@@ -122,35 +118,43 @@ __global__ void __launch_bounds__(IX_THREADS) k_cam_fill(int no, const int *__re
     }
 }
 
-// One CTA per camera k: for each observation a of k (point i), the earlier
-// observations b of point i belong to cameras l < k; count the entries of
-// every pair (k, l).  cnt is nc x nc, row k.
-__global__ void __launch_bounds__(IX_THREADS) k_pair_count(int nc, const int *__restrict__ cam_start,
+// Pair entries are produced per segment: up to seg_len consecutive
+// observations of one camera's list (camera seg_cam[q], from seg_first[q] in
+// cam_obs).  For each observation a of camera k (point i), the earlier
+// observations b of point i belong to cameras l < k: the entries (a, b) of
+// pair (k, l).
+
+// CTA per segment: its entries per pair (k, l), row q of cnt (nc wide).
+__global__ void __launch_bounds__(IX_THREADS) k_pair_count(int nc, int seg_len, const int *__restrict__ seg_cam,
+                                                            const int *__restrict__ seg_first,
+                                                            const int *__restrict__ cam_start,
                                                             const int *__restrict__ cam_obs,
                                                             const int *__restrict__ obs_pt,
                                                             const int *__restrict__ obs_cam,
-                                                            const int *__restrict__ pt_start,
-                                                            int *__restrict__ cnt)
+                                                            const int *__restrict__ pt_start, int *__restrict__ cnt)
 {
     extern __shared__ int hist[];  // nc
-    const int k = blockIdx.x;
+    const int q = blockIdx.x, k = seg_cam[q];
     for (int l = threadIdx.x; l < nc; l += IX_THREADS) hist[l] = 0;
     __syncthreads();
-    for (int idx = cam_start[k] + threadIdx.x; idx < cam_start[k + 1]; idx += IX_THREADS) {
+    const int first = seg_first[q], end = min(cam_start[k + 1], first + seg_len);
+    for (int idx = first + threadIdx.x; idx < end; idx += IX_THREADS) {
         const int a = cam_obs[idx];
-        for (int b = pt_start[obs_pt[a]]; b < a; ++b) atomicAdd(&hist[obs_cam[b]], 1);
+        for (int b = pt_start[obs_pt[a]]; b < a; ++b) atomicAdd(&hist[obs_cam[b]], 1);  // integer counts
     }
     __syncthreads();
-    for (int l = threadIdx.x; l < nc; l += IX_THREADS) cnt[(size_t)k * nc + l] = hist[l];
+    for (int l = threadIdx.x; l < nc; l += IX_THREADS) cnt[(size_t)q * nc + l] = hist[l];
 }
 
-// One CTA per camera k: write the entries of every pair (k, l) at
-// off[k * nc + l] onwards, in ascending point order.  The entry stream of
-// camera k (its observations in ascending point order, each followed by the
-// earlier observations of its point) is cut into chunks of IX_THREADS
-// entries; a chunk is sorted by (l, position) and each entry goes to its
+// CTA per segment: write its entries of every pair (k, l) from off[q * nc + l]
+// on, in ascending point order.  The segment is taken IX_THREADS observations
+// at a time; their entry stream (the observations in order, each followed by
+// the earlier observations of its point) is cut into chunks of IX_THREADS
+// entries, a chunk is sorted by (l, position), and each entry goes to its
 // pair's running offset plus its rank among the chunk's entries of that pair.
-__global__ void __launch_bounds__(IX_THREADS) k_pair_fill(int nc, const int *__restrict__ cam_start,
+__global__ void __launch_bounds__(IX_THREADS) k_pair_fill(int nc, int seg_len, const int *__restrict__ seg_cam,
+                                                           const int *__restrict__ seg_first,
+                                                           const int *__restrict__ cam_start,
                                                            const int *__restrict__ cam_obs,
                                                            const int *__restrict__ obs_pt,
                                                            const int *__restrict__ obs_cam,
@@ -161,18 +165,18 @@ __global__ void __launch_bounds__(IX_THREADS) k_pair_fill(int nc, const int *__r
     extern __shared__ int run[];  // nc running offsets
     __shared__ int goff[IX_THREADS], ga[IX_THREADS], eA[IX_THREADS], eB[IX_THREADS];
     __shared__ unsigned keys[IX_THREADS];
-    const int k = blockIdx.x, t = threadIdx.x;
-    for (int l = t; l < nc; l += IX_THREADS) run[l] = off[(size_t)k * nc + l];
-    const int end = cam_start[k + 1];
-    for (int c0 = cam_start[k]; c0 < end; c0 += IX_THREADS) {
-        const int idx = c0 + t;
+    const int q = blockIdx.x, k = seg_cam[q], t = threadIdx.x;
+    for (int l = t; l < nc; l += IX_THREADS) run[l] = off[(size_t)q * nc + l];
+    const int first = seg_first[q], end = min(cam_start[k + 1], first + seg_len);
+    for (int o0 = first; o0 < end; o0 += IX_THREADS) {
+        const int idx = o0 + t;
         int g = 0, a = -1;
         if (idx < end) {
             a = cam_obs[idx];
             g = a - pt_start[obs_pt[a]];
         }
         int total;
-        const int ex = block_exscan(g, &total);
+        const int ex = block_exscan(g, &total);  // its barriers also order run[] and the previous pass
         goff[t] = ex;
         ga[t] = a;
         __syncthreads();
@@ -197,17 +201,17 @@ __global__ void __launch_bounds__(IX_THREADS) k_pair_fill(int nc, const int *__r
             keys[t] = key;
             block_sort(keys);
             const unsigned v = keys[t];
-            int l = -1, first = 0;
+            int l = -1, lo_l = 0;
             if (v != 0xffffffffu) {
                 l = (int)(v >> 8);
-                first = lower_bound_u(keys, IX_THREADS, (unsigned)l << 8);
+                lo_l = lower_bound_u(keys, IX_THREADS, (unsigned)l << 8);
                 const int src = (int)(v & 0xffu);
-                const int dest = run[l] + (t - first);
+                const int dest = run[l] + (t - lo_l);
                 pa[dest] = eA[src];
                 pb[dest] = eB[src];
             }
             __syncthreads();
-            if (l >= 0 && (t == IX_THREADS - 1 || (keys[t + 1] >> 8) != (unsigned)l)) run[l] += t - first + 1;
+            if (l >= 0 && (t == IX_THREADS - 1 || (keys[t + 1] >> 8) != (unsigned)l)) run[l] += t - lo_l + 1;
             __syncthreads();
         }
     }
@@ -219,31 +223,46 @@ void launch_pt_start(int np, int no, const int *obs_pt, int *pt_start, cudaStrea
     note_launch(1);
 }
 
-void launch_cam_count(int no, const int *obs_cam, int *cnt, cudaStream_t s)
+int cam_fill_chunk(int nc, int no)
+{
+    // 8 passes of IX_THREADS per CTA, more when nc x chunks would pass 4M or
+    // the chunks the grid's 65535 rows
+    const long long want = std::max(((long long)no * nc + (1LL << 22) - 1) >> 22, ((long long)no + 65534) / 65535);
+    const long long c = std::max<long long>(8 * IX_THREADS, (want + IX_THREADS - 1) / IX_THREADS * IX_THREADS);
+    return (int)std::min<long long>(c, std::max(no, IX_THREADS));
+}
+
+void launch_cam_fill(int nc, int no, int chunk, const int *obs_cam, const int *off, int *cam_obs, cudaStream_t s)
 {
     if (no == 0) return;
-    k_cam_count<<<(no + 255) / 256, 256, 0, s>>>(no, obs_cam, cnt);
+    k_cam_fill<<<dim3(nc, (no + chunk - 1) / chunk), IX_THREADS, 0, s>>>(no, chunk, obs_cam, off, cam_obs);
     note_launch(1);
 }
 
-void launch_cam_fill(int nc, int no, const int *obs_cam, const int *cam_start, int *cam_obs, cudaStream_t s)
+int pair_segment_len(int nc, int no)
 {
-    k_cam_fill<<<nc, IX_THREADS, 0, s>>>(no, obs_cam, cam_start, cam_obs);
+    // one pass of IX_THREADS per CTA, more when segments x nc would pass 4M
+    const long long m = std::max<long long>(1, ((long long)no * nc + (256LL << 22) - 1) / (256LL << 22));
+    return (int)std::min<long long>(m * IX_THREADS, 1 << 30);
+}
+
+void launch_pair_count(int nc, int nseg, int seg_len, const int *seg_cam, const int *seg_first, const int *cam_start,
+                       const int *cam_obs, const int *obs_pt, const int *obs_cam, const int *pt_start, int *cnt,
+                       cudaStream_t s)
+{
+    if (nseg == 0) return;
+    k_pair_count<<<nseg, IX_THREADS, sizeof(int) * nc, s>>>(nc, seg_len, seg_cam, seg_first, cam_start, cam_obs,
+                                                            obs_pt, obs_cam, pt_start, cnt);
     note_launch(1);
 }
 
-void launch_pair_count(int nc, const int *cam_start, const int *cam_obs, const int *obs_pt, const int *obs_cam,
-                       const int *pt_start, int *cnt, cudaStream_t s)
+void launch_pair_fill(int nc, int nseg, int seg_len, const int *seg_cam, const int *seg_first, const int *cam_start,
+                      const int *cam_obs, const int *obs_pt, const int *obs_cam, const int *pt_start, const int *off,
+                      int *pa, int *pb, cudaStream_t s)
 {
-    k_pair_count<<<nc, IX_THREADS, sizeof(int) * nc, s>>>(nc, cam_start, cam_obs, obs_pt, obs_cam, pt_start, cnt);
-    note_launch(1);
-}
-
-void launch_pair_fill(int nc, const int *cam_start, const int *cam_obs, const int *obs_pt, const int *obs_cam,
-                      const int *pt_start, const int *off, int *pa, int *pb, cudaStream_t s)
-{
-    k_pair_fill<<<nc, IX_THREADS, sizeof(int) * nc, s>>>(nc, cam_start, cam_obs, obs_pt, obs_cam, pt_start, off, pa,
-                                                          pb);
+    if (nseg == 0) return;
+    k_pair_fill<<<nseg, IX_THREADS, sizeof(int) * nc, s>>>(nc, seg_len, seg_cam, seg_first, cam_start, cam_obs, obs_pt,
+                                                           obs_cam, pt_start, off, pa, pb);
     note_launch(1);
 }
 

@@ -188,12 +188,19 @@ void launch_chol_dataflow(const DeviceProblem &d, int mode, int epoch, double *x
 
 // index lists on the GPU, psba_index.cu
 void launch_pt_start(int np, int no, const int *obs_pt, int *pt_start, cudaStream_t s);
-void launch_cam_count(int no, const int *obs_cam, int *cnt, cudaStream_t s);
-void launch_cam_fill(int nc, int no, const int *obs_cam, const int *cam_start, int *cam_obs, cudaStream_t s);
-void launch_pair_count(int nc, const int *cam_start, const int *cam_obs, const int *obs_pt, const int *obs_cam,
-                       const int *pt_start, int *cnt, cudaStream_t s);
-void launch_pair_fill(int nc, const int *cam_start, const int *cam_obs, const int *obs_pt, const int *obs_cam,
-                      const int *pt_start, const int *off, int *pa, int *pb, cudaStream_t s);
+// cam_obs: CTA (k, s) writes camera k's observations of chunk s from
+// off[k * n_chunks + s] on; cam_fill_chunk gives the chunk length
+int cam_fill_chunk(int nc, int no);
+void launch_cam_fill(int nc, int no, int chunk, const int *obs_cam, const int *off, int *cam_obs, cudaStream_t s);
+// pair lists per segment of a camera's list (pair_segment_len observations):
+// counts per (segment, l), then the entries from the host-scanned offsets
+int pair_segment_len(int nc, int no);
+void launch_pair_count(int nc, int nseg, int seg_len, const int *seg_cam, const int *seg_first, const int *cam_start,
+                       const int *cam_obs, const int *obs_pt, const int *obs_cam, const int *pt_start, int *cnt,
+                       cudaStream_t s);
+void launch_pair_fill(int nc, int nseg, int seg_len, const int *seg_cam, const int *seg_first, const int *cam_start,
+                      const int *cam_obs, const int *obs_pt, const int *obs_cam, const int *pt_start, const int *off,
+                      int *pa, int *pb, cudaStream_t s);
 
 // variable intrinsics (cnp 11 / 16), psba_varcam.cu
 size_t varcam_cam_partial(int cnp);   // doubles per camera-unit partial

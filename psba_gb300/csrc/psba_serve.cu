@@ -344,7 +344,9 @@ size_t large_bytes(const psba_problem_desc &p, int cnp)
     const size_t per_pt = 3 * 3 + 6 * 2 + 9 + 3 * 6;
     const size_t doubles = no * per_obs + np * per_pt + N * 8 + nc * (c * c + 2 * CAMTAB) + 3 * Np * Np +
                            Np * TILE + (entries / SCHUR_CHUNK + nc * 8) * c * c;
-    return doubles * sizeof(double) + entries * 2 * sizeof(int) + ((size_t)16 << 20);
+    // index-build scratch: counts and offsets per (pair-list segment, camera)
+    const size_t segs = no / (size_t)pair_segment_len(p.n_cams, p.n_obs) + nc;
+    return doubles * sizeof(double) + entries * 2 * sizeof(int) + segs * nc * 2 * sizeof(int) + ((size_t)16 << 20);
 }
 
 void large_main(psba_server *s)

@@ -799,12 +799,21 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     TRY(dalloc(h, &d.cam_obs, (size_t)no));
     TRY(upload(h, d.obs_pt, p->obs_pt, (size_t)no));
     TRY(upload(h, d.obs_cam, p->obs_cam, (size_t)no));
+    // points by observation count, descending (stable): the per-point kernels
+    // give a warp points of similar length (views per point follow a power
+    // law); each point's own sums keep their order.  Per camera and per
+    // chunk of the observation array: observation counts, scanned in (camera,
+    // chunk) order into where each chunk's observations of the camera start
+    // in cam_obs.
+    const int cam_chunk = cam_fill_chunk(nc, no);
+    const int n_chunks = no > 0 ? (no + cam_chunk - 1) / cam_chunk : 0;
+    std::vector<int> cam_start(nc + 1, 0), chunk_off((size_t)nc * n_chunks, 0);
     {
-        // points by observation count, descending (stable): the per-point
-        // kernels give a warp points of similar length (views per point
-        // follow a power law); each point's own sums keep their order
         std::vector<int> deg(np, 0), order(np > 0 ? np : 1);
-        for (int o = 0; o < no; ++o) deg[p->obs_pt[o]]++;
+        for (int o = 0; o < no; ++o) {
+            deg[p->obs_pt[o]]++;
+            chunk_off[(size_t)p->obs_cam[o] * n_chunks + o / cam_chunk]++;
+        }
         int maxdeg = 0;
         for (int i = 0; i < np; ++i) maxdeg = std::max(maxdeg, deg[i]);
         std::vector<int> start(maxdeg + 2, 0);
@@ -813,41 +822,69 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
         for (int i = 0; i < np; ++i) order[start[maxdeg - deg[i]]++] = i;
         TRY(dalloc(h, &d.pt_order, (size_t)np));
         TRY(upload(h, d.pt_order, order.data(), (size_t)np));
-        TRY(sync(h));
+        int run = 0;
+        for (int k = 0; k < nc; ++k) {
+            cam_start[k] = run;
+            for (int s = 0; s < n_chunks; ++s) {
+                const int c = chunk_off[(size_t)k * n_chunks + s];
+                chunk_off[(size_t)k * n_chunks + s] = run;
+                run += c;
+            }
+        }
+        cam_start[nc] = run;
     }
-    int *d_cnt = nullptr, *d_cam_start = nullptr, *d_pair_cnt = nullptr, *d_off = nullptr;
-    TRY(dalloc(h, &d_cnt, (size_t)nc));
+    // pair-list segments: up to seg_len consecutive observations of one
+    // camera's list
+    const int seg_len = pair_segment_len(nc, no);
+    std::vector<int> seg_cam, seg_first, cam_seg(nc + 1, 0);
+    for (int k = 0; k < nc; ++k) {
+        for (int b = cam_start[k]; b < cam_start[k + 1]; b += seg_len) {
+            seg_cam.push_back(k);
+            seg_first.push_back(b);
+        }
+        cam_seg[k + 1] = (int)seg_cam.size();
+    }
+    const int nseg = (int)seg_cam.size();
+    int *d_cam_start = nullptr, *d_chunk_off = nullptr, *d_seg_cam = nullptr, *d_seg_first = nullptr;
+    int *d_seg_cnt = nullptr, *d_off = nullptr;
     TRY(dalloc(h, &d_cam_start, (size_t)nc + 1));
-    TRY(dalloc(h, &d_pair_cnt, (size_t)nc * nc));
-    TRY(dalloc(h, &d_off, (size_t)nc * nc));
-    PSBA_CUDA_TRY(cudaMemsetAsync(d_cnt, 0, sizeof(int) * nc, h->stream));
-    launch_pt_start(np, no, d.obs_pt, d.pt_start, h->stream);
-    launch_cam_count(no, d.obs_cam, d_cnt, h->stream);
-    std::vector<int> cam_start(nc + 1, 0);
-    PSBA_CUDA_TRY(cudaMemcpyAsync(cam_start.data() + 1, d_cnt, sizeof(int) * nc, cudaMemcpyDeviceToHost, h->stream));
-    TRY(sync(h));
-    for (int j = 0; j < nc; ++j) cam_start[j + 1] += cam_start[j];
+    TRY(dalloc(h, &d_chunk_off, std::max<size_t>(1, chunk_off.size())));
+    TRY(dalloc(h, &d_seg_cam, std::max(1, nseg)));
+    TRY(dalloc(h, &d_seg_first, std::max(1, nseg)));
+    TRY(dalloc(h, &d_seg_cnt, std::max<size_t>(1, (size_t)nseg * nc)));
+    TRY(dalloc(h, &d_off, std::max<size_t>(1, (size_t)nseg * nc)));
     TRY(upload(h, d_cam_start, cam_start.data(), (size_t)nc + 1));
-    launch_cam_fill(nc, no, d.obs_cam, d_cam_start, d.cam_obs, h->stream);
-    launch_pair_count(nc, d_cam_start, d.cam_obs, d.obs_pt, d.obs_cam, d.pt_start, d_pair_cnt, h->stream);
-    std::vector<int> pair_cnt((size_t)nc * nc);
-    PSBA_CUDA_TRY(cudaMemcpyAsync(pair_cnt.data(), d_pair_cnt, sizeof(int) * pair_cnt.size(), cudaMemcpyDeviceToHost,
-                                  h->stream));
+    TRY(upload(h, d_chunk_off, chunk_off.data(), chunk_off.size()));
+    TRY(upload(h, d_seg_cam, seg_cam.data(), (size_t)nseg));
+    TRY(upload(h, d_seg_first, seg_first.data(), (size_t)nseg));
+    launch_pt_start(np, no, d.obs_pt, d.pt_start, h->stream);
+    launch_cam_fill(nc, no, cam_chunk, d.obs_cam, d_chunk_off, d.cam_obs, h->stream);
+    launch_pair_count(nc, nseg, seg_len, d_seg_cam, d_seg_first, d_cam_start, d.cam_obs, d.obs_pt, d.obs_cam,
+                      d.pt_start, d_seg_cnt, h->stream);
+    std::vector<int> seg_cnt((size_t)nseg * nc), off((size_t)nseg * nc, 0);
+    if (!seg_cnt.empty())
+        PSBA_CUDA_TRY(cudaMemcpyAsync(seg_cnt.data(), d_seg_cnt, sizeof(int) * seg_cnt.size(),
+                                      cudaMemcpyDeviceToHost, h->stream));
     TRY(sync(h));
     // camera pairs k > l with common points, numbered in (k, l) order; the
-    // entries of each pair start at off[k * nc + l]
-    std::vector<int> pair_kl, off((size_t)nc * nc, 0);
+    // entries of pair (k, l) from segment q start at off[q * nc + l]
+    std::vector<int> pair_kl;
     std::vector<long long> pair_start(1, 0);
     for (int k = 0; k < nc; ++k)
         for (int l = 0; l < k; ++l) {
-            const int c = pair_cnt[(size_t)k * nc + l];
+            long long c = 0;
+            for (int q = cam_seg[k]; q < cam_seg[k + 1]; ++q) c += seg_cnt[(size_t)q * nc + l];
             if (c == 0) continue;
             if (pair_start.back() + c > (1LL << 31) - 1)
                 return set_error("too many camera-pair entries"), PSBA_ERR_ARG;
-            off[(size_t)k * nc + l] = (int)pair_start.back();
+            long long run = pair_start.back();
+            for (int q = cam_seg[k]; q < cam_seg[k + 1]; ++q) {
+                off[(size_t)q * nc + l] = (int)run;
+                run += seg_cnt[(size_t)q * nc + l];
+            }
             pair_kl.push_back(k);
             pair_kl.push_back(l);
-            pair_start.push_back(pair_start.back() + c);
+            pair_start.push_back(run);
         }
     const int n_pairs = (int)pair_kl.size() / 2;
     const long long n_entries = pair_start.back();
@@ -856,8 +893,8 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     TRY(dalloc(h, &d.pair_b, (size_t)n_entries));
     TRY(upload(h, d.pair_kl, pair_kl.data(), pair_kl.size()));
     TRY(upload(h, d_off, off.data(), off.size()));
-    launch_pair_fill(nc, d_cam_start, d.cam_obs, d.obs_pt, d.obs_cam, d.pt_start, d_off, d.pair_a, d.pair_b,
-                     h->stream);
+    launch_pair_fill(nc, nseg, seg_len, d_seg_cam, d_seg_first, d_cam_start, d.cam_obs, d.obs_pt, d.obs_cam,
+                     d.pt_start, d_off, d.pair_a, d.pair_b, h->stream);
     TRY(check_launch());
     // Schur work units; execution order longest first
     std::vector<SchurUnit> off_units, diag_units;

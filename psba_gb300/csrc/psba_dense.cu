@@ -1,20 +1,17 @@
 // Dense FP64 reduced-camera solve on sm_103a.
 //
 // S (Np x Np, lower triangle, Np a multiple of TILE) is factored S = L L^T
-// by one cooperative persistent kernel that runs a tile dataflow: every
-// TILE x TILE lower tile is a task; tasks are numbered column by column and
-// each CTA takes tasks c, c + G, c + 2G, ... in increasing order.  A task
-// waits (bounded spin on per-task flags in global memory, acquire/release)
-// only for tasks with smaller numbers, so with all CTAs resident (cooperative
-// launch) the smallest unfinished task can always run: no deadlock.
-//   tile (I,I):  A_II -= sum_J L_IJ L_IJ^T, then a CTA-wide Cholesky of the
-//                tile, its inverse, and y_I = L_II^-1 (b_I - sum_J L_IJ y_J)
-//                (the forward solve of L y = ea rides along)
-//   tile (I,K):  A_IK -= sum_{J<K} L_IJ L_KJ^T, then L_IK = A_IK L_KK^-T
-// After the factor, k_tri_solve (one CTA of 512 threads, one column of the
-// update per thread) solves L^T x = y with y in shared memory; the
-// refinement solve of the mixed form (mode 1) runs both triangular solves
-// there the same way.
+// by one cooperative persistent kernel over TILE x TILE lower tiles.  CTA 0
+// (the panel) walks the diagonal: it applies the last update to each
+// diagonal tile, factors it (cta_potrf, with the forward solve of rhs carried
+// along) and forms the sub-diagonal tile below it, which it keeps for the
+// next step.  The other CTAs (helpers) accumulate every other update
+// (left-looking) and solve the remaining tiles against the diagonal
+// inverses, in a fixed dependency order; waits are bounded spins on per-task
+// flags in global memory (acquire/release).  After the factor, k_tri_solve
+// (one CTA of 512 threads, one column of the update per thread) solves
+// L^T x = y with y in shared memory; the refinement solve of the mixed form
+// (mode 1) runs both triangular solves there the same way.
 //
 // This replaces the reference's explicit inverse (SPD_inv.cl: 3x3-block
 // Cholesky chain, kern_trigMat_inv, kern_trigMat_mul, then matVec_mul) with
@@ -22,6 +19,8 @@
 // or non-finite pivot (SPD_inv.cl:66-107) sets status 1; every task still
 // raises its flag, so nothing waits forever.  A spin that runs out of its
 // iteration budget sets status 2 and the kernel completes.
+#include <vector>
+
 #include "psba_internal.h"
 
 namespace psba {
@@ -29,23 +28,18 @@ namespace psba {
 constexpr int T = TILE;
 constexpr int TT = TILE * TILE;
 // Launch shape (compile-time tuning knobs): threads per CTA, update steps
-// staged per batch, a cap on CTAs per SM (0: as many as fit), and whether
-// CTAs claim tasks through an atomic counter (1) or take every grid-th task (0).
+// staged per batch, and a cap on CTAs per SM (0: as many as fit).
 #ifndef PSBA_CHOL_THREADS
-#define PSBA_CHOL_THREADS 128
+#define PSBA_CHOL_THREADS 256
 #endif
 #ifndef PSBA_CHOL_BJ
 #define PSBA_CHOL_BJ 8
 #endif
 #ifndef PSBA_CHOL_PER_SM
-#define PSBA_CHOL_PER_SM 0
-#endif
-#ifndef PSBA_CHOL_DYNAMIC
-#define PSBA_CHOL_DYNAMIC 0
+#define PSBA_CHOL_PER_SM 1  // the panel's FP64 chain runs alone on its SM
 #endif
 constexpr int CF_THREADS = PSBA_CHOL_THREADS;
 constexpr long long SPIN_LIMIT = 1LL << 22;  // ~0.5 s of polling with 64 ns sleeps
-constexpr int MAX_NP = 4096;                 // largest reduced system (dynamic shared memory of the solve)
 constexpr int BJ = PSBA_CHOL_BJ;             // update steps staged per batch in a tile task
 static_assert(BJ >= 2, "the diagonal factor reuses two staging tiles");
 
@@ -115,71 +109,229 @@ __device__ __forceinline__ void load_tile(double (*dst)[T + 1], const double *S,
     }
 }
 
-// All threads: Cholesky of the lower triangle of a (T x T, shared memory),
-// the factor into l (zero above the diagonal), its inverse into linv,
-// invd[k] = 1 / L_kk and y = L^-1 b.  Column s: the pivot from a[s][s], column
-// s of L, and the trailing update a[r][j] -= a[r][s] a[j][s] / a[s][s] for
-// s < j <= r; the inverse follows one column behind (right-looking:
-// X[k][.] = acc[k][.] / L_kk, acc[i][.] -= L[i][k] X[k][.] for i > k).  One
-// barrier per column, and each thread does at most two trailing updates and
-// one inverse update per column: on a GPU whose FP64 pipe takes tens of
-// cycles per warp instruction, the chain a single warp would run (~270
-// dependent FP64 operations) is what bounds the whole dense solve.
-// Returns false on a non-positive or non-finite pivot.
-__device__ bool cta_potrf(double (*a)[T + 1], double (*l)[T + 1], double (*acc)[T + 1], double (*linv)[T + 1],
-                          double *invd, const double *b, double *y)
+// ---------------------------------------------------------------------------
+// Diagonal-tile factor.  GB300 issues one FP64 warp instruction per ~64
+// cycles however many lanes are active, and an FP64 result is ready ~64
+// cycles after issue, so the factor of a 16 x 16 tile is bound by its chain
+// of dependent pivots (d_s, then 1/sqrt(d_s)) and by how much latency the
+// rest adds per column.  The plan below keeps everything but the pivot chain
+// off warp 0 and gives every other thread a fixed, index-free role, in
+// T + 1 phases separated by one CTA barrier each:
+//   warp 0    phase s: d_s = a[s][s] - (a[s][s-1] / L_{s-1,s-1})^2 (the last
+//             update of the pivot, one column ahead of the others), 1/L_ss.
+//   trailing  (warps 1, 2, 3, 5) own the entries a[r][j], 1 <= j <= r, and
+//             b[r] (as column T) in registers.  Phase s applies column s-1:
+//             a[r][j] -= a[r][s-1] a[j][s-1] / d_{s-1}; an entry is published
+//             to shared memory in the phase it becomes final, and its L
+//             value (a[r][j] / L_jj, y_r = b_r / L_rr) written in the next.
+//   inverse   (warps 6, 7) build X = L^-1 one column behind L: entry (i, c)
+//             takes X[i][c] -= L[i][k] X[k][c] in phase k + 2, c <= k < i,
+//             and X[i][c] /= L_ii in its last phase; entries are dealt to
+//             threads by interval colouring, so a thread has one at a time.
+//   warp 4    shares warp 0's sub-partition and stays idle.
+// Each role runs the same short instruction sequence in every lane (operands
+// picked by selects), so a warp issues ~3 FP64 instructions per phase.  The
+// plan is built at compile time and copied to shared memory once per launch
+// (divergent reads of constant memory serialise).
+
+enum : unsigned char { PF_NONE = 0, PF_OFF, PF_DIAG, PF_D11, PF_B, PF_COL0, PF_B0 };
+constexpr int PF_TRAIL = 128, PF_INV = 64, PF_INV_MAX = 16;
+constexpr int PF_BCOL = T;  // b rides along as column T
+
+struct PfEntry {
+    unsigned char kind, r, j;
+};
+struct PfPlan {
+    PfEntry tr[PF_TRAIL][2];
+    unsigned char inv_i[PF_INV][PF_INV_MAX], inv_c[PF_INV][PF_INV_MAX], inv_n[PF_INV];
+};
+
+// last phase in which an entry does work (update, publication or L value)
+constexpr int pf_last_busy(const PfEntry &e)
 {
-    __shared__ int bad;
-    const int tid = threadIdx.x;
-    for (int e = tid; e < TT; e += CF_THREADS) {
-        const int r = e / T, c = e % T;
-        l[r][c] = 0.0;
-        linv[r][c] = 0.0;
-        acc[r][c] = r == c ? 1.0 : 0.0;
-    }
-    if (tid == 0) bad = 0;
-    __syncthreads();
-    for (int s = 0; s <= T; ++s) {
-        if (s < T) {
-            const double d = a[s][s];
-            const double inv = rsqrt(d), inv2 = inv * inv;
-            if (tid == 0) {
-                invd[s] = inv;
-                if (!(d > 0.0) || !isfinite(d)) bad = 1;
-            }
-            // lower-triangle entries (r, j) with j >= s, numbered by column
-            // from the right: column T-1-q holds entries q(q+1)/2 .. (q+1)(q+2)/2 - 1
-            const int m = (T - s) * (T - s + 1) / 2;
-            for (int e = tid; e < m; e += CF_THREADS) {
-                int q = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
-                while ((q + 1) * (q + 2) / 2 <= e) ++q;
-                while (q * (q + 1) / 2 > e) --q;
-                const int j = T - 1 - q, r = j + (e - q * (q + 1) / 2);
-                if (j == s)
-                    l[r][s] = r == s ? d * inv : a[r][s] * inv;
-                else
-                    a[r][j] = fma(-a[r][s], a[j][s] * inv2, a[r][j]);
-            }
+    return e.kind == PF_OFF ? e.j + 1 : e.kind == PF_DIAG ? e.j + 1 : e.kind == PF_D11 ? 2 : e.kind == PF_B ? e.r + 1 : 1;
+}
+
+constexpr PfPlan make_pf_plan()
+{
+    PfPlan p{};
+    PfEntry ents[T * (T + 1) / 2 + T + 1] = {};
+    int n = 0;
+    for (int j = 1; j < T; ++j)
+        for (int r = j + 1; r < T; ++r) ents[n++] = PfEntry{PF_OFF, (unsigned char)r, (unsigned char)j};
+    for (int j = 2; j < T; ++j) ents[n++] = PfEntry{PF_DIAG, (unsigned char)j, (unsigned char)j};
+    ents[n++] = PfEntry{PF_D11, 1, 1};
+    for (int r = 1; r < T; ++r) ents[n++] = PfEntry{PF_B, (unsigned char)r, (unsigned char)PF_BCOL};
+    for (int r = 0; r < T; ++r) ents[n++] = PfEntry{PF_COL0, (unsigned char)r, 0};
+    ents[n++] = PfEntry{PF_B0, 0, (unsigned char)PF_BCOL};
+    // stable sort by last busy phase, latest first
+    for (int a = 1; a < n; ++a) {
+        const PfEntry v = ents[a];
+        int b = a;
+        while (b > 0 && pf_last_busy(ents[b - 1]) < pf_last_busy(v)) {
+            ents[b] = ents[b - 1];
+            --b;
         }
-        if (s >= 1) {
-            const int k = s - 1;
-            const double ik = invd[k];
-            const int n = (T - k) * (k + 1);
-            for (int e = tid; e < n; e += CF_THREADS) {
-                const int i = k + e / (k + 1), c = e % (k + 1);
-                const double xk = acc[k][c] * ik;
-                if (i == k)
-                    linv[k][c] = xk;
-                else
-                    acc[i][c] = fma(-l[i][k], xk, acc[i][c]);
+        ents[b] = v;
+    }
+    for (int u = 0; u < PF_TRAIL; ++u) {
+        p.tr[u][0] = ents[u];
+        p.tr[u][1] = PfEntry{PF_NONE, 0, 0};
+    }
+    for (int q = PF_TRAIL; q < n; ++q) p.tr[q - PF_TRAIL][1] = ents[q];
+    // inverse entries (i, c), i > c, busy in phases [c + 2, i + 1]: generated
+    // by start, each goes to the first thread whose previous entry has ended
+    for (int v = 0; v < PF_INV; ++v) p.inv_n[v] = 0;
+    for (int c = 0; c < T; ++c)
+        for (int i = c + 1; i < T; ++i)
+            for (int v = 0; v < PF_INV; ++v) {
+                const int m = p.inv_n[v];
+                if (m < PF_INV_MAX && (m == 0 || p.inv_i[v][m - 1] + 1 < c + 2)) {
+                    p.inv_i[v][m] = (unsigned char)i;
+                    p.inv_c[v][m] = (unsigned char)c;
+                    p.inv_n[v] = (unsigned char)(m + 1);
+                    break;
+                }
+            }
+    return p;
+}
+
+constexpr PfPlan kPfPlan = make_pf_plan();
+
+constexpr bool pf_plan_ok()
+{
+    // second entries are only busy in phases 1-2; every inverse entry placed
+    int placed = 0;
+    for (int u = 0; u < PF_TRAIL; ++u)
+        if (kPfPlan.tr[u][1].kind != PF_NONE && pf_last_busy(kPfPlan.tr[u][1]) > 2) return false;
+    for (int v = 0; v < PF_INV; ++v) placed += kPfPlan.inv_n[v];
+    return placed == T * (T - 1) / 2;
+}
+static_assert(pf_plan_ok(), "diagonal-tile factor plan");
+
+__constant__ PfPlan c_pf = kPfPlan;
+
+// the factor plan into shared memory (once per launch)
+__device__ void load_pf_plan(PfPlan &dst)
+{
+    const unsigned char *src = reinterpret_cast<const unsigned char *>(&c_pf);
+    unsigned char *d = reinterpret_cast<unsigned char *>(&dst);
+    for (int i = threadIdx.x; i < (int)sizeof(PfPlan); i += blockDim.x) d[i] = src[i];
+    __syncthreads();
+}
+
+// One entry of a trailing thread in phase s >= 1 (see the plan above): the
+// update a[r][j] -= a[r][k] (a[j][k] / d_k), k = s - 1, or the entry's L
+// value, as two FP64 instructions whatever the entry does.
+__device__ __forceinline__ void pf_entry(const PfEntry &e, double &v, int s, double ik2, double (*a)[T + 1],
+                                         double *bw, const double *invd, double (*l)[T + 1], double *y)
+{
+    const int r = e.r, j = e.j, k = s - 1;
+    const bool upd_kind = e.kind == PF_OFF || e.kind == PF_DIAG || e.kind == PF_B;
+    const int last = e.kind == PF_OFF ? j : e.kind == PF_DIAG ? j - 1 : r;  // last update phase
+    const bool upd = upd_kind && s <= last;
+    // the L value (or y) is due: OFF / B the phase after the last update,
+    // DIAG two phases after (warp 0 applies its final update), and the
+    // entries with no updates in phase 1 (column 0, b_0) or 2 (a[1][1])
+    const int due = e.kind == PF_OFF || e.kind == PF_B ? last + 1 : e.kind == PF_DIAG ? j + 1 : e.kind == PF_D11 ? 2 : 1;
+    const bool lval = e.kind != PF_NONE && s == due;
+    const int jj = j == PF_BCOL ? r : j;  // the pivot the L value divides by
+    double pa = 0.0, qa = 0.0;
+    if (upd) {
+        pa = e.kind == PF_B ? bw[k] : a[j == PF_BCOL ? 0 : j][k];  // row index kept inside the tile
+        qa = ik2;
+    } else if (lval) {
+        pa = (e.kind == PF_OFF || e.kind == PF_B) ? v : e.kind == PF_B0 ? bw[0] : a[r][jj];
+        qa = invd[jj];
+    }
+    const double t = pa * qa;
+    v = fma(upd ? -a[r][k] : 0.0, t, v);
+    if (upd && s == last) {
+        if (e.kind == PF_B) bw[r] = v;
+        else a[r][j] = v;
+    }
+    if (lval) {
+        if (j == PF_BCOL) y[r] = t;
+        else l[r][jj] = t;
+    }
+}
+
+// All threads (CF_THREADS == 256): Cholesky of the lower triangle of a, the
+// factor into l (zero above the diagonal), its inverse into linv (likewise),
+// invd[k] = 1 / L_kk and y = L^-1 b, following the plan pf (in shared
+// memory).  Returns false on a non-positive or non-finite pivot (checked once
+// at the end: a bad pivot only produces non-finite values downstream).
+__device__ bool cta_potrf(double (*a)[T + 1], double (*l)[T + 1], double (*linv)[T + 1], double *invd,
+                          const double *b, double *y, const PfPlan &pf)
+{
+    static_assert(CF_THREADS == 256, "the factor plan is laid out for eight warps");
+    __shared__ double bw[T];
+    __shared__ int bad;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int e = tid; e < TT; e += CF_THREADS) {
+        l[e / T][e % T] = 0.0;
+        linv[e / T][e % T] = 0.0;
+    }
+    if (tid < T) bw[tid] = b[tid];
+    if (tid == 0) bad = 0;
+    const int u = (warp >= 1 && warp <= 3) ? tid - 32 : warp == 5 ? tid - 64 : -1;
+    const int vi = warp >= 6 ? tid - 192 : -1;
+    PfEntry e0{PF_NONE, 0, 0}, e1{PF_NONE, 0, 0};
+    double v0 = 0.0, v1 = 0.0;
+    if (u >= 0) {
+        e0 = pf.tr[u][0];
+        e1 = pf.tr[u][1];
+        v0 = e0.j == PF_BCOL ? b[e0.r] : a[e0.r][e0.j];  // column T is the row padding: in bounds
+        v1 = e1.j == PF_BCOL ? b[e1.r] : a[e1.r][e1.j];
+    }
+    // inverse threads: the current entry (ci, cc) in registers, the list read
+    // only when an entry is done
+    const int n_inv = vi >= 0 ? pf.inv_n[vi] : 0;
+    int wi = 0, ci = -2, cc = T;
+    if (n_inv > 0) {
+        ci = pf.inv_i[vi][0];
+        cc = pf.inv_c[vi][0];
+    }
+    __syncthreads();
+    double inv_prev = 0.0, w = 0.0;
+    for (int s = 0; s <= T; ++s) {
+        if (warp == 0) {
+            if (tid == 0 && s < T) {
+                double d = a[s][s];
+                if (s > 0) {
+                    const double lp = a[s][s - 1] * inv_prev;
+                    d = fma(-lp, lp, d);
+                    a[s][s] = d;
+                }
+                inv_prev = rsqrt(d);
+                invd[s] = inv_prev;
+                linv[s][s] = inv_prev;
+            }
+        } else if (u >= 0) {
+            if (s >= 1) {
+                const double ik = invd[s - 1];
+                const double ik2 = ik * ik;
+                pf_entry(e0, v0, s, ik2, a, bw, invd, l, y);
+                if (s <= 2) pf_entry(e1, v1, s, ik2, a, bw, invd, l, y);
+            }
+        } else if (vi >= 0) {
+            if (s > ci + 1 && wi + 1 < n_inv) {  // entries are disjoint in time: at most one step
+                ++wi;
+                ci = pf.inv_i[vi][wi];
+                cc = pf.inv_c[vi][wi];
+                w = 0.0;
+            }
+            if (s >= cc + 2 && s <= ci + 1) {
+                const int k = s - 2;
+                w = fma(-l[ci][k], linv[k][cc], w);
+                if (s == ci + 1) linv[ci][cc] = w * invd[ci];
             }
         }
         __syncthreads();
     }
     if (tid < T) {
-        double sum = 0.0;
-        for (int k = 0; k <= tid; ++k) sum = fma(linv[tid][k], b[k], sum);
-        y[tid] = sum;
+        const double d = a[tid][tid];
+        if (!(d > 0.0) || !isfinite(d)) bad = 1;
     }
     __syncthreads();
     return bad == 0;
@@ -249,9 +401,152 @@ __device__ void cta_back(int Np, int nb, const double *__restrict__ S, const dou
     }
 }
 
-// The factor (tile dataflow) with the forward solve of rhs carried along on
-// the diagonal tasks; the back solve runs after it in k_tri_solve.
-__global__ void __launch_bounds__(CF_THREADS) k_chol_dataflow(int Np, int nb,
+// Dealt-out tile products.  A tile operation costs the largest number of
+// FP64 instructions any thread of a warp runs, so the products below are
+// spread evenly over the CTA.
+
+// a[r][c] -= sum_k L[r][k] L[c][k] for c <= r and, when WITH_B,
+// b[r] -= sum_k L[r][k] y[k]: the NE x T products (element, k) are cut into
+// consecutive runs of PER, one per thread; a run spans at most NACC
+// elements, whose partial sums go to part[NACC t ...].  Each element then
+// subtracts its partial sums in k order.  The accumulator and operands of a
+// product are picked by selects, so a warp issues one FMA per product.
+__device__ __forceinline__ void tri_of(int e, int &r, int &c)
+{
+    r = (int)((sqrtf(8.0f * (float)e + 1.0f) - 1.0f) * 0.5f);
+    while ((r + 1) * (r + 2) / 2 <= e) ++r;
+    while (r * (r + 1) / 2 > e) --r;
+    c = e - r * (r + 1) / 2;
+}
+
+template <bool WITH_B>
+struct LowerUpdate {
+    static constexpr int NTRI = T * (T + 1) / 2;
+    static constexpr int NE = NTRI + (WITH_B ? T : 0);
+    static constexpr int PER = (NE * T + CF_THREADS - 1) / CF_THREADS;
+    static constexpr int NACC = (T - 1 + PER + T - 1) / T;  // elements one run can touch
+    static constexpr int PART = NACC * CF_THREADS;          // doubles of partial sums
+};
+
+template <bool WITH_B>
+__device__ void update_lower(double (*a)[T + 1], const double (*L)[T + 1], double *b, const double *y, double *part)
+{
+    using U = LowerUpdate<WITH_B>;
+    constexpr int NTRI = U::NTRI, NE = U::NE, PER = U::PER, NACC = U::NACC;
+    const int tid = threadIdx.x;
+    const int f0 = tid * PER, e0 = f0 / T;
+    const double *xs[NACC], *ys[NACC];
+    double p[NACC];
+#pragma unroll
+    for (int j = 0; j < NACC; ++j) {
+        const int ej = min(e0 + j, NE - 1);
+        int r, c;
+        if (ej < NTRI) {
+            tri_of(ej, r, c);
+            xs[j] = L[r];
+            ys[j] = L[c];
+        } else {
+            xs[j] = L[ej - NTRI];
+            ys[j] = y;
+        }
+        p[j] = 0.0;
+    }
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+        const int f = f0 + i;
+        const int k = f % T, idx = f / T - e0;
+        const bool valid = f < NE * T;
+        const double *xp = xs[0], *yp = ys[0];
+        double acc = p[0];
+#pragma unroll
+        for (int j = 1; j < NACC; ++j) {
+            xp = idx == j ? xs[j] : xp;
+            yp = idx == j ? ys[j] : yp;
+            acc = idx == j ? p[j] : acc;
+        }
+        const double v = fma(valid ? xp[k] : 0.0, valid ? yp[k] : 0.0, acc);
+#pragma unroll
+        for (int j = 0; j < NACC; ++j) p[j] = idx == j ? v : p[j];
+    }
+#pragma unroll
+    for (int j = 0; j < NACC; ++j) part[NACC * tid + j] = p[j];
+    __syncthreads();
+    for (int e2 = tid; e2 < NE; e2 += CF_THREADS) {
+        const int tlo = (e2 * T) / PER, thi = (e2 * T + T - 1) / PER;
+        int r = 0, c = 0;
+        if (e2 < NTRI) tri_of(e2, r, c);
+        double v = e2 < NTRI ? a[r][c] : b[e2 - NTRI];
+        for (int t = tlo; t <= thi; ++t) v -= part[NACC * t + (e2 - (t * PER) / T)];
+        if (e2 < NTRI) a[r][c] = v;
+        else b[e2 - NTRI] = v;
+    }
+    __syncthreads();
+}
+
+// out = A Linv^T restricted to the lower triangle of Linv (out[r][c] =
+// sum_{k <= c} A[r][k] Linv[c][k]): columns c and T-1-c of a row go to one
+// thread, T + 1 products each.
+__device__ void tile_trsm(double (*out)[T + 1], const double (*A)[T + 1], const double (*Li)[T + 1])
+{
+    for (int p = threadIdx.x; p < TT / 2; p += CF_THREADS) {
+        const int r = p / (T / 2), c0 = p % (T / 2), c1 = T - 1 - c0;
+        double s0 = 0.0, s1 = 0.0;
+#pragma unroll
+        for (int i = 0; i < T + 1; ++i) {
+            const bool first = i <= c0;
+            const int c = first ? c0 : c1, k = first ? i : i - c0 - 1;
+            const double v = fma(A[r][k], Li[c][k], first ? s0 : s1);
+            s0 = first ? v : s0;
+            s1 = first ? s1 : v;
+        }
+        out[r][c0] = s0;
+        out[r][c1] = s1;
+    }
+}
+
+__device__ __forceinline__ void store_tile(double *S, int Np, int I, int K, const double (*t)[T + 1])
+{
+    for (int e = threadIdx.x; e < TT; e += CF_THREADS) S[(size_t)(I * T + e / T) * Np + K * T + e % T] = t[e / T][e % T];
+}
+
+// Thread 0 reads the status word; every thread gets the same answer.
+__device__ bool block_failed(const int *status)
+{
+    __shared__ int f;
+    __syncthreads();
+    if (threadIdx.x == 0) f = ld_acquire(status) != 0;
+    __syncthreads();
+    return f != 0;
+}
+
+// After the CTA barrier, thread 0's release store orders every thread's
+// earlier writes (the barrier puts them before it) ahead of the flag.
+__device__ __forceinline__ void block_release(int *flag, int epoch)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) st_release(flag, epoch);
+}
+
+// Flags: tile (I, K) at tile_task(I, K); that slot is raised for the
+// diagonal tile (I, I) when L_II, its inverse and y_I are stored, and for the
+// sub-diagonal tile (I+1, I) when L_{I+1,I} is stored.  The partial diagonal
+// PD(I) = A_II - sum_{J <= I-2} L_IJ L_IJ^T (with b_I likewise) raises
+// n_fact + I; the partial sub-diagonal SUB(I) = A_{I+1,I} - sum_{J <= I-1}
+// L_{I+1,J} L_IJ^T raises n_fact + nb + I.
+//
+// The factor with the forward solve of rhs carried along.  CTA 0 (the panel)
+// walks the diagonal: step I applies the last update to PD(I) with L_{I,I-1}
+// (its own, kept in shared memory), factors the tile (cta_potrf), forms
+// L_{I+1,I} = SUB(I) Linv_II^T and keeps it, then stores L_II, Linv_II, y_I
+// and L_{I+1,I}.  The other CTAs (helpers) run the task list: the tiles
+// (I, K) with I >= K + 2 (left-looking updates, then the triangular solve
+// with Linv_KK), and the PD and SUB accumulations, in the order
+//   P(0), C(0), PD(2), SUB(1), P(1), C(1), PD(3), SUB(2), P(2), ...
+// (P = panel step, C(K) = the tiles of column K) -- every task depends only on
+// tasks before it, each helper takes every (G-1)-th task in that order and
+// the panel its steps in order, so with all CTAs resident (cooperative
+// launch) the first unfinished task can always run: no deadlock.
+__global__ void __launch_bounds__(CF_THREADS) k_chol_dataflow(int Np, int nb, int n_tasks,
                                                               const int2 *__restrict__ tasks,
                                                               double *__restrict__ S,
                                                               double *__restrict__ Linv,
@@ -259,119 +554,163 @@ __global__ void __launch_bounds__(CF_THREADS) k_chol_dataflow(int Np, int nb,
                                                               int *__restrict__ flags, int epoch,
                                                               int *__restrict__ status)
 {
+    static_assert(BJ >= 4, "the panel keeps four tiles in the staging area");
+    static_assert(LowerUpdate<true>::PART <= BJ * T * (T + 1), "update_lower's partial sums fit in the staging area");
     __shared__ double a[T][T + 1], linv[T][T + 1];
     __shared__ double bi[BJ][T][T + 1], bk[BJ][T][T + 1], by[BJ][T];
     __shared__ double bvec[T], yvec[T], invd[T];
     __shared__ int ready_n;
     const int n_fact = nb * (nb + 1) / 2;
-    const int n_tasks = n_fact;
     const int tid = threadIdx.x;
-#if PSBA_CHOL_DYNAMIC
-    // tasks claimed in increasing order: the smallest unfinished claimed task
-    // has all its (smaller) dependencies claimed, so it can always run
-    __shared__ int claim;
-    while (true) {
-        if (tid == 0) claim = atomicAdd(status + 1, 1);
+    double *part = &bk[0][0][0];
+    if (blockIdx.x == 0) {
+        // ---- panel.  The tiles of step I+1 (SUB(I), PD(I+1)) are polled for
+        // together and loaded in one batch right after the factor of step I;
+        // L_II, Linv_II, y_I and L_{I+1,I} are stored and their flags raised at
+        // the end of the step.  The panel tracks failure itself (a bad pivot
+        // of its own, a wait that ran out), so it never reads the status word.
+        double(*lsub)[T + 1] = bi[2];  // L_{I,I-1} from the previous step
+        double(*asub)[T + 1] = bi[3];
+        __shared__ PfPlan s_pf;
+        load_pf_plan(s_pf);
+        bool failed = false;
+        load_tile(a, S, Np, 0, 0);
+        if (tid < T) bvec[tid] = __ldcg(rhs + tid);
         __syncthreads();
-        const int t = claim;
-        __syncthreads();
-        if (t >= n_tasks) break;
-#else
-    for (int t = blockIdx.x; t < n_tasks; t += gridDim.x) {
-#endif
-        if (t < n_fact) {
-            CHOL_MARK(t, 0);
-            const int I = tasks[t].x, K = tasks[t].y;
-            load_tile(a, S, Np, I, K);
-            if (I == K && tid < T) bvec[tid] = __ldcg(rhs + I * T + tid);
-            __syncthreads();
-            // Updates J = 0 .. K-1 in order.  The flags of the next BJ steps are
-            // polled at once (one L2 round trip); the ready ones have all their
-            // tiles loaded together and are applied from shared memory, so an
-            // update costs one round trip per batch instead of two per step.
-            // Each thread updates its own elements in the same order as one
-            // step at a time would: the arithmetic does not depend on batching.
-            int J = 0;
-            while (J < K) {
-                const int nmax = min(BJ, K - J);
-                if (tid == 0) ready_n = nmax;
-                __syncthreads();
-                if (tid < nmax) {
-                    const bool ok = ld_acquire(flags + tile_task(I, J + tid, nb)) == epoch &&
-                                    (I == K || ld_acquire(flags + tile_task(K, J + tid, nb)) == epoch);
-                    if (!ok) atomicMin(&ready_n, tid);
-                }
-                __syncthreads();
-                int n = ready_n;
-                if (n == 0) {  // the next step is not done yet: wait for it alone
-                    block_wait(flags + tile_task(I, J, nb), epoch, status);
-                    if (I != K) block_wait(flags + tile_task(K, J, nb), epoch, status);
-                    n = 1;
-                }
-                for (int e = tid; e < n * TT; e += CF_THREADS) {
-                    const int q = e / TT, r = (e % TT) / T, c = e % T;
-                    bi[q][r][c] = __ldcg(S + (size_t)(I * T + r) * Np + (J + q) * T + c);
-                    if (I != K) bk[q][r][c] = __ldcg(S + (size_t)(K * T + r) * Np + (J + q) * T + c);
-                }
-                if (I == K)
-                    for (int e = tid; e < n * T; e += CF_THREADS) by[e / T][e % T] = __ldcg(rhs + (J + e / T) * T + e % T);
-                __syncthreads();
-                for (int q = 0; q < n; ++q) {
-                    double(*lip)[T + 1] = bi[q];
-                    double(*lkp)[T + 1] = I == K ? bi[q] : bk[q];
-                    for (int e = tid; e < TT; e += CF_THREADS) {
-                        const int r = e / T, c = e % T;
-                        double s = a[r][c];
-#pragma unroll
-                        for (int k = 0; k < T; ++k) s = fma(-lip[r][k], lkp[c][k], s);
-                        a[r][c] = s;
-                    }
-                    if (I == K && tid < T) {
-                        double s = bvec[tid];
-#pragma unroll
-                        for (int k = 0; k < T; ++k) s = fma(-lip[tid][k], by[q][k], s);
-                        bvec[tid] = s;
-                    }
-                }
-                __syncthreads();
-                J += n;
-            }
-            CHOL_MARK(t, 1);
-            const bool failed = ld_acquire(status) != 0;
-            if (I == K) {
-                if (!failed) {
-                    // the staging tiles are free now: L in bi[0], the inverse's accumulator in bi[1]
-                    const bool good = cta_potrf(a, bi[0], bi[1], linv, invd, bvec, yvec);
-                    if (tid == 0 && !good) atomicCAS(status, 0, 1);
-                    for (int e = tid; e < TT; e += CF_THREADS) {
-                        const int r = e / T, c = e % T;
-                        S[(size_t)(I * T + r) * Np + I * T + c] = bi[0][r][c];
-                        Linv[(size_t)I * TT + e] = linv[r][c];
-                    }
-                    if (tid < T) rhs[I * T + tid] = yvec[tid];
-                }
-            } else {
-                block_wait(flags + tile_task(K, K, nb), epoch, status);
-                for (int e = tid; e < TT; e += CF_THREADS) linv[e / T][e % T] = __ldcg(Linv + (size_t)K * TT + e);
-                __syncthreads();
-                if (ld_acquire(status) == 0) {
-                    for (int e = tid; e < TT; e += CF_THREADS) {
-                        const int r = e / T, c = e % T;
-                        double s = 0.0;
-                        for (int k = 0; k <= c; ++k) s = fma(a[r][k], linv[c][k], s);
-                        S[(size_t)(I * T + r) * Np + K * T + c] = s;
-                    }
+        for (int I = 0; I < nb; ++I) {
+            const int td = tile_task(I, I, nb);
+            CHOL_MARK(td, 0);
+            if (I >= 1 && !failed) update_lower<true>(a, lsub, bvec, yvec, part);
+            CHOL_MARK(td, 1);
+            if (!failed) {
+                const bool good = cta_potrf(a, bi[0], linv, invd, bvec, yvec, s_pf);
+                if (!good) {
+                    failed = true;
+                    if (tid == 0) atomicCAS(status, 0, 1);
                 }
             }
-            CHOL_MARK(t, 2);
+            CHOL_MARK(td, 2);
+            if (I + 1 < nb) {
+                // a and bvec are free after the factor: the next diagonal tile goes there
+                if (I >= 1 && !block_wait(flags + n_fact + nb + I, epoch, status)) failed = true;
+                if (I + 1 >= 2 && !block_wait(flags + n_fact + I + 1, epoch, status)) failed = true;
+                for (int e2 = tid; e2 < TT; e2 += CF_THREADS) {
+                    const int r = e2 / T, c = e2 % T;
+                    asub[r][c] = __ldcg(S + (size_t)((I + 1) * T + r) * Np + I * T + c);
+                    a[r][c] = __ldcg(S + (size_t)((I + 1) * T + r) * Np + (I + 1) * T + c);
+                }
+                if (tid < T) bvec[tid] = __ldcg(rhs + (I + 1) * T + tid);
+                __syncthreads();
+                if (!failed) tile_trsm(lsub, asub, linv);
+                __syncthreads();
+            }
+            CHOL_MARK(td, 3);
+            if (!failed) {
+                store_tile(S, Np, I, I, bi[0]);
+                for (int e2 = tid; e2 < TT; e2 += CF_THREADS) Linv[(size_t)I * TT + e2] = linv[e2 / T][e2 % T];
+                if (tid < T) rhs[I * T + tid] = yvec[tid];
+                if (I + 1 < nb) store_tile(S, Np, I + 1, I, lsub);
+            }
             __syncthreads();
             if (tid == 0) {
-                __threadfence();
-                st_release(flags + t, epoch);
+                st_release(flags + td, epoch);
+                if (I + 1 < nb) st_release(flags + tile_task(I + 1, I, nb), epoch);
             }
-            CHOL_MARK(t, 3);
         }
+        return;
+    }
+    // ---- helpers
+    for (int t = blockIdx.x - 1; t < n_tasks; t += gridDim.x - 1) {
+        const int I = tasks[t].x, K = tasks[t].y;
+        const int kind = I - K;  // 0: PD(I), 1: SUB(K), >= 2: tile (I, K)
+        const int mark = kind == 0 ? n_fact + I : kind == 1 ? n_fact + nb + K : tile_task(I, K, nb);
+        CHOL_MARK(mark, 0);
+        load_tile(a, S, Np, I, K);
+        if (kind == 0 && tid < T) bvec[tid] = __ldcg(rhs + I * T + tid);
         __syncthreads();
+        // Updates J = 0 .. n_upd-1 in order.  The flags of the next BJ steps
+        // are polled at once (one L2 round trip); the ready ones have all their
+        // tiles loaded together and are applied from shared memory.  Each
+        // element is updated in the same order as one step at a time would.
+        const int n_upd = kind == 0 ? I - 1 : K;
+        int J = 0;
+        while (J < n_upd) {
+            const int nmax = min(BJ, n_upd - J);
+            if (tid == 0) ready_n = nmax;
+            __syncthreads();
+            if (tid < nmax) {
+                const bool ok = ld_acquire(flags + tile_task(I, J + tid, nb)) == epoch &&
+                                (kind == 0 || ld_acquire(flags + tile_task(K, J + tid, nb)) == epoch);
+                if (!ok) atomicMin(&ready_n, tid);
+            }
+            __syncthreads();
+            int n = ready_n;
+            if (n == 0) {  // the next step is not done yet: wait for it alone
+                block_wait(flags + tile_task(I, J, nb), epoch, status);
+                if (kind != 0) block_wait(flags + tile_task(K, J, nb), epoch, status);
+                n = 1;
+            }
+            for (int e2 = tid; e2 < n * TT; e2 += CF_THREADS) {
+                const int q = e2 / TT, r = (e2 % TT) / T, c = e2 % T;
+                bi[q][r][c] = __ldcg(S + (size_t)(I * T + r) * Np + (J + q) * T + c);
+                if (kind != 0) bk[q][r][c] = __ldcg(S + (size_t)(K * T + r) * Np + (J + q) * T + c);
+            }
+            if (kind == 0)
+                for (int e2 = tid; e2 < n * T; e2 += CF_THREADS) by[e2 / T][e2 % T] = __ldcg(rhs + (J + e2 / T) * T + e2 % T);
+            __syncthreads();
+            if (kind == 0) {
+                // the partial sums use bk, which the diagonal accumulation leaves free
+                for (int q = 0; q < n; ++q) update_lower<true>(a, bi[q], bvec, by[q], part);
+            } else {
+                for (int q = 0; q < n; ++q)
+                    for (int e2 = tid; e2 < TT; e2 += CF_THREADS) {
+                        const int r = e2 / T, c = e2 % T;
+                        double sacc = a[r][c];
+#pragma unroll
+                        for (int k = 0; k < T; ++k) sacc = fma(-bi[q][r][k], bk[q][c][k], sacc);
+                        a[r][c] = sacc;
+                    }
+            }
+            __syncthreads();
+            J += n;
+        }
+        CHOL_MARK(mark, 1);
+        const bool failed = block_failed(status);
+        if (kind == 0) {
+            if (!failed) {
+                store_tile(S, Np, I, I, a);
+                if (tid < T) rhs[I * T + tid] = bvec[tid];
+            }
+        } else if (kind == 1) {
+            if (!failed) store_tile(S, Np, I, K, a);
+        } else {
+            block_wait(flags + tile_task(K, K, nb), epoch, status);
+            for (int e2 = tid; e2 < TT; e2 += CF_THREADS) linv[e2 / T][e2 % T] = __ldcg(Linv + (size_t)K * TT + e2);
+            __syncthreads();
+            if (!block_failed(status)) {
+                tile_trsm(bi[0], a, linv);
+                __syncthreads();
+                store_tile(S, Np, I, K, bi[0]);
+            }
+        }
+        CHOL_MARK(mark, 2);
+        block_release(flags + mark, epoch);
+        CHOL_MARK(mark, 3);
+        __syncthreads();
+    }
+}
+
+// Helper tasks in dependency order (see k_chol_dataflow): after panel step K
+// come the tiles (I, K), I >= K + 2, then PD(K + 2) and SUB(K + 1).
+void chol_task_list(int nb, std::vector<int2> &tasks)
+{
+    tasks.clear();
+    for (int K = 0; K < nb; ++K) {
+        for (int I = K + 2; I < nb; ++I) tasks.push_back(make_int2(I, K));
+        if (K + 2 < nb) {
+            tasks.push_back(make_int2(K + 2, K + 2));  // PD(K + 2)
+            tasks.push_back(make_int2(K + 2, K + 1));  // SUB(K + 1)
+        }
     }
 }
 
@@ -416,12 +755,13 @@ void launch_chol_dataflow(const DeviceProblem &d, int mode, int epoch, double *x
     int nb = d.Np / T;
     int Np = d.Np;
     if (mode == 0) {
-        const int grid = chol_grid(nb * (nb + 1) / 2);
+        int n_tasks = d.chol_n_tasks;
+        const int grid = chol_grid(n_tasks + 1);
         const int2 *tasks = d.chol_tasks;
         double *S = d.S, *Linv = d.Linv, *rhs = d.rhs;
         int *flags = d.chol_flags, *status = d.status;
-        void *args[] = {&Np, &nb, (void *)&tasks, &S, &Linv, &rhs, &flags, &epoch, &status};
-        cudaMemsetAsync(d.status, 0, 2 * sizeof(int), s);  // result word and task claim counter
+        void *args[] = {&Np, &nb, &n_tasks, (void *)&tasks, &S, &Linv, &rhs, &flags, &epoch, &status};
+        cudaMemsetAsync(d.status, 0, 2 * sizeof(int), s);
         cudaLaunchCooperativeKernel((const void *)k_chol_dataflow, dim3(grid), dim3(CF_THREADS), args, 0, s);
         note_launch(1);
     }

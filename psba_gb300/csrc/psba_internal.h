@@ -126,7 +126,8 @@ struct DeviceProblem {
     double *xref = nullptr;       // Np: refinement correction
     double *Linv = nullptr;       // (Np / TILE) * TILE * TILE inverses of the diagonal blocks
     int *status = nullptr;        // Cholesky status word (0 ok, 1 not SPD, 2 wait budget exhausted)
-    int2 *chol_tasks = nullptr;   // (I, K) of every lower tile, column-major
+    int2 *chol_tasks = nullptr;   // helper tasks of the dense factor, in dependency order
+    int chol_n_tasks = 0;
     int *chol_flags = nullptr;    // one flag per dataflow task (value = epoch when done)
     int chol_n_flags = 0;
     double *dp = nullptr;         // N + 3 np
@@ -185,6 +186,8 @@ void launch_scale(double *out, const double *x, const double *num, const double 
 // solve into xsol; mode 1 solves again with the existing factor.  One
 // cooperative launch; epoch must increase from launch to launch.
 void launch_chol_dataflow(const DeviceProblem &d, int mode, int epoch, double *x_out, cudaStream_t s);
+// the dense factor's helper tasks, in dependency order
+void chol_task_list(int nb, std::vector<int2> &tasks);
 
 // index lists on the GPU, psba_index.cu
 void launch_pt_start(int np, int no, const int *obs_pt, int *pt_start, cudaStream_t s);

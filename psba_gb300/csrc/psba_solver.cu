@@ -972,8 +972,8 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     {
         const int nb = d.Np / TILE;
         std::vector<int2> tasks;
-        for (int K = 0; K < nb; ++K)
-            for (int I = K; I < nb; ++I) tasks.push_back(make_int2(I, K));
+        chol_task_list(nb, tasks);
+        d.chol_n_tasks = (int)tasks.size();
         d.chol_n_flags = nb * (nb + 1) / 2 + 2 * nb;
         TRY(dalloc(h, &d.chol_tasks, tasks.size()));
         TRY(dalloc(h, &d.chol_flags, (size_t)d.chol_n_flags));

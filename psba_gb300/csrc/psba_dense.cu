@@ -220,69 +220,151 @@ __device__ void load_pf_plan(PfPlan &dst)
     __syncthreads();
 }
 
-// One entry of a trailing thread in phase s >= 1 (see the plan above): the
-// update a[r][j] -= a[r][k] (a[j][k] / d_k), k = s - 1, or the entry's L
-// value, as two FP64 instructions whatever the entry does.
-__device__ __forceinline__ void pf_entry(const PfEntry &e, double &v, int s, double ik2, double (*a)[T + 1],
-                                         double *bw, const double *invd, double (*l)[T + 1], double *y)
+// The factor's workspace: one shared block of doubles, so that every access
+// is an offset from one base (fixed per entry, plus a phase constant once
+// the phase loop is unrolled).
+constexpr int PW_ROW = T + 1;            // padded row
+constexpr int PW_A = 0;                  // the tile (published entries, pivots)
+constexpr int PW_L = T * PW_ROW;         // the factor L
+constexpr int PW_LINV = 2 * T * PW_ROW;  // its inverse
+constexpr int PW_BW = 3 * T * PW_ROW;    // b being reduced
+constexpr int PW_INVD = PW_BW + T;       // 1 / L_kk
+constexpr int PW_Y = PW_BW + 2 * T;      // y = L^-1 b
+constexpr int PW_B = PW_BW + 3 * T;      // b (input)
+constexpr int PW_SIZE = PW_BW + 4 * T;
+
+// One entry of a trailing thread, decoded once per factor into offsets: the
+// entry's row (xo), the other operand of its update (oo: row j of the tile,
+// or b), the source of its L value when that is not the entry itself (lo),
+// the pivot inverse it divides by (qo), where it is published (po) and where
+// its L value goes (dofs), its last update phase (0: none) and the phase its
+// L value is due.
+struct PfSlot {
+    int xo, oo, lo, qo, po, dofs, last, due;
+    bool lself;
+};
+
+__device__ __forceinline__ PfSlot pf_slot(const PfEntry &e)
 {
-    const int r = e.r, j = e.j, k = s - 1;
-    const bool upd_kind = e.kind == PF_OFF || e.kind == PF_DIAG || e.kind == PF_B;
-    const int last = e.kind == PF_OFF ? j : e.kind == PF_DIAG ? j - 1 : r;  // last update phase
-    const bool upd = upd_kind && s <= last;
-    // the L value (or y) is due: OFF / B the phase after the last update,
-    // DIAG two phases after (warp 0 applies its final update), and the
-    // entries with no updates in phase 1 (column 0, b_0) or 2 (a[1][1])
-    const int due = e.kind == PF_OFF || e.kind == PF_B ? last + 1 : e.kind == PF_DIAG ? j + 1 : e.kind == PF_D11 ? 2 : 1;
-    const bool lval = e.kind != PF_NONE && s == due;
-    const int jj = j == PF_BCOL ? r : j;  // the pivot the L value divides by
-    double pa = 0.0, qa = 0.0;
-    if (upd) {
-        pa = e.kind == PF_B ? bw[k] : a[j == PF_BCOL ? 0 : j][k];  // row index kept inside the tile
-        qa = ik2;
-    } else if (lval) {
-        pa = (e.kind == PF_OFF || e.kind == PF_B) ? v : e.kind == PF_B0 ? bw[0] : a[r][jj];
-        qa = invd[jj];
-    }
-    const double t = pa * qa;
-    v = fma(upd ? -a[r][k] : 0.0, t, v);
-    if (upd && s == last) {
-        if (e.kind == PF_B) bw[r] = v;
-        else a[r][j] = v;
-    }
-    if (lval) {
-        if (j == PF_BCOL) y[r] = t;
-        else l[r][jj] = t;
+    const int r = e.r, j = e.j;
+    switch (e.kind) {
+    case PF_OFF:
+        return PfSlot{r * PW_ROW, j * PW_ROW, 0, PW_INVD + j, r * PW_ROW + j, PW_L + r * PW_ROW + j, j, j + 1, true};
+    case PF_DIAG:  // its L value is d_j / sqrt(d_j), d_j left in a[j][j] by warp 0
+        return PfSlot{j * PW_ROW, j * PW_ROW, j * PW_ROW + j, PW_INVD + j, j * PW_ROW + j, PW_L + j * PW_ROW + j, j - 1,
+                      j + 1, false};
+    case PF_D11:
+        return PfSlot{PW_ROW, PW_ROW, PW_ROW + 1, PW_INVD + 1, 0, PW_L + PW_ROW + 1, 0, 2, false};
+    case PF_B:
+        return PfSlot{r * PW_ROW, PW_BW, 0, PW_INVD + r, PW_BW + r, PW_Y + r, r, r + 1, true};
+    case PF_COL0:
+        return PfSlot{r * PW_ROW, 0, r * PW_ROW, PW_INVD, 0, PW_L + r * PW_ROW, 0, 1, false};
+    case PF_B0:
+        return PfSlot{0, PW_BW, PW_BW, PW_INVD, 0, PW_Y, 0, 1, false};
+    default:
+        return PfSlot{0, 0, 0, 0, 0, 0, 0, 0, true};
     }
 }
 
-// All threads (CF_THREADS == 256): Cholesky of the lower triangle of a, the
-// factor into l (zero above the diagonal), its inverse into linv (likewise),
-// invd[k] = 1 / L_kk and y = L^-1 b, following the plan pf (in shared
-// memory).  Returns false on a non-positive or non-finite pivot (checked once
-// at the end: a bad pivot only produces non-finite values downstream).
-__device__ bool cta_potrf(double (*a)[T + 1], double (*l)[T + 1], double (*linv)[T + 1], double *invd,
-                          const double *b, double *y, const PfPlan &pf)
+// Phase s >= 1 of one entry: the update v -= a[r][k] (other[k] / d_k),
+// k = s - 1, or its L value, as two FP64 instructions whatever the entry
+// does (loads unconditional and in bounds, operands picked by selects).
+template <int S>
+__device__ __forceinline__ void pf_step(const PfSlot &q, double &v, double ik2, double *W)
+{
+    constexpr int k = S - 1;
+    const bool upd = S <= q.last, lval = S == q.due;
+    const double xk = W[q.xo + k];
+    const double ok = W[q.oo + k];
+    const double lraw = W[q.lo];
+    const double qi = W[q.qo];
+    const double lv = q.lself ? v : lraw;
+    const double pa = upd ? ok : lval ? lv : 0.0;
+    const double qa = upd ? ik2 : lval ? qi : 0.0;
+    const double t = pa * qa;
+    v = fma(upd ? -xk : 0.0, t, v);
+    if (upd && S == q.last) W[q.po] = v;
+    if (lval) W[q.dofs] = t;
+}
+
+// Phase S of the whole CTA (see the plan above).
+template <int S>
+__device__ __forceinline__ void pf_phase(double *W, int warp, int u, int vi, const PfPlan &pf, const PfSlot &q0,
+                                         const PfSlot &q1, double &v0, double &v1, double &inv_prev, double &w,
+                                         int &wi, int n_inv, int &ci, int &cc)
+{
+    if (warp == 0) {
+        if (S < T && threadIdx.x == 0) {
+            double d = W[PW_A + S * PW_ROW + S];
+            if (S > 0) {
+                const double lp = W[PW_A + S * PW_ROW + S - 1] * inv_prev;
+                d = fma(-lp, lp, d);
+                W[PW_A + S * PW_ROW + S] = d;
+            }
+            inv_prev = rsqrt(d);
+            W[PW_INVD + S] = inv_prev;
+            W[PW_LINV + S * PW_ROW + S] = inv_prev;
+        }
+    } else if (u >= 0) {
+        if (S >= 1) {
+            const double ik = W[PW_INVD + (S >= 1 ? S - 1 : 0)];
+            const double ik2 = ik * ik;
+            pf_step<S>(q0, v0, ik2, W);
+            if (S <= 2) pf_step<S>(q1, v1, ik2, W);
+        }
+    } else if (vi >= 0) {
+        if (S >= 2) {
+            constexpr int k = S >= 2 ? S - 2 : 0;
+            if (S > ci + 1 && wi + 1 < n_inv) {  // entries are disjoint in time: at most one step
+                ++wi;
+                ci = pf.inv_i[vi][wi];
+                cc = pf.inv_c[vi][wi];
+                w = 0.0;
+            }
+            if (S >= cc + 2 && S <= ci + 1) {
+                w = fma(-W[PW_L + ci * PW_ROW + k], W[PW_LINV + k * PW_ROW + cc], w);
+                if (S == ci + 1) W[PW_LINV + ci * PW_ROW + cc] = w * W[PW_INVD + ci];
+            }
+        }
+    }
+    __syncthreads();
+}
+
+template <int S>
+__device__ __forceinline__ void pf_phases(double *W, int warp, int u, int vi, const PfPlan &pf, const PfSlot &q0,
+                                          const PfSlot &q1, double &v0, double &v1, double &inv_prev, double &w,
+                                          int &wi, int n_inv, int &ci, int &cc)
+{
+    if constexpr (S <= T) {
+        pf_phase<S>(W, warp, u, vi, pf, q0, q1, v0, v1, inv_prev, w, wi, n_inv, ci, cc);
+        pf_phases<S + 1>(W, warp, u, vi, pf, q0, q1, v0, v1, inv_prev, w, wi, n_inv, ci, cc);
+    }
+}
+
+// All threads (CF_THREADS == 256): Cholesky of the lower triangle of the
+// tile W[PW_A..] into W[PW_L..] (zero above the diagonal), its inverse into
+// W[PW_LINV..] (likewise), 1 / L_kk into W[PW_INVD..] and y = L^-1 b (b in
+// W[PW_B..]) into W[PW_Y..], following the plan pf (in shared memory).
+// Returns false on a non-positive or non-finite pivot (checked once at the
+// end: a bad pivot only produces non-finite values downstream).
+__device__ bool cta_potrf(double *W, const PfPlan &pf)
 {
     static_assert(CF_THREADS == 256, "the factor plan is laid out for eight warps");
-    __shared__ double bw[T];
     __shared__ int bad;
     const int tid = threadIdx.x, warp = tid >> 5;
-    for (int e = tid; e < TT; e += CF_THREADS) {
-        l[e / T][e % T] = 0.0;
-        linv[e / T][e % T] = 0.0;
-    }
-    if (tid < T) bw[tid] = b[tid];
+    for (int e = tid; e < 2 * T * PW_ROW; e += CF_THREADS) W[PW_L + e] = 0.0;  // L and its inverse
+    if (tid < T) W[PW_BW + tid] = W[PW_B + tid];
     if (tid == 0) bad = 0;
     const int u = (warp >= 1 && warp <= 3) ? tid - 32 : warp == 5 ? tid - 64 : -1;
     const int vi = warp >= 6 ? tid - 192 : -1;
-    PfEntry e0{PF_NONE, 0, 0}, e1{PF_NONE, 0, 0};
+    PfSlot q0 = pf_slot(PfEntry{PF_NONE, 0, 0}), q1 = q0;
     double v0 = 0.0, v1 = 0.0;
     if (u >= 0) {
-        e0 = pf.tr[u][0];
-        e1 = pf.tr[u][1];
-        v0 = e0.j == PF_BCOL ? b[e0.r] : a[e0.r][e0.j];  // column T is the row padding: in bounds
-        v1 = e1.j == PF_BCOL ? b[e1.r] : a[e1.r][e1.j];
+        const PfEntry e0 = pf.tr[u][0], e1 = pf.tr[u][1];
+        q0 = pf_slot(e0);
+        q1 = pf_slot(e1);
+        v0 = W[e0.j == PF_BCOL ? PW_B + e0.r : PW_A + e0.r * PW_ROW + e0.j];
+        v1 = W[e1.j == PF_BCOL ? PW_B + e1.r : PW_A + e1.r * PW_ROW + e1.j];
     }
     // inverse threads: the current entry (ci, cc) in registers, the list read
     // only when an entry is done
@@ -294,43 +376,9 @@ __device__ bool cta_potrf(double (*a)[T + 1], double (*l)[T + 1], double (*linv)
     }
     __syncthreads();
     double inv_prev = 0.0, w = 0.0;
-    for (int s = 0; s <= T; ++s) {
-        if (warp == 0) {
-            if (tid == 0 && s < T) {
-                double d = a[s][s];
-                if (s > 0) {
-                    const double lp = a[s][s - 1] * inv_prev;
-                    d = fma(-lp, lp, d);
-                    a[s][s] = d;
-                }
-                inv_prev = rsqrt(d);
-                invd[s] = inv_prev;
-                linv[s][s] = inv_prev;
-            }
-        } else if (u >= 0) {
-            if (s >= 1) {
-                const double ik = invd[s - 1];
-                const double ik2 = ik * ik;
-                pf_entry(e0, v0, s, ik2, a, bw, invd, l, y);
-                if (s <= 2) pf_entry(e1, v1, s, ik2, a, bw, invd, l, y);
-            }
-        } else if (vi >= 0) {
-            if (s > ci + 1 && wi + 1 < n_inv) {  // entries are disjoint in time: at most one step
-                ++wi;
-                ci = pf.inv_i[vi][wi];
-                cc = pf.inv_c[vi][wi];
-                w = 0.0;
-            }
-            if (s >= cc + 2 && s <= ci + 1) {
-                const int k = s - 2;
-                w = fma(-l[ci][k], linv[k][cc], w);
-                if (s == ci + 1) linv[ci][cc] = w * invd[ci];
-            }
-        }
-        __syncthreads();
-    }
+    pf_phases<0>(W, warp, u, vi, pf, q0, q1, v0, v1, inv_prev, w, wi, n_inv, ci, cc);
     if (tid < T) {
-        const double d = a[tid][tid];
+        const double d = W[PW_A + tid * PW_ROW + tid];
         if (!(d > 0.0) || !isfinite(d)) bad = 1;
     }
     __syncthreads();
@@ -546,7 +594,7 @@ __device__ __forceinline__ void block_release(int *flag, int epoch)
 // tasks before it, each helper takes every (G-1)-th task in that order and
 // the panel its steps in order, so with all CTAs resident (cooperative
 // launch) the first unfinished task can always run: no deadlock.
-__global__ void __launch_bounds__(CF_THREADS) k_chol_dataflow(int Np, int nb, int n_tasks,
+__global__ void __launch_bounds__(CF_THREADS, 1) k_chol_dataflow(int Np, int nb, int n_tasks,
                                                               const int2 *__restrict__ tasks,
                                                               double *__restrict__ S,
                                                               double *__restrict__ Linv,
@@ -558,7 +606,7 @@ __global__ void __launch_bounds__(CF_THREADS) k_chol_dataflow(int Np, int nb, in
     static_assert(LowerUpdate<true>::PART <= BJ * T * (T + 1), "update_lower's partial sums fit in the staging area");
     __shared__ double a[T][T + 1], linv[T][T + 1];
     __shared__ double bi[BJ][T][T + 1], bk[BJ][T][T + 1], by[BJ][T];
-    __shared__ double bvec[T], yvec[T], invd[T];
+    __shared__ double bvec[T];
     __shared__ int ready_n;
     const int n_fact = nb * (nb + 1) / 2;
     const int tid = threadIdx.x;
@@ -571,19 +619,25 @@ __global__ void __launch_bounds__(CF_THREADS) k_chol_dataflow(int Np, int nb, in
         // of its own, a wait that ran out), so it never reads the status word.
         double(*lsub)[T + 1] = bi[2];  // L_{I,I-1} from the previous step
         double(*asub)[T + 1] = bi[3];
+        static_assert(LowerUpdate<true>::PART <= 2 * T * (T + 1), "update_lower's partial sums fit in bk[0..1]");
+        static_assert(2 * T * (T + 1) + PW_SIZE <= BJ * T * (T + 1), "the factor workspace fits after the partial sums");
+        double *W = &bk[2][0][0];  // bk[0..1] hold update_lower's partial sums
+        double(*wa)[T + 1] = reinterpret_cast<double(*)[T + 1]>(W + PW_A);
+        double(*wl)[T + 1] = reinterpret_cast<double(*)[T + 1]>(W + PW_L);
+        double(*wli)[T + 1] = reinterpret_cast<double(*)[T + 1]>(W + PW_LINV);
         __shared__ PfPlan s_pf;
         load_pf_plan(s_pf);
         bool failed = false;
-        load_tile(a, S, Np, 0, 0);
-        if (tid < T) bvec[tid] = __ldcg(rhs + tid);
+        load_tile(wa, S, Np, 0, 0);
+        if (tid < T) W[PW_B + tid] = __ldcg(rhs + tid);
         __syncthreads();
         for (int I = 0; I < nb; ++I) {
             const int td = tile_task(I, I, nb);
             CHOL_MARK(td, 0);
-            if (I >= 1 && !failed) update_lower<true>(a, lsub, bvec, yvec, part);
+            if (I >= 1 && !failed) update_lower<true>(wa, lsub, W + PW_B, W + PW_Y, part);
             CHOL_MARK(td, 1);
             if (!failed) {
-                const bool good = cta_potrf(a, bi[0], linv, invd, bvec, yvec, s_pf);
+                const bool good = cta_potrf(W, s_pf);
                 if (!good) {
                     failed = true;
                     if (tid == 0) atomicCAS(status, 0, 1);
@@ -591,24 +645,24 @@ __global__ void __launch_bounds__(CF_THREADS) k_chol_dataflow(int Np, int nb, in
             }
             CHOL_MARK(td, 2);
             if (I + 1 < nb) {
-                // a and bvec are free after the factor: the next diagonal tile goes there
+                // the tile and b are free after the factor: the next diagonal tile goes there
                 if (I >= 1 && !block_wait(flags + n_fact + nb + I, epoch, status)) failed = true;
                 if (I + 1 >= 2 && !block_wait(flags + n_fact + I + 1, epoch, status)) failed = true;
                 for (int e2 = tid; e2 < TT; e2 += CF_THREADS) {
                     const int r = e2 / T, c = e2 % T;
                     asub[r][c] = __ldcg(S + (size_t)((I + 1) * T + r) * Np + I * T + c);
-                    a[r][c] = __ldcg(S + (size_t)((I + 1) * T + r) * Np + (I + 1) * T + c);
+                    wa[r][c] = __ldcg(S + (size_t)((I + 1) * T + r) * Np + (I + 1) * T + c);
                 }
-                if (tid < T) bvec[tid] = __ldcg(rhs + (I + 1) * T + tid);
+                if (tid < T) W[PW_B + tid] = __ldcg(rhs + (I + 1) * T + tid);
                 __syncthreads();
-                if (!failed) tile_trsm(lsub, asub, linv);
+                if (!failed) tile_trsm(lsub, asub, wli);
                 __syncthreads();
             }
             CHOL_MARK(td, 3);
             if (!failed) {
-                store_tile(S, Np, I, I, bi[0]);
-                for (int e2 = tid; e2 < TT; e2 += CF_THREADS) Linv[(size_t)I * TT + e2] = linv[e2 / T][e2 % T];
-                if (tid < T) rhs[I * T + tid] = yvec[tid];
+                store_tile(S, Np, I, I, wl);
+                for (int e2 = tid; e2 < TT; e2 += CF_THREADS) Linv[(size_t)I * TT + e2] = wli[e2 / T][e2 % T];
+                if (tid < T) rhs[I * T + tid] = W[PW_Y + tid];
                 if (I + 1 < nb) store_tile(S, Np, I + 1, I, lsub);
             }
             __syncthreads();

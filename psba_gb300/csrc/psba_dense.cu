@@ -386,9 +386,25 @@ __device__ bool cta_potrf(double *W, const PfPlan &pf)
 }
 
 // Single-CTA triangular solves over the factor (S lower = L, Linv = diagonal
-// tile inverses) with the right-hand side in shared memory.  Each column step
-// reads one row panel of L with coalesced loads (16 independent loads per
-// thread), so a step costs about one L2 round trip.
+// tile inverses) with the right-hand side in shared memory.  A block step is
+// the 16 x 16 product with the diagonal inverse, then the update of the other
+// blocks, one row (forward) or column (back) of it per thread, reading one
+// row panel of L with independent loads.  Both are bound by the SM's FP64
+// rate (N^2 / 2 multiply-adds on one SM).  The back solve spreads its
+// diagonal product over 256 threads (one product each, summed by a fixed
+// shuffle tree over 16 lanes) and loads the values a thread needs for the
+// next block step (its Linv entry, its 16 panel values) while the current
+// one runs.
+
+// One lane of the 16 x 16 diagonal product: 16 lanes hold the products of one
+// output, summed in a fixed order.
+__device__ __forceinline__ double half_warp_sum(double p)
+{
+#pragma unroll
+    for (int off = T / 2; off > 0; off >>= 1) p += __shfl_xor_sync(0xffffffffu, p, off);
+    return p;
+}
+
 // forward: b <- L^-1 b (right-looking: y_K = Linv_K b_K, then b_I -= L_IK y_K)
 __device__ void cta_forward(int Np, int nb, const double *__restrict__ S, const double *__restrict__ Linv,
                             double *bs, double *tmp)
@@ -424,18 +440,41 @@ __device__ void cta_forward(int Np, int nb, const double *__restrict__ S, const 
 __device__ void cta_back(int Np, int nb, const double *__restrict__ S, const double *__restrict__ Linv,
                          double *ys, double *xs, double *__restrict__ x)
 {
-    const int tid = threadIdx.x;
-    for (int K = nb - 1; K >= 0; --K) {
-        if (tid < T) {
-            const double *Li = Linv + (size_t)K * TT;
-            double v = 0.0;
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const int dc = tid / T, dk = tid % T;  // diagonal product: output column, term
+    auto load_diag = [&](int K) {
+        return (tid < TT && dk >= dc) ? __ldcg(Linv + (size_t)K * TT + dk * T + dc) : 0.0;
+    };
+    auto load_panel = [&](int K, double (&v)[T]) {
+        if (tid < K * T) {
+            const double *base = S + (size_t)(K * T) * Np + tid;
 #pragma unroll
-            for (int k = 0; k < T; ++k) v = fma(k >= tid ? __ldcg(Li + k * T + tid) : 0.0, ys[K * T + k], v);
-            xs[tid] = v;
-            x[K * T + tid] = v;
+            for (int c = 0; c < T; ++c) v[c] = __ldcg(base + (size_t)c * Np);
+        }
+    };
+    double curL = load_diag(nb - 1), curS[T] = {}, nxtS[T] = {};
+    load_panel(nb - 1, curS);
+    for (int K = nb - 1; K >= 0; --K) {
+        double nxtL = 0.0;
+        if (K > 0) {
+            nxtL = load_diag(K - 1);
+            load_panel(K - 1, nxtS);
+        }
+        if (tid < TT) {
+            const double v = half_warp_sum(curL * ys[K * T + dk]);
+            if (dk == 0) {
+                xs[dc] = v;
+                x[K * T + dc] = v;
+            }
         }
         __syncthreads();
-        for (int col = tid; col < K * T; col += blockDim.x) {
+        if (tid < K * T) {
+            double s = 0.0;
+#pragma unroll
+            for (int c = 0; c < T; ++c) s = fma(curS[c], xs[c], s);
+            ys[tid] -= s;
+        }
+        for (int col = tid + nthr; col < K * T; col += nthr) {  // columns beyond the prefetched one
             const double *base = S + (size_t)(K * T) * Np + col;
             double v[T];
 #pragma unroll
@@ -446,6 +485,9 @@ __device__ void cta_back(int Np, int nb, const double *__restrict__ S, const dou
             ys[col] -= s;
         }
         __syncthreads();
+        curL = nxtL;
+#pragma unroll
+        for (int c = 0; c < T; ++c) curS[c] = nxtS[c];
     }
 }
 

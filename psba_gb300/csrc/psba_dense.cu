@@ -288,6 +288,10 @@ __device__ __forceinline__ void pf_step(const PfSlot &q, double &v, double ik2, 
 }
 
 // Phase S of the whole CTA (see the plan above).
+// The phases synchronise the seven warps with a role (named barrier 1); warp
+// 4 joins the CTA only at the factor's start and end.
+__device__ __forceinline__ void pf_barrier() { asm volatile("bar.sync 1, %0;" ::"n"(CF_THREADS - 32) : "memory"); }
+
 template <int S>
 __device__ __forceinline__ void pf_phase(double *W, int warp, int u, int vi, const PfPlan &pf, const PfSlot &q0,
                                          const PfSlot &q1, double &v0, double &v1, double &inv_prev, double &w,
@@ -327,7 +331,7 @@ __device__ __forceinline__ void pf_phase(double *W, int warp, int u, int vi, con
             }
         }
     }
-    __syncthreads();
+    pf_barrier();
 }
 
 template <int S>
@@ -342,19 +346,28 @@ __device__ __forceinline__ void pf_phases(double *W, int warp, int u, int vi, co
 }
 
 // All threads (CF_THREADS == 256): Cholesky of the lower triangle of the
-// tile W[PW_A..] into W[PW_L..] (zero above the diagonal), its inverse into
-// W[PW_LINV..] (likewise), 1 / L_kk into W[PW_INVD..] and y = L^-1 b (b in
+// tile W[PW_A..] into the lower triangle of W[PW_L..], its inverse into the
+// lower triangle of W[PW_LINV..] (the upper triangles are left as they were:
+// nothing reads them), 1 / L_kk into W[PW_INVD..] and y = L^-1 b (b in
 // W[PW_B..]) into W[PW_Y..], following the plan pf (in shared memory).
 // Returns false on a non-positive or non-finite pivot (checked once at the
 // end: a bad pivot only produces non-finite values downstream).
-__device__ bool cta_potrf(double *W, const PfPlan &pf)
+// warp 4's work during the factor: none
+struct NoSide {
+    __device__ __forceinline__ void run(const int *) {}
+};
+
+template <typename Side = NoSide>
+__device__ bool cta_potrf(double *W, const PfPlan &pf, Side &&side = Side())
 {
     static_assert(CF_THREADS == 256, "the factor plan is laid out for eight warps");
-    __shared__ int bad;
+    __shared__ int bad, fdone;
     const int tid = threadIdx.x, warp = tid >> 5;
-    for (int e = tid; e < 2 * T * PW_ROW; e += CF_THREADS) W[PW_L + e] = 0.0;  // L and its inverse
     if (tid < T) W[PW_BW + tid] = W[PW_B + tid];
-    if (tid == 0) bad = 0;
+    if (tid == 0) {
+        bad = 0;
+        fdone = 0;
+    }
     const int u = (warp >= 1 && warp <= 3) ? tid - 32 : warp == 5 ? tid - 64 : -1;
     const int vi = warp >= 6 ? tid - 192 : -1;
     PfSlot q0 = pf_slot(PfEntry{PF_NONE, 0, 0}), q1 = q0;
@@ -376,7 +389,12 @@ __device__ bool cta_potrf(double *W, const PfPlan &pf)
     }
     __syncthreads();
     double inv_prev = 0.0, w = 0.0;
-    pf_phases<0>(W, warp, u, vi, pf, q0, q1, v0, v1, inv_prev, w, wi, n_inv, ci, cc);
+    if (warp == 4) {
+        side.run(&fdone);
+    } else {
+        pf_phases<0>(W, warp, u, vi, pf, q0, q1, v0, v1, inv_prev, w, wi, n_inv, ci, cc);
+        if (tid == 0) *(volatile int *)&fdone = 1;
+    }
     if (tid < T) {
         const double d = W[PW_A + tid * PW_ROW + tid];
         if (!(d > 0.0) || !isfinite(d)) bad = 1;
@@ -509,21 +527,28 @@ __device__ __forceinline__ void tri_of(int e, int &r, int &c)
     c = e - r * (r + 1) / 2;
 }
 
-template <bool WITH_B>
+template <bool WITH_B, int NT = CF_THREADS>
 struct LowerUpdate {
     static constexpr int NTRI = T * (T + 1) / 2;
     static constexpr int NE = NTRI + (WITH_B ? T : 0);
-    static constexpr int PER = (NE * T + CF_THREADS - 1) / CF_THREADS;
+    static constexpr int PER = (NE * T + NT - 1) / NT;
     static constexpr int NACC = (T - 1 + PER + T - 1) / T;  // elements one run can touch
-    static constexpr int PART = NACC * CF_THREADS;          // doubles of partial sums
+    static constexpr int PART = NACC * NT;                  // doubles of partial sums
 };
 
-template <bool WITH_B>
+// NT == CF_THREADS: the whole CTA, CTA barriers.  NT == CF_THREADS - 32: every
+// warp but warp 4 (the panel's), on named barrier 1.
+template <bool WITH_B, int NT = CF_THREADS>
 __device__ void update_lower(double (*a)[T + 1], const double (*L)[T + 1], double *b, const double *y, double *part)
 {
-    using U = LowerUpdate<WITH_B>;
+    static_assert(NT == CF_THREADS || NT == CF_THREADS - 32, "whole CTA or all warps but warp 4");
+    using U = LowerUpdate<WITH_B, NT>;
     constexpr int NTRI = U::NTRI, NE = U::NE, PER = U::PER, NACC = U::NACC;
-    const int tid = threadIdx.x;
+    auto sync = [] {
+        if (NT == CF_THREADS) __syncthreads();
+        else asm volatile("bar.sync 1, %0;" ::"n"(NT) : "memory");
+    };
+    const int tid = NT == CF_THREADS ? (int)threadIdx.x : (int)threadIdx.x - ((int)threadIdx.x >= 160 ? 32 : 0);
     const int f0 = tid * PER, e0 = f0 / T;
     const double *xs[NACC], *ys[NACC];
     double p[NACC];
@@ -560,8 +585,8 @@ __device__ void update_lower(double (*a)[T + 1], const double (*L)[T + 1], doubl
     }
 #pragma unroll
     for (int j = 0; j < NACC; ++j) part[NACC * tid + j] = p[j];
-    __syncthreads();
-    for (int e2 = tid; e2 < NE; e2 += CF_THREADS) {
+    sync();
+    for (int e2 = tid; e2 < NE; e2 += NT) {
         const int tlo = (e2 * T) / PER, thi = (e2 * T + T - 1) / PER;
         int r = 0, c = 0;
         if (e2 < NTRI) tri_of(e2, r, c);
@@ -570,7 +595,7 @@ __device__ void update_lower(double (*a)[T + 1], const double (*L)[T + 1], doubl
         if (e2 < NTRI) a[r][c] = v;
         else b[e2 - NTRI] = v;
     }
-    __syncthreads();
+    sync();
 }
 
 // out = A Linv^T restricted to the lower triangle of Linv (out[r][c] =
@@ -617,6 +642,53 @@ __device__ __forceinline__ void block_release(int *flag, int epoch)
     if (threadIdx.x == 0) st_release(flag, epoch);
 }
 
+// Warp 4 of the panel during a factor (it shares warp 0's sub-partition, has
+// no part in the plan and skips the factor's phase barriers): it raises the
+// flags of the previous step's outputs (stored before that step ended; the
+// release store waits for them here, off the pivot chain), then waits for
+// the flags of the next step's tiles (the sub-diagonal SUB(I) and the
+// diagonal PD(I+1) with its b) and copies those tiles into staging buffers.
+// It stops waiting when the factor is done (*fdone, set by thread 0 after
+// the last phase) or its budget runs out; *done says whether the tiles are
+// there, else the panel loads them itself after the factor.
+struct PanelSide {
+    int *rel0, *rel1;          // flags to raise (null: none)
+    const int *fa, *fb;        // flags the next tiles need (null: none)
+    const double *Smat, *rhs;
+    double (*asub)[T + 1], (*anext)[T + 1];
+    double *bnext;
+    int *done;
+    int epoch, Np, I;
+    bool want;                 // a next step exists
+
+    __device__ void run(const int *fdone)
+    {
+        const int lane = threadIdx.x & 31;
+        if (lane == 0) {
+            if (rel0) st_release(rel0, epoch);
+            if (rel1) st_release(rel1, epoch);
+        }
+        if (!want) return;
+        bool up = false;
+        for (long long it = 0; it < SPIN_LIMIT; ++it) {
+            // every lane acquires the flags itself, so its own loads below are ordered after them
+            up = (fa == nullptr || ld_acquire(fa) == epoch) && (fb == nullptr || ld_acquire(fb) == epoch);
+            if (up || *(const volatile int *)fdone) break;
+            __nanosleep(64);
+        }
+        if (!up) return;
+        for (int e = lane; e < 2 * TT; e += 32) {
+            const int t = e / TT, r = (e % TT) / T, c = e % T;
+            const double v = __ldcg(Smat + (size_t)((I + 1) * T + r) * Np + (I + t) * T + c);
+            if (t == 0) asub[r][c] = v;
+            else anext[r][c] = v;
+        }
+        if (lane < T) bnext[lane] = __ldcg(rhs + (I + 1) * T + lane);
+        __syncwarp();
+        if (lane == 0) *done = 1;
+    }
+};
+
 // Flags: tile (I, K) at tile_task(I, K); that slot is raised for the
 // diagonal tile (I, I) when L_II, its inverse and y_I are stored, and for the
 // sub-diagonal tile (I+1, I) when L_{I+1,I} is stored.  The partial diagonal
@@ -644,7 +716,7 @@ __global__ void __launch_bounds__(CF_THREADS, 1) k_chol_dataflow(int Np, int nb,
                                                               int *__restrict__ flags, int epoch,
                                                               int *__restrict__ status)
 {
-    static_assert(BJ >= 4, "the panel keeps four tiles in the staging area");
+    static_assert(BJ >= 6, "the panel keeps six tiles in the staging area");
     static_assert(LowerUpdate<true>::PART <= BJ * T * (T + 1), "update_lower's partial sums fit in the staging area");
     __shared__ double a[T][T + 1], linv[T][T + 1];
     __shared__ double bi[BJ][T][T + 1], bk[BJ][T][T + 1], by[BJ][T];
@@ -654,65 +726,103 @@ __global__ void __launch_bounds__(CF_THREADS, 1) k_chol_dataflow(int Np, int nb,
     const int tid = threadIdx.x;
     double *part = &bk[0][0][0];
     if (blockIdx.x == 0) {
-        // ---- panel.  The tiles of step I+1 (SUB(I), PD(I+1)) are polled for
-        // together and loaded in one batch right after the factor of step I;
-        // L_II, Linv_II, y_I and L_{I+1,I} are stored and their flags raised at
-        // the end of the step.  The panel tracks failure itself (a bad pivot
-        // of its own, a wait that ran out), so it never reads the status word.
+        // ---- panel.  Step I: warp 4 stores step I-1's outputs (L_{I-1,I-1},
+        // its inverse, y_{I-1}, L_{I,I-1}) and raises their flags while the
+        // other warps apply the last update to the diagonal tile; during the
+        // factor warp 4 fetches the tiles of step I+1 (PanelSide); then
+        // L_{I+1,I} is formed.  The panel tracks failure itself (a bad pivot of
+        // its own, a wait that ran out), so it never reads the status word.
         double(*lsub)[T + 1] = bi[2];  // L_{I,I-1} from the previous step
         double(*asub)[T + 1] = bi[3];
-        static_assert(LowerUpdate<true>::PART <= 2 * T * (T + 1), "update_lower's partial sums fit in bk[0..1]");
+        static_assert(LowerUpdate<true>::PART <= 2 * T * (T + 1) && LowerUpdate<true, CF_THREADS - 32>::PART <= 2 * T * (T + 1),
+                      "update_lower's partial sums fit in bk[0..1]");
         static_assert(2 * T * (T + 1) + PW_SIZE <= BJ * T * (T + 1), "the factor workspace fits after the partial sums");
         double *W = &bk[2][0][0];  // bk[0..1] hold update_lower's partial sums
         double(*wa)[T + 1] = reinterpret_cast<double(*)[T + 1]>(W + PW_A);
         double(*wl)[T + 1] = reinterpret_cast<double(*)[T + 1]>(W + PW_L);
         double(*wli)[T + 1] = reinterpret_cast<double(*)[T + 1]>(W + PW_LINV);
+        double(*anext)[T + 1] = bi[5];  // the next diagonal tile, fetched during the factor
+        double *bnext = by[0];
         __shared__ PfPlan s_pf;
+        __shared__ int pf_done;
         load_pf_plan(s_pf);
         bool failed = false;
+        const int warp = tid >> 5, lane = tid & 31;
         load_tile(wa, S, Np, 0, 0);
         if (tid < T) W[PW_B + tid] = __ldcg(rhs + tid);
         __syncthreads();
         for (int I = 0; I < nb; ++I) {
             const int td = tile_task(I, I, nb);
             CHOL_MARK(td, 0);
-            if (I >= 1 && !failed) update_lower<true>(wa, lsub, W + PW_B, W + PW_Y, part);
+            if (I >= 1) {
+                // warp 4 stores step I-1's outputs and raises their flags (its
+                // release waits for the stores, off the pivot chain) while the
+                // other warps apply the last update to the diagonal tile
+                if (warp == 4) {
+                    if (!failed) {
+                        const int Jp = I - 1;
+                        for (int e2 = lane; e2 < TT; e2 += 32) {
+                            const int r = e2 / T, c = e2 % T;
+                            S[(size_t)(Jp * T + r) * Np + Jp * T + c] = wl[r][c];
+                            Linv[(size_t)Jp * TT + e2] = wli[r][c];
+                            S[(size_t)(I * T + r) * Np + Jp * T + c] = lsub[r][c];
+                        }
+                        if (lane < T) rhs[Jp * T + lane] = W[PW_Y + lane];
+                    }
+                    __syncwarp();
+                    if (lane == 0) {
+                        st_release(flags + tile_task(I - 1, I - 1, nb), epoch);
+                        st_release(flags + tile_task(I, I - 1, nb), epoch);
+                    }
+                } else if (!failed) {
+                    update_lower<true, CF_THREADS - 32>(wa, lsub, W + PW_B, W + PW_Y, part);
+                }
+            }
             CHOL_MARK(td, 1);
+            if (tid == 0) pf_done = 0;
             if (!failed) {
-                const bool good = cta_potrf(W, s_pf);
+                PanelSide side{nullptr, nullptr,
+                               I >= 1 ? flags + n_fact + nb + I : nullptr,
+                               I + 1 >= 2 ? flags + n_fact + I + 1 : nullptr,
+                               S, rhs, asub, anext, bnext, &pf_done, epoch, Np, I, I + 1 < nb};
+                const bool good = cta_potrf(W, s_pf, side);
                 if (!good) {
                     failed = true;
                     if (tid == 0) atomicCAS(status, 0, 1);
                 }
+            } else {
+                __syncthreads();
             }
             CHOL_MARK(td, 2);
             if (I + 1 < nb) {
                 // the tile and b are free after the factor: the next diagonal tile goes there
-                if (I >= 1 && !block_wait(flags + n_fact + nb + I, epoch, status)) failed = true;
-                if (I + 1 >= 2 && !block_wait(flags + n_fact + I + 1, epoch, status)) failed = true;
-                for (int e2 = tid; e2 < TT; e2 += CF_THREADS) {
-                    const int r = e2 / T, c = e2 % T;
-                    asub[r][c] = __ldcg(S + (size_t)((I + 1) * T + r) * Np + I * T + c);
-                    wa[r][c] = __ldcg(S + (size_t)((I + 1) * T + r) * Np + (I + 1) * T + c);
+                if (pf_done) {
+                    for (int e2 = tid; e2 < TT; e2 += CF_THREADS) wa[e2 / T][e2 % T] = anext[e2 / T][e2 % T];
+                    if (tid < T) W[PW_B + tid] = bnext[tid];
+                } else {
+                    if (I >= 1 && !block_wait(flags + n_fact + nb + I, epoch, status)) failed = true;
+                    if (I + 1 >= 2 && !block_wait(flags + n_fact + I + 1, epoch, status)) failed = true;
+                    for (int e2 = tid; e2 < TT; e2 += CF_THREADS) {
+                        const int r = e2 / T, c = e2 % T;
+                        asub[r][c] = __ldcg(S + (size_t)((I + 1) * T + r) * Np + I * T + c);
+                        wa[r][c] = __ldcg(S + (size_t)((I + 1) * T + r) * Np + (I + 1) * T + c);
+                    }
+                    if (tid < T) W[PW_B + tid] = __ldcg(rhs + (I + 1) * T + tid);
                 }
-                if (tid < T) W[PW_B + tid] = __ldcg(rhs + (I + 1) * T + tid);
                 __syncthreads();
                 if (!failed) tile_trsm(lsub, asub, wli);
                 __syncthreads();
             }
             CHOL_MARK(td, 3);
-            if (!failed) {
-                store_tile(S, Np, I, I, wl);
-                for (int e2 = tid; e2 < TT; e2 += CF_THREADS) Linv[(size_t)I * TT + e2] = wli[e2 / T][e2 % T];
-                if (tid < T) rhs[I * T + tid] = W[PW_Y + tid];
-                if (I + 1 < nb) store_tile(S, Np, I + 1, I, lsub);
-            }
-            __syncthreads();
-            if (tid == 0) {
-                st_release(flags + td, epoch);
-                if (I + 1 < nb) st_release(flags + tile_task(I + 1, I, nb), epoch);
-            }
         }
+        // the last step's outputs
+        if (!failed) {
+            store_tile(S, Np, nb - 1, nb - 1, wl);
+            for (int e2 = tid; e2 < TT; e2 += CF_THREADS) Linv[(size_t)(nb - 1) * TT + e2] = wli[e2 / T][e2 % T];
+            if (tid < T) rhs[(nb - 1) * T + tid] = W[PW_Y + tid];
+        }
+        __syncthreads();
+        if (tid == 0) st_release(flags + tile_task(nb - 1, nb - 1, nb), epoch);
         return;
     }
     // ---- helpers

@@ -116,23 +116,30 @@ __device__ __forceinline__ void load_tile(double (*dst)[T + 1], const double *S,
 // of dependent pivots (d_s, then 1/sqrt(d_s)) and by how much latency the
 // rest adds per column.  The plan below keeps everything but the pivot chain
 // off warp 0 and gives every other thread a fixed, index-free role, in
-// T + 1 phases separated by one CTA barrier each:
+// T + 1 phases separated by one barrier each (named barrier 1, the seven warps
+// with a role):
 //   warp 0    phase s: d_s = a[s][s] - (a[s][s-1] / L_{s-1,s-1})^2 (the last
-//             update of the pivot, one column ahead of the others), 1/L_ss.
-//   trailing  (warps 1, 2, 3, 5) own the entries a[r][j], 1 <= j <= r, and
+//             update of the pivot, one column ahead of the others), 1/L_ss
+//             and 1/d_s.
+//   trailing  (warps 2, 3, 6, 7) own the entries a[r][j], 1 <= j <= r, and
 //             b[r] (as column T) in registers.  Phase s applies column s-1:
 //             a[r][j] -= a[r][s-1] a[j][s-1] / d_{s-1}; an entry is published
 //             to shared memory in the phase it becomes final, and its L
 //             value (a[r][j] / L_jj, y_r = b_r / L_rr) written in the next.
-//   inverse   (warps 6, 7) build X = L^-1 one column behind L: entry (i, c)
+//   inverse   (warps 1, 5) build X = L^-1 one column behind L: entry (i, c)
 //             takes X[i][c] -= L[i][k] X[k][c] in phase k + 2, c <= k < i,
 //             and X[i][c] /= L_ii in its last phase; entries are dealt to
 //             threads by interval colouring, so a thread has one at a time.
-//   warp 4    shares warp 0's sub-partition and stays idle.
+//   warp 4    shares warp 0's sub-partition and takes no part in the phases
+//             (the panel gives it the step's stores and fetches).
 // Each role runs the same short instruction sequence in every lane (operands
-// picked by selects), so a warp issues ~3 FP64 instructions per phase.  The
-// plan is built at compile time and copied to shared memory once per launch
-// (divergent reads of constant memory serialise).
+// picked by selects), so a trailing warp issues two FP64 instructions per
+// phase.  The roles run alongside the chain but still slow it (the chain
+// alone: ~710 cycles per column; all roles: ~840); this placement of the
+// roles and the published 1/d_s measured 7% faster than trailing on warps
+// 1, 2, 3, 5 computing 1/d_s themselves.  The plan is built at compile time
+// and copied to shared memory once per launch (divergent reads of constant
+// memory serialise).
 
 enum : unsigned char { PF_NONE = 0, PF_OFF, PF_DIAG, PF_D11, PF_B, PF_COL0, PF_B0 };
 constexpr int PF_TRAIL = 128, PF_INV = 64, PF_INV_MAX = 16;
@@ -231,7 +238,8 @@ constexpr int PW_BW = 3 * T * PW_ROW;    // b being reduced
 constexpr int PW_INVD = PW_BW + T;       // 1 / L_kk
 constexpr int PW_Y = PW_BW + 2 * T;      // y = L^-1 b
 constexpr int PW_B = PW_BW + 3 * T;      // b (input)
-constexpr int PW_SIZE = PW_BW + 4 * T;
+constexpr int PW_INV2 = PW_BW + 4 * T;   // 1 / d_k (warp 0 publishes it with 1 / L_kk)
+constexpr int PW_SIZE = PW_BW + 5 * T;
 
 // One entry of a trailing thread, decoded once per factor into offsets: the
 // entry's row (xo), the other operand of its update (oo: row j of the tile,
@@ -307,12 +315,12 @@ __device__ __forceinline__ void pf_phase(double *W, int warp, int u, int vi, con
             }
             inv_prev = rsqrt(d);
             W[PW_INVD + S] = inv_prev;
+            W[PW_INV2 + S] = inv_prev * inv_prev;
             W[PW_LINV + S * PW_ROW + S] = inv_prev;
         }
     } else if (u >= 0) {
         if (S >= 1) {
-            const double ik = W[PW_INVD + (S >= 1 ? S - 1 : 0)];
-            const double ik2 = ik * ik;
+            const double ik2 = W[PW_INV2 + (S >= 1 ? S - 1 : 0)];
             pf_step<S>(q0, v0, ik2, W);
             if (S <= 2) pf_step<S>(q1, v1, ik2, W);
         }
@@ -368,8 +376,8 @@ __device__ bool cta_potrf(double *W, const PfPlan &pf, Side &&side = Side())
         bad = 0;
         fdone = 0;
     }
-    const int u = (warp >= 1 && warp <= 3) ? tid - 32 : warp == 5 ? tid - 64 : -1;
-    const int vi = warp >= 6 ? tid - 192 : -1;
+    const int u = (warp == 2 || warp == 3) ? tid - 64 : (warp == 6 || warp == 7) ? tid - 128 : -1;
+    const int vi = warp == 1 ? tid - 32 : warp == 5 ? tid - 128 : -1;
     PfSlot q0 = pf_slot(PfEntry{PF_NONE, 0, 0}), q1 = q0;
     double v0 = 0.0, v1 = 0.0;
     if (u >= 0) {

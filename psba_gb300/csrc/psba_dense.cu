@@ -702,7 +702,9 @@ struct PanelSide {
 // sub-diagonal tile (I+1, I) when L_{I+1,I} is stored.  The partial diagonal
 // PD(I) = A_II - sum_{J <= I-2} L_IJ L_IJ^T (with b_I likewise) raises
 // n_fact + I; the partial sub-diagonal SUB(I) = A_{I+1,I} - sum_{J <= I-1}
-// L_{I+1,J} L_IJ^T raises n_fact + nb + I.
+// L_{I+1,J} L_IJ^T raises n_fact + nb + I; the second-subdiagonal tile
+// (K+2, K) raises n_fact + 2 nb + K when its accumulation (before its solve)
+// is in pre[K].
 //
 // The factor with the forward solve of rhs carried along.  CTA 0 (the panel)
 // walks the diagonal: step I applies the last update to PD(I) with L_{I,I-1}
@@ -721,6 +723,7 @@ __global__ void __launch_bounds__(CF_THREADS, 1) k_chol_dataflow(int Np, int nb,
                                                               double *__restrict__ S,
                                                               double *__restrict__ Linv,
                                                               double *__restrict__ rhs,
+                                                              double *__restrict__ pre,
                                                               int *__restrict__ flags, int epoch,
                                                               int *__restrict__ status)
 {
@@ -847,9 +850,10 @@ __global__ void __launch_bounds__(CF_THREADS, 1) k_chol_dataflow(int Np, int nb,
         // tiles loaded together and are applied from shared memory.  Each
         // element is updated in the same order as one step at a time would.
         const int n_upd = kind == 0 ? I - 1 : K;
+        const int n_main = kind <= 1 ? n_upd - 1 : n_upd;  // PD and SUB take their last step below
         int J = 0;
-        while (J < n_upd) {
-            const int nmax = min(BJ, n_upd - J);
+        while (J < n_main) {
+            const int nmax = min(BJ, n_main - J);
             if (tid == 0) ready_n = nmax;
             __syncthreads();
             if (tid < nmax) {
@@ -887,6 +891,43 @@ __global__ void __launch_bounds__(CF_THREADS, 1) k_chol_dataflow(int Np, int nb,
             }
             __syncthreads();
             J += n;
+        }
+        if (kind <= 1) {
+            // Last step, J = I - 2: L_{I,J} is the second-subdiagonal tile, whose
+            // own task publishes it before its solve (PRE) and solves it once
+            // the panel raises Linv_JJ.  PD and SUB solve it here themselves
+            // (the same arithmetic, so the same bits) as soon as Linv_JJ is
+            // up, which saves the panel a hand-off per step.
+            const int Jl = I - 2;
+            block_wait(flags + n_fact + 2 * nb + Jl, epoch, status);
+            block_wait(flags + tile_task(Jl, Jl, nb), epoch, status);
+            if (kind == 1) block_wait(flags + tile_task(K, Jl, nb), epoch, status);
+            for (int e2 = tid; e2 < TT; e2 += CF_THREADS) {
+                const int r = e2 / T, c = e2 % T;
+                bi[1][r][c] = __ldcg(pre + (size_t)Jl * TT + e2);
+                linv[r][c] = __ldcg(Linv + (size_t)Jl * TT + e2);
+                if (kind == 1) bi[2][r][c] = __ldcg(S + (size_t)(K * T + r) * Np + Jl * T + c);
+            }
+            if (kind == 0 && tid < T) by[0][tid] = __ldcg(rhs + Jl * T + tid);
+            __syncthreads();
+            tile_trsm(bi[0], bi[1], linv);
+            __syncthreads();
+            if (kind == 0) {
+                update_lower<true>(a, bi[0], bvec, by[0], part);
+            } else {
+                for (int e2 = tid; e2 < TT; e2 += CF_THREADS) {
+                    const int r = e2 / T, c = e2 % T;
+                    double sacc = a[r][c];
+#pragma unroll
+                    for (int k = 0; k < T; ++k) sacc = fma(-bi[0][r][k], bi[2][c][k], sacc);
+                    a[r][c] = sacc;
+                }
+                __syncthreads();
+            }
+        } else if (kind == 2) {
+            // the second-subdiagonal tile before its solve, for PD(K + 2) and SUB(K + 1)
+            for (int e2 = tid; e2 < TT; e2 += CF_THREADS) pre[(size_t)K * TT + e2] = a[e2 / T][e2 % T];
+            block_release(flags + n_fact + 2 * nb + K, epoch);
         }
         CHOL_MARK(mark, 1);
         const bool failed = block_failed(status);
@@ -972,9 +1013,9 @@ void launch_chol_dataflow(const DeviceProblem &d, int mode, int epoch, double *x
         int n_tasks = d.chol_n_tasks;
         const int grid = chol_grid(n_tasks + 1);
         const int2 *tasks = d.chol_tasks;
-        double *S = d.S, *Linv = d.Linv, *rhs = d.rhs;
+        double *S = d.S, *Linv = d.Linv, *rhs = d.rhs, *pre = d.chol_pre;
         int *flags = d.chol_flags, *status = d.status;
-        void *args[] = {&Np, &nb, &n_tasks, (void *)&tasks, &S, &Linv, &rhs, &flags, &epoch, &status};
+        void *args[] = {&Np, &nb, &n_tasks, (void *)&tasks, &S, &Linv, &rhs, &pre, &flags, &epoch, &status};
         cudaMemsetAsync(d.status, 0, 2 * sizeof(int), s);
         cudaLaunchCooperativeKernel((const void *)k_chol_dataflow, dim3(grid), dim3(CF_THREADS), args, 0, s);
         note_launch(1);

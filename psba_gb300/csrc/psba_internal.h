@@ -128,6 +128,7 @@ struct DeviceProblem {
     int *status = nullptr;        // Cholesky status word (0 ok, 1 not SPD, 2 wait budget exhausted)
     int2 *chol_tasks = nullptr;   // helper tasks of the dense factor, in dependency order
     int chol_n_tasks = 0;
+    double *chol_pre = nullptr;   // second-subdiagonal tiles before their solve (Np / TILE tiles)
     int *chol_flags = nullptr;    // one flag per dataflow task (value = epoch when done)
     int chol_n_flags = 0;
     double *dp = nullptr;         // N + 3 np

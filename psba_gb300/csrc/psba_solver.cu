@@ -974,7 +974,8 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
         std::vector<int2> tasks;
         chol_task_list(nb, tasks);
         d.chol_n_tasks = (int)tasks.size();
-        d.chol_n_flags = nb * (nb + 1) / 2 + 2 * nb;
+        d.chol_n_flags = nb * (nb + 1) / 2 + 3 * nb;
+        TRY(dalloc(h, &d.chol_pre, (size_t)nb * TILE * TILE));
         TRY(dalloc(h, &d.chol_tasks, tasks.size()));
         TRY(dalloc(h, &d.chol_flags, (size_t)d.chol_n_flags));
         TRY(upload(h, d.chol_tasks, tasks.data(), tasks.size()));

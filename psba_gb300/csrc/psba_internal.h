@@ -19,7 +19,9 @@ constexpr int MNP = 2;   // image coordinates
 constexpr int CAMTAB = 56;  // doubles per camera table entry (CamTab)
 constexpr int TILE = 16;    // dense Cholesky tile size
 constexpr int SCHUR_CHUNK = 32;  // pair-list entries per off-diagonal Schur work unit
-constexpr int DIAG_CHUNK = 16;   // observations per diagonal Schur work unit
+constexpr int DIAG_CHUNK = 16;   // observations per diagonal Schur work unit (11/16-parameter cameras)
+constexpr int SD_THREADS = 128, SD_PER = 8;     // 6-parameter cameras: one CTA per unit, 8 observations a thread
+constexpr int DIAG_SUPER = SD_THREADS * SD_PER;  // observations per diagonal unit, 6-parameter cameras
 constexpr int CAM_CHUNK = 512;   // observations per camera-reduction work unit
 constexpr int RED_THREADS = 256; // threads of the reduction kernels
 

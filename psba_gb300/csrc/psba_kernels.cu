@@ -678,28 +678,48 @@ __device__ __forceinline__ void diag_products(const R *y, const R *w, double g0,
     }
 }
 
+// Diagonal blocks U_k - sum Y W^T (lower 21) and the ea sums (6): one CTA of
+// SD_THREADS per unit of <= DIAG_SUPER observations of one camera, SD_PER
+// consecutive observations per thread (FP64: accumulated directly; mixed:
+// FP32 products over the thread's observations, then one FP64 addition).
+// The CTA then sums its threads' partials in a fixed order (each output by
+// four threads over 32 partials each, then the four) and writes one partial
+// per unit, so a camera has only a handful for k_schur_reduce.
 template <typename R>
-__global__ void __launch_bounds__(128) k_schur_diag(int n_units, const SchurUnit *__restrict__ units,
-                                                    const int *__restrict__ cam_obs,
-                                                    const int *__restrict__ obs_pt,
-                                                    const R *__restrict__ Y,
-                                                    const R *__restrict__ W,
-                                                    const double *__restrict__ gb,
-                                                    double *__restrict__ partial)
+__global__ void __launch_bounds__(SD_THREADS) k_schur_diag(const SchurUnit *__restrict__ units,
+                                                           const int *__restrict__ cam_obs,
+                                                           const int *__restrict__ obs_pt,
+                                                           const R *__restrict__ Y,
+                                                           const R *__restrict__ W,
+                                                           const double *__restrict__ gb,
+                                                           double *__restrict__ partial)
 {
-    const int uid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (uid >= n_units) return;
-    const SchurUnit u = units[uid];
+    static_assert(SD_THREADS == 128 && DIAG_NV * 4 <= SD_THREADS, "four summing threads per output");
+    __shared__ double red[DIAG_NV][SD_THREADS + 1];
+    const SchurUnit u = units[blockIdx.x];
+    const int t = threadIdx.x;
     double acc[DIAG_NV];
 #pragma unroll
     for (int e = 0; e < DIAG_NV; ++e) acc[e] = 0.0;
-    for (int t0 = 0; t0 < u.count; t0 += FLUSH) {
+    const int o1 = min(u.count, (t + 1) * SD_PER);
+    if constexpr (is_fp64<R>()) {
+        for (int o = t * SD_PER; o < o1; ++o) {
+            const int a = __ldg(cam_obs + u.begin + o);
+            const int i = __ldg(obs_pt + a);
+            R w[18], y[18];
+            ldn<R, 18>(W + 18 * (size_t)a, w);
+            ldn<R, 18>(Y + 18 * (size_t)a, y);
+            const double g0 = __ldg(gb + 3 * (size_t)i), g1 = __ldg(gb + 3 * (size_t)i + 1),
+                         g2 = __ldg(gb + 3 * (size_t)i + 2);
+            diag_products<R>(y, w, g0, g1, g2, acc, acc + 21);
+        }
+    } else {
+        static_assert(SD_PER <= FLUSH, "one FP32 flush per thread");
         R part[21];
 #pragma unroll
         for (int e = 0; e < 21; ++e) part[e] = (R)0;
-        const int tend = min(u.count, t0 + FLUSH);
-        for (int t = t0; t < tend; ++t) {
-            const int a = __ldg(cam_obs + u.begin + t);
+        for (int o = t * SD_PER; o < o1; ++o) {
+            const int a = __ldg(cam_obs + u.begin + o);
             const int i = __ldg(obs_pt + a);
             R w[18], y[18];
             ldn<R, 18>(W + 18 * (size_t)a, w);
@@ -709,11 +729,21 @@ __global__ void __launch_bounds__(128) k_schur_diag(int n_units, const SchurUnit
             diag_products<R>(y, w, g0, g1, g2, part, acc + 21);
         }
 #pragma unroll
-        for (int e = 0; e < 21; ++e) acc[e] += (double)part[e];
+        for (int e = 0; e < 21; ++e) acc[e] = (double)part[e];
     }
-    double *p = partial + (size_t)u.out * DIAG_NV;
 #pragma unroll
-    for (int e = 0; e < DIAG_NV; ++e) p[e] = acc[e];
+    for (int e = 0; e < DIAG_NV; ++e) red[e][t] = acc[e];
+    __syncthreads();
+    double s = 0.0;
+    const int v = t >> 2, g = t & 3;
+    if (v < DIAG_NV) {
+#pragma unroll 8
+        for (int q = 0; q < SD_THREADS / 4; ++q) s += red[v][g * (SD_THREADS / 4) + q];
+    }
+    __syncthreads();
+    if (v < DIAG_NV) red[v][g] = s;
+    __syncthreads();
+    if (t < DIAG_NV) partial[(size_t)u.out * DIAG_NV + t] = (red[t][0] + red[t][1]) + (red[t][2] + red[t][3]);
 }
 
 // Sum unit partials into S (lower) and rhs = ea.
@@ -785,12 +815,12 @@ void launch_schur_diag(const DeviceProblem &d, cudaStream_t s)
     double *diag_partial = d.schur_partial + (size_t)d.n_off_units * 36;
     if (d.n_diag_units == 0) return;
     if (d.prec == PSBA_PREC_FP64)
-        k_schur_diag<double><<<ceil_div(d.n_diag_units, 128), 128, 0, s>>>(
-            d.n_diag_units, d.diag_units, d.cam_obs, d.obs_pt, d.Y, d.W, d.g + d.N, diag_partial);
+        k_schur_diag<double><<<d.n_diag_units, SD_THREADS, 0, s>>>(d.diag_units, d.cam_obs, d.obs_pt, d.Y, d.W,
+                                                                   d.g + d.N, diag_partial);
     else
-        k_schur_diag<float><<<ceil_div(d.n_diag_units, 128), 128, 0, s>>>(
-            d.n_diag_units, d.diag_units, d.cam_obs, d.obs_pt, (const float *)d.Y, (const float *)d.W,
-            d.g + d.N, diag_partial);
+        k_schur_diag<float><<<d.n_diag_units, SD_THREADS, 0, s>>>(d.diag_units, d.cam_obs, d.obs_pt,
+                                                                  (const float *)d.Y, (const float *)d.W,
+                                                                  d.g + d.N, diag_partial);
     note_launch(1);
 }
 

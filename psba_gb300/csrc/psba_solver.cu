@@ -906,9 +906,10 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
         }
         off_start[q + 1] = (int)off_units.size();
     }
+    const int dchunk = d.cnp == 6 ? DIAG_SUPER : DIAG_CHUNK;
     for (int j = 0; j < nc; ++j) {
-        for (int b = cam_start[j]; b < cam_start[j + 1]; b += DIAG_CHUNK) {
-            const int cnt = std::min(DIAG_CHUNK, cam_start[j + 1] - b);
+        for (int b = cam_start[j]; b < cam_start[j + 1]; b += dchunk) {
+            const int cnt = std::min(dchunk, cam_start[j + 1] - b);
             diag_units.push_back({j, b, cnt, (int)diag_units.size()});
         }
         diag_start[j + 1] = (int)diag_units.size();

@@ -232,12 +232,14 @@ def test_mixed_power_law_matched_final_cost():
     # This power-law scene has two LM minima 0.7% apart: the FP64 oracle ends
     # at 14,137,773.7 with tau = 1e-3 or 2e-3 and at 14,237,019.5 with tau =
     # 5e-4 or 1e-2, so a trajectory that differs in the last bits may end in
-    # either.  What the mixed form must not do is stop short of the minimum it
-    # reached: FP64 LM (oracle) restarted from its endpoint must not lower the
-    # cost by more than 1e-6 relative.
+    # either, and the valley is flat (the mixed form takes 200-300 iterations).
+    # What the mixed form must not do is stop short of the minimum it reached:
+    # run to a stopping criterion, then FP64 LM (oracle) restarted from its
+    # endpoint must not lower the cost by more than 1e-6 relative.
     sc = scenes.circle_scene(seed=2, n_cams=24, n_pts=3000, name="circle24")
     with P.Solver(sc) as s:
-        g = s.levmar(allow_switch=0, max_iter=100, precision=P.PREC_MIXED)
+        g = s.levmar(allow_switch=0, max_iter=400, precision=P.PREC_MIXED)
+    assert g.status != P.ITER_CONTINUE
     sess = oracle.Session(sc)
     try:
         polish = sess.levmar(oracle.default_opts(allow_switch=0, max_iter=100), cams=g.cams, pts=g.pts)

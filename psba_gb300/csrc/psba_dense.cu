@@ -19,11 +19,14 @@
 // or non-finite pivot (SPD_inv.cl:66-107) sets status 1; every task still
 // raises its flag, so nothing waits forever.  A spin that runs out of its
 // iteration budget sets status 2 and the kernel completes.
+#include <cooperative_groups.h>
 #include <vector>
 
 #include "psba_internal.h"
 
 namespace psba {
+
+namespace cg = cooperative_groups;
 
 constexpr int T = TILE;
 constexpr int TT = TILE * TILE;
@@ -34,6 +37,9 @@ constexpr int TT = TILE * TILE;
 #endif
 #ifndef PSBA_CHOL_BJ
 #define PSBA_CHOL_BJ 8
+#endif
+#ifndef PSBA_TRI_CLUSTER
+#define PSBA_TRI_CLUSTER 1  // triangular solves on a cluster of CTAs (else one CTA)
 #endif
 #ifndef PSBA_CHOL_PER_SM
 #define PSBA_CHOL_PER_SM 1  // the panel's FP64 chain runs alone on its SM
@@ -56,8 +62,15 @@ __device__ __forceinline__ void trace_mark(int t, int k)
     }
 }
 #define CHOL_MARK(t, k) trace_mark(t, k)
+// back-solve step K of the cluster solve, on the step's owner
+#define TRI_MARK(K, k)                                                          \
+    do {                                                                        \
+        if ((K) % 8 == (int)cg::this_cluster().block_rank() && (K) < 8192)     \
+            trace_mark(40000 + (K), k);                                         \
+    } while (0)
 #else
 #define CHOL_MARK(t, k)
+#define TRI_MARK(K, k)
 #endif
 
 __device__ __forceinline__ int ld_acquire(const int *p)
@@ -1005,6 +1018,174 @@ __global__ void __launch_bounds__(TS_THREADS) k_tri_solve(int forward, int Np, i
     cta_back(Np, nb, S, Linv, vec, tmp, x);
 }
 
+// ---------------------------------------------------------------------------
+// The triangular solves on a thread-block cluster of TC_CTAS CTAs (one SM
+// each).  One SM's FP64 rate bounds a one-CTA solve (N^2 / 2 multiply-adds);
+// the cluster spreads the updates over TC_CTAS SMs and passes each step's
+// solved block through distributed shared memory with one cluster barrier
+// per step (~400 cycles on GB300, against 1-2 us for a flag in L2).
+// Block I of the vector is owned by CTA I mod TC_CTAS, which holds it in
+// shared memory.  Step K: the owner solves block K (16 x 16 product with
+// the diagonal inverse, 256 threads, fixed shuffle tree), publishes it and
+// arrives at the barrier; while the barrier completes, every CTA applies the
+// previous step's block to its other blocks; after it, every CTA reads block
+// K from the owner and first updates the block the next step needs (if it
+// owns it), so the next owner can solve and arrive at once.  The diagonal
+// inverse entries and the coefficients of that first update are loaded a
+// step ahead.  Each vector entry takes its updates in step order: results
+// do not depend on timing.
+constexpr int TC_CTAS = 8, TC_THREADS = 256;
+
+__device__ __forceinline__ void cl_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
+__device__ __forceinline__ void cl_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
+
+// v[c] -= sum_r P(r, c) xs[r] for the columns (back) or rows (forward) listed
+// by idx(q), q < n: four threads per entry, four terms each, fixed tree
+template <typename Coef, typename Idx>
+__device__ __forceinline__ void cl_update(double *v, const double *xs, int n, Coef coef, Idx idx)
+{
+    const int g = threadIdx.x & 3;
+    for (int q0 = 0; q0 < n; q0 += TC_THREADS / 4) {
+        const int q = q0 + (threadIdx.x >> 2);
+        double s = 0.0;
+        int c = 0;
+        if (q < n) {
+            c = idx(q);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) s = fma(coef(4 * g + j, c), xs[4 * g + j], s);
+        }
+        s += __shfl_xor_sync(0xffffffffu, s, 1);
+        s += __shfl_xor_sync(0xffffffffu, s, 2);
+        if (q < n && g == 0) v[c] -= s;
+    }
+}
+
+__global__ void __launch_bounds__(TC_THREADS) k_tri_cluster(int forward, int Np, int nb,
+                                                            const double *__restrict__ S,
+                                                            const double *__restrict__ Linv,
+                                                            const double *__restrict__ rhs,
+                                                            double *__restrict__ x, const int *__restrict__ status)
+{
+    static_assert(TC_THREADS == TT, "one thread per term of the 16 x 16 diagonal product");
+    extern __shared__ double vec[];  // Np; this CTA's blocks are the valid ones
+    __shared__ double xb[2][T], xs[2][T];
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank(), tid = threadIdx.x;
+    if (*status != 0) return;  // the same word for every CTA: all leave together
+    for (int I = rank; I < nb; I += TC_CTAS)
+        if (tid < T) vec[I * T + tid] = rhs[I * T + tid];
+    const int dr = tid / T, dk = tid % T;
+    auto mine = [&](int I) { return I >= 0 && I < nb && I % TC_CTAS == rank; };
+    auto n_between = [&](int lo, int hi) {  // entries of my blocks I with lo < I < hi
+        int n = 0;
+        for (int I = rank; I < nb; I += TC_CTAS)
+            if (I > lo && I < hi) ++n;
+        return n * T;
+    };
+    auto entry_between = [&](int lo, int q) {  // q-th entry of my blocks above lo, ascending
+        const int first = lo < rank ? rank : rank + ((lo - rank) / TC_CTAS + 1) * TC_CTAS;
+        return (first + (q / T) * TC_CTAS) * T + q % T;
+    };
+    __syncthreads();
+    // the critical update: four terms of one entry of the next step's block
+    // per thread (threads 0..63), its coefficients loaded one step ahead
+    const int cq = tid >> 2, cg4 = tid & 3;
+    auto crit_apply = [&](double *v, const double *xs_, const double (&cf)[4], int entry) {
+        double s = 0.0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) s = fma(cf[j], xs_[4 * cg4 + j], s);
+        s += __shfl_xor_sync(0xffffffffu, s, 1);
+        s += __shfl_xor_sync(0xffffffffu, s, 2);
+        if (cq < T && cg4 == 0) v[entry] -= s;
+    };
+    if (forward) {
+        // L y = b: step K solves y_K = Linv_K b_K, then b_I -= L_IK y_K for I > K
+        auto ldiag = [&](int K) { return mine(K) && dk <= dr ? __ldcg(Linv + (size_t)K * TT + dr * T + dk) : 0.0; };
+        auto lcrit = [&](int K, double (&cf)[4]) {  // rows of block K+1, columns of block K
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                cf[j] = (cq < T && mine(K + 1)) ? __ldcg(S + (size_t)((K + 1) * T + cq) * Np + K * T + 4 * cg4 + j) : 0.0;
+        };
+        double pl = ldiag(0), cf[4];
+        lcrit(0, cf);
+        int pend = -1;
+        for (int K = 0; K < nb; ++K) {
+            if (mine(K)) {
+                const double yv = half_warp_sum(pl * vec[K * T + dk]);
+                if (dk == 0) xb[K & 1][dr] = yv;
+            }
+            __syncthreads();
+            if (mine(K) && tid < T) vec[K * T + tid] = xb[K & 1][tid];
+            cl_arrive();
+            const double pl_next = K + 1 < nb ? ldiag(K + 1) : 0.0;
+            if (pend >= 0) {  // the previous step's block, applied to my blocks above pend + 1
+                const int P = pend;
+                const double *xp = xs[P & 1];
+                cl_update(vec, xp, n_between(P + 1, nb),
+                          [&](int r, int i) { return __ldcg(S + (size_t)i * Np + P * T + r); },
+                          [&](int q) { return entry_between(P + 1, q); });
+            }
+            cl_wait();
+            if (tid < T) xs[K & 1][tid] = cl.map_shared_rank(&xb[K & 1][0], K % TC_CTAS)[tid];
+            __syncthreads();
+            if (mine(K + 1)) crit_apply(vec, xs[K & 1], cf, (K + 1) * T + cq);
+            __syncthreads();
+            if (K + 1 < nb) lcrit(K + 1, cf);
+            pl = pl_next;
+            pend = K;
+        }
+        // the last step's block reaches no block above it
+        cl_arrive();
+        cl_wait();
+    }
+    {
+        // L^T x = y: step K solves x_K = Linv_K^T y_K, then y_I -= L_KI^T x_K for I < K
+        auto ldiag = [&](int K) { return mine(K) && dk >= dr ? __ldcg(Linv + (size_t)K * TT + dk * T + dr) : 0.0; };
+        auto lcrit = [&](int K, double (&cf)[4]) {  // rows of block K, columns of block K-1
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                cf[j] = (cq < T && mine(K - 1)) ? __ldcg(S + (size_t)(K * T + 4 * cg4 + j) * Np + (K - 1) * T + cq) : 0.0;
+        };
+        double pl = ldiag(nb - 1), cf[4];
+        lcrit(nb - 1, cf);
+        int pend = -1;
+        for (int K = nb - 1; K >= 0; --K) {
+            TRI_MARK(K, 0);
+            if (mine(K)) {
+                const double xv = half_warp_sum(pl * vec[K * T + dk]);
+                if (dk == 0) {
+                    xb[K & 1][dr] = xv;
+                    x[K * T + dr] = xv;
+                }
+            }
+            __syncthreads();
+            cl_arrive();
+            TRI_MARK(K, 1);
+            const double pl_next = K > 0 ? ldiag(K - 1) : 0.0;
+            if (pend >= 0) {  // the previous step's block, applied to my blocks below pend - 1
+                const int P = pend;
+                const double *xp = xs[P & 1];
+                cl_update(vec, xp, n_between(-1, P - 1),
+                          [&](int r, int c) { return __ldcg(S + (size_t)(P * T + r) * Np + c); },
+                          [&](int q) { return entry_between(-1, q); });
+            }
+            TRI_MARK(K, 2);
+            cl_wait();
+            TRI_MARK(K, 3);
+            if (tid < T) xs[K & 1][tid] = cl.map_shared_rank(&xb[K & 1][0], K % TC_CTAS)[tid];
+            __syncthreads();
+            if (mine(K - 1)) crit_apply(vec, xs[K & 1], cf, (K - 1) * T + cq);
+            __syncthreads();
+            if (K > 0) lcrit(K - 1, cf);
+            pl = pl_next;
+            pend = K;
+        }
+        // no CTA may leave while another can still read its shared memory
+        cl_arrive();
+        cl_wait();
+    }
+}
+
 void launch_chol_dataflow(const DeviceProblem &d, int mode, int epoch, double *x_out, cudaStream_t s)
 {
     int nb = d.Np / T;
@@ -1020,7 +1201,27 @@ void launch_chol_dataflow(const DeviceProblem &d, int mode, int epoch, double *x
         cudaLaunchCooperativeKernel((const void *)k_chol_dataflow, dim3(grid), dim3(CF_THREADS), args, 0, s);
         note_launch(1);
     }
+#if PSBA_TRI_CLUSTER
+    {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(TC_CTAS);
+        cfg.blockDim = dim3(TC_THREADS);
+        cfg.dynamicSmemBytes = sizeof(double) * Np;
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = TC_CTAS;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        const double *S = d.S, *Linv = d.Linv, *rhs = d.rhs;
+        cudaLaunchKernelEx(&cfg, k_tri_cluster, (int)(mode == 1), Np, nb, S, Linv, rhs, x_out,
+                           (const int *)d.status);
+    }
+#else
     k_tri_solve<<<1, TS_THREADS, sizeof(double) * Np, s>>>(mode == 1, Np, nb, d.S, d.Linv, d.rhs, x_out, d.status);
+#endif
     note_launch(1);
 }
 

@@ -1153,12 +1153,12 @@ __global__ void __launch_bounds__(TC_THREADS) k_tri_cluster(int forward, int Np,
             TRI_MARK(K, 0);
             if (mine(K)) {
                 const double xv = half_warp_sum(pl * vec[K * T + dk]);
-                if (dk == 0) {
-                    xb[K & 1][dr] = xv;
-                    x[K * T + dr] = xv;
-                }
+                if (dk == 0) xb[K & 1][dr] = xv;
             }
             __syncthreads();
+            // x_K replaces y_K in the owner's vector (no global store before the
+            // release: the arrive would wait for it)
+            if (mine(K) && tid < T) vec[K * T + tid] = xb[K & 1][tid];
             cl_arrive();
             TRI_MARK(K, 1);
             const double pl_next = K > 0 ? ldiag(K - 1) : 0.0;
@@ -1183,6 +1183,8 @@ __global__ void __launch_bounds__(TC_THREADS) k_tri_cluster(int forward, int Np,
         // no CTA may leave while another can still read its shared memory
         cl_arrive();
         cl_wait();
+        for (int I = rank; I < nb; I += TC_CTAS)
+            if (tid < T) x[I * T + tid] = vec[I * T + tid];
     }
 }
 

@@ -982,7 +982,7 @@ void chol_task_list(int nb, std::vector<int2> &tasks)
     }
 }
 
-int chol_grid(int n_tasks)
+int chol_grid(int n_tasks, int grid_cap)
 {
     static int per_sm = -1, sms = 0;
     if (per_sm < 0) {
@@ -993,7 +993,9 @@ int chol_grid(int n_tasks)
         if (per_sm < 1) per_sm = 1;
         if (PSBA_CHOL_PER_SM > 0 && per_sm > PSBA_CHOL_PER_SM) per_sm = PSBA_CHOL_PER_SM;
     }
-    const int cap = per_sm * sms;
+    int cap = per_sm * sms;
+    if (grid_cap > 0 && grid_cap < cap) cap = grid_cap;
+    if (cap < 2) cap = 2;  // the panel and at least one helper
     return n_tasks < cap ? n_tasks : cap;
 }
 
@@ -1194,7 +1196,7 @@ void launch_chol_dataflow(const DeviceProblem &d, int mode, int epoch, double *x
     int Np = d.Np;
     if (mode == 0) {
         int n_tasks = d.chol_n_tasks;
-        const int grid = chol_grid(n_tasks + 1);
+        const int grid = chol_grid(n_tasks + 1, d.chol_grid_cap);
         const int2 *tasks = d.chol_tasks;
         double *S = d.S, *Linv = d.Linv, *rhs = d.rhs, *pre = d.chol_pre;
         int *flags = d.chol_flags, *status = d.status;

@@ -130,6 +130,7 @@ struct DeviceProblem {
     int *status = nullptr;        // Cholesky status word (0 ok, 1 not SPD, 2 wait budget exhausted)
     int2 *chol_tasks = nullptr;   // helper tasks of the dense factor, in dependency order
     int chol_n_tasks = 0;
+    int chol_grid_cap = 0;        // CTAs of the dense factor at most (0: one per SM)
     double *chol_pre = nullptr;   // second-subdiagonal tiles before their solve (Np / TILE tiles)
     int *chol_flags = nullptr;    // one flag per dataflow task (value = epoch when done)
     int chol_n_flags = 0;
@@ -189,6 +190,9 @@ void launch_scale(double *out, const double *x, const double *num, const double 
 // solve into xsol; mode 1 solves again with the existing factor.  One
 // cooperative launch; epoch must increase from launch to launch.
 void launch_chol_dataflow(const DeviceProblem &d, int mode, int epoch, double *x_out, cudaStream_t s);
+// at most cap CTAs for a handle's dense factor (0: one per SM); for callers
+// that run several handles side by side
+void set_chol_grid_cap(psba_handle *h, int cap);
 // the dense factor's helper tasks, in dependency order
 void chol_task_list(int nb, std::vector<int2> &tasks);
 

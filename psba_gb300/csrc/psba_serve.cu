@@ -146,6 +146,7 @@ struct psba_server {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int device = 0, grid_cap = 1;
+    int large_chol_cap = 0;  // dense-factor CTAs per large-lane solve: the SMs shared among the lanes
     // scheduling state (guarded by mu)
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
@@ -387,6 +388,8 @@ void large_main(psba_server *s)
         psba_result res{};
         int itno = 0;
         int rc = psba_create(&desc, &h);
+        // the lanes' dense factors run side by side: each takes its share of the SMs
+        if (rc == PSBA_OK) set_chol_grid_cap(h, s->large_chol_cap);
         if (rc == PSBA_OK) rc = psba_levmar(h, &s->lm, &itno, &res);
         r->cams.resize((size_t)r->cnp * r->nc);
         r->pts.resize(3 * (size_t)r->np);
@@ -517,6 +520,7 @@ int psba_server_create(const psba_server_opts *so, const psba_opts *lm, psba_ser
     }
     std::memset(s->h_probs, 0, sizeof(BatchProblem) * M);
     s->grid_cap = batch_blocks_per_sm(s->precision, so->threads) * sms;
+    if (with_large) s->large_chol_cap = std::max(2, sms / so->large_lanes);
     s->alloc.reset(s->pool_size);
     s->slots.assign(M, nullptr);
     s->worker = std::thread(worker_main, s);

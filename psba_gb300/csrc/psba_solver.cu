@@ -735,6 +735,13 @@ int trust_region_impl(psba_handle *h, const psba_opts *o, int *itno, psba_result
 
 }  // namespace
 
+namespace psba {
+void set_chol_grid_cap(psba_handle *h, int cap)
+{
+    if (h) h->d.chol_grid_cap = cap;
+}
+}  // namespace psba
+
 // ===========================================================================
 // C ABI
 

@@ -20,7 +20,7 @@ estimate.  The metric is LM iterations per second.
   one launch per LM trial), timed live with CUDA events inside the timed
   solves; FP64-bound, so its peak is the measured FP64 FMA rate.
   roofline_chol: the same for the dense solve (k_chol_dataflow +
-  k_tri_solve); roofline_schur: for the whole Schur-complement stage.
+  k_tri_cluster); roofline_schur: for the whole Schur-complement stage.
 * variable_intrinsics: 52 cameras x 64,053 points with 11- and
   16-parameter cameras, mixed and FP64 forms, LM iterations/s.
 * batched: 1,024 small problems in one persistent launch (mixed form,
@@ -529,7 +529,7 @@ def main():
                      "hbm": {"achieved": soff_bytes / soff_avg_s / 1e9, "peak": peak_gbs, "unit": "GB/s",
                              "frac": soff_bytes / soff_avg_s / 1e9 / peak_gbs, "algorithmic_bytes": soff_bytes,
                              "peak_source": peak_kind}},
-        "roofline_chol": {"kernel": "k_chol_dataflow + k_tri_solve: Cholesky of S + mu I and the triangular "
+        "roofline_chol": {"kernel": "k_chol_dataflow + k_tri_cluster: Cholesky of S + mu I and the triangular "
                                     "solves, one pair of launches per LM trial, N = %d" % Np,
                      "bound": "fp64", "achieved": chol_flops / chol_avg_s / 1e12, "peak": fp64_peak,
                      "unit": "TFLOP/s", "frac": chol_flops / chol_avg_s / 1e12 / fp64_peak,

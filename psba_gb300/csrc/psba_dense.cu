@@ -62,11 +62,14 @@ __device__ __forceinline__ void trace_mark(int t, int k)
     }
 }
 #define CHOL_MARK(t, k) trace_mark(t, k)
-// back-solve step K of the cluster solve, on the step's owner
-#define TRI_MARK(K, k)                                                          \
-    do {                                                                        \
-        if ((K) % 8 == (int)cg::this_cluster().block_rank() && (K) < 8192)     \
-            trace_mark(40000 + (K), k);                                         \
+// back-solve step K of the cluster solve, on the step's owner: clock64 into
+// shared memory (a global store before the barrier's release would delay it),
+// copied out after the solve
+#define TRI_TRACE_STEPS 128
+#define TRI_MARK(K, k)                                                                                       \
+    do {                                                                                                     \
+        if (threadIdx.x == 0 && (K) % 8 == (int)cg::this_cluster().block_rank() && (K) < TRI_TRACE_STEPS) \
+            tri_tr[(K)][(k)] = clock64();                                                                    \
     } while (0)
 #else
 #define CHOL_MARK(t, k)
@@ -1033,8 +1036,8 @@ __global__ void __launch_bounds__(TS_THREADS) k_tri_solve(int forward, int Np, i
 // previous step's block to its other blocks; after it, every CTA reads block
 // K from the owner and first updates the block the next step needs (if it
 // owns it), so the next owner can solve and arrive at once.  The diagonal
-// inverse entries and the coefficients of that first update are loaded a
-// step ahead.  Each vector entry takes its updates in step order: results
+// inverse entries and the coefficients of both updates are loaded a step
+// ahead, after the arrive.  Each vector entry takes its updates in step order: results
 // do not depend on timing.
 constexpr int TC_CTAS = 8, TC_THREADS = 256;
 
@@ -1042,9 +1045,12 @@ __device__ __forceinline__ void cl_arrive() { asm volatile("barrier.cluster.arri
 __device__ __forceinline__ void cl_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
 
 // v[c] -= sum_r P(r, c) xs[r] for the columns (back) or rows (forward) listed
-// by idx(q), q < n: four threads per entry, four terms each, fixed tree
+// by idx(q), q < n: four threads per entry, four terms each, fixed tree.  The
+// first pass (q < TC_THREADS / 4) takes its four coefficients from first[],
+// loaded by the caller a step ahead; later passes load them here.
 template <typename Coef, typename Idx>
-__device__ __forceinline__ void cl_update(double *v, const double *xs, int n, Coef coef, Idx idx)
+__device__ __forceinline__ void cl_update(double *v, const double *xs, int n, const double (&first)[4], Coef coef,
+                                          Idx idx)
 {
     const int g = threadIdx.x & 3;
     for (int q0 = 0; q0 < n; q0 += TC_THREADS / 4) {
@@ -1053,8 +1059,13 @@ __device__ __forceinline__ void cl_update(double *v, const double *xs, int n, Co
         int c = 0;
         if (q < n) {
             c = idx(q);
+            if (q0 == 0) {
 #pragma unroll
-            for (int j = 0; j < 4; ++j) s = fma(coef(4 * g + j, c), xs[4 * g + j], s);
+                for (int j = 0; j < 4; ++j) s = fma(first[j], xs[4 * g + j], s);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; ++j) s = fma(coef(4 * g + j, c), xs[4 * g + j], s);
+            }
         }
         s += __shfl_xor_sync(0xffffffffu, s, 1);
         s += __shfl_xor_sync(0xffffffffu, s, 2);
@@ -1071,47 +1082,60 @@ __global__ void __launch_bounds__(TC_THREADS) k_tri_cluster(int forward, int Np,
     static_assert(TC_THREADS == TT, "one thread per term of the 16 x 16 diagonal product");
     extern __shared__ double vec[];  // Np; this CTA's blocks are the valid ones
     __shared__ double xb[2][T], xs[2][T];
+#ifdef PSBA_CHOL_TRACE
+    __shared__ long long tri_tr[TRI_TRACE_STEPS][8];
+#endif
     cg::cluster_group cl = cg::this_cluster();
     const int rank = (int)cl.block_rank(), tid = threadIdx.x;
     if (*status != 0) return;  // the same word for every CTA: all leave together
     for (int I = rank; I < nb; I += TC_CTAS)
         if (tid < T) vec[I * T + tid] = rhs[I * T + tid];
     const int dr = tid / T, dk = tid % T;
+    const int cq = tid >> 2, cg4 = tid & 3;  // one entry of a block, four terms (threads 0..63)
     auto mine = [&](int I) { return I >= 0 && I < nb && I % TC_CTAS == rank; };
-    auto n_between = [&](int lo, int hi) {  // entries of my blocks I with lo < I < hi
-        int n = 0;
-        for (int I = rank; I < nb; I += TC_CTAS)
-            if (I > lo && I < hi) ++n;
-        return n * T;
+    // my first block above lo, and the entries of my blocks I with lo < I < hi
+    auto first_above = [&](int lo) { return lo < rank ? rank : rank + ((lo - rank) / TC_CTAS + 1) * TC_CTAS; };
+    auto n_between = [&](int lo, int hi) {
+        const int f = first_above(lo);
+        return f < hi ? ((hi - 1 - f) / TC_CTAS + 1) * T : 0;
     };
     auto entry_between = [&](int lo, int q) {  // q-th entry of my blocks above lo, ascending
-        const int first = lo < rank ? rank : rank + ((lo - rank) / TC_CTAS + 1) * TC_CTAS;
-        return (first + (q / T) * TC_CTAS) * T + q % T;
+        return (first_above(lo) + (q / T) * TC_CTAS) * T + q % T;
     };
-    __syncthreads();
-    // the critical update: four terms of one entry of the next step's block
-    // per thread (threads 0..63), its coefficients loaded one step ahead
-    const int cq = tid >> 2, cg4 = tid & 3;
-    auto crit_apply = [&](double *v, const double *xs_, const double (&cf)[4], int entry) {
+    // the next step's block update, from coefficients loaded a step ahead
+    auto crit_apply = [&](const double *xs_, const double (&cf)[4], int entry) {
         double s = 0.0;
 #pragma unroll
         for (int j = 0; j < 4; ++j) s = fma(cf[j], xs_[4 * cg4 + j], s);
         s += __shfl_xor_sync(0xffffffffu, s, 1);
         s += __shfl_xor_sync(0xffffffffu, s, 2);
-        if (cq < T && cg4 == 0) v[entry] -= s;
+        if (cq < T && cg4 == 0) vec[entry] -= s;
     };
+    __syncthreads();
+    // Every register loaded for the next step goes to the other half of a
+    // ping-pong pair (the loop is unrolled by two), so nothing waits for a
+    // load until the step that uses it; all loads are issued after the
+    // arrive (a load in flight at the arrive would hold up its release).
     if (forward) {
         // L y = b: step K solves y_K = Linv_K b_K, then b_I -= L_IK y_K for I > K
-        auto ldiag = [&](int K) { return mine(K) && dk <= dr ? __ldcg(Linv + (size_t)K * TT + dr * T + dk) : 0.0; };
+        auto ldiag = [&](int K) {
+            return mine(K) && dk <= dr ? __ldcg(Linv + (size_t)K * TT + dr * T + dk) : 0.0;
+        };
         auto lcrit = [&](int K, double (&cf)[4]) {  // rows of block K+1, columns of block K
 #pragma unroll
             for (int j = 0; j < 4; ++j)
-                cf[j] = (cq < T && mine(K + 1)) ? __ldcg(S + (size_t)((K + 1) * T + cq) * Np + K * T + 4 * cg4 + j) : 0.0;
+                cf[j] = (cq < T && mine(K + 1)) ? __ldcg(S + (size_t)((K + 1) * T + cq) * Np + K * T + 4 * cg4 + j)
+                                                : 0.0;
         };
-        double pl = ldiag(0), cf[4];
-        lcrit(0, cf);
+        auto ldef = [&](int P, double (&df)[4]) {  // rows of my blocks above P + 1, columns of block P
+            const int n = n_between(P + 1, nb);
+            const int i = cq < n ? entry_between(P + 1, cq) : 0;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) df[j] = cq < n ? __ldcg(S + (size_t)i * Np + P * T + 4 * cg4 + j) : 0.0;
+        };
         int pend = -1;
-        for (int K = 0; K < nb; ++K) {
+        auto step = [&](int K, double &pl, double &pln, double (&cf)[4], double (&cfn)[4], double (&df)[4],
+                        double (&dfn)[4]) {
             if (mine(K)) {
                 const double yv = half_warp_sum(pl * vec[K * T + dk]);
                 if (dk == 0) xb[K & 1][dr] = yv;
@@ -1119,22 +1143,27 @@ __global__ void __launch_bounds__(TC_THREADS) k_tri_cluster(int forward, int Np,
             __syncthreads();
             if (mine(K) && tid < T) vec[K * T + tid] = xb[K & 1][tid];
             cl_arrive();
-            const double pl_next = K + 1 < nb ? ldiag(K + 1) : 0.0;
+            pln = K + 1 < nb ? ldiag(K + 1) : 0.0;
+            lcrit(K + 1, cfn);
+            ldef(K, dfn);
             if (pend >= 0) {  // the previous step's block, applied to my blocks above pend + 1
                 const int P = pend;
-                const double *xp = xs[P & 1];
-                cl_update(vec, xp, n_between(P + 1, nb),
+                cl_update(vec, xs[P & 1], n_between(P + 1, nb), df,
                           [&](int r, int i) { return __ldcg(S + (size_t)i * Np + P * T + r); },
                           [&](int q) { return entry_between(P + 1, q); });
             }
             cl_wait();
             if (tid < T) xs[K & 1][tid] = cl.map_shared_rank(&xb[K & 1][0], K % TC_CTAS)[tid];
             __syncthreads();
-            if (mine(K + 1)) crit_apply(vec, xs[K & 1], cf, (K + 1) * T + cq);
+            if (mine(K + 1)) crit_apply(xs[K & 1], cf, (K + 1) * T + cq);
             __syncthreads();
-            if (K + 1 < nb) lcrit(K + 1, cf);
-            pl = pl_next;
             pend = K;
+        };
+        double plA = ldiag(0), plB = 0.0, cfA[4], cfB[4], dfA[4] = {0.0, 0.0, 0.0, 0.0}, dfB[4];
+        lcrit(0, cfA);
+        for (int K = 0; K < nb; K += 2) {
+            step(K, plA, plB, cfA, cfB, dfA, dfB);
+            if (K + 1 < nb) step(K + 1, plB, plA, cfB, cfA, dfB, dfA);
         }
         // the last step's block reaches no block above it
         cl_arrive();
@@ -1142,45 +1171,61 @@ __global__ void __launch_bounds__(TC_THREADS) k_tri_cluster(int forward, int Np,
     }
     {
         // L^T x = y: step K solves x_K = Linv_K^T y_K, then y_I -= L_KI^T x_K for I < K
-        auto ldiag = [&](int K) { return mine(K) && dk >= dr ? __ldcg(Linv + (size_t)K * TT + dk * T + dr) : 0.0; };
+        auto ldiag = [&](int K) {
+            return mine(K) && dk >= dr ? __ldcg(Linv + (size_t)K * TT + dk * T + dr) : 0.0;
+        };
         auto lcrit = [&](int K, double (&cf)[4]) {  // rows of block K, columns of block K-1
 #pragma unroll
             for (int j = 0; j < 4; ++j)
-                cf[j] = (cq < T && mine(K - 1)) ? __ldcg(S + (size_t)(K * T + 4 * cg4 + j) * Np + (K - 1) * T + cq) : 0.0;
+                cf[j] = (cq < T && mine(K - 1)) ? __ldcg(S + (size_t)(K * T + 4 * cg4 + j) * Np + (K - 1) * T + cq)
+                                                : 0.0;
         };
-        double pl = ldiag(nb - 1), cf[4];
-        lcrit(nb - 1, cf);
+        auto ldef = [&](int P, double (&df)[4]) {  // rows of block P, columns of my blocks below P - 1
+            const int n = n_between(-1, P - 1);
+            const int c = cq < n ? entry_between(-1, cq) : 0;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) df[j] = cq < n ? __ldcg(S + (size_t)(P * T + 4 * cg4 + j) * Np + c) : 0.0;
+        };
         int pend = -1;
-        for (int K = nb - 1; K >= 0; --K) {
+        auto step = [&](int K, double &pl, double &pln, double (&cf)[4], double (&cfn)[4], double (&df)[4],
+                        double (&dfn)[4]) {
             TRI_MARK(K, 0);
             if (mine(K)) {
                 const double xv = half_warp_sum(pl * vec[K * T + dk]);
                 if (dk == 0) xb[K & 1][dr] = xv;
             }
-            __syncthreads();
-            // x_K replaces y_K in the owner's vector (no global store before the
-            // release: the arrive would wait for it)
-            if (mine(K) && tid < T) vec[K * T + tid] = xb[K & 1][tid];
-            cl_arrive();
             TRI_MARK(K, 1);
-            const double pl_next = K > 0 ? ldiag(K - 1) : 0.0;
+            __syncthreads();
+            // x_K replaces y_K in the owner's vector (no global store before the release)
+            if (mine(K) && tid < T) vec[K * T + tid] = xb[K & 1][tid];
+            TRI_MARK(K, 2);
+            cl_arrive();
+            TRI_MARK(K, 3);
+            pln = K > 0 ? ldiag(K - 1) : 0.0;
+            lcrit(K - 1, cfn);
+            ldef(K, dfn);
             if (pend >= 0) {  // the previous step's block, applied to my blocks below pend - 1
                 const int P = pend;
-                const double *xp = xs[P & 1];
-                cl_update(vec, xp, n_between(-1, P - 1),
+                cl_update(vec, xs[P & 1], n_between(-1, P - 1), df,
                           [&](int r, int c) { return __ldcg(S + (size_t)(P * T + r) * Np + c); },
                           [&](int q) { return entry_between(-1, q); });
             }
-            TRI_MARK(K, 2);
+            TRI_MARK(K, 4);
             cl_wait();
-            TRI_MARK(K, 3);
+            TRI_MARK(K, 5);
             if (tid < T) xs[K & 1][tid] = cl.map_shared_rank(&xb[K & 1][0], K % TC_CTAS)[tid];
             __syncthreads();
-            if (mine(K - 1)) crit_apply(vec, xs[K & 1], cf, (K - 1) * T + cq);
+            TRI_MARK(K, 6);
+            if (mine(K - 1)) crit_apply(xs[K & 1], cf, (K - 1) * T + cq);
             __syncthreads();
-            if (K > 0) lcrit(K - 1, cf);
-            pl = pl_next;
+            TRI_MARK(K, 7);
             pend = K;
+        };
+        double plA = ldiag(nb - 1), plB = 0.0, cfA[4], cfB[4], dfA[4] = {0.0, 0.0, 0.0, 0.0}, dfB[4];
+        lcrit(nb - 1, cfA);
+        for (int K = nb - 1; K >= 0; K -= 2) {
+            step(K, plA, plB, cfA, cfB, dfA, dfB);
+            if (K - 1 >= 0) step(K - 1, plB, plA, cfB, cfA, dfB, dfA);
         }
         // no CTA may leave while another can still read its shared memory
         cl_arrive();
@@ -1188,6 +1233,10 @@ __global__ void __launch_bounds__(TC_THREADS) k_tri_cluster(int forward, int Np,
         for (int I = rank; I < nb; I += TC_CTAS)
             if (tid < T) x[I * T + tid] = vec[I * T + tid];
     }
+#ifdef PSBA_CHOL_TRACE
+    for (int K = rank; K < nb && K < TRI_TRACE_STEPS; K += TC_CTAS)
+        if (tid < 8) g_chol_trace[4 * 40000 + 8 * K + tid] = tri_tr[K][tid];
+#endif
 }
 
 void launch_chol_dataflow(const DeviceProblem &d, int mode, int epoch, double *x_out, cudaStream_t s)

@@ -247,6 +247,14 @@ void launch_linearize(const DeviceProblem &d, double coeff, cudaStream_t s)
 
 // ---------------------------------------------------------------------------
 // Residual and its squared norm at (camera table, pts [+ dpb]); block partials.
+// The 17 table values the projection uses (rotation, translation, K) are
+// staged per block in shared memory when the cameras fit (stage_nc > 0):
+// neighbouring observations belong to different cameras, so reading them
+// from the table makes every load of a warp touch up to 32 cache lines.
+constexpr int RES_TAB = 17;  // M (9), t (3), fx sk cx fy cy (5)
+
+__device__ __forceinline__ int res_tab_src(int k) { return k < 9 ? k : 36 + (k - 9); }
+
 __global__ void __launch_bounds__(256) k_residual(int no, const int *__restrict__ obs_pt,
                                                   const int *__restrict__ obs_cam,
                                                   const double *__restrict__ meas,
@@ -255,9 +263,13 @@ __global__ void __launch_bounds__(256) k_residual(int no, const int *__restrict_
                                                   const double *__restrict__ tab,
                                                   const double *__restrict__ wt,
                                                   double *__restrict__ ex_out,
-                                                  double *__restrict__ partial)
+                                                  double *__restrict__ partial, int stage_nc)
 {
     __shared__ double red[256];
+    extern __shared__ double s_tab[];  // stage_nc * RES_TAB
+    for (int e = threadIdx.x; e < stage_nc * RES_TAB; e += blockDim.x)
+        s_tab[e] = __ldg(tab + (size_t)CAMTAB * (e / RES_TAB) + res_tab_src(e % RES_TAB));
+    if (stage_nc > 0) __syncthreads();
     const int o = blockIdx.x * blockDim.x + threadIdx.x;
     double sq = 0.0;
     if (o < no) {
@@ -266,13 +278,21 @@ __global__ void __launch_bounds__(256) k_residual(int no, const int *__restrict_
 #pragma unroll
         for (int m = 0; m < 3; ++m)
             X[m] = dpb ? __ldg(pts + 3 * i + m) + __ldg(dpb + 3 * i + m) : __ldg(pts + 3 * i + m);
-        const double *T = tab + (size_t)CAMTAB * j;
-        const double xc = __ldg(T + 0) * X[0] + __ldg(T + 1) * X[1] + __ldg(T + 2) * X[2] + __ldg(T + 36);
-        const double yc = __ldg(T + 3) * X[0] + __ldg(T + 4) * X[1] + __ldg(T + 5) * X[2] + __ldg(T + 37);
-        const double zc = __ldg(T + 6) * X[0] + __ldg(T + 7) * X[1] + __ldg(T + 8) * X[2] + __ldg(T + 38);
+        double Tv[RES_TAB];
+        if (stage_nc > 0) {
+#pragma unroll
+            for (int k = 0; k < RES_TAB; ++k) Tv[k] = s_tab[j * RES_TAB + k];
+        } else {
+            const double *T = tab + (size_t)CAMTAB * j;
+#pragma unroll
+            for (int k = 0; k < RES_TAB; ++k) Tv[k] = __ldg(T + res_tab_src(k));
+        }
+        const double xc = Tv[0] * X[0] + Tv[1] * X[1] + Tv[2] * X[2] + Tv[9];
+        const double yc = Tv[3] * X[0] + Tv[4] * X[1] + Tv[5] * X[2] + Tv[10];
+        const double zc = Tv[6] * X[0] + Tv[7] * X[1] + Tv[8] * X[2] + Tv[11];
         const double iz = 1.0 / zc;
-        const double u = (__ldg(T + 39) * xc + __ldg(T + 40) * yc + __ldg(T + 41) * zc) * iz;
-        const double v = (__ldg(T + 42) * yc + __ldg(T + 43) * zc) * iz;
+        const double u = (Tv[12] * xc + Tv[13] * yc + Tv[14] * zc) * iz;
+        const double v = (Tv[15] * yc + Tv[16] * zc) * iz;
         const double2 m2 = *reinterpret_cast<const double2 *>(meas + 2 * (size_t)o);
         double e0 = m2.x - u, e1 = m2.y - v;
         if (wt) {
@@ -292,14 +312,22 @@ __global__ void __launch_bounds__(256) k_residual(int no, const int *__restrict_
     if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
 }
 
+// cameras whose residual-table values a block stages (0: read the table)
+int residual_stage_nc(const DeviceProblem &d)
+{
+    return (size_t)d.nc * RES_TAB * sizeof(double) <= 48 * 1024 ? d.nc : 0;
+}
+
 int residual_blocks(const DeviceProblem &d) { return ceil_div(d.no > 0 ? d.no : 1, 256); }
 
 void launch_residual(const DeviceProblem &d, const double *tab, const double *pts, const double *dpb,
                      double *ex_out, double *partial, int nblocks, cudaStream_t s)
 {
     if (d.cnp == 16) return launch_residual_dist(d, tab, pts, dpb, ex_out, partial, nblocks, s);
-    k_residual<<<nblocks, 256, 0, s>>>(d.no, d.obs_pt, d.obs_cam, d.meas, pts, dpb, tab, d.wt, ex_out,
-                                        partial); note_launch(1);
+    const int snc = residual_stage_nc(d);
+    k_residual<<<nblocks, 256, sizeof(double) * RES_TAB * snc, s>>>(d.no, d.obs_pt, d.obs_cam, d.meas, pts, dpb,
+                                                                    tab, d.wt, ex_out, partial, snc);
+    note_launch(1);
 }
 
 // ---------------------------------------------------------------------------
@@ -863,12 +891,18 @@ __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int *__re
                                                 const R *__restrict__ W, const double *__restrict__ Vinv,
                                                 const double *__restrict__ g, double mu,
                                                 double *__restrict__ dp, double *__restrict__ eb,
-                                                double *__restrict__ partial)
+                                                double *__restrict__ partial, int stage)
 {
     __shared__ double r0[256], r1[256];
+    extern __shared__ double s_dpa[];  // the camera part of dp (ncp doubles) when staged
     // four lanes per point (points in pt_order): lane c < 3 sums component c
     // of W^T dpa over the point's observations in order, lane 3 only takes
     // part in the exchange; lane 0 finishes the point
+    if (stage) {
+        for (int e = threadIdx.x; e < ncp; e += blockDim.x) s_dpa[e] = dp[e];
+        __syncthreads();
+    }
+    const double *dpa = stage ? s_dpa : dp;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     const int slot = t >> 2, c = t & 3;
     int i = -1;
@@ -880,7 +914,7 @@ __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int *__re
 #pragma unroll 2
             for (int o = pt_start[i]; o < end; ++o) {
                 const R *w = W + 18 * (size_t)o;
-                const double *da = dp + 6 * (size_t)__ldg(obs_cam + o);
+                const double *da = dpa + 6 * (size_t)__ldg(obs_cam + o);
 #pragma unroll
                 for (int k = 0; k < 6; ++k) e = e + (double)w[3 * k + c] * da[k];
             }
@@ -931,12 +965,17 @@ int eb_blocks(const DeviceProblem &d) { return ceil_div(4LL * (d.np > 0 ? d.np :
 void launch_eb_dpb(const DeviceProblem &d, double mu, cudaStream_t s)
 {
     if (d.cnp != 6) return launch_eb_dpb_v(d, mu, eb_blocks(d), s);
+    // the camera part of dp in shared memory when it fits: each observation
+    // reads its camera's six values
+    const int stage = (size_t)d.N * sizeof(double) <= 48 * 1024 ? 1 : 0;
+    const size_t smem = stage ? sizeof(double) * d.N : 0;
     if (d.prec == PSBA_PREC_FP64)
-        k_eb_dpb<double><<<eb_blocks(d), 256, 0, s>>>(d.np, d.N, d.pt_start, d.pt_order, d.obs_cam, d.W, d.Vinv, d.g, mu,
-                                                        d.dp, d.eb, d.red_partial);
+        k_eb_dpb<double><<<eb_blocks(d), 256, smem, s>>>(d.np, d.N, d.pt_start, d.pt_order, d.obs_cam, d.W, d.Vinv,
+                                                           d.g, mu, d.dp, d.eb, d.red_partial, stage);
     else
-        k_eb_dpb<float><<<eb_blocks(d), 256, 0, s>>>(d.np, d.N, d.pt_start, d.pt_order, d.obs_cam, (const float *)d.W,
-                                                       d.Vinv, d.g, mu, d.dp, d.eb, d.red_partial);
+        k_eb_dpb<float><<<eb_blocks(d), 256, smem, s>>>(d.np, d.N, d.pt_start, d.pt_order, d.obs_cam,
+                                                          (const float *)d.W, d.Vinv, d.g, mu, d.dp, d.eb,
+                                                          d.red_partial, stage);
     note_launch(1);
 }
 

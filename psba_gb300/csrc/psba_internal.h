@@ -18,7 +18,8 @@ constexpr int PNP = 3;   // point parameters
 constexpr int MNP = 2;   // image coordinates
 constexpr int CAMTAB = 56;  // doubles per camera table entry (CamTab)
 constexpr int TILE = 16;    // dense Cholesky tile size
-constexpr int SCHUR_CHUNK = 32;  // pair-list entries per off-diagonal Schur work unit
+constexpr int SCHUR_CHUNK = 32;  // pair-list entries per off-diagonal Schur work unit (11/16-parameter cameras)
+constexpr int OFF_MIN_LEN = 8;   // 6-parameter cameras: fewest pair-list entries per off-diagonal chunk
 constexpr int DIAG_CHUNK = 16;   // observations per diagonal Schur work unit (11/16-parameter cameras)
 constexpr int SD_THREADS = 128, SD_PER = 8;     // 6-parameter cameras: one CTA per unit, 8 observations a thread
 constexpr int DIAG_SUPER = SD_THREADS * SD_PER;  // observations per diagonal unit, 6-parameter cameras
@@ -92,9 +93,21 @@ struct DeviceProblem {
     int *pair_a = nullptr;     // entries: observation of camera k
     int *pair_b = nullptr;     // entries: observation of camera l
     long long n_pair_entries = 0;
+    // off-diagonal Schur work, two layouts whose partial slots are numbered in
+    // pair-list order (each pair's slots form one range):
+    // units of <= SCHUR_CHUNK entries of one pair, one slot each, longest
+    // first (FP32 products, and 11/16-parameter cameras);
     SchurUnit *off_units = nullptr;
     int n_off_units = 0;
     int *off_unit_start = nullptr;  // per pair: first unit (n_pairs + 1)
+    // 6-parameter cameras, FP64 products: the pair list cut into equal chunks
+    // (SchurUnit: first pair, first entry, entries, first slot), one per thread
+    // of one resident wave, a slot per pair a chunk touches
+    SchurUnit *off_chunks = nullptr;
+    int n_off_chunks = 0;
+    int n_off_chunk_slots = 0;
+    int *off_chunk_start = nullptr;  // per pair: first slot (n_pairs + 1)
+    int *pair_start = nullptr;       // per pair: first entry (n_pairs + 1)
     SchurUnit *diag_units = nullptr;  // per camera chunks of cam_obs
     int n_diag_units = 0;
     int *diag_unit_start = nullptr;   // per camera (nc + 1)
@@ -119,7 +132,7 @@ struct DeviceProblem {
     // per-trial
     double *Vinv = nullptr;       // 6 per point
     double *Y = nullptr;          // 18 per obs
-    double *schur_partial = nullptr;  // (n_off_units * 36 + n_diag_units * 27)
+    double *schur_partial = nullptr;  // off-diagonal slots (off_partial_slots), then the diagonal units'
     double *S = nullptr;          // Np x Np (lower)
     double *Ssave = nullptr;      // copy of S (TR fallback, refinement)
     double *rhs = nullptr;        // Np (ea on entry, y after the forward solve)
@@ -164,6 +177,13 @@ void launch_vinv(const DeviceProblem &d, double mu, cudaStream_t s);
 void launch_yblocks(const DeviceProblem &d, cudaStream_t s);
 void launch_schur(const DeviceProblem &d, double mu, cudaStream_t s);
 void launch_schur_off(const DeviceProblem &d, cudaStream_t s);
+// threads of one resident wave of the 6-parameter off-diagonal Schur kernel on this device
+int schur_off_wave_threads();
+// off-diagonal partial slots reserved ahead of the diagonal partials (the larger layout)
+inline size_t off_partial_slots(const DeviceProblem &d)
+{
+    return (size_t)(d.n_off_units > d.n_off_chunk_slots ? d.n_off_units : d.n_off_chunk_slots);
+}
 void launch_schur_diag(const DeviceProblem &d, cudaStream_t s);
 void launch_schur_reduce(const DeviceProblem &d, double mu, cudaStream_t s);
 // Back-substitution: eb, dpb and partial sums for |dp|^2 and dp.(mu dp + g).

@@ -610,12 +610,15 @@ void launch_yblocks(const DeviceProblem &d, cudaStream_t s)
 // ---------------------------------------------------------------------------
 // Schur complement S = U + mu I - sum_i Y_ik W_il^T (compute_S.cl:39-77) and
 // ea = ga - sum_i Y_ij gb_i (compute_ea.cl:21-36).
-// Off-diagonal blocks (k > l): one thread per unit of <= SCHUR_CHUNK common
-// points of a camera pair, all 36 entries of the 6x6 product.
-// Diagonal blocks: one thread per unit of a camera's observations, the 21
-// lower entries plus the 6 ea sums.  Units are then summed in order.
+// Off-diagonal blocks (k > l), all 36 entries of each 6x6 product, into
+// partial slots.  Diagonal blocks: one CTA per unit of a camera's
+// observations, the 21 lower entries plus the 6 ea sums.  The slots are then
+// summed in order (k_schur_reduce).
+//
+// FP32 products: one thread per unit of <= SCHUR_CHUNK entries of one pair,
+// units longest first; FP32 sums of FLUSH products, then FP64.
 template <typename R>
-__global__ void __launch_bounds__(128) k_schur_off(int n_units, const SchurUnit *__restrict__ units,
+__global__ void __launch_bounds__(128) k_schur_off_units(int n_units, const SchurUnit *__restrict__ units,
                                                    const int *__restrict__ pa,
                                                    const int *__restrict__ pb,
                                                    const R *__restrict__ Y,
@@ -628,8 +631,13 @@ __global__ void __launch_bounds__(128) k_schur_off(int n_units, const SchurUnit 
     double acc[36];
 #pragma unroll
     for (int e = 0; e < 36; ++e) acc[e] = 0.0;
-    if constexpr (is_fp64<R>()) {
-        for (int t = 0; t < u.count; ++t) {
+    static_assert(!is_fp64<R>(), "FP64 products take the chunked kernel");
+    for (int t0 = 0; t0 < u.count; t0 += FLUSH) {
+        R part[36];
+#pragma unroll
+        for (int e = 0; e < 36; ++e) part[e] = (R)0;
+        const int tend = min(u.count, t0 + FLUSH);
+        for (int t = t0; t < tend; ++t) {
             const int a = __ldg(pa + u.begin + t), b = __ldg(pb + u.begin + t);
             R w[18], y[18];
             ldn<R, 18>(W + 18 * (size_t)b, w);
@@ -638,42 +646,93 @@ __global__ void __launch_bounds__(128) k_schur_off(int n_units, const SchurUnit 
             for (int r = 0; r < 6; ++r)
 #pragma unroll
                 for (int c = 0; c < 6; ++c) {
-                    double s = acc[r * 6 + c];
-                    s = fma((double)y[3 * r], (double)w[3 * c], s);
-                    s = fma((double)y[3 * r + 1], (double)w[3 * c + 1], s);
-                    s = fma((double)y[3 * r + 2], (double)w[3 * c + 2], s);
-                    acc[r * 6 + c] = s;
+                    R s = part[r * 6 + c];
+                    s = fma(y[3 * r], w[3 * c], s);
+                    s = fma(y[3 * r + 1], w[3 * c + 1], s);
+                    s = fma(y[3 * r + 2], w[3 * c + 2], s);
+                    part[r * 6 + c] = s;
                 }
         }
-    } else {
-        for (int t0 = 0; t0 < u.count; t0 += FLUSH) {
-            R part[36];
 #pragma unroll
-            for (int e = 0; e < 36; ++e) part[e] = (R)0;
-            const int tend = min(u.count, t0 + FLUSH);
-            for (int t = t0; t < tend; ++t) {
-                const int a = __ldg(pa + u.begin + t), b = __ldg(pb + u.begin + t);
-                R w[18], y[18];
-                ldn<R, 18>(W + 18 * (size_t)b, w);
-                ldn<R, 18>(Y + 18 * (size_t)a, y);
-#pragma unroll
-                for (int r = 0; r < 6; ++r)
-#pragma unroll
-                    for (int c = 0; c < 6; ++c) {
-                        R s = part[r * 6 + c];
-                        s = fma(y[3 * r], w[3 * c], s);
-                        s = fma(y[3 * r + 1], w[3 * c + 1], s);
-                        s = fma(y[3 * r + 2], w[3 * c + 2], s);
-                        part[r * 6 + c] = s;
-                    }
-            }
-#pragma unroll
-            for (int e = 0; e < 36; ++e) acc[e] += (double)part[e];
-        }
+        for (int e = 0; e < 36; ++e) acc[e] += (double)part[e];
     }
     double *p = partial + (size_t)u.out * 36;
 #pragma unroll
     for (int e = 0; e < 36; ++e) p[e] = acc[e];
+}
+
+// FP64 products (6-parameter cameras): the pair list cut into equal chunks,
+// one per thread of one resident wave, so that every SM issues the same
+// number of FP64 multiply-adds; a thread writes its sums to the next slot
+// whenever its chunk passes into the next pair.
+template <typename R>
+__device__ __forceinline__ void off_products(const R *y, const R *w, R *acc)
+{
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            R s = acc[r * 6 + c];
+            s = fma(y[3 * r], w[3 * c], s);
+            s = fma(y[3 * r + 1], w[3 * c + 1], s);
+            s = fma(y[3 * r + 2], w[3 * c + 2], s);
+            acc[r * 6 + c] = s;
+        }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128) k_schur_off(int n_chunks, const SchurUnit *__restrict__ chunks,
+                                                   const int *__restrict__ pair_start,
+                                                   const int *__restrict__ pa,
+                                                   const int *__restrict__ pb,
+                                                   const R *__restrict__ Y,
+                                                   const R *__restrict__ W,
+                                                   double *__restrict__ partial)
+{
+    const int uid = blockIdx.x * blockDim.x + threadIdx.x;
+    if (uid >= n_chunks) return;
+    const SchurUnit u = chunks[uid];
+    int q = u.slot, slot = u.out;
+    int next = __ldg(pair_start + q + 1);  // first entry of the next pair
+    const int end = u.begin + u.count;
+    double acc[36];
+#pragma unroll
+    for (int e = 0; e < 36; ++e) acc[e] = 0.0;
+    static_assert(is_fp64<R>(), "FP64 products; FP32 products take the unit kernel");
+    for (int t = u.begin; t < end; ++t) {
+        if (t == next) {
+            double *p = partial + (size_t)slot * 36;
+#pragma unroll
+            for (int e = 0; e < 36; ++e) {
+                p[e] = acc[e];
+                acc[e] = 0.0;
+            }
+            ++slot;
+            ++q;
+            next = __ldg(pair_start + q + 1);
+        }
+        const int a = __ldg(pa + t), b = __ldg(pb + t);
+        R w[18], y[18];
+        ldn<R, 18>(W + 18 * (size_t)b, w);
+        ldn<R, 18>(Y + 18 * (size_t)a, y);
+        off_products<R>(y, w, acc);
+    }
+    double *p = partial + (size_t)slot * 36;
+#pragma unroll
+    for (int e = 0; e < 36; ++e) p[e] = acc[e];
+}
+
+int schur_off_wave_threads()
+{
+    static int threads = 0;
+    if (threads == 0) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_schur_off<double>, 128, 0);
+        threads = std::max(1, sms) * std::max(1, per_sm) * 128;
+    }
+    return threads;
 }
 
 constexpr int DIAG_NV = 27;  // 21 lower entries + 6 ea sums
@@ -828,10 +887,10 @@ void launch_schur_off(const DeviceProblem &d, cudaStream_t s)
     if (d.cnp != 6) return launch_schur_off_v(d, s);
     if (d.n_off_units == 0) return;
     if (d.prec == PSBA_PREC_FP64)
-        k_schur_off<double><<<ceil_div(d.n_off_units, 128), 128, 0, s>>>(d.n_off_units, d.off_units, d.pair_a,
-                                                                           d.pair_b, d.Y, d.W, d.schur_partial);
+        k_schur_off<double><<<ceil_div(d.n_off_chunks, 128), 128, 0, s>>>(
+            d.n_off_chunks, d.off_chunks, d.pair_start, d.pair_a, d.pair_b, d.Y, d.W, d.schur_partial);
     else
-        k_schur_off<float><<<ceil_div(d.n_off_units, 128), 128, 0, s>>>(
+        k_schur_off_units<float><<<ceil_div(d.n_off_units, 128), 128, 0, s>>>(
             d.n_off_units, d.off_units, d.pair_a, d.pair_b, (const float *)d.Y, (const float *)d.W,
             d.schur_partial);
     note_launch(1);
@@ -840,7 +899,7 @@ void launch_schur_off(const DeviceProblem &d, cudaStream_t s)
 void launch_schur_diag(const DeviceProblem &d, cudaStream_t s)
 {
     if (d.cnp != 6) return launch_schur_diag_v(d, s);
-    double *diag_partial = d.schur_partial + (size_t)d.n_off_units * 36;
+    double *diag_partial = d.schur_partial + off_partial_slots(d) * 36;
     if (d.n_diag_units == 0) return;
     if (d.prec == PSBA_PREC_FP64)
         k_schur_diag<double><<<d.n_diag_units, SD_THREADS, 0, s>>>(d.diag_units, d.cam_obs, d.obs_pt, d.Y, d.W,
@@ -864,10 +923,11 @@ void launch_schur_reduce(const DeviceProblem &d, double mu, cudaStream_t s)
         return;
     }
     double *off_partial = d.schur_partial;
-    double *diag_partial = d.schur_partial + (size_t)d.n_off_units * 36;
+    double *diag_partial = d.schur_partial + off_partial_slots(d) * 36;
     const int total = d.n_pairs * 36 + d.nc * DIAG_NV;
+    const int *off_start = d.prec == PSBA_PREC_FP64 ? d.off_chunk_start : d.off_unit_start;
     k_schur_reduce<<<ceil_div(total, 128), 128, 0, s>>>(d.n_pairs, d.nc, d.Np, d.pair_kl,
-                                                          d.off_unit_start, off_partial,
+                                                          off_start, off_partial,
                                                           d.diag_unit_start, diag_partial, d.U, d.g,
                                                           mu, d.S, d.rhs); note_launch(1);
     if (d.Np > d.N) k_pad_identity<<<1, TILE, 0, s>>>(d.N, d.Np, d.S, d.rhs); note_launch(1);

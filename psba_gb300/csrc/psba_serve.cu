@@ -341,10 +341,14 @@ size_t large_bytes(const psba_problem_desc &p, int cnp)
         entries += (b - a) * (b - a - 1) / 2;
     }
     const size_t N = c * nc, Np = (N + TILE - 1) / TILE * TILE;
+    // off-diagonal partial slots: 6-parameter cameras, one per chunk plus one
+    // per pair boundary inside a chunk; otherwise one per unit
+    const size_t off_units = c == 6 ? std::min(entries / OFF_MIN_LEN + 1, (size_t)schur_off_wave_threads())
+                                    : entries / SCHUR_CHUNK;
     const size_t per_obs = 2 + 2 * c + 6 + 2 * 3 * c + 3 * 2 + 3 + 4;
     const size_t per_pt = 3 * 3 + 6 * 2 + 9 + 3 * 6;
     const size_t doubles = no * per_obs + np * per_pt + N * 8 + nc * (c * c + 2 * CAMTAB) + 3 * Np * Np +
-                           Np * TILE + (entries / SCHUR_CHUNK + nc * 8) * c * c +
+                           Np * TILE + (off_units + nc * 8) * c * c +
                            (no / (c == 6 ? DIAG_SUPER : DIAG_CHUNK) + nc) * (c * (c + 1) / 2 + c);  // diagonal-unit partials
     // index-build scratch: counts and offsets per (pair-list segment, camera)
     const size_t segs = no / (size_t)pair_segment_len(p.n_cams, p.n_obs) + nc;

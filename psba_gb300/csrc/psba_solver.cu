@@ -904,14 +904,36 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
                      d.pt_start, d_off, d.pair_a, d.pair_b, h->stream);
     TRY(check_launch());
     // Schur work units; execution order longest first
-    std::vector<SchurUnit> off_units, diag_units;
-    std::vector<int> off_start(n_pairs + 1, 0), diag_start(nc + 1, 0);
+    std::vector<SchurUnit> off_units, off_chunks, diag_units;
+    std::vector<int> off_start(n_pairs + 1, 0), chunk_start(n_pairs + 1, 0), diag_start(nc + 1, 0);
     for (int q = 0; q < n_pairs; ++q) {
         for (long long b = pair_start[q]; b < pair_start[q + 1]; b += SCHUR_CHUNK) {
             const int cnt = (int)std::min<long long>(SCHUR_CHUNK, pair_start[q + 1] - b);
             off_units.push_back({q, (int)b, cnt, (int)off_units.size()});
         }
         off_start[q + 1] = (int)off_units.size();
+    }
+    int n_chunk_slots = 0;
+    if (d.cnp == 6) {
+        // the pair list in equal chunks, one per thread of one resident wave,
+        // so every SM gets the same number of products; a chunk writes one
+        // slot per pair it touches, slots numbered in list order
+        const long long G = std::max(1, schur_off_wave_threads());
+        const long long len = std::max<long long>(OFF_MIN_LEN, (n_entries + G - 1) / G);
+        int q = 0;
+        for (long long b = 0; b < n_entries; b += len) {
+            const long long e = std::min(n_entries, b + len);
+            while (pair_start[q + 1] <= b) ++q;
+            off_chunks.push_back({q, (int)b, (int)(e - b), n_chunk_slots});
+            for (long long sb = b, qq = q;; ++qq) {
+                if (sb == pair_start[qq]) chunk_start[qq] = n_chunk_slots;
+                ++n_chunk_slots;
+                const long long se = std::min(e, pair_start[qq + 1]);
+                if (se == e) break;
+                sb = se;
+            }
+        }
+        chunk_start[n_pairs] = n_chunk_slots;
     }
     const int dchunk = d.cnp == 6 ? DIAG_SUPER : DIAG_CHUNK;
     for (int j = 0; j < nc; ++j) {
@@ -934,6 +956,8 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     d.n_pairs = n_pairs;
     d.n_pair_entries = n_entries;
     d.n_off_units = (int)off_units.size();
+    d.n_off_chunks = (int)off_chunks.size();
+    d.n_off_chunk_slots = n_chunk_slots;
     d.n_diag_units = (int)diag_units.size();
     d.n_cam_units = (int)cam_units.size();
 
@@ -944,6 +968,11 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     TRY(dalloc(h, &d.meas, 2 * (size_t)no));
     TRY(dalloc(h, &d.off_units, off_units.size()));
     TRY(dalloc(h, &d.off_unit_start, (size_t)n_pairs + 1));
+    if (d.cnp == 6) {
+        TRY(dalloc(h, &d.pair_start, (size_t)n_pairs + 1));
+        TRY(dalloc(h, &d.off_chunk_start, (size_t)n_pairs + 1));
+        TRY(dalloc(h, &d.off_chunks, off_chunks.size()));
+    }
     TRY(dalloc(h, &d.diag_units, diag_units.size()));
     TRY(dalloc(h, &d.diag_unit_start, (size_t)nc + 1));
     TRY(dalloc(h, &d.cam_units, cam_units.size()));
@@ -968,7 +997,7 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     TRY(dalloc(h, &d.cam_partial, cam_nv * cam_units.size()));
     TRY(dalloc(h, &d.Vinv, 6 * (size_t)np));
     TRY(dalloc(h, &d.Y, 3 * cnp * (size_t)no));
-    TRY(dalloc(h, &d.schur_partial, cnp * cnp * off_units.size() + diag_nv * diag_units.size()));
+    TRY(dalloc(h, &d.schur_partial, cnp * cnp * off_partial_slots(d) + diag_nv * diag_units.size()));
     TRY(dalloc(h, &d.S, (size_t)d.Np * d.Np));
     TRY(dalloc(h, &d.Ssave, (size_t)d.Np * d.Np));
     TRY(dalloc(h, &d.rhs, (size_t)d.Np));
@@ -1028,6 +1057,12 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     }
     TRY(upload(h, d.off_units, off_units.data(), off_units.size()));
     TRY(upload(h, d.off_unit_start, off_start.data(), off_start.size()));
+    if (d.cnp == 6) {
+        const std::vector<int> ps(pair_start.begin(), pair_start.end());
+        TRY(upload(h, d.pair_start, ps.data(), ps.size()));
+        TRY(upload(h, d.off_chunk_start, chunk_start.data(), chunk_start.size()));
+        TRY(upload(h, d.off_chunks, off_chunks.data(), off_chunks.size()));
+    }
     TRY(upload(h, d.diag_units, diag_units.data(), diag_units.size()));
     TRY(upload(h, d.diag_unit_start, diag_start.data(), diag_start.size()));
     TRY(upload(h, d.cam_units, cam_units.data(), cam_units.size()));

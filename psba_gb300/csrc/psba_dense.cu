@@ -19,6 +19,7 @@
 // or non-finite pivot (SPD_inv.cl:66-107) sets status 1; every task still
 // raises its flag, so nothing waits forever.  A spin that runs out of its
 // iteration budget sets status 2 and the kernel completes.
+#include <cfloat>
 #include <cooperative_groups.h>
 #include <vector>
 
@@ -170,7 +171,7 @@ struct PfPlan {
 };
 
 // last phase in which an entry does work (update, publication or L value)
-constexpr int pf_last_busy(const PfEntry &e)
+__host__ __device__ constexpr int pf_last_busy(const PfEntry &e)
 {
     return e.kind == PF_OFF ? e.j + 1 : e.kind == PF_DIAG ? e.j + 1 : e.kind == PF_D11 ? 2 : e.kind == PF_B ? e.r + 1 : 1;
 }
@@ -251,11 +252,12 @@ constexpr int PW_A = 0;                  // the tile (published entries, pivots)
 constexpr int PW_L = T * PW_ROW;         // the factor L
 constexpr int PW_LINV = 2 * T * PW_ROW;  // its inverse
 constexpr int PW_BW = 3 * T * PW_ROW;    // b being reduced
-constexpr int PW_INVD = PW_BW + T;       // 1 / L_kk
+constexpr int PW_INVD = PW_BW + T;       // 1 / L_kk = d_k^-1/2 (final pass)
 constexpr int PW_Y = PW_BW + 2 * T;      // y = L^-1 b
 constexpr int PW_B = PW_BW + 3 * T;      // b (input)
-constexpr int PW_INV2 = PW_BW + 4 * T;   // 1 / d_k (warp 0 publishes it with 1 / L_kk)
-constexpr int PW_SIZE = PW_BW + 5 * T;
+constexpr int PW_INV2 = PW_BW + 4 * T;   // 1 / d_k (warp 0 publishes it)
+constexpr int PW_ASQ = PW_BW + 5 * T;    // a_k,k-1^2 (published with a_k,k-1)
+constexpr int PW_SIZE = PW_BW + 6 * T;
 
 // One entry of a trailing thread, decoded once per factor into offsets: the
 // entry's row (xo), the other operand of its update (oo: row j of the tile,
@@ -266,6 +268,7 @@ constexpr int PW_SIZE = PW_BW + 5 * T;
 struct PfSlot {
     int xo, oo, lo, qo, po, dofs, last, due;
     bool lself;
+    int sqo;  // entry (j + 1, j): where its square goes when final, else -1
 };
 
 __device__ __forceinline__ PfSlot pf_slot(const PfEntry &e)
@@ -273,20 +276,21 @@ __device__ __forceinline__ PfSlot pf_slot(const PfEntry &e)
     const int r = e.r, j = e.j;
     switch (e.kind) {
     case PF_OFF:
-        return PfSlot{r * PW_ROW, j * PW_ROW, 0, PW_INVD + j, r * PW_ROW + j, PW_L + r * PW_ROW + j, j, j + 1, true};
-    case PF_DIAG:  // its L value is d_j / sqrt(d_j), d_j left in a[j][j] by warp 0
-        return PfSlot{j * PW_ROW, j * PW_ROW, j * PW_ROW + j, PW_INVD + j, j * PW_ROW + j, PW_L + j * PW_ROW + j, j - 1,
-                      j + 1, false};
+        return PfSlot{r * PW_ROW, j * PW_ROW, 0, PW_INV2 + j, r * PW_ROW + j, PW_L + r * PW_ROW + j, j, j + 1, true,
+                      r == j + 1 ? PW_ASQ + r : -1};
+    case PF_DIAG:  // d_j is left in a[j][j] by warp 0; its M value (1) is not read
+        return PfSlot{j * PW_ROW, j * PW_ROW, j * PW_ROW + j, PW_INV2 + j, j * PW_ROW + j, PW_L + j * PW_ROW + j, j - 1,
+                      j + 1, false, -1};
     case PF_D11:
-        return PfSlot{PW_ROW, PW_ROW, PW_ROW + 1, PW_INVD + 1, 0, PW_L + PW_ROW + 1, 0, 2, false};
-    case PF_B:
-        return PfSlot{r * PW_ROW, PW_BW, 0, PW_INVD + r, PW_BW + r, PW_Y + r, r, r + 1, true};
+        return PfSlot{PW_ROW, PW_ROW, PW_ROW + 1, PW_INV2 + 1, 0, PW_L + PW_ROW + 1, 0, 2, false, -1};
+    case PF_B:  // its M value is not read: the final pass forms y from the entry
+        return PfSlot{r * PW_ROW, PW_BW, 0, PW_INV2 + r, PW_BW + r, PW_Y + r, r, r + 1, true, -1};
     case PF_COL0:
-        return PfSlot{r * PW_ROW, 0, r * PW_ROW, PW_INVD, 0, PW_L + r * PW_ROW, 0, 1, false};
+        return PfSlot{r * PW_ROW, 0, r * PW_ROW, PW_INV2, 0, PW_L + r * PW_ROW, 0, 1, false, -1};
     case PF_B0:
-        return PfSlot{0, PW_BW, PW_BW, PW_INVD, 0, PW_Y, 0, 1, false};
+        return PfSlot{0, PW_BW, PW_BW, PW_INV2, 0, PW_Y, 0, 1, false, -1};
     default:
-        return PfSlot{0, 0, 0, 0, 0, 0, 0, 0, true};
+        return PfSlot{0, 0, 0, 0, 0, 0, 0, 0, true, -1};
     }
 }
 
@@ -306,9 +310,26 @@ __device__ __forceinline__ void pf_step(const PfSlot &q, double &v, double ik2, 
     const double pa = upd ? ok : lval ? lv : 0.0;
     const double qa = upd ? ik2 : lval ? qi : 0.0;
     const double t = pa * qa;
-    v = fma(upd ? -xk : 0.0, t, v);
-    if (upd && S == q.last) W[q.po] = v;
+    const double xs = upd ? xk : 0.0;  // a select of the value; the sign rides on the FMA
+    v = fma(-xs, t, v);
+    if (upd && S == q.last) {
+        W[q.po] = v;
+        if (q.sqo >= 0) W[q.sqo] = v * v;
+    }
     if (lval) W[q.dofs] = t;
+}
+
+// 1 / x for the pivot chain: the hardware's approximate reciprocal
+// (rcp.approx.ftz.f64, ~2^-20 relative error) and one step of the order-3
+// Householder iteration for f(y) = 1/y - x: with e = 1 - x y,
+// y <- y (1 + e + e^2), cubing the relative error.  Within 1 ulp of 1.0 / x
+// for x in [2^-80, 2^80], in ~200 cycles against ~330 for the division.
+__device__ __forceinline__ double rcp_fast(double x)
+{
+    double y;
+    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    const double e = fma(-x, y, 1.0);
+    return fma(y, fma(e, e, e), y);
 }
 
 // Phase S of the whole CTA (see the plan above).
@@ -317,25 +338,34 @@ __device__ __forceinline__ void pf_step(const PfSlot &q, double &v, double ik2, 
 __device__ __forceinline__ void pf_barrier() { asm volatile("bar.sync 1, %0;" ::"n"(CF_THREADS - 32) : "memory"); }
 
 template <int S>
-__device__ __forceinline__ void pf_phase(double *W, int warp, int u, int vi, const PfPlan &pf, const PfSlot &q0,
-                                         const PfSlot &q1, double &v0, double &v1, double &inv_prev, double &w,
-                                         int &wi, int n_inv, int &ci, int &cc)
+__device__ __forceinline__ void pf_phase(double *W, int warp, int u, int vi, int wlast, const PfPlan &pf,
+                                         const PfSlot &q0, const PfSlot &q1, double &v0, double &v1,
+                                         double &inv_prev, double &w, int &wi, int n_inv, int &ci, int &cc)
 {
     if (warp == 0) {
+        // the last phase has no pivot: 1 / sqrt(d_j) for the final pass
+        if (S == T && threadIdx.x < T) W[PW_INVD + threadIdx.x] = rsqrt(W[PW_A + threadIdx.x * PW_ROW + threadIdx.x]);
+        // the pivot chain: d_S = a_SS - a_S,S-1^2 / d_S-1 and 1 / d_S, no root
         if (S < T && threadIdx.x == 0) {
             double d = W[PW_A + S * PW_ROW + S];
             if (S > 0) {
-                const double lp = W[PW_A + S * PW_ROW + S - 1] * inv_prev;
-                d = fma(-lp, lp, d);
+                double asq;
+                if (S == 1) {
+                    const double a = W[PW_A + PW_ROW];
+                    asq = a * a;
+                } else {
+                    asq = W[PW_ASQ + S];
+                }
+                d = fma(-asq, inv_prev, d);
                 W[PW_A + S * PW_ROW + S] = d;
             }
-            inv_prev = rsqrt(d);
-            W[PW_INVD + S] = inv_prev;
-            W[PW_INV2 + S] = inv_prev * inv_prev;
-            W[PW_LINV + S * PW_ROW + S] = inv_prev;
+            inv_prev = rcp_fast(d);
+            W[PW_INV2 + S] = inv_prev;
         }
     } else if (u >= 0) {
-        if (S >= 1) {
+        // a trailing warp whose entries are all done skips the phase (its
+        // FP64 instructions would hold up the pipe that the chain shares)
+        if (S >= 1 && S <= wlast) {
             const double ik2 = W[PW_INV2 + (S >= 1 ? S - 1 : 0)];
             pf_step<S>(q0, v0, ik2, W);
             if (S <= 2) pf_step<S>(q1, v1, ik2, W);
@@ -351,7 +381,7 @@ __device__ __forceinline__ void pf_phase(double *W, int warp, int u, int vi, con
             }
             if (S >= cc + 2 && S <= ci + 1) {
                 w = fma(-W[PW_L + ci * PW_ROW + k], W[PW_LINV + k * PW_ROW + cc], w);
-                if (S == ci + 1) W[PW_LINV + ci * PW_ROW + cc] = w * W[PW_INVD + ci];
+                if (S == ci + 1) W[PW_LINV + ci * PW_ROW + cc] = w;
             }
         }
     }
@@ -359,13 +389,13 @@ __device__ __forceinline__ void pf_phase(double *W, int warp, int u, int vi, con
 }
 
 template <int S>
-__device__ __forceinline__ void pf_phases(double *W, int warp, int u, int vi, const PfPlan &pf, const PfSlot &q0,
-                                          const PfSlot &q1, double &v0, double &v1, double &inv_prev, double &w,
-                                          int &wi, int n_inv, int &ci, int &cc)
+__device__ __forceinline__ void pf_phases(double *W, int warp, int u, int vi, int wlast, const PfPlan &pf,
+                                          const PfSlot &q0, const PfSlot &q1, double &v0, double &v1,
+                                          double &inv_prev, double &w, int &wi, int n_inv, int &ci, int &cc)
 {
     if constexpr (S <= T) {
-        pf_phase<S>(W, warp, u, vi, pf, q0, q1, v0, v1, inv_prev, w, wi, n_inv, ci, cc);
-        pf_phases<S + 1>(W, warp, u, vi, pf, q0, q1, v0, v1, inv_prev, w, wi, n_inv, ci, cc);
+        pf_phase<S>(W, warp, u, vi, wlast, pf, q0, q1, v0, v1, inv_prev, w, wi, n_inv, ci, cc);
+        pf_phases<S + 1>(W, warp, u, vi, wlast, pf, q0, q1, v0, v1, inv_prev, w, wi, n_inv, ci, cc);
     }
 }
 
@@ -396,12 +426,15 @@ __device__ bool cta_potrf(double *W, const PfPlan &pf, Side &&side = Side())
     const int vi = warp == 1 ? tid - 32 : warp == 5 ? tid - 128 : -1;
     PfSlot q0 = pf_slot(PfEntry{PF_NONE, 0, 0}), q1 = q0;
     double v0 = 0.0, v1 = 0.0;
+    int wlast = 0;  // a trailing warp's last busy phase
     if (u >= 0) {
         const PfEntry e0 = pf.tr[u][0], e1 = pf.tr[u][1];
         q0 = pf_slot(e0);
         q1 = pf_slot(e1);
         v0 = W[e0.j == PF_BCOL ? PW_B + e0.r : PW_A + e0.r * PW_ROW + e0.j];
         v1 = W[e1.j == PF_BCOL ? PW_B + e1.r : PW_A + e1.r * PW_ROW + e1.j];
+        const int busy = e0.kind == PF_NONE ? 0 : pf_last_busy(e0);
+        wlast = __reduce_max_sync(0xffffffffu, max(busy, e1.kind == PF_NONE ? 0 : pf_last_busy(e1)));
     }
     // inverse threads: the current entry (ci, cc) in registers, the list read
     // only when an entry is done
@@ -416,12 +449,29 @@ __device__ bool cta_potrf(double *W, const PfPlan &pf, Side &&side = Side())
     if (warp == 4) {
         side.run(&fdone);
     } else {
-        pf_phases<0>(W, warp, u, vi, pf, q0, q1, v0, v1, inv_prev, w, wi, n_inv, ci, cc);
+        // after the CTA barrier above: until then the panel's side warp may
+        // still be storing the previous tile's inverse from this workspace
+        if (tid < T) W[PW_LINV + tid * PW_ROW + tid] = 1.0;  // M^-1 has a unit diagonal
+        pf_phases<0>(W, warp, u, vi, wlast, pf, q0, q1, v0, v1, inv_prev, w, wi, n_inv, ci, cc);
+        // the phases leave the pivots d_j on the diagonal, the final entries
+        // a_rj below it, M = a_rj / d_j in W[PW_L..], M^-1 in W[PW_LINV..]
+        // and 1 / sqrt(d_j) in W[PW_INVD..]; with D^1/2 = diag(sqrt(d_j)):
+        // L = a D^-1/2, L^-1 = D^-1/2 M^-1, y = D^-1/2 z
+        static_assert(T == 16, "entry (r, j) = (e >> 4, e & 15)");
+        const int rt = tid < 128 ? tid : tid - 32;  // 0 .. 223 over the seven warps with a role
+        for (int e = rt; e < T * T; e += CF_THREADS - 32) {
+            const int r = e >> 4, j = e & (T - 1);
+            if (j <= r) {
+                W[PW_L + r * PW_ROW + j] = W[PW_A + r * PW_ROW + j] * W[PW_INVD + j];
+                W[PW_LINV + r * PW_ROW + j] *= W[PW_INVD + r];
+            }
+            if (e < T) W[PW_Y + e] = W[PW_BW + e] * W[PW_INVD + e];
+        }
         if (tid == 0) *(volatile int *)&fdone = 1;
     }
     if (tid < T) {
         const double d = W[PW_A + tid * PW_ROW + tid];
-        if (!(d > 0.0) || !isfinite(d)) bad = 1;
+        if (!(d >= DBL_MIN) || !isfinite(d)) bad = 1;  // the reciprocal flushes subnormals
     }
     __syncthreads();
     return bad == 0;

@@ -942,8 +942,15 @@ void launch_schur(const DeviceProblem &d, double mu, cudaStream_t s)
 
 // ---------------------------------------------------------------------------
 // eb = gb - sum_j W_ij^T dpa_j (compute_eb.cl:25-39), dpb = V^-1 eb
-// (compute_dpb.cl:19-34), one thread per point; block partials of |dpb|^2
-// and dpb (mu dpb + gb) for the gain ratio (levmar.cpp:271-280).
+// (compute_dpb.cl:19-34); block partials of |dpb|^2 and dpb (mu dpb + gb)
+// for the gain ratio (levmar.cpp:271-280).  The sums over a point's
+// observations take three lanes (ten points a warp, lanes 30 and 31 idle,
+// eight warps); the rest of a point takes one thread, so its FP64
+// instructions issue with most lanes busy.
+// Points per k_eb_dpb block: three lanes per point, ten points per warp
+// (lanes 30 and 31 idle), eight warps.
+constexpr int EB_PPW = 10, EB_PPB = 8 * EB_PPW;
+
 template <typename R>
 __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int *__restrict__ pt_start,
                                                 const int *__restrict__ pt_order,
@@ -953,40 +960,46 @@ __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int *__re
                                                 double *__restrict__ dp, double *__restrict__ eb,
                                                 double *__restrict__ partial, int stage)
 {
-    __shared__ double r0[256], r1[256];
+    __shared__ double s_sum[EB_PPB][3];
+    __shared__ double r0[8], r1[8];
     extern __shared__ double s_dpa[];  // the camera part of dp (ncp doubles) when staged
-    // four lanes per point (points in pt_order): lane c < 3 sums component c
-    // of W^T dpa over the point's observations in order, lane 3 only takes
-    // part in the exchange; lane 0 finishes the point
     if (stage) {
         for (int e = threadIdx.x; e < ncp; e += blockDim.x) s_dpa[e] = dp[e];
         __syncthreads();
     }
     const double *dpa = stage ? s_dpa : dp;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    const int slot = t >> 2, c = t & 3;
-    int i = -1;
-    double e = 0.0;
-    if (slot < np) {
-        i = pt_order[slot];
-        if (c < 3) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // three lanes per point (points in pt_order): lane c sums component c of
+    // W^T dpa over the point's observations in order
+    {
+        const int pw = lane / 3, c = lane - 3 * pw;
+        const int slot = blockIdx.x * EB_PPB + warp * EB_PPW + pw;
+        // one accumulator per camera parameter: six short chains instead of
+        // one of six multiply-adds per observation (a point has up to ~40)
+        double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        if (lane < 3 * EB_PPW && slot < np) {
+            const int i = pt_order[slot];
             const int end = pt_start[i + 1];
 #pragma unroll 2
             for (int o = pt_start[i]; o < end; ++o) {
                 const R *w = W + 18 * (size_t)o;
                 const double *da = dpa + 6 * (size_t)__ldg(obs_cam + o);
 #pragma unroll
-                for (int k = 0; k < 6; ++k) e = e + (double)w[3 * k + c] * da[k];
+                for (int k = 0; k < 6; ++k) acc[k] = fma((double)w[3 * k + c], da[k], acc[k]);
             }
         }
+        const double e = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + (acc[4] + acc[5]);
+        if (lane < 3 * EB_PPW) s_sum[warp * EB_PPW + pw][c] = e;
     }
-    const int base = (threadIdx.x & 31) & ~3;
-    const double w0 = __shfl_sync(0xffffffffu, e, base), w1 = __shfl_sync(0xffffffffu, e, base + 1),
-                 w2 = __shfl_sync(0xffffffffu, e, base + 2);
+    __syncthreads();
+    // one thread per point finishes it: eb = gb - W^T dpa, dpb = V^-1 eb
     double s_sq = 0.0, s_rho = 0.0;
-    if (slot < np && c == 0) {
+    const int t = threadIdx.x;
+    const int slot = blockIdx.x * EB_PPB + t;
+    if (t < EB_PPB && slot < np) {
+        const int i = pt_order[slot];
         const double *gb = g + ncp + 3 * (size_t)i;
-        const double e0 = gb[0] - w0, e1 = gb[1] - w1, e2 = gb[2] - w2;
+        const double e0 = gb[0] - s_sum[t][0], e1 = gb[1] - s_sum[t][1], e2 = gb[2] - s_sum[t][2];
         eb[3 * (size_t)i] = e0;
         eb[3 * (size_t)i + 1] = e1;
         eb[3 * (size_t)i + 2] = e2;
@@ -1002,25 +1015,35 @@ __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int *__re
         s_sq = d0 * d0 + d1 * d1 + d2 * d2;
         s_rho = d0 * (mu * d0 + gb[0]) + d1 * (mu * d1 + gb[1]) + d2 * (mu * d2 + gb[2]);
     }
-    r0[threadIdx.x] = s_sq;
-    r1[threadIdx.x] = s_rho;
-    __syncthreads();
-    for (int st = 128; st > 0; st >>= 1) {
-        if (threadIdx.x < st) {
-            r0[threadIdx.x] += r0[threadIdx.x + st];
-            r1[threadIdx.x] += r1[threadIdx.x + st];
+    // block sums in a fixed order: the finishing warps, then the warps' sums
+    constexpr int FW = (EB_PPB + 31) / 32;
+    if (warp < FW) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            s_sq += __shfl_xor_sync(0xffffffffu, s_sq, off);
+            s_rho += __shfl_xor_sync(0xffffffffu, s_rho, off);
         }
-        __syncthreads();
+        if (lane == 0) {
+            r0[warp] = s_sq;
+            r1[warp] = s_rho;
+        }
     }
+    __syncthreads();
     if (threadIdx.x == 0) {
-        partial[2 * blockIdx.x] = r0[0];
-        partial[2 * blockIdx.x + 1] = r1[0];
+        double a = r0[0], b = r1[0];
+#pragma unroll
+        for (int w = 1; w < FW; ++w) {
+            a += r0[w];
+            b += r1[w];
+        }
+        partial[2 * blockIdx.x] = a;
+        partial[2 * blockIdx.x + 1] = b;
     }
 }
 
-// four threads per point in k_eb_dpb (the variable-intrinsics version uses
-// one, and its surplus blocks write zero partials)
-int eb_blocks(const DeviceProblem &d) { return ceil_div(4LL * (d.np > 0 ? d.np : 1), 256); }
+// EB_PPB points per k_eb_dpb block (the variable-intrinsics version uses one
+// thread per point, and its surplus blocks write zero partials)
+int eb_blocks(const DeviceProblem &d) { return ceil_div((long long)(d.np > 0 ? d.np : 1), EB_PPB); }
 
 void launch_eb_dpb(const DeviceProblem &d, double mu, cudaStream_t s)
 {

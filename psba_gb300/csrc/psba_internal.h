@@ -24,6 +24,10 @@ constexpr int DIAG_CHUNK = 16;   // observations per diagonal Schur work unit (1
 constexpr int SD_THREADS = 128, SD_PER = 8;     // 6-parameter cameras: one CTA per unit, 8 observations a thread
 constexpr int DIAG_SUPER = SD_THREADS * SD_PER;  // observations per diagonal unit, 6-parameter cameras
 constexpr int CAM_CHUNK = 512;   // observations per camera-reduction work unit
+// eb/dpb kernel: warps of up to EB_PPW points (in pt_order), three lanes per
+// point times m = eb_lanes_per_point(views), EB_WARPS warps a block
+constexpr int EB_PPW = 10, EB_WARPS = 8, EB_PPB = EB_PPW * EB_WARPS;
+inline int eb_lanes_per_point(int views) { return views <= 10 ? 1 : views <= 20 ? 2 : views <= 30 ? 3 : 4; }
 constexpr int RED_THREADS = 256; // threads of the reduction kernels
 
 // Per-camera table, computed once per parameter vector on the device:
@@ -86,6 +90,8 @@ struct DeviceProblem {
     int *obs_pt = nullptr, *obs_cam = nullptr;
     int *pt_start = nullptr;   // np + 1
     int *pt_order = nullptr;   // np: points by observation count, descending (per-point kernels' order)
+    int2 *eb_warps = nullptr;  // eb/dpb warps: first slot in pt_order, m; padded to EB_WARPS, plus a sentinel
+    int n_eb_warps = 0;
     int *cam_obs = nullptr;    // observations sorted by (camera, point)
     // camera pair lists for the off-diagonal Schur blocks (k > l)
     int n_pairs = 0;           // nonempty pairs

@@ -944,15 +944,13 @@ void launch_schur(const DeviceProblem &d, double mu, cudaStream_t s)
 // eb = gb - sum_j W_ij^T dpa_j (compute_eb.cl:25-39), dpb = V^-1 eb
 // (compute_dpb.cl:19-34); block partials of |dpb|^2 and dpb (mu dpb + gb)
 // for the gain ratio (levmar.cpp:271-280).  The sums over a point's
-// observations take three lanes (ten points a warp, lanes 30 and 31 idle,
-// eight warps); the rest of a point takes one thread, so its FP64
-// instructions issue with most lanes busy.
-// Points per k_eb_dpb block: three lanes per point, ten points per warp
-// (lanes 30 and 31 idle), eight warps.
-constexpr int EB_PPW = 10, EB_PPB = 8 * EB_PPW;
-
+// observations take 3 m lanes, m = 1..4 by its views (points in pt_order,
+// up to ten a warp, eight warps a block, per the eb_warps schedule), so no
+// lane walks more than ~10 observations; the rest of a point takes one
+// thread, so its FP64 instructions issue with most lanes busy.
 template <typename R>
-__global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int *__restrict__ pt_start,
+__global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int2 *__restrict__ eb_warps,
+                                                const int *__restrict__ pt_start,
                                                 const int *__restrict__ pt_order,
                                                 const int *__restrict__ obs_cam,
                                                 const R *__restrict__ W, const double *__restrict__ Vinv,
@@ -960,8 +958,9 @@ __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int *__re
                                                 double *__restrict__ dp, double *__restrict__ eb,
                                                 double *__restrict__ partial, int stage)
 {
+    static_assert(EB_WARPS == 8, "eight warps a block");
     __shared__ double s_sum[EB_PPB][3];
-    __shared__ double r0[8], r1[8];
+    __shared__ double r0[EB_WARPS], r1[EB_WARPS];
     extern __shared__ double s_dpa[];  // the camera part of dp (ncp doubles) when staged
     if (stage) {
         for (int e = threadIdx.x; e < ncp; e += blockDim.x) s_dpa[e] = dp[e];
@@ -969,34 +968,44 @@ __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int *__re
     }
     const double *dpa = stage ? s_dpa : dp;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    // three lanes per point (points in pt_order): lane c sums component c of
-    // W^T dpa over the point's observations in order
+    const int first = eb_warps[blockIdx.x * EB_WARPS].x;  // the block's points: [first, last) in pt_order
+    const int last = eb_warps[(blockIdx.x + 1) * EB_WARPS].x;
+    // the warp's points: 3 m lanes each; lane (s, c) sums component c of
+    // W^T dpa over the observations s, s + m, s + 2m, ... of its point
     {
-        const int pw = lane / 3, c = lane - 3 * pw;
-        const int slot = blockIdx.x * EB_PPB + warp * EB_PPW + pw;
-        // one accumulator per camera parameter: six short chains instead of
-        // one of six multiply-adds per observation (a point has up to ~40)
+        const int2 wi = eb_warps[blockIdx.x * EB_WARPS + warp];
+        const int npw = eb_warps[blockIdx.x * EB_WARPS + warp + 1].x - wi.x, m = wi.y;
+        const int lpp = 3 * m, pw = lane / lpp, r = lane - lpp * pw, s = r / 3, c = r - 3 * s;
+        // one accumulator per camera parameter: six short chains
         double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-        if (lane < 3 * EB_PPW && slot < np) {
-            const int i = pt_order[slot];
+        if (pw < npw) {
+            const int i = pt_order[wi.x + pw];
             const int end = pt_start[i + 1];
 #pragma unroll 2
-            for (int o = pt_start[i]; o < end; ++o) {
+            for (int o = pt_start[i] + s; o < end; o += m) {
                 const R *w = W + 18 * (size_t)o;
                 const double *da = dpa + 6 * (size_t)__ldg(obs_cam + o);
 #pragma unroll
                 for (int k = 0; k < 6; ++k) acc[k] = fma((double)w[3 * k + c], da[k], acc[k]);
             }
         }
-        const double e = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + (acc[4] + acc[5]);
-        if (lane < 3 * EB_PPW) s_sum[warp * EB_PPW + pw][c] = e;
+        const double part = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + (acc[4] + acc[5]);
+        // the m partial sums of a component, in order of s (each lane's own
+        // partial is what is exchanged, not a running sum)
+        double e = part;
+#pragma unroll
+        for (int q = 1; q < 4; ++q) {
+            const double v = __shfl_sync(0xffffffffu, part, min(lpp * pw + 3 * q + c, 31));
+            if (q < m) e += v;
+        }
+        if (pw < npw && s == 0) s_sum[wi.x + pw - first][c] = e;
     }
     __syncthreads();
     // one thread per point finishes it: eb = gb - W^T dpa, dpb = V^-1 eb
     double s_sq = 0.0, s_rho = 0.0;
     const int t = threadIdx.x;
-    const int slot = blockIdx.x * EB_PPB + t;
-    if (t < EB_PPB && slot < np) {
+    const int slot = first + t;
+    if (slot < last) {
         const int i = pt_order[slot];
         const double *gb = g + ncp + 3 * (size_t)i;
         const double e0 = gb[0] - s_sum[t][0], e1 = gb[1] - s_sum[t][1], e2 = gb[2] - s_sum[t][2];
@@ -1041,9 +1050,10 @@ __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int *__re
     }
 }
 
-// EB_PPB points per k_eb_dpb block (the variable-intrinsics version uses one
-// thread per point, and its surplus blocks write zero partials)
-int eb_blocks(const DeviceProblem &d) { return ceil_div((long long)(d.np > 0 ? d.np : 1), EB_PPB); }
+// k_eb_dpb blocks: EB_WARPS warps of the schedule each, at least np / EB_PPB
+// (the variable-intrinsics version uses one thread per point, and its
+// surplus blocks write zero partials)
+int eb_blocks(const DeviceProblem &d) { return d.n_eb_warps / EB_WARPS; }
 
 void launch_eb_dpb(const DeviceProblem &d, double mu, cudaStream_t s)
 {
@@ -1053,10 +1063,10 @@ void launch_eb_dpb(const DeviceProblem &d, double mu, cudaStream_t s)
     const int stage = (size_t)d.N * sizeof(double) <= 48 * 1024 ? 1 : 0;
     const size_t smem = stage ? sizeof(double) * d.N : 0;
     if (d.prec == PSBA_PREC_FP64)
-        k_eb_dpb<double><<<eb_blocks(d), 256, smem, s>>>(d.np, d.N, d.pt_start, d.pt_order, d.obs_cam, d.W, d.Vinv,
-                                                           d.g, mu, d.dp, d.eb, d.red_partial, stage);
+        k_eb_dpb<double><<<eb_blocks(d), 256, smem, s>>>(d.np, d.N, d.eb_warps, d.pt_start, d.pt_order, d.obs_cam,
+                                                           d.W, d.Vinv, d.g, mu, d.dp, d.eb, d.red_partial, stage);
     else
-        k_eb_dpb<float><<<eb_blocks(d), 256, smem, s>>>(d.np, d.N, d.pt_start, d.pt_order, d.obs_cam,
+        k_eb_dpb<float><<<eb_blocks(d), 256, smem, s>>>(d.np, d.N, d.eb_warps, d.pt_start, d.pt_order, d.obs_cam,
                                                           (const float *)d.W, d.Vinv, d.g, mu, d.dp, d.eb,
                                                           d.red_partial, stage);
     note_launch(1);

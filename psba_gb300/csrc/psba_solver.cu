@@ -829,6 +829,19 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
         for (int i = 0; i < np; ++i) order[start[maxdeg - deg[i]]++] = i;
         TRY(dalloc(h, &d.pt_order, (size_t)np));
         TRY(upload(h, d.pt_order, order.data(), (size_t)np));
+        // eb/dpb warps over the points in this order: m lane triples per
+        // point share its observations, so no lane walks more than ~10
+        std::vector<int2> ebw;
+        for (int s = 0; s < np;) {
+            const int m = eb_lanes_per_point(deg[order[s]]);
+            ebw.push_back(make_int2(s, m));
+            s += std::min(EB_PPW / m, np - s);
+        }
+        while (ebw.empty() || ebw.size() % EB_WARPS) ebw.push_back(make_int2(np, 1));
+        ebw.push_back(make_int2(np, 1));
+        d.n_eb_warps = (int)ebw.size() - 1;
+        TRY(dalloc(h, &d.eb_warps, ebw.size()));
+        TRY(upload(h, d.eb_warps, ebw.data(), ebw.size()));
         int run = 0;
         for (int k = 0; k < nc; ++k) {
             cam_start[k] = run;

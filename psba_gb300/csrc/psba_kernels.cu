@@ -332,71 +332,91 @@ void launch_residual(const DeviceProblem &d, const double *tab, const double *pt
 
 // ---------------------------------------------------------------------------
 // Per-point sums: V_i = coeff sum B^T B (compute_V.cl:24-37) and
-// gb_i = coeff sum B^T e (compute_g.cl:42-57), ascending camera order.
+// gb_i = coeff sum B^T e (compute_g.cl:42-57): 3 m lanes a point, each
+// summing every (3 m)-th observation in ascending camera order, then the
+// lanes' sums added in a fixed order.
 // V is accumulated in FP64 in both forms (in the mixed form from FP32
 // products): an FP32 running sum of B^T B can turn the nearly singular V of a
 // point seen from two close cameras indefinite, which moved the mixed form's
 // LM fixed point by 7e-3 of the cost on a 24-camera power-law scene.
 template <typename R>
-__global__ void k_point_blocks(int np, int ncp, const int *__restrict__ pt_start,
-                               const int *__restrict__ pt_order, const R *__restrict__ B,
-                               const R *__restrict__ ex, R coeff, double *__restrict__ V,
-                               double *__restrict__ g, double *__restrict__ uvdiag)
+__global__ void __launch_bounds__(256) k_point_blocks(int np, int ncp, const int2 *__restrict__ eb_warps,
+                                                      const int *__restrict__ pt_start,
+                                                      const int *__restrict__ pt_order, const R *__restrict__ B,
+                                                      const R *__restrict__ ex, R coeff, double *__restrict__ V,
+                                                      double *__restrict__ g, double *__restrict__ uvdiag)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= np) return;
-    const int i = pt_order[t];  // points by observation count: a warp's points have similar loops
-    double v00 = 0, v01 = 0, v02 = 0, v11 = 0, v12 = 0, v22 = 0;
-    double g0 = 0, g1 = 0, g2 = 0;  // gradient: FP64 sums of exact products in both forms
-    const int e = pt_start[i + 1];
-#pragma unroll 4
-    for (int o = pt_start[i]; o < e; ++o) {
-        R b[6], ee[2];
-        ldn<R, 6>(B + 6 * (size_t)o, b);
-        ld2<R>(ex + 2 * (size_t)o, ee[0], ee[1]);
-        const R b0 = b[0], b1 = b[1], b2 = b[2], c0 = b[3], c1 = b[4], c2 = b[5];
-        const R e0 = ee[0], e1 = ee[1];
-        if constexpr (is_fp64<R>()) {
-            v00 = v00 + b0 * b0 + c0 * c0;
-            v01 = v01 + b0 * b1 + c0 * c1;
-            v02 = v02 + b0 * b2 + c0 * c2;
-            v11 = v11 + b1 * b1 + c1 * c1;
-            v12 = v12 + b1 * b2 + c1 * c2;
-            v22 = v22 + b2 * b2 + c2 * c2;
-        } else {
-            v00 += (double)(b0 * b0 + c0 * c0);
-            v01 += (double)(b0 * b1 + c0 * c1);
-            v02 += (double)(b0 * b2 + c0 * c2);
-            v11 += (double)(b1 * b1 + c1 * c1);
-            v12 += (double)(b1 * b2 + c1 * c2);
-            v22 += (double)(b2 * b2 + c2 * c2);
+    // the eb/dpb warp schedule (points in pt_order, 3 m lanes a point): lane
+    // r of a point sums its observations r, r + L, r + 2L, ... (L = 3 m), so
+    // no lane walks more than ~4 of them; lane 0 then adds the L partial sums
+    // in order of r
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int2 wi = eb_warps[blockIdx.x * EB_WARPS + warp];
+    const int npw = eb_warps[blockIdx.x * EB_WARPS + warp + 1].x - wi.x;
+    const int L = 3 * wi.y, pw = lane / L, r = lane - L * pw;
+    const bool live = pw < npw;
+    const int i = live ? pt_order[wi.x + pw] : 0;
+    double a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // v00 v01 v02 v11 v12 v22, then the gradient (FP64 sums of exact products in both forms)
+    if (live) {
+        const int e = pt_start[i + 1];
+#pragma unroll 2
+        for (int o = pt_start[i] + r; o < e; o += L) {
+            R b[6], ee[2];
+            ldn<R, 6>(B + 6 * (size_t)o, b);
+            ld2<R>(ex + 2 * (size_t)o, ee[0], ee[1]);
+            const R b0 = b[0], b1 = b[1], b2 = b[2], c0 = b[3], c1 = b[4], c2 = b[5];
+            const R e0 = ee[0], e1 = ee[1];
+            if constexpr (is_fp64<R>()) {
+                a[0] = a[0] + b0 * b0 + c0 * c0;
+                a[1] = a[1] + b0 * b1 + c0 * c1;
+                a[2] = a[2] + b0 * b2 + c0 * c2;
+                a[3] = a[3] + b1 * b1 + c1 * c1;
+                a[4] = a[4] + b1 * b2 + c1 * c2;
+                a[5] = a[5] + b2 * b2 + c2 * c2;
+            } else {
+                a[0] += (double)(b0 * b0 + c0 * c0);
+                a[1] += (double)(b0 * b1 + c0 * c1);
+                a[2] += (double)(b0 * b2 + c0 * c2);
+                a[3] += (double)(b1 * b1 + c1 * c1);
+                a[4] += (double)(b1 * b2 + c1 * c2);
+                a[5] += (double)(b2 * b2 + c2 * c2);
+            }
+            a[6] = a[6] + (double)b0 * (double)e0 + (double)c0 * (double)e1;
+            a[7] = a[7] + (double)b1 * (double)e0 + (double)c1 * (double)e1;
+            a[8] = a[8] + (double)b2 * (double)e0 + (double)c2 * (double)e1;
         }
-        g0 = g0 + (double)b0 * (double)e0 + (double)c0 * (double)e1;
-        g1 = g1 + (double)b1 * (double)e0 + (double)c1 * (double)e1;
-        g2 = g2 + (double)b2 * (double)e0 + (double)c2 * (double)e1;
     }
+    double s[9];
+#pragma unroll
+    for (int v = 0; v < 9; ++v) s[v] = a[v];
+    for (int q = 1; q < L; ++q) {  // L is the same for the whole warp
+        const int src = min(L * pw + q, 31);
+#pragma unroll
+        for (int v = 0; v < 9; ++v) s[v] += __shfl_sync(0xffffffffu, a[v], src);
+    }
+    if (!live || r != 0) return;
     const double cf = (double)coeff;
     double *Vi = V + 6 * (size_t)i;
-    Vi[0] = cf * v00; Vi[1] = cf * v01; Vi[2] = cf * v02;
-    Vi[3] = cf * v11; Vi[4] = cf * v12; Vi[5] = cf * v22;
+    Vi[0] = cf * s[0]; Vi[1] = cf * s[1]; Vi[2] = cf * s[2];
+    Vi[3] = cf * s[3]; Vi[4] = cf * s[4]; Vi[5] = cf * s[5];
     uvdiag[ncp + 3 * (size_t)i] = Vi[0];
     uvdiag[ncp + 3 * (size_t)i + 1] = Vi[3];
     uvdiag[ncp + 3 * (size_t)i + 2] = Vi[5];
-    g[ncp + 3 * (size_t)i] = cf * g0;
-    g[ncp + 3 * (size_t)i + 1] = cf * g1;
-    g[ncp + 3 * (size_t)i + 2] = cf * g2;
+    g[ncp + 3 * (size_t)i] = cf * s[6];
+    g[ncp + 3 * (size_t)i + 1] = cf * s[7];
+    g[ncp + 3 * (size_t)i + 2] = cf * s[8];
 }
 
 void launch_point_blocks(const DeviceProblem &d, double coeff, cudaStream_t s)
 {
     if (d.np == 0) return;
     if (d.prec == PSBA_PREC_FP64)
-        k_point_blocks<double><<<ceil_div(d.np, 128), 128, 0, s>>>(d.np, d.N, d.pt_start, d.pt_order, d.B, d.ex,
-                                                                     coeff, d.V, d.g, d.uvdiag);
+        k_point_blocks<double><<<eb_blocks(d), 256, 0, s>>>(d.np, d.N, d.eb_warps, d.pt_start, d.pt_order, d.B,
+                                                              d.ex, coeff, d.V, d.g, d.uvdiag);
     else
-        k_point_blocks<float><<<ceil_div(d.np, 128), 128, 0, s>>>(d.np, d.N, d.pt_start, d.pt_order,
-                                                                    (const float *)d.B, (const float *)d.ex,
-                                                                    (float)coeff, d.V, d.g, d.uvdiag);
+        k_point_blocks<float><<<eb_blocks(d), 256, 0, s>>>(d.np, d.N, d.eb_warps, d.pt_start, d.pt_order,
+                                                             (const float *)d.B, (const float *)d.ex, (float)coeff,
+                                                             d.V, d.g, d.uvdiag);
     note_launch(1);
 }
 

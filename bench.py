@@ -16,9 +16,11 @@ estimate.  The metric is LM iterations per second.
   than L2 anyway).
 * e2e: the same metric through the C ABI from host buffers: psba_create
   (upload, index lists) + psba_levmar + psba_get_params per step, host clock.
-* roofline: the dominant kernel, k_schur_off (off-diagonal Schur blocks,
-  one launch per LM trial), timed live with CUDA events inside the timed
-  solves; FP64-bound, so its peak is the measured FP64 FMA rate.
+* roofline: the dominant kernel, k_schur (the Schur complement's
+  off-diagonal blocks in equal chunks of the pair list, and its diagonal
+  blocks in the same launch; one launch per LM trial), timed live with CUDA
+  events inside the timed solves; FP64-bound, so its peak is the measured
+  FP64 FMA rate.
   roofline_chol: the same for the dense solve (k_chol_dataflow +
   k_tri_cluster); roofline_schur: for the whole Schur-complement stage.
 * variable_intrinsics: 52 cameras x 64,053 points with 11- and
@@ -50,8 +52,8 @@ METRIC = "LM iterations/s (plain FP64 Levenberg-Marquardt, 88 cams x 64,298 pts)
 UNIT = "iterations/s"
 
 # DRAM bytes (read + write) per launch from one ncu capture of this workload
-# (profiles/k_schur_off_circle88.md, profiles/k_chol_dataflow_circle88.md).
-SCHUR_OFF_TRAFFIC = 154.2e6
+# (profiles/k_schur_circle88.md, profiles/k_chol_dataflow_circle88.md).
+SCHUR_TRAFFIC = 154.2e6
 CHOL_TRAFFIC = 1.30e6  # profiles/k_chol_dataflow_circle88.md: S (2.2 MB) stays in L2
 
 
@@ -488,7 +490,7 @@ def main():
         h2d, d2h = a, b
     e2e_value = e2e_iters / e2e_s if e2e_s > 0 else None
 
-    # ---- rooflines: the dominant kernel (k_schur_off), the dense solve and the whole Schur stage
+    # ---- rooflines: the dominant kernel (k_schur), the dense solve and the whole Schur stage
     peak_gbs, peak_kind = measured_peaks()
     fp64_peak = P.measure_peak("fp64")
     schur_ms = sum(stages[k][0] for k in ("schur_off", "schur_diag", "schur_reduce"))
@@ -497,11 +499,13 @@ def main():
     achieved_gbs = schur_bytes(sc) / schur_avg_s / 1e9
     fp64_achieved = schur_flops(cfg) / schur_avg_s / 1e12
     chol_avg_s = stages["cholesky"][0] / max(stages["cholesky"][1], 1) / 1e3
-    # k_schur_off alone: 6x6x3 FMAs per camera-pair entry; algorithmic bytes
-    # are Y and W of every observation (FP64) and the two pair-entry lists
+    # k_schur (the "schur_off" stage: the diagonal units run in the same
+    # launch): 6x6x3 FMAs per camera-pair entry and (21 + 6) x 3 per
+    # observation; algorithmic bytes are Y and W of every observation (FP64),
+    # the two pair-entry lists and the camera-sorted observation list
     soff_avg_s = stages["schur_off"][0] / max(stages["schur_off"][1], 1) / 1e3
-    soff_flops = 2 * 108 * cfg["pair_entries"]
-    soff_bytes = 2 * sc.n_obs * 18 * 8 + 2 * 4 * cfg["pair_entries"]
+    soff_flops = schur_flops(cfg)
+    soff_bytes = 2 * sc.n_obs * 18 * 8 + 2 * 4 * cfg["pair_entries"] + 4 * sc.n_obs
     Np = -(-6 * sc.n_cams // 16) * 16
     chol_flops = Np ** 3 / 3 + 2 * Np ** 2
     chol_bytes = Np * Np * 8 + 2 * Np * 8
@@ -519,13 +523,13 @@ def main():
         "final_cost": costs[-1], "wall_ms_per_step": 1e3 * wall / args.steps,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "steps": args.e2e_steps},
-        "roofline": {"kernel": "k_schur_off<double>: off-diagonal blocks of the Schur complement, one launch "
+        "roofline": {"kernel": "k_schur: off-diagonal and diagonal blocks of the Schur complement, one launch "
                                "per LM trial (the largest share of the launch list)",
                      "bound": "fp64", "achieved": soff_flops / soff_avg_s / 1e12, "peak": fp64_peak,
                      "unit": "TFLOP/s", "frac": soff_flops / soff_avg_s / 1e12 / fp64_peak,
                      "peak_source": "measured FP64 FMA rate (psba_measure_peak); MEASURED_PEAKS.json "
                                     "carries no FP64 figure",
-                     "traffic": SCHUR_OFF_TRAFFIC, "algorithmic_flops": soff_flops, "avg_ms": soff_avg_s * 1e3,
+                     "traffic": SCHUR_TRAFFIC, "algorithmic_flops": soff_flops, "avg_ms": soff_avg_s * 1e3,
                      "hbm": {"achieved": soff_bytes / soff_avg_s / 1e9, "peak": peak_gbs, "unit": "GB/s",
                              "frac": soff_bytes / soff_avg_s / 1e9 / peak_gbs, "algorithmic_bytes": soff_bytes,
                              "peak_source": peak_kind}},
@@ -539,10 +543,10 @@ def main():
                      "hbm": {"achieved": chol_bytes / chol_avg_s / 1e9, "peak": peak_gbs, "unit": "GB/s",
                              "frac": chol_bytes / chol_avg_s / 1e9 / peak_gbs, "algorithmic_bytes": chol_bytes,
                              "peak_source": peak_kind}},
-        "roofline_schur": {"kernel": "schur (k_schur_off + k_schur_diag + k_schur_reduce), per trial",
+        "roofline_schur": {"kernel": "schur (k_schur + k_schur_reduce), per trial",
                            "bound": "fp64", "achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                            "frac": fp64_achieved / fp64_peak, "flops": schur_flops(cfg),
-                           "traffic": SCHUR_OFF_TRAFFIC, "traffic_kernel": "k_schur_off",
+                           "traffic": SCHUR_TRAFFIC, "traffic_kernel": "k_schur",
                            "avg_ms": schur_avg_s * 1e3,
                            "hbm": {"achieved": achieved_gbs, "peak": peak_gbs, "unit": "GB/s",
                                    "frac": achieved_gbs / peak_gbs, "algorithmic_bytes": schur_bytes(sc),

@@ -701,15 +701,11 @@ __device__ __forceinline__ void off_products(const R *y, const R *w, R *acc)
 }
 
 template <typename R>
-__global__ void __launch_bounds__(128) k_schur_off(int n_chunks, const SchurUnit *__restrict__ chunks,
-                                                   const int *__restrict__ pair_start,
-                                                   const int *__restrict__ pa,
-                                                   const int *__restrict__ pb,
-                                                   const R *__restrict__ Y,
-                                                   const R *__restrict__ W,
-                                                   double *__restrict__ partial)
+__device__ __forceinline__ void schur_off_chunk(int uid, int n_chunks, const SchurUnit *__restrict__ chunks,
+                                                const int *__restrict__ pair_start, const int *__restrict__ pa,
+                                                const int *__restrict__ pb, const R *__restrict__ Y,
+                                                const R *__restrict__ W, double *__restrict__ partial)
 {
-    const int uid = blockIdx.x * blockDim.x + threadIdx.x;
     if (uid >= n_chunks) return;
     const SchurUnit u = chunks[uid];
     int q = u.slot, slot = u.out;
@@ -742,18 +738,6 @@ __global__ void __launch_bounds__(128) k_schur_off(int n_chunks, const SchurUnit
     for (int e = 0; e < 36; ++e) p[e] = acc[e];
 }
 
-int schur_off_wave_threads()
-{
-    static int threads = 0;
-    if (threads == 0) {
-        int dev = 0, sms = 0, per_sm = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_schur_off<double>, 128, 0);
-        threads = std::max(1, sms) * std::max(1, per_sm) * 128;
-    }
-    return threads;
-}
 
 constexpr int DIAG_NV = 27;  // 21 lower entries + 6 ea sums
 
@@ -793,17 +777,13 @@ __device__ __forceinline__ void diag_products(const R *y, const R *w, double g0,
 // four threads over 32 partials each, then the four) and writes one partial
 // per unit, so a camera has only a handful for k_schur_reduce.
 template <typename R>
-__global__ void __launch_bounds__(SD_THREADS) k_schur_diag(const SchurUnit *__restrict__ units,
-                                                           const int *__restrict__ cam_obs,
-                                                           const int *__restrict__ obs_pt,
-                                                           const R *__restrict__ Y,
-                                                           const R *__restrict__ W,
-                                                           const double *__restrict__ gb,
-                                                           double *__restrict__ partial)
+__device__ __forceinline__ void schur_diag_cta(const SchurUnit u, const int *__restrict__ cam_obs,
+                                               const int *__restrict__ obs_pt, const R *__restrict__ Y,
+                                               const R *__restrict__ W, const double *__restrict__ gb,
+                                               double *__restrict__ partial)
 {
     static_assert(SD_THREADS == 128 && DIAG_NV * 4 <= SD_THREADS, "four summing threads per output");
     __shared__ double red[DIAG_NV][SD_THREADS + 1];
-    const SchurUnit u = units[blockIdx.x];
     const int t = threadIdx.x;
     double acc[DIAG_NV];
 #pragma unroll
@@ -851,6 +831,51 @@ __global__ void __launch_bounds__(SD_THREADS) k_schur_diag(const SchurUnit *__re
     if (v < DIAG_NV) red[v][g] = s;
     __syncthreads();
     if (t < DIAG_NV) partial[(size_t)u.out * DIAG_NV + t] = (red[t][0] + red[t][1]) + (red[t][2] + red[t][3]);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(SD_THREADS) k_schur_diag(const SchurUnit *__restrict__ units,
+                                                           const int *__restrict__ cam_obs,
+                                                           const int *__restrict__ obs_pt,
+                                                           const R *__restrict__ Y,
+                                                           const R *__restrict__ W,
+                                                           const double *__restrict__ gb,
+                                                           double *__restrict__ partial)
+{
+    schur_diag_cta<R>(units[blockIdx.x], cam_obs, obs_pt, Y, W, gb, partial);
+}
+
+// FP64 products, 6-parameter cameras: the off-diagonal chunks (blocks below
+// off_ctas, 128 threads each) and the diagonal units (the rest) in one
+// launch.  Blocks are handed out in index order, so the off-diagonal chunks
+// fill one resident wave and the diagonal units run in its tail.
+__global__ void __launch_bounds__(128) k_schur(int n_chunks, int off_ctas, const SchurUnit *__restrict__ chunks,
+                                               const int *__restrict__ pair_start, const int *__restrict__ pa,
+                                               const int *__restrict__ pb, const SchurUnit *__restrict__ diag_units,
+                                               const int *__restrict__ cam_obs, const int *__restrict__ obs_pt,
+                                               const double *__restrict__ Y, const double *__restrict__ W,
+                                               const double *__restrict__ gb, double *__restrict__ off_partial,
+                                               double *__restrict__ diag_partial)
+{
+    static_assert(SD_THREADS == 128, "one block size for both parts");
+    if ((int)blockIdx.x < off_ctas)
+        schur_off_chunk<double>(blockIdx.x * 128 + threadIdx.x, n_chunks, chunks, pair_start, pa, pb, Y, W,
+                                off_partial);
+    else
+        schur_diag_cta<double>(diag_units[blockIdx.x - off_ctas], cam_obs, obs_pt, Y, W, gb, diag_partial);
+}
+
+int schur_off_wave_threads()
+{
+    static int threads = 0;
+    if (threads == 0) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_schur, 128, 0);
+        threads = std::max(1, sms) * std::max(1, per_sm) * 128;
+    }
+    return threads;
 }
 
 // Sum unit partials into S (lower) and rhs = ea.
@@ -905,14 +930,19 @@ __global__ void k_pad_identity(int N, int Np, double *S, double *rhs)
 void launch_schur_off(const DeviceProblem &d, cudaStream_t s)
 {
     if (d.cnp != 6) return launch_schur_off_v(d, s);
+    if (d.prec == PSBA_PREC_FP64) {
+        // the diagonal units ride in the same launch (k_schur)
+        const int off_ctas = ceil_div(d.n_off_chunks, 128);
+        if (off_ctas + d.n_diag_units == 0) return;
+        k_schur<<<off_ctas + d.n_diag_units, 128, 0, s>>>(
+            d.n_off_chunks, off_ctas, d.off_chunks, d.pair_start, d.pair_a, d.pair_b, d.diag_units, d.cam_obs,
+            d.obs_pt, d.Y, d.W, d.g + d.N, d.schur_partial, d.schur_partial + off_partial_slots(d) * 36);
+        note_launch(1);
+        return;
+    }
     if (d.n_off_units == 0) return;
-    if (d.prec == PSBA_PREC_FP64)
-        k_schur_off<double><<<ceil_div(d.n_off_chunks, 128), 128, 0, s>>>(
-            d.n_off_chunks, d.off_chunks, d.pair_start, d.pair_a, d.pair_b, d.Y, d.W, d.schur_partial);
-    else
-        k_schur_off_units<float><<<ceil_div(d.n_off_units, 128), 128, 0, s>>>(
-            d.n_off_units, d.off_units, d.pair_a, d.pair_b, (const float *)d.Y, (const float *)d.W,
-            d.schur_partial);
+    k_schur_off_units<float><<<ceil_div(d.n_off_units, 128), 128, 0, s>>>(
+        d.n_off_units, d.off_units, d.pair_a, d.pair_b, (const float *)d.Y, (const float *)d.W, d.schur_partial);
     note_launch(1);
 }
 
@@ -921,13 +951,9 @@ void launch_schur_diag(const DeviceProblem &d, cudaStream_t s)
     if (d.cnp != 6) return launch_schur_diag_v(d, s);
     double *diag_partial = d.schur_partial + off_partial_slots(d) * 36;
     if (d.n_diag_units == 0) return;
-    if (d.prec == PSBA_PREC_FP64)
-        k_schur_diag<double><<<d.n_diag_units, SD_THREADS, 0, s>>>(d.diag_units, d.cam_obs, d.obs_pt, d.Y, d.W,
-                                                                   d.g + d.N, diag_partial);
-    else
-        k_schur_diag<float><<<d.n_diag_units, SD_THREADS, 0, s>>>(d.diag_units, d.cam_obs, d.obs_pt,
-                                                                  (const float *)d.Y, (const float *)d.W,
-                                                                  d.g + d.N, diag_partial);
+    if (d.prec == PSBA_PREC_FP64) return;  // run by k_schur with the off-diagonal chunks
+    k_schur_diag<float><<<d.n_diag_units, SD_THREADS, 0, s>>>(d.diag_units, d.cam_obs, d.obs_pt, (const float *)d.Y,
+                                                              (const float *)d.W, d.g + d.N, diag_partial);
     note_launch(1);
 }
 

@@ -53,7 +53,7 @@ UNIT = "iterations/s"
 
 # DRAM bytes (read + write) per launch from one ncu capture of this workload
 # (profiles/k_schur_circle88.md, profiles/k_chol_dataflow_circle88.md).
-SCHUR_TRAFFIC = 154.2e6
+SCHUR_TRAFFIC = 250.1e6
 CHOL_TRAFFIC = 1.30e6  # profiles/k_chol_dataflow_circle88.md: S (2.2 MB) stays in L2
 
 

@@ -64,71 +64,76 @@ constexpr int FLUSH = 8;
 // With cnp > 6 the intrinsics (fx, cx, cy, ar, skew) and, for cnp 16, the
 // distortion (k1, k2, p1, p2, k3) are parameters 6.. of the camera, moved by
 // dpa like the pose; with cnp 6 they come from the fixed K array.
-__global__ void k_cam_tables(int nc, int cnp, const double *__restrict__ K, const double *__restrict__ q0,
-                             const double *__restrict__ cams, const double *__restrict__ dpa,
-                             double *__restrict__ tab)
+// One lane per camera, four warps per block by role, so that no warp issues
+// the whole table's FP64 instructions one after another (a warp issues one
+// FP64 instruction per ~64 cycles): every warp forms q = q(v) (x) q0, then
+// warp 0 writes M, t and the intrinsics, warp 1 + m writes D[m].
+__global__ void __launch_bounds__(128) k_cam_tables(int nc, int cnp, const double *__restrict__ K,
+                                                    const double *__restrict__ q0, const double *__restrict__ cams,
+                                                    const double *__restrict__ dpa, double *__restrict__ tab)
 {
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int role = threadIdx.x >> 5;
+    const int j = blockIdx.x * 32 + (threadIdx.x & 31);
     if (j >= nc) return;
     const double *cj = cams + (size_t)cnp * j;
     const double *dj = dpa ? dpa + (size_t)cnp * j : nullptr;
-    double vl[3], t[3];
-    for (int m = 0; m < 3; ++m) {
-        vl[m] = dj ? cj[m] + dj[m] : cj[m];
-        t[m] = dj ? cj[3 + m] + dj[3 + m] : cj[3 + m];
-    }
+    double vl[3];
+    for (int m = 0; m < 3; ++m) vl[m] = dj ? cj[m] + dj[m] : cj[m];
     const double s0 = q0[4 * j], a1 = q0[4 * j + 1], a2 = q0[4 * j + 2], a3 = q0[4 * j + 3];
     const double sl = sqrt(1.0 - vl[0] * vl[0] - vl[1] * vl[1] - vl[2] * vl[2]);
     const double s = sl * s0 - (a1 * vl[0] + a2 * vl[1] + a3 * vl[2]);
     const double a = s0 * vl[0] + sl * a1 + a3 * vl[1] - a2 * vl[2];
     const double b = s0 * vl[1] + sl * a2 + a1 * vl[2] - a3 * vl[0];
     const double c = s0 * vl[2] + sl * a3 + a2 * vl[0] - a1 * vl[1];
-    CamTab T;
-    const double d = s * s - (a * a + b * b + c * c);
-    T.M[0] = d + 2 * a * a;      T.M[1] = 2 * (a * b - s * c); T.M[2] = 2 * (a * c + s * b);
-    T.M[3] = 2 * (a * b + s * c); T.M[4] = d + 2 * b * b;      T.M[5] = 2 * (b * c - s * a);
-    T.M[6] = 2 * (a * c - s * b); T.M[7] = 2 * (b * c + s * a); T.M[8] = d + 2 * c * c;
-    // dM/d(s, a, b, c)
+    CamTab *T = reinterpret_cast<CamTab *>(tab + (size_t)CAMTAB * j);
+    if (role == 0) {
+        const double d = s * s - (a * a + b * b + c * c);
+        T->M[0] = d + 2 * a * a;      T->M[1] = 2 * (a * b - s * c); T->M[2] = 2 * (a * c + s * b);
+        T->M[3] = 2 * (a * b + s * c); T->M[4] = d + 2 * b * b;      T->M[5] = 2 * (b * c - s * a);
+        T->M[6] = 2 * (a * c - s * b); T->M[7] = 2 * (b * c + s * a); T->M[8] = d + 2 * c * c;
+        for (int m = 0; m < 3; ++m) T->t[m] = dj ? cj[3 + m] + dj[3 + m] : cj[3 + m];
+        double kk[5], kc[5] = {0, 0, 0, 0, 0};
+        if (cnp > 6) {
+            for (int m = 0; m < 5; ++m) kk[m] = dj ? cj[6 + m] + dj[6 + m] : cj[6 + m];
+            if (cnp == 16)
+                for (int m = 0; m < 5; ++m) kc[m] = dj ? cj[11 + m] + dj[11 + m] : cj[11 + m];
+        } else {
+            for (int m = 0; m < 5; ++m) kk[m] = K[5 * j + m];
+        }
+        T->fx = kk[0]; T->cx = kk[1]; T->cy = kk[2]; T->fy = kk[0] * kk[3]; T->sk = kk[4];
+        T->ar = kk[3];
+        for (int m = 0; m < 5; ++m) T->kc[m] = kc[m];
+        for (int m = 0; m < 6; ++m) T->pad[m] = 0.0;
+        return;
+    }
+    // D[m] = dM/dv_m through q(v), with dM/d(s, a, b, c) and
+    // dq/dv_m = (s0 ds - a0_m, a0 ds + s0 e_m + e_m x a0), ds = -v_m / s_l
+    const int m = role - 1;
     const double dS[9] = {2 * s, -2 * c, 2 * b, 2 * c, 2 * s, -2 * a, -2 * b, 2 * a, 2 * s};
     const double dA[9] = {2 * a, 2 * b, 2 * c, 2 * b, -2 * a, -2 * s, 2 * c, 2 * s, -2 * a};
     const double dB[9] = {-2 * b, 2 * a, 2 * s, 2 * a, 2 * b, 2 * c, -2 * s, 2 * c, -2 * b};
     const double dC[9] = {-2 * c, -2 * s, 2 * a, 2 * s, -2 * c, 2 * b, 2 * a, 2 * b, 2 * c};
-    const double av[3] = {a1, a2, a3};
-    for (int m = 0; m < 3; ++m) {
-        const double ds = -vl[m] / sl;
-        // dq/dv_m = (s0 ds - a0_m,  a0 ds + s0 e_m + e_m x a0)
-        double e_x_a[3] = {0, 0, 0};
-        if (m == 0) { e_x_a[1] = -a3; e_x_a[2] = a2; }
-        if (m == 1) { e_x_a[0] = a3; e_x_a[2] = -a1; }
-        if (m == 2) { e_x_a[0] = -a2; e_x_a[1] = a1; }
-        const double dq0 = s0 * ds - av[m];
-        double dqv[3];
-        for (int r = 0; r < 3; ++r) dqv[r] = av[r] * ds + (r == m ? s0 : 0.0) + e_x_a[r];
-        for (int e = 0; e < 9; ++e)
-            T.D[9 * m + e] = dS[e] * dq0 + dA[e] * dqv[0] + dB[e] * dqv[1] + dC[e] * dqv[2];
-    }
-    T.t[0] = t[0]; T.t[1] = t[1]; T.t[2] = t[2];
-    double kk[5], kc[5] = {0, 0, 0, 0, 0};
-    if (cnp > 6) {
-        for (int m = 0; m < 5; ++m) kk[m] = dj ? cj[6 + m] + dj[6 + m] : cj[6 + m];
-        if (cnp == 16)
-            for (int m = 0; m < 5; ++m) kc[m] = dj ? cj[11 + m] + dj[11 + m] : cj[11 + m];
-    } else {
-        for (int m = 0; m < 5; ++m) kk[m] = K[5 * j + m];
-    }
-    T.fx = kk[0]; T.cx = kk[1]; T.cy = kk[2]; T.fy = kk[0] * kk[3]; T.sk = kk[4];
-    T.ar = kk[3];
-    for (int m = 0; m < 5; ++m) T.kc[m] = kc[m];
-    for (int m = 0; m < 6; ++m) T.pad[m] = 0.0;
-    double *o = tab + (size_t)CAMTAB * j;
-    const double *src = reinterpret_cast<const double *>(&T);
-    for (int e = 0; e < CAMTAB; ++e) o[e] = src[e];
+    const double vm = m == 0 ? vl[0] : m == 1 ? vl[1] : vl[2];
+    const double am = m == 0 ? a1 : m == 1 ? a2 : a3;
+    const double ds = -vm / sl;
+    // e_m x a0
+    const double x0 = m == 1 ? a3 : m == 2 ? -a2 : 0.0;
+    const double x1 = m == 0 ? -a3 : m == 2 ? a1 : 0.0;
+    const double x2 = m == 0 ? a2 : m == 1 ? -a1 : 0.0;
+    const double dq0 = s0 * ds - am;
+    const double dq1 = a1 * ds + (m == 0 ? s0 : 0.0) + x0;
+    const double dq2 = a2 * ds + (m == 1 ? s0 : 0.0) + x1;
+    const double dq3 = a3 * ds + (m == 2 ? s0 : 0.0) + x2;
+    double *D = T->D + 9 * m;
+#pragma unroll
+    for (int e = 0; e < 9; ++e) D[e] = dS[e] * dq0 + dA[e] * dq1 + dB[e] * dq2 + dC[e] * dq3;
 }
 
 void launch_cam_tables(const DeviceProblem &d, const double *cams, const double *dpa, double *tab,
                        cudaStream_t s)
 {
-    k_cam_tables<<<ceil_div(d.nc, 128), 128, 0, s>>>(d.nc, d.cnp, d.K, d.q0, cams, dpa, tab); note_launch(1);
+    k_cam_tables<<<ceil_div(d.nc, 32), 128, 0, s>>>(d.nc, d.cnp, d.K, d.q0, cams, dpa, tab);
+    note_launch(1);
 }
 
 // ---------------------------------------------------------------------------

@@ -23,7 +23,8 @@ constexpr int OFF_MIN_LEN = 8;   // 6-parameter cameras: fewest pair-list entrie
 constexpr int DIAG_CHUNK = 16;   // observations per diagonal Schur work unit (11/16-parameter cameras)
 constexpr int SD_THREADS = 128, SD_PER = 8;     // 6-parameter cameras: one CTA per unit, 8 observations a thread
 constexpr int DIAG_SUPER = SD_THREADS * SD_PER;  // observations per diagonal unit, 6-parameter cameras
-constexpr int CAM_CHUNK = 512;   // observations per camera-reduction work unit
+constexpr int CAM_CHUNK = 512;   // observations per camera-reduction work unit (11/16-parameter cameras)
+constexpr int CAM_PER = 8, CAM_SUPER = 128 * CAM_PER;  // 6-parameter cameras: 8 observations a thread, 128 threads
 // eb/dpb kernel: warps of up to EB_PPW points (in pt_order), three lanes per
 // point times m = eb_lanes_per_point(views), EB_WARPS warps a block
 constexpr int EB_PPW = 10, EB_WARPS = 8, EB_PPB = EB_PPW * EB_WARPS;

@@ -428,11 +428,17 @@ void launch_point_blocks(const DeviceProblem &d, double coeff, cudaStream_t s)
 // ---------------------------------------------------------------------------
 // Per-camera sums U_j = coeff sum A^T A (compute_U.cl:21-34) and
 // ga_j = coeff sum A^T e (compute_g.cl:25-41) over the camera-sorted list,
-// split in units of CAM_CHUNK observations; fixed-order tree per unit, then
-// units summed in order.
+// split in units of CAM_SUPER observations; a fixed-order sum per unit,
+// then the units summed in order.
 constexpr int CAM_THREADS = 128;
 constexpr int CAM_NV = 27;  // 21 upper-triangle entries of A^T A + 6 of A^T e
+static_assert(CAM_SUPER == CAM_THREADS * CAM_PER, "camera unit size");
 
+// One CTA per unit of <= CAM_SUPER observations of a camera, CAM_PER
+// consecutive observations a thread (FP64: accumulated directly; FP32: the
+// products summed over the thread's observations, then one FP64 addition);
+// the CTA then sums its threads' partials in a fixed order, each output by
+// four threads over 32 partials, then the four.
 template <typename R>
 __global__ void __launch_bounds__(CAM_THREADS) k_camera_partial(const CamUnit *__restrict__ units,
                                                                 const int *__restrict__ cam_obs,
@@ -440,45 +446,57 @@ __global__ void __launch_bounds__(CAM_THREADS) k_camera_partial(const CamUnit *_
                                                                 const R *__restrict__ ex,
                                                                 double *__restrict__ partial)
 {
-    __shared__ double red[CAM_NV][CAM_THREADS];
+    static_assert(CAM_THREADS == 128 && CAM_NV * 4 <= CAM_THREADS && CAM_PER <= FLUSH, "camera unit layout");
+    __shared__ double red[CAM_NV][CAM_THREADS + 1];
     const CamUnit u = units[blockIdx.x];
+    const int t = threadIdx.x;
     double acc[CAM_NV];
 #pragma unroll
     for (int v = 0; v < CAM_NV; ++v) acc[v] = 0.0;
-    for (int t0 = threadIdx.x; t0 < u.count; t0 += CAM_THREADS * FLUSH) {
-        // FP64: accumulate directly; FP32: FLUSH products per FP64 addition
-        R part[CAM_NV];
+    R part[21];
 #pragma unroll
-        for (int v = 0; v < CAM_NV; ++v) part[v] = (R)0;
-        const int tend = min(u.count, t0 + CAM_THREADS * FLUSH);
-        for (int t = t0; t < tend; t += CAM_THREADS) {
-            const int o = cam_obs[u.begin + t];
-            R a[12], e2[2];
-            ldn<R, 12>(A + 12 * (size_t)o, a);
-            ld2<R>(ex + 2 * (size_t)o, e2[0], e2[1]);
-            int v = 0;
+    for (int v = 0; v < 21; ++v) part[v] = (R)0;
+    const int k1 = min(u.count, (t + 1) * CAM_PER);
+    for (int kk = t * CAM_PER; kk < k1; ++kk) {
+        const int o = __ldg(cam_obs + u.begin + kk);
+        R a[12], e2[2];
+        ldn<R, 12>(A + 12 * (size_t)o, a);
+        ld2<R>(ex + 2 * (size_t)o, e2[0], e2[1]);
+        int v = 0;
+        if constexpr (is_fp64<R>()) {
+#pragma unroll
+            for (int r = 0; r < 6; ++r)
+#pragma unroll
+                for (int c = r; c < 6; ++c, ++v) acc[v] = acc[v] + a[r] * a[c] + a[6 + r] * a[6 + c];
+        } else {
 #pragma unroll
             for (int r = 0; r < 6; ++r)
 #pragma unroll
                 for (int c = r; c < 6; ++c, ++v) part[v] = part[v] + a[r] * a[c] + a[6 + r] * a[6 + c];
-            // the gradient sets the LM fixed point: FP64 sums of the exact
-            // products of the stored values in both forms
-#pragma unroll
-            for (int k = 0; k < 6; ++k)
-                acc[21 + k] = acc[21 + k] + (double)a[k] * (double)e2[0] + (double)a[6 + k] * (double)e2[1];
         }
+        // the gradient sets the LM fixed point: FP64 sums of the exact
+        // products of the stored values in both forms
 #pragma unroll
-        for (int v = 0; v < 21; ++v) acc[v] += (double)part[v];
+        for (int q = 0; q < 6; ++q)
+            acc[21 + q] = acc[21 + q] + (double)a[q] * (double)e2[0] + (double)a[6 + q] * (double)e2[1];
+    }
+    if constexpr (!is_fp64<R>()) {
+#pragma unroll
+        for (int v = 0; v < 21; ++v) acc[v] = (double)part[v];
     }
 #pragma unroll
-    for (int v = 0; v < CAM_NV; ++v) red[v][threadIdx.x] = acc[v];
+    for (int v = 0; v < CAM_NV; ++v) red[v][t] = acc[v];
     __syncthreads();
-    for (int st = CAM_THREADS / 2; st > 0; st >>= 1) {
-        if (threadIdx.x < st)
-            for (int v = 0; v < CAM_NV; ++v) red[v][threadIdx.x] += red[v][threadIdx.x + st];
-        __syncthreads();
+    double s = 0.0;
+    const int v = t >> 2, g = t & 3;
+    if (v < CAM_NV) {
+#pragma unroll 8
+        for (int q = 0; q < CAM_THREADS / 4; ++q) s += red[v][g * (CAM_THREADS / 4) + q];
     }
-    if (threadIdx.x < CAM_NV) partial[(size_t)blockIdx.x * CAM_NV + threadIdx.x] = red[threadIdx.x][0];
+    __syncthreads();
+    if (v < CAM_NV) red[v][g] = s;
+    __syncthreads();
+    if (t < CAM_NV) partial[(size_t)blockIdx.x * CAM_NV + t] = (red[t][0] + red[t][1]) + (red[t][2] + red[t][3]);
 }
 
 __global__ void k_camera_finish(int nc, const int *__restrict__ unit_start,

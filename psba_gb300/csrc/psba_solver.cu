@@ -962,8 +962,9 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     std::vector<CamUnit> cam_units;
     std::vector<int> cam_unit_start(nc + 1, 0);
     for (int j = 0; j < nc; ++j) {
-        for (int b = cam_start[j]; b < cam_start[j + 1]; b += CAM_CHUNK)
-            cam_units.push_back({j, b, std::min(CAM_CHUNK, cam_start[j + 1] - b), 0});
+        const int cchunk = d.cnp == 6 ? CAM_SUPER : CAM_CHUNK;
+        for (int b = cam_start[j]; b < cam_start[j + 1]; b += cchunk)
+            cam_units.push_back({j, b, std::min(cchunk, cam_start[j + 1] - b), 0});
         cam_unit_start[j + 1] = (int)cam_units.size();
     }
     d.n_pairs = n_pairs;

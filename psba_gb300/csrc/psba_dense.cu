@@ -8,10 +8,9 @@
 // next step.  The other CTAs (helpers) accumulate every other update
 // (left-looking) and solve the remaining tiles against the diagonal
 // inverses, in a fixed dependency order; waits are bounded spins on per-task
-// flags in global memory (acquire/release).  After the factor, k_tri_solve
-// (one CTA of 512 threads, one column of the update per thread) solves
-// L^T x = y with y in shared memory; the refinement solve of the mixed form
-// (mode 1) runs both triangular solves there the same way.
+// flags in global memory (acquire/release).  After the factor, the back
+// solve L^T x = y runs on a thread-block cluster (k_tri_cluster; k_tri_solve,
+// one CTA, when PSBA_TRI_CLUSTER is 0).
 //
 // This replaces the reference's explicit inverse (SPD_inv.cl: 3x3-block
 // Cholesky chain, kern_trigMat_inv, kern_trigMat_mul, then matVec_mul) with
@@ -477,16 +476,15 @@ __device__ bool cta_potrf(double *W, const PfPlan &pf, Side &&side = Side())
     return bad == 0;
 }
 
-// Single-CTA triangular solves over the factor (S lower = L, Linv = diagonal
+// The single-CTA back solve over the factor (S lower = L, Linv = diagonal
 // tile inverses) with the right-hand side in shared memory.  A block step is
 // the 16 x 16 product with the diagonal inverse, then the update of the other
-// blocks, one row (forward) or column (back) of it per thread, reading one
-// row panel of L with independent loads.  Both are bound by the SM's FP64
-// rate (N^2 / 2 multiply-adds on one SM).  The back solve spreads its
-// diagonal product over 256 threads (one product each, summed by a fixed
-// shuffle tree over 16 lanes) and loads the values a thread needs for the
-// next block step (its Linv entry, its 16 panel values) while the current
-// one runs.
+// blocks, one column of it per thread, reading one row panel of L with
+// independent loads; it is bound by the SM's FP64 rate (N^2 / 2
+// multiply-adds on one SM).  The diagonal product is spread over 256 threads
+// (one product each, summed by a fixed shuffle tree over 16 lanes), and the
+// values a thread needs for the next block step (its Linv entry, its 16
+// panel values) are loaded while the current one runs.
 
 // One lane of the 16 x 16 diagonal product: 16 lanes hold the products of one
 // output, summed in a fixed order.
@@ -495,36 +493,6 @@ __device__ __forceinline__ double half_warp_sum(double p)
 #pragma unroll
     for (int off = T / 2; off > 0; off >>= 1) p += __shfl_xor_sync(0xffffffffu, p, off);
     return p;
-}
-
-// forward: b <- L^-1 b (right-looking: y_K = Linv_K b_K, then b_I -= L_IK y_K)
-__device__ void cta_forward(int Np, int nb, const double *__restrict__ S, const double *__restrict__ Linv,
-                            double *bs, double *tmp)
-{
-    const int tid = threadIdx.x;
-    for (int K = 0; K < nb; ++K) {
-        if (tid < T) {
-            const double *Li = Linv + (size_t)K * TT + tid * T;
-            double y = 0.0;
-#pragma unroll
-            for (int k = 0; k < T; ++k) y = fma(k <= tid ? __ldcg(Li + k) : 0.0, bs[K * T + k], y);
-            tmp[tid] = y;
-        }
-        __syncthreads();
-        if (tid < T) bs[K * T + tid] = tmp[tid];
-        for (int i = (K + 1) * T + tid; i < Np; i += blockDim.x) {
-            const double2 *row = reinterpret_cast<const double2 *>(S + (size_t)i * Np + K * T);
-            double s = 0.0;
-#pragma unroll
-            for (int c = 0; c < T / 2; ++c) {
-                const double2 v = __ldcg(row + c);
-                s = fma(v.x, tmp[2 * c], s);
-                s = fma(v.y, tmp[2 * c + 1], s);
-            }
-            bs[i] -= s;
-        }
-        __syncthreads();
-    }
 }
 
 // back: x <- L^-T y (right-looking over the columns of L^T: x_K = Linv_K^T y_K,
@@ -1052,14 +1020,12 @@ int chol_grid(int n_tasks, int grid_cap)
     return n_tasks < cap ? n_tasks : cap;
 }
 
-// Triangular solves in one CTA of TS_THREADS threads with the right-hand side
-// in shared memory: forward = 1 solves L y = rhs then L^T x = y (the
-// refinement solve), forward = 0 only L^T x = rhs (after the factor, whose
-// diagonal tasks already applied L^-1).  A failed factor (status != 0)
-// leaves x untouched.
+// The back solve L^T x = rhs in one CTA of TS_THREADS threads with the
+// right-hand side in shared memory (the factor's diagonal tasks already
+// applied L^-1 to rhs).  A failed factor (status != 0) leaves x untouched.
 constexpr int TS_THREADS = 512;
 
-__global__ void __launch_bounds__(TS_THREADS) k_tri_solve(int forward, int Np, int nb, const double *__restrict__ S,
+__global__ void __launch_bounds__(TS_THREADS) k_tri_solve(int Np, int nb, const double *__restrict__ S,
                                                            const double *__restrict__ Linv,
                                                            const double *__restrict__ rhs, double *__restrict__ x,
                                                            const int *__restrict__ status)
@@ -1069,12 +1035,11 @@ __global__ void __launch_bounds__(TS_THREADS) k_tri_solve(int forward, int Np, i
     if (*status != 0) return;
     for (int i = threadIdx.x; i < Np; i += blockDim.x) vec[i] = rhs[i];
     __syncthreads();
-    if (forward) cta_forward(Np, nb, S, Linv, vec, tmp);
     cta_back(Np, nb, S, Linv, vec, tmp, x);
 }
 
 // ---------------------------------------------------------------------------
-// The triangular solves on a thread-block cluster of TC_CTAS CTAs (one SM
+// The back solve on a thread-block cluster of TC_CTAS CTAs (one SM
 // each).  One SM's FP64 rate bounds a one-CTA solve (N^2 / 2 multiply-adds);
 // the cluster spreads the updates over TC_CTAS SMs and passes each step's
 // solved block through distributed shared memory with one cluster barrier
@@ -1094,7 +1059,7 @@ constexpr int TC_CTAS = 8, TC_THREADS = 256;
 __device__ __forceinline__ void cl_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
 __device__ __forceinline__ void cl_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
 
-// v[c] -= sum_r P(r, c) xs[r] for the columns (back) or rows (forward) listed
+// v[c] -= sum_r P(r, c) xs[r] for the columns listed
 // by idx(q), q < n: four threads per entry, four terms each, fixed tree.  The
 // first pass (q < TC_THREADS / 4) takes its four coefficients from first[],
 // loaded by the caller a step ahead; later passes load them here.
@@ -1123,7 +1088,7 @@ __device__ __forceinline__ void cl_update(double *v, const double *xs, int n, co
     }
 }
 
-__global__ void __launch_bounds__(TC_THREADS) k_tri_cluster(int forward, int Np, int nb,
+__global__ void __launch_bounds__(TC_THREADS) k_tri_cluster(int Np, int nb,
                                                             const double *__restrict__ S,
                                                             const double *__restrict__ Linv,
                                                             const double *__restrict__ rhs,
@@ -1166,59 +1131,6 @@ __global__ void __launch_bounds__(TC_THREADS) k_tri_cluster(int forward, int Np,
     // ping-pong pair (the loop is unrolled by two), so nothing waits for a
     // load until the step that uses it; all loads are issued after the
     // arrive (a load in flight at the arrive would hold up its release).
-    if (forward) {
-        // L y = b: step K solves y_K = Linv_K b_K, then b_I -= L_IK y_K for I > K
-        auto ldiag = [&](int K) {
-            return mine(K) && dk <= dr ? __ldcg(Linv + (size_t)K * TT + dr * T + dk) : 0.0;
-        };
-        auto lcrit = [&](int K, double (&cf)[4]) {  // rows of block K+1, columns of block K
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-                cf[j] = (cq < T && mine(K + 1)) ? __ldcg(S + (size_t)((K + 1) * T + cq) * Np + K * T + 4 * cg4 + j)
-                                                : 0.0;
-        };
-        auto ldef = [&](int P, double (&df)[4]) {  // rows of my blocks above P + 1, columns of block P
-            const int n = n_between(P + 1, nb);
-            const int i = cq < n ? entry_between(P + 1, cq) : 0;
-#pragma unroll
-            for (int j = 0; j < 4; ++j) df[j] = cq < n ? __ldcg(S + (size_t)i * Np + P * T + 4 * cg4 + j) : 0.0;
-        };
-        int pend = -1;
-        auto step = [&](int K, double &pl, double &pln, double (&cf)[4], double (&cfn)[4], double (&df)[4],
-                        double (&dfn)[4]) {
-            if (mine(K)) {
-                const double yv = half_warp_sum(pl * vec[K * T + dk]);
-                if (dk == 0) xb[K & 1][dr] = yv;
-            }
-            __syncthreads();
-            if (mine(K) && tid < T) vec[K * T + tid] = xb[K & 1][tid];
-            cl_arrive();
-            pln = K + 1 < nb ? ldiag(K + 1) : 0.0;
-            lcrit(K + 1, cfn);
-            ldef(K, dfn);
-            if (pend >= 0) {  // the previous step's block, applied to my blocks above pend + 1
-                const int P = pend;
-                cl_update(vec, xs[P & 1], n_between(P + 1, nb), df,
-                          [&](int r, int i) { return __ldcg(S + (size_t)i * Np + P * T + r); },
-                          [&](int q) { return entry_between(P + 1, q); });
-            }
-            cl_wait();
-            if (tid < T) xs[K & 1][tid] = cl.map_shared_rank(&xb[K & 1][0], K % TC_CTAS)[tid];
-            __syncthreads();
-            if (mine(K + 1)) crit_apply(xs[K & 1], cf, (K + 1) * T + cq);
-            __syncthreads();
-            pend = K;
-        };
-        double plA = ldiag(0), plB = 0.0, cfA[4], cfB[4], dfA[4] = {0.0, 0.0, 0.0, 0.0}, dfB[4];
-        lcrit(0, cfA);
-        for (int K = 0; K < nb; K += 2) {
-            step(K, plA, plB, cfA, cfB, dfA, dfB);
-            if (K + 1 < nb) step(K + 1, plB, plA, cfB, cfA, dfB, dfA);
-        }
-        // the last step's block reaches no block above it
-        cl_arrive();
-        cl_wait();
-    }
     {
         // L^T x = y: step K solves x_K = Linv_K^T y_K, then y_I -= L_KI^T x_K for I < K
         auto ldiag = [&](int K) {
@@ -1289,11 +1201,11 @@ __global__ void __launch_bounds__(TC_THREADS) k_tri_cluster(int forward, int Np,
 #endif
 }
 
-void launch_chol_dataflow(const DeviceProblem &d, int mode, int epoch, double *x_out, cudaStream_t s)
+void launch_chol_dataflow(const DeviceProblem &d, int epoch, double *x_out, cudaStream_t s)
 {
     int nb = d.Np / T;
     int Np = d.Np;
-    if (mode == 0) {
+    {
         int n_tasks = d.chol_n_tasks;
         const int grid = chol_grid(n_tasks + 1, d.chol_grid_cap);
         const int2 *tasks = d.chol_tasks;
@@ -1319,45 +1231,12 @@ void launch_chol_dataflow(const DeviceProblem &d, int mode, int epoch, double *x
         cfg.attrs = attr;
         cfg.numAttrs = 1;
         const double *S = d.S, *Linv = d.Linv, *rhs = d.rhs;
-        cudaLaunchKernelEx(&cfg, k_tri_cluster, (int)(mode == 1), Np, nb, S, Linv, rhs, x_out,
+        cudaLaunchKernelEx(&cfg, k_tri_cluster, Np, nb, S, Linv, rhs, x_out,
                            (const int *)d.status);
     }
 #else
-    k_tri_solve<<<1, TS_THREADS, sizeof(double) * Np, s>>>(mode == 1, Np, nb, d.S, d.Linv, d.rhs, x_out, d.status);
+    k_tri_solve<<<1, TS_THREADS, sizeof(double) * Np, s>>>(Np, nb, d.S, d.Linv, d.rhs, x_out, d.status);
 #endif
-    note_launch(1);
-}
-
-// Iterative refinement residual r = b - S x with the symmetric S given by its
-// lower triangle (one warp per row, lanes over columns, fixed-order warp sum).
-__global__ void k_refine_residual(int Np, const double *__restrict__ S, const double *__restrict__ x,
-                                  const double *__restrict__ b, double *__restrict__ r)
-{
-    const int row = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
-    const int lane = threadIdx.x % 32;
-    if (row >= Np) return;
-    double s = 0.0;
-    for (int c = lane; c < Np; c += 32) {
-        const double v = c <= row ? S[(size_t)row * Np + c] : S[(size_t)c * Np + row];
-        s = fma(v, x[c], s);
-    }
-    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
-    if (lane == 0) r[row] = b[row] - s;
-}
-
-__global__ void k_add_inplace(int n, double *x, const double *dx)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) x[i] = x[i] + dx[i];
-}
-
-void launch_refine(const DeviceProblem &d, int epoch, cudaStream_t s)
-{
-    // r = rhs_save - Ssave x  (into rhs), solve with the existing factor into xref, x += xref
-    k_refine_residual<<<(d.Np + 7) / 8, 256, 0, s>>>(d.Np, d.Ssave, d.xsol, d.rhs_save, d.rhs);
-    note_launch(1);
-    launch_chol_dataflow(d, 1, epoch, d.xref, s);
-    k_add_inplace<<<(d.Np + 255) / 256, 256, 0, s>>>(d.Np, d.xsol, d.xref);
     note_launch(1);
 }
 

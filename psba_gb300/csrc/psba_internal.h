@@ -141,11 +141,9 @@ struct DeviceProblem {
     double *Y = nullptr;          // 18 per obs
     double *schur_partial = nullptr;  // off-diagonal slots (off_partial_slots), then the diagonal units'
     double *S = nullptr;          // Np x Np (lower)
-    double *Ssave = nullptr;      // copy of S (TR fallback, refinement)
+    double *Ssave = nullptr;      // copy of S (trust-region modified-Cholesky fallback)
     double *rhs = nullptr;        // Np (ea on entry, y after the forward solve)
     double *xsol = nullptr;       // Np
-    double *rhs_save = nullptr;   // Np: ea before the solve (refinement)
-    double *xref = nullptr;       // Np: refinement correction
     double *Linv = nullptr;       // (Np / TILE) * TILE * TILE inverses of the diagonal blocks
     int *status = nullptr;        // Cholesky status word (0 ok, 1 not SPD, 2 wait budget exhausted)
     int2 *chol_tasks = nullptr;   // helper tasks of the dense factor, in dependency order
@@ -212,11 +210,11 @@ void launch_axpby(double *out, const double *x, double a, const double *y, doubl
 void launch_scale(double *out, const double *x, const double *num, const double *den,
                   double den_scale, double sign, long long n, cudaStream_t s);
 
-// Dense reduced-camera solve (psba_dense.cu): mode 0 factors S (Np x Np,
-// lower) in place with the forward solve of rhs carried along and the back
-// solve into xsol; mode 1 solves again with the existing factor.  One
-// cooperative launch; epoch must increase from launch to launch.
-void launch_chol_dataflow(const DeviceProblem &d, int mode, int epoch, double *x_out, cudaStream_t s);
+// Dense reduced-camera solve (psba_dense.cu): factors S (Np x Np, lower) in
+// place with the forward solve of rhs carried along (one cooperative
+// launch), then the back solve into x_out; epoch must increase from launch
+// to launch.
+void launch_chol_dataflow(const DeviceProblem &d, int epoch, double *x_out, cudaStream_t s);
 // at most cap CTAs for a handle's dense factor (0: one per SM); for callers
 // that run several handles side by side
 void set_chol_grid_cap(psba_handle *h, int cap);
@@ -252,9 +250,6 @@ void launch_eb_dpb_v(const DeviceProblem &d, double mu, int nblocks, cudaStream_
 void launch_jmultiply_v(const DeviceProblem &d, const double *x, double *out, cudaStream_t s);
 void launch_residual_dist(const DeviceProblem &d, const double *tab, const double *pts, const double *dpb,
                           double *ex_out, double *partial, int nblocks, cudaStream_t s);
-// One step of iterative refinement of S x = rhs_save with the factor in S/Linv
-// and the original matrix in Ssave (mixed precision); updates xsol.
-void launch_refine(const DeviceProblem &d, int epoch, cudaStream_t s);
 // Modified Cholesky (trust-region lambda fallback) and its diagonal correction.
 void launch_cholmod(double *S, int n, int ld, double *E, double *work, cudaStream_t s);
 

@@ -343,13 +343,7 @@ void enqueue_step(psba_handle *h, double mu)
     DeviceProblem &d = h->d;
     {
         StageScope sc(h, ST_CHOL);
-        if (d.prec == PSBA_PREC_MIXED) {
-            cudaMemcpyAsync(d.Ssave, d.S, sizeof(double) * (size_t)d.Np * d.Np, cudaMemcpyDeviceToDevice,
-                            h->stream);
-            cudaMemcpyAsync(d.rhs_save, d.rhs, sizeof(double) * d.Np, cudaMemcpyDeviceToDevice, h->stream);
-        }
-        launch_chol_dataflow(d, 0, ++h->chol_epoch, d.xsol, h->stream);
-        if (d.prec == PSBA_PREC_MIXED) launch_refine(d, ++h->chol_epoch, h->stream);
+        launch_chol_dataflow(d, ++h->chol_epoch, d.xsol, h->stream);
         cudaMemcpyAsync(d.dp, d.xsol, sizeof(double) * d.N, cudaMemcpyDeviceToDevice, h->stream);
     }
     {
@@ -1016,8 +1010,6 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     TRY(dalloc(h, &d.Ssave, (size_t)d.Np * d.Np));
     TRY(dalloc(h, &d.rhs, (size_t)d.Np));
     TRY(dalloc(h, &d.xsol, (size_t)d.Np));
-    TRY(dalloc(h, &d.rhs_save, (size_t)d.Np));
-    TRY(dalloc(h, &d.xref, (size_t)d.Np));
     TRY(dalloc(h, &d.Linv, (size_t)d.Np * TILE));
     TRY(dalloc(h, &d.status, 4));
     {

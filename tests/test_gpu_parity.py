@@ -187,7 +187,7 @@ def test_hybrid_matched_final_cost():
 
 # ---------------------------------------------------------------- mixed precision
 # Jacobian, residual, W, V and Y in FP32; U, S, ea accumulated in FP64; the
-# damped V^-1, Y's products, Cholesky, refinement, step, cost and gain ratio
+# damped V^-1, Y's products, Cholesky, the solves, step, cost and gain ratio
 # in FP64.  Stage tolerance:
 # 1e-5 of the array's largest magnitude (FP32 rounding of quantities built
 # from a handful of FP32 operations); solves: final cost within 1e-6 of the
@@ -215,7 +215,7 @@ def test_mixed_stages(golden):
         assert st == 0
         N = 6 * sc.n_cams
         Sf = np.tril(S) + np.tril(S, -1).T
-        # refined solve of the (mixed-precision) reduced system
+        # the FP64 solve of the (mixed-precision) reduced system
         assert np.abs(Sf @ dp[:N] - ea).max() <= 1e-9 * np.abs(ea).max()
 
 

@@ -22,7 +22,10 @@ estimate.  The metric is LM iterations per second.
   events inside the timed solves; FP64-bound, so its peak is the measured
   FP64 FMA rate.
   roofline_chol: the same for the dense solve (k_chol_dataflow +
-  k_tri_cluster); roofline_schur: for the whole Schur-complement stage.
+  k_tri_cluster).  Only these two stages carry events in the timed solves.
+* stage_ms / stage_share and roofline_schur (the whole Schur-complement
+  stage): from one more solve after the timed region with every stage timed
+  (events around every stage cost ~4 us each on the stream).
 * variable_intrinsics: 52 cameras x 64,053 points with 11- and
   16-parameter cameras, mixed and FP64 forms, LM iterations/s.
 * batched: 1,024 small problems in one persistent launch (mixed form,
@@ -410,8 +413,11 @@ def main():
         solver.reset_params()
         solver.levmar(opts, fetch=False, trace_cap=0)
 
-    # ---- timed region: K solves from the same initial estimate, problem resident in HBM
-    solver.set_stage_timing(True)
+    # ---- timed region: K solves from the same initial estimate, problem resident in HBM.
+    # Only the two roofline stages carry events here (each timed stage costs
+    # two events per occurrence on the stream); the per-stage breakdown comes
+    # from one more solve with every stage timed, after the timed region.
+    solver.set_stage_timing(True, stages=("schur_off", "cholesky"))
     clocks = ClockSampler(local)
     clocks.start()
     launches0 = P.kernel_launches()
@@ -430,6 +436,10 @@ def main():
     wall = time.perf_counter() - t0
     launches = P.kernel_launches() - launches0
     clk = clocks.stop()
+    live = solver.stage_timing()
+    solver.set_stage_timing(True)
+    solver.reset_params()
+    solver.levmar(opts, fetch=False, trace_cap=0)
     stages = solver.stage_timing()
     solver.set_stage_timing(False)
 
@@ -443,7 +453,6 @@ def main():
         for _ in range(min(1, args.warmup)):
             solver.reset_params()
             solver.levmar(mopts, fetch=False, trace_cap=0)
-        solver.set_stage_timing(True)
         m_ms, m_iters, m_costs = [], 0, []
         for _ in range(args.steps):
             solver.reset_params()
@@ -452,6 +461,9 @@ def main():
             m_ms.append(r.device_ms)
             m_iters += r.iterations
             m_costs.append(r.final_cost)
+        solver.set_stage_timing(True)  # the breakdown: one more solve with every stage timed
+        solver.reset_params()
+        solver.levmar(mopts, fetch=False, trace_cap=0)
         m_stages = solver.stage_timing()
         solver.set_stage_timing(False)
         mixed = {"value": m_iters / (sum(m_ms) / 1e3), "unit": UNIT, "ms_per_step": sum(m_ms) / len(m_ms),
@@ -498,12 +510,12 @@ def main():
     schur_avg_s = schur_ms / schur_n / 1e3
     achieved_gbs = schur_bytes(sc) / schur_avg_s / 1e9
     fp64_achieved = schur_flops(cfg) / schur_avg_s / 1e12
-    chol_avg_s = stages["cholesky"][0] / max(stages["cholesky"][1], 1) / 1e3
+    chol_avg_s = live["cholesky"][0] / max(live["cholesky"][1], 1) / 1e3
     # k_schur (the "schur_off" stage: the diagonal units run in the same
     # launch): 6x6x3 FMAs per camera-pair entry and (21 + 6) x 3 per
     # observation; algorithmic bytes are Y and W of every observation (FP64),
     # the two pair-entry lists and the camera-sorted observation list
-    soff_avg_s = stages["schur_off"][0] / max(stages["schur_off"][1], 1) / 1e3
+    soff_avg_s = live["schur_off"][0] / max(live["schur_off"][1], 1) / 1e3
     soff_flops = schur_flops(cfg)
     soff_bytes = 2 * sc.n_obs * 18 * 8 + 2 * 4 * cfg["pair_entries"] + 4 * sc.n_obs
     Np = -(-6 * sc.n_cams // 16) * 16

@@ -220,6 +220,10 @@ int psba_eval_cholmod(int n, double *S, double *E);
  * solves, eb/dpb, trial cost. */
 #define PSBA_N_STAGES 11
 int psba_set_stage_timing(psba_handle *h, int enable);
+/* Times only the stages whose bit is set (bit k: stage k in the order above)
+ * and clears the totals; 0 turns timing off.  Each timed stage costs two
+ * events per occurrence on the stream. */
+int psba_set_stage_mask(psba_handle *h, unsigned mask);
 /* Fills total_ms[k] and counts[k] for k < n; returns the number of stages. */
 int psba_get_stage_timing(psba_handle *h, double *total_ms, long long *counts, int n);
 

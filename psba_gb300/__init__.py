@@ -68,7 +68,7 @@ EXPORTS = ("psba_default_opts", "psba_create", "psba_destroy", "psba_get_params"
            "psba_levmar", "psba_trust_region", "psba_solve_hybrid", "psba_eval_residual",
            "psba_eval_jacobian", "psba_eval_normal", "psba_eval_reduced", "psba_eval_step",
            "psba_eval_jmultiply", "psba_eval_cholmod", "psba_last_error", "psba_stream",
-           "psba_device_bytes", "psba_version", "psba_set_stage_timing", "psba_get_stage_timing",
+           "psba_device_bytes", "psba_version", "psba_set_stage_timing", "psba_set_stage_mask", "psba_get_stage_timing",
            "psba_transfer_bytes", "psba_kernel_launches", "psba_measure_peak", "psba_cost_noalloc",
            "psba_batch_create", "psba_batch_destroy", "psba_batch_levmar", "psba_batch_get_params",
            "psba_batch_reset_params", "psba_batch_set_threads", "psba_batch_set_lanes_per_pair",
@@ -121,6 +121,7 @@ def lib():
         L.psba_device_bytes.restype = C.c_size_t
         L.psba_version.restype = C.c_char_p
         L.psba_set_stage_timing.argtypes = [C.c_void_p, C.c_int]
+        L.psba_set_stage_mask.argtypes = [C.c_void_p, C.c_uint]
         L.psba_get_stage_timing.argtypes = [C.c_void_p, _dp, C.POINTER(C.c_longlong), C.c_int]
         L.psba_transfer_bytes.argtypes = [C.c_void_p, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]
         L.psba_kernel_launches.restype = C.c_longlong
@@ -227,8 +228,16 @@ class Solver:
         _check(lib().psba_transfer_bytes(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
-    def set_stage_timing(self, enable=True):
-        _check(lib().psba_set_stage_timing(self.h, 1 if enable else 0))
+    def set_stage_timing(self, enable=True, stages=None):
+        """Stage timing with CUDA events: every stage, or only the named
+        ones (names from STAGES); clears the totals."""
+        if stages is None:
+            _check(lib().psba_set_stage_timing(self.h, 1 if enable else 0))
+            return
+        mask = 0
+        for name in stages:
+            mask |= 1 << STAGES.index(name)
+        _check(lib().psba_set_stage_mask(self.h, mask if enable else 0))
 
     def stage_timing(self):
         ms = np.zeros(len(STAGES))

@@ -65,7 +65,7 @@ struct StageTimer {
 
 struct psba_handle {
     DeviceProblem d;
-    bool timing = false;
+    unsigned timing = 0;  // stages timed with events: bit k for stage k
     StageTimer timers[ST_N];
     size_t h2d_bytes = 0, d2h_bytes = 0;
     cudaStream_t stream = nullptr;
@@ -203,11 +203,11 @@ struct StageScope {
     int k;
     StageScope(psba_handle *h_, int k_) : h(h_), k(k_)
     {
-        if (h->timing) cudaEventRecord(h->timers[k].a, h->stream);
+        if ((h->timing >> k) & 1u) cudaEventRecord(h->timers[k].a, h->stream);
     }
     ~StageScope()
     {
-        if (h->timing) {
+        if ((h->timing >> k) & 1u) {
             cudaEventRecord(h->timers[k].b, h->stream);
             h->timers[k].pending = true;
         }
@@ -1428,9 +1428,14 @@ int psba_eval_cholmod(int n, double *S, double *E)
 
 int psba_set_stage_timing(psba_handle *h, int enable)
 {
+    return psba_set_stage_mask(h, enable != 0 ? (1u << ST_N) - 1u : 0u);
+}
+
+int psba_set_stage_mask(psba_handle *h, unsigned mask)
+{
     if (!h) return set_error("null handle"), PSBA_ERR_ARG;
     TRY(sync(h));
-    h->timing = enable != 0;
+    h->timing = mask & ((1u << ST_N) - 1u);
     for (int k = 0; k < ST_N; ++k) {
         h->timers[k].pending = false;
         h->timers[k].total_ms = 0.0;

@@ -249,3 +249,27 @@ def test_mixed_power_law_matched_final_cost():
     assert g.final_cost - polish.final_cost <= 1e-6 * polish.final_cost
     minima = (14137773.708272452, 14237019.484916667)
     assert min(abs(g.final_cost - m) / m for m in minima) <= 1e-6
+
+
+def test_stage_timing_mask():
+    # timing only some stages leaves the others' counts at zero and does not
+    # change the solve; timing every stage counts each stage of the run
+    sc = scenes.small_lm_scene(3)
+    with P.Solver(sc) as s:
+        base = s.levmar(allow_switch=0, max_iter=5)
+        s.reset_params()
+        s.set_stage_timing(True, stages=("schur_off", "cholesky"))
+        part = s.levmar(allow_switch=0, max_iter=5)
+        t = s.stage_timing()
+        assert part.final_cost == base.final_cost
+        for name, (ms, n) in t.items():
+            if name in ("schur_off", "cholesky"):
+                assert n == part.n_trials and ms > 0.0
+            else:
+                assert n == 0 and ms == 0.0
+        s.reset_params()
+        s.set_stage_timing(True)
+        s.levmar(allow_switch=0, max_iter=5)
+        t = s.stage_timing()
+        assert t["linearize"][1] > 0 and t["trial_cost"][1] == part.n_trials
+        s.set_stage_timing(False)

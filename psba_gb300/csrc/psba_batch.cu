@@ -501,7 +501,6 @@ __device__ void solve_problem(const BatchProblem &p, const Arenas<R> &ar, const 
                               double *sh, int *shi, double *shd)
 {
     const int N = p.N;
-    const bool mixed = sizeof(R) == 4;
     double *dp = ar.d + p.d_dp, *tab = ar.d + p.d_tab, *tab2 = ar.d + p.d_tab2;
     double *cams = ar.d + p.d_cams, *pts = ar.d + p.d_pts;
     // shd: 0 mu, 1 p_L2, 2 ex_L2, 3 new cost; shi: 1 iter_flag, 2 nu, 3 itno, 4 trials, 5 lin, 6 first, 7 loop
@@ -563,39 +562,7 @@ __device__ void solve_problem(const BatchProblem &p, const Arenas<R> &ar, const 
             stage_schur<R>(p, ar, mu);
             __syncthreads();
             double *S = ar.d + p.d_S, *rhs = ar.d + p.d_rhs, *x = ar.d + p.d_x;
-            if (mixed) {
-                double *S0 = ar.d + p.d_S0, *rhs0 = ar.d + p.d_rhs0;
-                for (long long e = threadIdx.x; e < (long long)N * N; e += blockDim.x) S0[e] = S[e];
-                for (int k = threadIdx.x; k < N; k += blockDim.x) rhs0[k] = rhs[k];
-                __syncthreads();
-            }
             const int st = stage_cholesky_solve(S, N, rhs, x, sh, shi);
-            if (st == 0 && mixed) {
-                // one step of FP64 iterative refinement: r = rhs0 - S0 x, solve L L^T d = r, x += d
-                double *S0 = ar.d + p.d_S0, *rhs0 = ar.d + p.d_rhs0;
-                for (int r = threadIdx.x; r < N; r += blockDim.x) {
-                    double s = 0.0;
-                    for (int c = 0; c < N; ++c) s += (c <= r ? S0[(size_t)r * N + c] : S0[(size_t)c * N + r]) * x[c];
-                    rhs[r] = rhs0[r] - s;
-                }
-                __syncthreads();
-                for (int k = 0; k < N; ++k) {
-                    if (threadIdx.x == 0) rhs[k] = rhs[k] / S[(size_t)k * N + k];
-                    __syncthreads();
-                    const double yk = rhs[k];
-                    for (int i = k + 1 + threadIdx.x; i < N; i += blockDim.x) rhs[i] -= S[(size_t)i * N + k] * yk;
-                    __syncthreads();
-                }
-                for (int k = N - 1; k >= 0; --k) {
-                    if (threadIdx.x == 0) rhs0[k] = rhs[k] / S[(size_t)k * N + k];  // reuse rhs0 for the correction
-                    __syncthreads();
-                    const double xk = rhs0[k];
-                    for (int i = threadIdx.x; i < k; i += blockDim.x) rhs[i] -= S[(size_t)k * N + i] * xk;
-                    __syncthreads();
-                }
-                for (int k = threadIdx.x; k < N; k += blockDim.x) x[k] += rhs0[k];
-                __syncthreads();
-            }
             if (threadIdx.x == 0) shi[4]++;
             int decided = 0;  // 0: retry with larger mu, 1: accepted, 2: stop
             if (st == 0) {
@@ -815,11 +782,9 @@ bool build_problem_layout(const psba_problem_desc &p, ProblemLayout &L, std::str
     bp.d_uvdiag = dres((size_t)N + 3 * (size_t)np);
     bp.d_dp = dres((size_t)N + 3 * (size_t)np);
     bp.d_S = dres((size_t)N * N);
-    bp.d_S0 = dres((size_t)N * N);
     bp.d_tab = dres((size_t)CAMTAB * nc);
     bp.d_tab2 = dres((size_t)CAMTAB * nc);
     bp.d_rhs = dres((size_t)N);
-    bp.d_rhs0 = dres((size_t)N);
     bp.d_x = dres((size_t)N);
     // one LM iteration: per-observation work plus the in-CTA FP64 Cholesky
     L.work = (double)no + 0.02 * std::pow((double)N, 3) / 64.0;
@@ -829,8 +794,8 @@ bool build_problem_layout(const psba_problem_desc &p, ProblemLayout &L, std::str
 void rebase_problem(BatchProblem &bp, long long db, long long ib, long long rb)
 {
     for (long long *f : {&bp.d_K, &bp.d_q0, &bp.d_cams, &bp.d_pts, &bp.d_cams0, &bp.d_pts0, &bp.d_meas, &bp.d_V,
-                         &bp.d_Vinv, &bp.d_U, &bp.d_g, &bp.d_uvdiag, &bp.d_dp, &bp.d_S, &bp.d_S0, &bp.d_tab,
-                         &bp.d_tab2, &bp.d_rhs, &bp.d_rhs0, &bp.d_x})
+                         &bp.d_Vinv, &bp.d_U, &bp.d_g, &bp.d_uvdiag, &bp.d_dp, &bp.d_S, &bp.d_tab,
+                         &bp.d_tab2, &bp.d_rhs, &bp.d_x})
         *f += db;
     for (long long *f : {&bp.i_obs_pt, &bp.i_obs_cam, &bp.i_pt_start, &bp.i_cam_start, &bp.i_cam_obs,
                          &bp.i_pair_start, &bp.i_pair_kl, &bp.i_pair_a, &bp.i_pair_b})

@@ -19,7 +19,7 @@ struct BatchProblem {
     long long i_obs_pt, i_obs_cam, i_pt_start, i_cam_start, i_cam_obs, i_pair_start, i_pair_kl, i_pair_a,
         i_pair_b;                                                                  // int arena
     long long r_ex, r_A, r_B, r_W, r_Y;                                            // R arena
-    long long d_V, d_Vinv, d_U, d_g, d_uvdiag, d_dp, d_S, d_S0, d_tab, d_tab2, d_rhs, d_rhs0, d_x;  // double arena
+    long long d_V, d_Vinv, d_U, d_g, d_uvdiag, d_dp, d_S, d_tab, d_tab2, d_rhs, d_x;  // double arena
 };
 
 // A problem's LM state between launches (and its result at the end): the

@@ -146,6 +146,7 @@ struct DeviceProblem {
     double *xsol = nullptr;       // Np
     double *Linv = nullptr;       // (Np / TILE) * TILE * TILE inverses of the diagonal blocks
     int *status = nullptr;        // Cholesky status word (0 ok, 1 not SPD, 2 wait budget exhausted)
+    int *tickets = nullptr;       // 2 words, zero between launches: last-block tickets (eb/dpb, residual)
     int2 *chol_tasks = nullptr;   // helper tasks of the dense factor, in dependency order
     int chol_n_tasks = 0;
     int chol_grid_cap = 0;        // CTAs of the dense factor at most (0: one per SM)
@@ -171,10 +172,12 @@ void launch_cam_tables(const DeviceProblem &d, const double *cams, const double 
 void launch_linearize(const DeviceProblem &d, double coeff, cudaStream_t s);
 void launch_point_blocks(const DeviceProblem &d, double coeff, cudaStream_t s);
 void launch_camera_blocks(const DeviceProblem &d, double coeff, cudaStream_t s);
-// Residual only (ex) at the current parameters, and its sum of squares.
+// Residual only (ex, when ex_out is set) at the parameters given by tab,
+// pts (+ dpb), and its sum of squares into *sum_dst (block partials in
+// partial; the launch's last block sums them).
 void launch_residual(const DeviceProblem &d, const double *tab, const double *pts,
                      const double *dpb, double *ex_out, double *partial, int nblocks,
-                     cudaStream_t s);
+                     double *sum_dst, cudaStream_t s);
 int residual_blocks(const DeviceProblem &d);
 
 // Damping trial: V^-1, Y, Schur complement, ea.

@@ -59,6 +59,38 @@ template <typename R> __host__ __device__ constexpr bool is_fp64() { return size
 constexpr int FLUSH = 8;
 
 // ---------------------------------------------------------------------------
+// The last block of a launch to finish (by a ticket in global memory) sums
+// the launch's per-block partials into *dst in index order, so the result
+// does not depend on which block that is, and resets the ticket for the next
+// launch.  Thread 0 of every block calls it after writing the block's
+// partial; blockDim.x == 256.
+__device__ bool take_last_ticket(int *ticket)
+{
+    __shared__ int last;
+    if (threadIdx.x == 0) {
+        __threadfence();  // the block's partial before its ticket
+        last = atomicAdd(ticket, 1) == (int)gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last) __threadfence();
+    return last;
+}
+
+__device__ void sum_partials_block(const double *partial, int n, double *dst)
+{
+    __shared__ double r[256];
+    double a = 0.0;
+    for (int k = threadIdx.x; k < n; k += 256) a += __ldcg(partial + k);
+    r[threadIdx.x] = a;
+    __syncthreads();
+    for (int st = 128; st > 0; st >>= 1) {
+        if (threadIdx.x < st) r[threadIdx.x] += r[threadIdx.x + st];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *dst = r[0];
+}
+
+// ---------------------------------------------------------------------------
 // Camera tables.  q = q(v) (x) q0 (compute_exQT.cl:82-87), M = matrix of
 // X -> q (0,X) conj(q), D[m] = dM/dv_m through q(v) with s = sqrt(1-|v|^2).
 // With cnp > 6 the intrinsics (fx, cx, cy, ar, skew) and, for cnp 16, the
@@ -268,7 +300,8 @@ __global__ void __launch_bounds__(256) k_residual(int no, const int *__restrict_
                                                   const double *__restrict__ tab,
                                                   const double *__restrict__ wt,
                                                   double *__restrict__ ex_out,
-                                                  double *__restrict__ partial, int stage_nc)
+                                                  double *__restrict__ partial, int stage_nc,
+                                                  double *__restrict__ sum_dst, int *__restrict__ ticket)
 {
     __shared__ double red[256];
     extern __shared__ double s_tab[];  // stage_nc * RES_TAB
@@ -315,6 +348,10 @@ __global__ void __launch_bounds__(256) k_residual(int no, const int *__restrict_
         __syncthreads();
     }
     if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+    if (sum_dst && take_last_ticket(ticket)) {
+        sum_partials_block(partial, gridDim.x, sum_dst);
+        if (threadIdx.x == 0) *ticket = 0;
+    }
 }
 
 // cameras whose residual-table values a block stages (0: read the table)
@@ -326,12 +363,17 @@ int residual_stage_nc(const DeviceProblem &d)
 int residual_blocks(const DeviceProblem &d) { return ceil_div(d.no > 0 ? d.no : 1, 256); }
 
 void launch_residual(const DeviceProblem &d, const double *tab, const double *pts, const double *dpb,
-                     double *ex_out, double *partial, int nblocks, cudaStream_t s)
+                     double *ex_out, double *partial, int nblocks, double *sum_dst, cudaStream_t s)
 {
-    if (d.cnp == 16) return launch_residual_dist(d, tab, pts, dpb, ex_out, partial, nblocks, s);
+    if (d.cnp == 16) {
+        launch_residual_dist(d, tab, pts, dpb, ex_out, partial, nblocks, s);
+        launch_sum_partials(partial, nblocks, sum_dst, s);
+        return;
+    }
     const int snc = residual_stage_nc(d);
     k_residual<<<nblocks, 256, sizeof(double) * RES_TAB * snc, s>>>(d.no, d.obs_pt, d.obs_cam, d.meas, pts, dpb,
-                                                                    tab, d.wt, ex_out, partial, snc);
+                                                                    tab, d.wt, ex_out, partial, snc, sum_dst,
+                                                                    d.tickets);
     note_launch(1);
 }
 
@@ -1009,6 +1051,41 @@ void launch_schur(const DeviceProblem &d, double mu, cudaStream_t s)
     launch_schur_reduce(d, mu, s);
 }
 
+// dp_L2 = |dp|^2 and rho_den = dp (mu dp + g) from the camera part of dp and
+// the per-block sums of the point part, in a fixed order; the Cholesky
+// status.  One block of 256 threads.
+__device__ void finish_trial_block(int ncp, int nblocks, const double *__restrict__ dp,
+                                   const double *__restrict__ g, double mu, const double *partial,
+                                   const int *__restrict__ status, TrialScalars *__restrict__ out)
+{
+    __shared__ double r0[256], r1[256];
+    double a = 0.0, b = 0.0;
+    for (int k = threadIdx.x; k < ncp; k += 256) {
+        const double x = __ldcg(dp + k);
+        a += x * x;
+        b += x * (mu * x + g[k]);
+    }
+    for (int k = threadIdx.x; k < nblocks; k += 256) {
+        a += __ldcg(partial + 2 * k);
+        b += __ldcg(partial + 2 * k + 1);
+    }
+    r0[threadIdx.x] = a;
+    r1[threadIdx.x] = b;
+    __syncthreads();
+    for (int st = 128; st > 0; st >>= 1) {
+        if (threadIdx.x < st) {
+            r0[threadIdx.x] += r0[threadIdx.x + st];
+            r1[threadIdx.x] += r1[threadIdx.x + st];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out->dp_L2 = r0[0];
+        out->rho_den = r1[0];
+        out->chol_status = *status;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // eb = gb - sum_j W_ij^T dpa_j (compute_eb.cl:25-39), dpb = V^-1 eb
 // (compute_dpb.cl:19-34); block partials of |dpb|^2 and dpb (mu dpb + gb)
@@ -1025,7 +1102,9 @@ __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int2 *__r
                                                 const R *__restrict__ W, const double *__restrict__ Vinv,
                                                 const double *__restrict__ g, double mu,
                                                 double *__restrict__ dp, double *__restrict__ eb,
-                                                double *__restrict__ partial, int stage)
+                                                double *__restrict__ partial, int stage,
+                                                const int *__restrict__ status, int *__restrict__ ticket,
+                                                TrialScalars *__restrict__ out)
 {
     static_assert(EB_WARPS == 8, "eight warps a block");
     __shared__ double s_sum[EB_PPB][3];
@@ -1117,6 +1196,12 @@ __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int2 *__r
         partial[2 * blockIdx.x] = a;
         partial[2 * blockIdx.x + 1] = b;
     }
+    // the last block adds the camera part and every block's sums (the
+    // trial's step scalars)
+    if (take_last_ticket(ticket)) {
+        finish_trial_block(ncp, gridDim.x, dp, g, mu, partial, status, out);
+        if (threadIdx.x == 0) *ticket = 0;
+    }
 }
 
 // k_eb_dpb blocks: EB_WARPS warps of the schedule each, at least np / EB_PPB
@@ -1133,51 +1218,29 @@ void launch_eb_dpb(const DeviceProblem &d, double mu, cudaStream_t s)
     const size_t smem = stage ? sizeof(double) * d.N : 0;
     if (d.prec == PSBA_PREC_FP64)
         k_eb_dpb<double><<<eb_blocks(d), 256, smem, s>>>(d.np, d.N, d.eb_warps, d.pt_start, d.pt_order, d.obs_cam,
-                                                           d.W, d.Vinv, d.g, mu, d.dp, d.eb, d.red_partial, stage);
+                                                           d.W, d.Vinv, d.g, mu, d.dp, d.eb, d.red_partial, stage,
+                                                           d.status, d.tickets, d.scal);
     else
         k_eb_dpb<float><<<eb_blocks(d), 256, smem, s>>>(d.np, d.N, d.eb_warps, d.pt_start, d.pt_order, d.obs_cam,
                                                           (const float *)d.W, d.Vinv, d.g, mu, d.dp, d.eb,
-                                                          d.red_partial, stage);
+                                                          d.red_partial, stage, d.status, d.tickets, d.scal);
     note_launch(1);
 }
 
 // Sum the dpa part and the per-block partials of the back-substitution in a
-// fixed order; copy the Cholesky status.  One block.
+// fixed order; copy the Cholesky status.  One block (11/16-parameter
+// cameras; for 6-parameter cameras k_eb_dpb's last block does this).
 __global__ void k_finish_trial(int ncp, int nblocks, const double *__restrict__ dp,
                                const double *__restrict__ g, double mu,
                                const double *__restrict__ partial, const int *__restrict__ status,
                                TrialScalars *__restrict__ out)
 {
-    __shared__ double r0[256], r1[256];
-    double a = 0.0, b = 0.0;
-    for (int k = threadIdx.x; k < ncp; k += 256) {
-        const double x = dp[k];
-        a += x * x;
-        b += x * (mu * x + g[k]);
-    }
-    for (int k = threadIdx.x; k < nblocks; k += 256) {
-        a += partial[2 * k];
-        b += partial[2 * k + 1];
-    }
-    r0[threadIdx.x] = a;
-    r1[threadIdx.x] = b;
-    __syncthreads();
-    for (int st = 128; st > 0; st >>= 1) {
-        if (threadIdx.x < st) {
-            r0[threadIdx.x] += r0[threadIdx.x + st];
-            r1[threadIdx.x] += r1[threadIdx.x + st];
-        }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        out->dp_L2 = r0[0];
-        out->rho_den = r1[0];
-        out->chol_status = *status;
-    }
+    finish_trial_block(ncp, nblocks, dp, g, mu, partial, status, out);
 }
 
 void launch_finish_trial(const DeviceProblem &d, double mu, cudaStream_t s)
 {
+    if (d.cnp == 6) return;  // k_eb_dpb's last block did it
     k_finish_trial<<<1, 256, 0, s>>>(d.N, eb_blocks(d), d.dp, d.g, mu, d.red_partial, d.status,
                                      d.scal); note_launch(1);
 }

@@ -275,8 +275,7 @@ void enqueue_cost_current(psba_handle *h, double *ex_out)
     DeviceProblem &d = h->d;
     launch_cam_tables(d, d.cams, nullptr, d.camtab, h->stream);
     const int nb = residual_blocks(d);
-    launch_residual(d, d.camtab, d.pts, nullptr, ex_out, d.red_partial, nb, h->stream);
-    launch_sum_partials(d.red_partial, nb, h->scratch + SC_COST, h->stream);
+    launch_residual(d, d.camtab, d.pts, nullptr, ex_out, d.red_partial, nb, h->scratch + SC_COST, h->stream);
 }
 
 // Cost at p + step (into scal->new_cost).
@@ -288,8 +287,7 @@ void enqueue_cost_trial(psba_handle *h, const double *step)
     const int nb = residual_blocks(d);
     // partials after the eb partials region so they do not collide
     double *part = d.red_partial + 2 * eb_blocks(d) + 8;
-    launch_residual(d, d.camtab_new, d.pts, step + d.N, nullptr, part, nb, h->stream);
-    launch_sum_partials(part, nb, &d.scal->new_cost, h->stream);
+    launch_residual(d, d.camtab_new, d.pts, step + d.N, nullptr, part, nb, &d.scal->new_cost, h->stream);
 }
 
 // Jacobian, U, V, W, g with factor coeff at the current parameters.
@@ -1012,6 +1010,7 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     TRY(dalloc(h, &d.xsol, (size_t)d.Np));
     TRY(dalloc(h, &d.Linv, (size_t)d.Np * TILE));
     TRY(dalloc(h, &d.status, 4));
+    TRY(dalloc(h, &d.tickets, 2));
     {
         const int nb = d.Np / TILE;
         std::vector<int2> tasks;
@@ -1079,6 +1078,7 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     PSBA_CUDA_TRY(cudaMemcpyAsync(d.pts0, d.pts, sizeof(double) * 3 * (size_t)np, cudaMemcpyDeviceToDevice,
                                   h->stream));
     PSBA_CUDA_TRY(cudaMemsetAsync(d.status, 0, 4 * sizeof(int), h->stream));
+    PSBA_CUDA_TRY(cudaMemsetAsync(d.tickets, 0, 2 * sizeof(int), h->stream));
     PSBA_CUDA_TRY(cudaMemsetAsync(d.scal, 0, sizeof(TrialScalars), h->stream));
     PSBA_CUDA_TRY(cudaMemsetAsync(h->scratch, 0, 64 * sizeof(double), h->stream));
     return sync(h);  // host vectors go out of scope after the copies complete

@@ -703,14 +703,11 @@ void launch_yblocks(const DeviceProblem &d, cudaStream_t s)
 // FP32 products: one thread per unit of <= SCHUR_CHUNK entries of one pair,
 // units longest first; FP32 sums of FLUSH products, then FP64.
 template <typename R>
-__global__ void __launch_bounds__(128) k_schur_off_units(int n_units, const SchurUnit *__restrict__ units,
-                                                   const int *__restrict__ pa,
-                                                   const int *__restrict__ pb,
-                                                   const R *__restrict__ Y,
-                                                   const R *__restrict__ W,
-                                                   double *__restrict__ partial)
+__device__ __forceinline__ void schur_off_unit(int uid, int n_units, const SchurUnit *__restrict__ units,
+                                               const int *__restrict__ pa, const int *__restrict__ pb,
+                                               const R *__restrict__ Y, const R *__restrict__ W,
+                                               double *__restrict__ partial)
 {
-    const int uid = blockIdx.x * blockDim.x + threadIdx.x;
     if (uid >= n_units) return;
     const SchurUnit u = units[uid];
     double acc[36];
@@ -898,17 +895,6 @@ __device__ __forceinline__ void schur_diag_cta(const SchurUnit u, const int *__r
     if (t < DIAG_NV) partial[(size_t)u.out * DIAG_NV + t] = (red[t][0] + red[t][1]) + (red[t][2] + red[t][3]);
 }
 
-template <typename R>
-__global__ void __launch_bounds__(SD_THREADS) k_schur_diag(const SchurUnit *__restrict__ units,
-                                                           const int *__restrict__ cam_obs,
-                                                           const int *__restrict__ obs_pt,
-                                                           const R *__restrict__ Y,
-                                                           const R *__restrict__ W,
-                                                           const double *__restrict__ gb,
-                                                           double *__restrict__ partial)
-{
-    schur_diag_cta<R>(units[blockIdx.x], cam_obs, obs_pt, Y, W, gb, partial);
-}
 
 // FP64 products, 6-parameter cameras: the off-diagonal chunks (blocks below
 // off_ctas, 128 threads each) and the diagonal units (the rest) in one
@@ -941,6 +927,23 @@ int schur_off_wave_threads()
         threads = std::max(1, sms) * std::max(1, per_sm) * 128;
     }
     return threads;
+}
+
+// FP32 products: the off-diagonal units (blocks below off_ctas) and the
+// diagonal units (the rest) in one launch, so the diagonal CTAs run in the
+// off-diagonal units' last wave.
+__global__ void __launch_bounds__(128) k_schur_f32(int n_units, int off_ctas, const SchurUnit *__restrict__ units,
+                                                   const int *__restrict__ pa, const int *__restrict__ pb,
+                                                   const SchurUnit *__restrict__ diag_units,
+                                                   const int *__restrict__ cam_obs, const int *__restrict__ obs_pt,
+                                                   const float *__restrict__ Y, const float *__restrict__ W,
+                                                   const double *__restrict__ gb, double *__restrict__ off_partial,
+                                                   double *__restrict__ diag_partial)
+{
+    if ((int)blockIdx.x < off_ctas)
+        schur_off_unit<float>(blockIdx.x * 128 + threadIdx.x, n_units, units, pa, pb, Y, W, off_partial);
+    else
+        schur_diag_cta<float>(diag_units[blockIdx.x - off_ctas], cam_obs, obs_pt, Y, W, gb, diag_partial);
 }
 
 // Sum unit partials into S (lower) and rhs = ea.
@@ -1005,21 +1008,20 @@ void launch_schur_off(const DeviceProblem &d, cudaStream_t s)
         note_launch(1);
         return;
     }
-    if (d.n_off_units == 0) return;
-    k_schur_off_units<float><<<ceil_div(d.n_off_units, 128), 128, 0, s>>>(
-        d.n_off_units, d.off_units, d.pair_a, d.pair_b, (const float *)d.Y, (const float *)d.W, d.schur_partial);
+    const int off_ctas = ceil_div(d.n_off_units, 128);
+    if (off_ctas + d.n_diag_units == 0) return;
+    k_schur_f32<<<off_ctas + d.n_diag_units, 128, 0, s>>>(
+        d.n_off_units, off_ctas, d.off_units, d.pair_a, d.pair_b, d.diag_units, d.cam_obs, d.obs_pt,
+        (const float *)d.Y, (const float *)d.W, d.g + d.N, d.schur_partial,
+        d.schur_partial + off_partial_slots(d) * 36);
     note_launch(1);
 }
 
 void launch_schur_diag(const DeviceProblem &d, cudaStream_t s)
 {
-    if (d.cnp != 6) return launch_schur_diag_v(d, s);
-    double *diag_partial = d.schur_partial + off_partial_slots(d) * 36;
-    if (d.n_diag_units == 0) return;
-    if (d.prec == PSBA_PREC_FP64) return;  // run by k_schur with the off-diagonal chunks
-    k_schur_diag<float><<<d.n_diag_units, SD_THREADS, 0, s>>>(d.diag_units, d.cam_obs, d.obs_pt, (const float *)d.Y,
-                                                              (const float *)d.W, d.g + d.N, diag_partial);
-    note_launch(1);
+    // 6-parameter cameras: the diagonal units run in the off-diagonal launch
+    // (k_schur, k_schur_f32)
+    if (d.cnp != 6) launch_schur_diag_v(d, s);
 }
 
 void launch_schur_reduce(const DeviceProblem &d, double mu, cudaStream_t s)

@@ -373,7 +373,7 @@ void launch_residual(const DeviceProblem &d, const double *tab, const double *pt
     const int snc = residual_stage_nc(d);
     k_residual<<<nblocks, 256, sizeof(double) * RES_TAB * snc, s>>>(d.no, d.obs_pt, d.obs_cam, d.meas, pts, dpb,
                                                                     tab, d.wt, ex_out, partial, snc, sum_dst,
-                                                                    d.tickets);
+                                                                    d.tickets + 1);
     note_launch(1);
 }
 

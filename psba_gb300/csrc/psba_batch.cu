@@ -407,15 +407,16 @@ __device__ int stage_cholesky_solve(double *S, int N, double *rhs, double *x, do
 {
     if (threadIdx.x == 0) shi[0] = 0;
     __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     for (int k = 0; k < N; ++k) {
         if (threadIdx.x == 0) {
             const double d = S[(size_t)k * N + k];
             if (!(d > 0.0) || !isfinite(d)) {
                 shi[0] = 1;
             } else {
-                const double l = sqrt(d);
-                S[(size_t)k * N + k] = l;
-                sh[0] = 1.0 / l;
+                const double r = rsqrt(d);  // one root on the column chain: L_kk = d / sqrt(d)
+                S[(size_t)k * N + k] = d * r;
+                sh[0] = r;
             }
         }
         __syncthreads();
@@ -423,10 +424,10 @@ __device__ int stage_cholesky_solve(double *S, int N, double *rhs, double *x, do
         const double inv = sh[0];
         for (int i = k + 1 + threadIdx.x; i < N; i += blockDim.x) S[(size_t)i * N + k] *= inv;
         __syncthreads();
-        const int m = N - k - 1;
-        for (long long e = threadIdx.x; e < (long long)m * m; e += blockDim.x) {
-            const int i = k + 1 + (int)(e / m), j = k + 1 + (int)(e % m);
-            if (j <= i) S[(size_t)i * N + j] -= S[(size_t)i * N + k] * S[(size_t)j * N + k];
+        // trailing update, lower triangle: a warp per row, lanes over its columns
+        for (int i = k + 1 + warp; i < N; i += nwarps) {
+            const double lik = S[(size_t)i * N + k];
+            for (int j = k + 1 + lane; j <= i; j += 32) S[(size_t)i * N + j] -= lik * S[(size_t)j * N + k];
         }
         __syncthreads();
     }

@@ -414,15 +414,26 @@ __device__ int stage_cholesky_solve(double *S, int N, double *rhs, double *x, do
             if (!(d > 0.0) || !isfinite(d)) {
                 shi[0] = 1;
             } else {
-                const double r = rsqrt(d);  // one root on the column chain: L_kk = d / sqrt(d)
+                // one root on the column chain: L_kk = d / sqrt(d); the forward
+                // solve rides along (y_k = rhs_k / L_kk), and 1 / L_kk waits in
+                // x[k] for the back solve
+                const double r = rsqrt(d);
                 S[(size_t)k * N + k] = d * r;
+                const double yk = rhs[k] * r;
+                rhs[k] = yk;
+                x[k] = r;
                 sh[0] = r;
+                sh[1] = yk;
             }
         }
         __syncthreads();
         if (shi[0]) return 1;
-        const double inv = sh[0];
-        for (int i = k + 1 + threadIdx.x; i < N; i += blockDim.x) S[(size_t)i * N + k] *= inv;
+        const double inv = sh[0], yk = sh[1];
+        for (int i = k + 1 + threadIdx.x; i < N; i += blockDim.x) {
+            const double l = S[(size_t)i * N + k] * inv;
+            S[(size_t)i * N + k] = l;
+            rhs[i] -= l * yk;
+        }
         __syncthreads();
         // trailing update, lower triangle: a warp per row, lanes over its columns
         for (int i = k + 1 + warp; i < N; i += nwarps) {
@@ -431,17 +442,9 @@ __device__ int stage_cholesky_solve(double *S, int N, double *rhs, double *x, do
         }
         __syncthreads();
     }
-    // forward: L y = rhs (y in rhs)
-    for (int k = 0; k < N; ++k) {
-        if (threadIdx.x == 0) rhs[k] = rhs[k] / S[(size_t)k * N + k];
-        __syncthreads();
-        const double yk = rhs[k];
-        for (int i = k + 1 + threadIdx.x; i < N; i += blockDim.x) rhs[i] -= S[(size_t)i * N + k] * yk;
-        __syncthreads();
-    }
-    // back: L^T x = y
+    // back: L^T x = y (y in rhs, 1 / L_kk in x[k])
     for (int k = N - 1; k >= 0; --k) {
-        if (threadIdx.x == 0) x[k] = rhs[k] / S[(size_t)k * N + k];
+        if (threadIdx.x == 0) x[k] = rhs[k] * x[k];
         __syncthreads();
         const double xk = x[k];
         for (int i = threadIdx.x; i < k; i += blockDim.x) rhs[i] -= S[(size_t)k * N + i] * xk;

@@ -1267,23 +1267,31 @@ void launch_sum_partials(const double *partial, int n, double *dst, cudaStream_t
     k_sum_partials<<<1, 256, 0, s>>>(partial, n, dst); note_launch(1);
 }
 
+// max(0, x[k]) over k (maxElmOfUV starts from 0, sba_func.cpp:433-440), NaN
+// ignored as fmax does: per block, then combined with an integer atomicMax
+// on the bit patterns, which order like the values for non-negative
+// doubles; *dst is zeroed first.  Exact in any order.
 __global__ void k_max_uvdiag(const double *__restrict__ x, int n, double *__restrict__ dst)
 {
     __shared__ double r[256];
-    double m = 0.0;  // maxElmOfUV starts from 0 (sba_func.cpp:433-440)
-    for (int k = threadIdx.x; k < n; k += 256) m = fmax(m, x[k]);
+    double m = 0.0;
+    for (int k = blockIdx.x * 256 + threadIdx.x; k < n; k += gridDim.x * 256) m = fmax(m, x[k]);
     r[threadIdx.x] = m;
     __syncthreads();
     for (int st = 128; st > 0; st >>= 1) {
         if (threadIdx.x < st) r[threadIdx.x] = fmax(r[threadIdx.x], r[threadIdx.x + st]);
         __syncthreads();
     }
-    if (threadIdx.x == 0) *dst = r[0];
+    if (threadIdx.x == 0 && r[0] > 0.0)
+        atomicMax(reinterpret_cast<unsigned long long *>(dst), (unsigned long long)__double_as_longlong(r[0]));
 }
 
 void launch_max_uvdiag(const DeviceProblem &d, double *dst, cudaStream_t s)
 {
-    k_max_uvdiag<<<1, 256, 0, s>>>(d.uvdiag, d.N + 3 * d.np, dst); note_launch(1);
+    const int n = d.N + 3 * d.np;
+    cudaMemsetAsync(dst, 0, sizeof(double), s);
+    k_max_uvdiag<<<std::max(1, std::min(ceil_div(n, 256 * 8), 304)), 256, 0, s>>>(d.uvdiag, n, dst);
+    note_launch(1);
 }
 
 // Two-pass fixed-order reductions over long vectors.

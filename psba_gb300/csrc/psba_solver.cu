@@ -911,6 +911,7 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     // Schur work units; execution order longest first
     std::vector<SchurUnit> off_units, off_chunks, diag_units;
     std::vector<int> off_start(n_pairs + 1, 0), chunk_start(n_pairs + 1, 0), diag_start(nc + 1, 0);
+    off_units.reserve((size_t)(n_entries / SCHUR_CHUNK) + (size_t)n_pairs);
     for (int q = 0; q < n_pairs; ++q) {
         for (long long b = pair_start[q]; b < pair_start[q + 1]; b += SCHUR_CHUNK) {
             const int cnt = (int)std::min<long long>(SCHUR_CHUNK, pair_start[q + 1] - b);
@@ -925,6 +926,7 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
         // slot per pair it touches, slots numbered in list order
         const long long G = std::max(1, schur_off_wave_threads());
         const long long len = std::max<long long>(OFF_MIN_LEN, (n_entries + G - 1) / G);
+        off_chunks.reserve((size_t)(n_entries / len) + 1);
         int q = 0;
         for (long long b = 0; b < n_entries; b += len) {
             const long long e = std::min(n_entries, b + len);
@@ -948,9 +950,17 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
         }
         diag_start[j + 1] = (int)diag_units.size();
     }
-    auto by_count = [](const SchurUnit &x, const SchurUnit &y) { return x.count > y.count; };
-    std::stable_sort(off_units.begin(), off_units.end(), by_count);
-    std::stable_sort(diag_units.begin(), diag_units.end(), by_count);
+    // stable order by count, descending (a counting sort: counts are 1..maxc)
+    auto sort_by_count = [](std::vector<SchurUnit> &u, int maxc) {
+        std::vector<int> start((size_t)maxc + 2, 0);
+        for (const SchurUnit &x : u) start[maxc - x.count + 1]++;
+        for (int c = 0; c <= maxc; ++c) start[c + 1] += start[c];
+        std::vector<SchurUnit> out(u.size());
+        for (const SchurUnit &x : u) out[start[maxc - x.count]++] = x;
+        u.swap(out);
+    };
+    sort_by_count(off_units, SCHUR_CHUNK);
+    sort_by_count(diag_units, dchunk);
     std::vector<CamUnit> cam_units;
     std::vector<int> cam_unit_start(nc + 1, 0);
     for (int j = 0; j < nc; ++j) {

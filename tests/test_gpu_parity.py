@@ -160,6 +160,22 @@ def test_levmar_is_deterministic():
     assert np.array_equal(a.cams, b.cams) and np.array_equal(a.pts, b.pts)
 
 
+@pytest.mark.parametrize("precision", [P.PREC_FP64, P.PREC_MIXED])
+def test_levmar_power_law_bitwise_repeatable(precision):
+    # heavy points (views above 10: split over lane triples), pair-list chunks
+    # that span pairs, Schur units in one launch, last-block sums and the
+    # cluster solve: every sum has a fixed order, so two handles agree bitwise
+    sc = scenes.circle_scene(seed=1, n_cams=24, n_pts=3000, name="circle24")
+    runs = []
+    for _ in range(2):
+        with P.Solver(sc) as s:
+            runs.append(s.levmar(allow_switch=0, max_iter=8, precision=precision))
+    a, b = runs
+    assert a.final_cost == b.final_cost
+    assert np.array_equal(a.trace, b.trace)
+    assert np.array_equal(a.cams, b.cams) and np.array_equal(a.pts, b.pts)
+
+
 def test_levmar_power_law_scene():
     sc = scenes.circle_scene(seed=1, n_cams=24, n_pts=3000, name="circle24")
     o, g = _lm(sc, max_iter=10)

@@ -680,13 +680,119 @@ __global__ void __launch_bounds__(256) k_yblocks(int no, const int *__restrict__
     stn<R, 18>(Y + 18 * (size_t)o, y);
 }
 
+// Bulk asynchronous copies between global and shared memory (the copy
+// engine of the SM, no registers in flight): a global -> shared copy signals
+// an mbarrier with its byte count; a shared -> global copy is a bulk group.
+// Addresses and sizes are multiples of 16 bytes.
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned long long *bar)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+// waits for phase 0 of the barrier, at most `limit` polls; false if it ran out
+__device__ __forceinline__ bool mbar_wait0(unsigned long long *bar, long long limit)
+{
+    for (long long it = 0; it < limit; ++it) {
+        unsigned done;
+        asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
+                     : "=r"(done)
+                     : "r"(smem_u32(bar))
+                     : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+__device__ __forceinline__ void bulk_s2g(void *dst, const void *src, unsigned bytes)
+{
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_u32(src)),
+                 "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+    asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+
+// Y = W V^-1 (FP64) for YB_ROWS consecutive observations per CTA: their W
+// rows (contiguous, 144 bytes each) come into shared memory by one bulk copy,
+// each thread forms its row of Y there (16-byte shared loads at a 144-byte
+// stride: no bank conflicts), and one bulk copy writes the CTA's Y rows
+// back.  Same arithmetic as k_yblocks.  A copy that does not complete within
+// the poll budget sets status[2] (the trial then reports the wait budget
+// exhausted) and the CTA leaves.
+constexpr int YB_ROWS = 256;
+constexpr long long YB_POLL_LIMIT = 1LL << 22;
+
+__global__ void __launch_bounds__(YB_ROWS) k_yblocks_bulk(int no, const int *__restrict__ obs_pt,
+                                                          const double *__restrict__ W,
+                                                          const double *__restrict__ Vinv, double *__restrict__ Y,
+                                                          int *__restrict__ status)
+{
+    extern __shared__ __align__(16) double yb_sm[];  // W rows, then Y rows
+    __shared__ __align__(8) unsigned long long bar;
+    double *sw = yb_sm, *sy = yb_sm + YB_ROWS * 18;
+    const int o0 = blockIdx.x * YB_ROWS, rows = min(YB_ROWS, no - o0), t = threadIdx.x;
+    const unsigned bytes = (unsigned)rows * 18u * 8u;
+    if (t == 0) mbar_init(&bar);
+    __syncthreads();
+    if (t == 0) bulk_g2s(sw, W + 18 * (size_t)o0, bytes, &bar);
+    double s00 = 0, s01 = 0, s02 = 0, s11 = 0, s12 = 0, s22 = 0;
+    if (t < rows) {  // the point's V^-1 while the rows arrive
+        const double *vi = Vinv + 6 * (size_t)__ldg(obs_pt + o0 + t);
+        s00 = __ldg(vi); s01 = __ldg(vi + 1); s02 = __ldg(vi + 2);
+        s11 = __ldg(vi + 3); s12 = __ldg(vi + 4); s22 = __ldg(vi + 5);
+    }
+    if (!mbar_wait0(&bar, YB_POLL_LIMIT)) {
+        if (t == 0) atomicExch(status + 2, 2);
+        mbar_wait0(&bar, YB_POLL_LIMIT);  // the copy may still land in this CTA's memory
+        return;
+    }
+    if (t < rows) {
+        const double2 *w2 = reinterpret_cast<const double2 *>(sw + 18 * t);
+        double w[18], y[18];
+#pragma unroll
+        for (int e = 0; e < 9; ++e) {
+            const double2 v = w2[e];
+            w[2 * e] = v.x;
+            w[2 * e + 1] = v.y;
+        }
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+            const double w0 = w[3 * r], w1 = w[3 * r + 1], w2v = w[3 * r + 2];
+            y[3 * r + 0] = w0 * s00 + w1 * s01 + w2v * s02;
+            y[3 * r + 1] = w0 * s01 + w1 * s11 + w2v * s12;
+            y[3 * r + 2] = w0 * s02 + w1 * s12 + w2v * s22;
+        }
+        double2 *y2 = reinterpret_cast<double2 *>(sy + 18 * t);
+#pragma unroll
+        for (int e = 0; e < 9; ++e) y2[e] = make_double2(y[2 * e], y[2 * e + 1]);
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the rows, visible to the bulk copy
+    __syncthreads();
+    if (t == 0) bulk_s2g(Y + 18 * (size_t)o0, sy, bytes);
+}
+
 void launch_yblocks(const DeviceProblem &d, cudaStream_t s)
 {
     if (d.cnp != 6) return launch_yblocks_v(d, s);
     if (d.no == 0) return;
-    if (d.prec == PSBA_PREC_FP64)
-        k_yblocks<double><<<ceil_div(d.no, 256), 256, 0, s>>>(d.no, d.obs_pt, d.W, d.Vinv, d.Y);
-    else
+    if (d.prec == PSBA_PREC_FP64) {
+        static bool smem_set = false;
+        const int smem = (int)(2 * YB_ROWS * 18 * sizeof(double));
+        if (!smem_set) {
+            cudaFuncSetAttribute(k_yblocks_bulk, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            smem_set = true;
+        }
+        k_yblocks_bulk<<<ceil_div(d.no, YB_ROWS), YB_ROWS, smem, s>>>(d.no, d.obs_pt, d.W, d.Vinv, d.Y, d.status);
+    } else
         k_yblocks<float><<<ceil_div(d.no, 256), 256, 0, s>>>(d.no, d.obs_pt, (const float *)d.W, d.Vinv,
                                                                (float *)d.Y);
     note_launch(1);
@@ -1084,7 +1190,7 @@ __device__ void finish_trial_block(int ncp, int nblocks, const double *__restric
     if (threadIdx.x == 0) {
         out->dp_L2 = r0[0];
         out->rho_den = r1[0];
-        out->chol_status = *status;
+        out->chol_status = status[0] != 0 ? status[0] : (status[2] != 0 ? 2 : 0);  // [2]: a bulk copy's wait
     }
 }
 

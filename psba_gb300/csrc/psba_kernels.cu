@@ -259,11 +259,18 @@ __global__ void __launch_bounds__(256) k_linearize(int no, const int *__restrict
     }
     stn<R, 12>(A + 12 * (size_t)o, a);
     stn<R, 6>(B + 6 * (size_t)o, bb);
+    // W with coeff folded into a copy of B: the solver's coeff is 1 or 2, a
+    // power of two, so coeff (a b + a' b') and a (coeff b) + a' (coeff b') are
+    // the same number.  The y row of A has a zero for t_x (a[9], also after
+    // whitening, whose factor is triangular), so row 3 takes one product.
+    R cb[6];
+#pragma unroll
+    for (int m = 0; m < 6; ++m) cb[m] = coeff * bb[m];
     R w[18];
 #pragma unroll
     for (int r = 0; r < 6; ++r)
 #pragma unroll
-        for (int c = 0; c < 3; ++c) w[r * 3 + c] = coeff * (a[r] * bb[c] + a[6 + r] * bb[3 + c]);
+        for (int c = 0; c < 3; ++c) w[r * 3 + c] = r == 3 ? a[3] * cb[c] : a[r] * cb[c] + a[6 + r] * cb[3 + c];
     stn<R, 18>(W + 18 * (size_t)o, w);
 }
 

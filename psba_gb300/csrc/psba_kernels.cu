@@ -1244,7 +1244,7 @@ __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int2 *__r
         if (pw < npw) {
             const int i = pt_order[wi.x + pw];
             const int end = pt_start[i + 1];
-#pragma unroll 2
+#pragma unroll 4
             for (int o = pt_start[i] + s; o < end; o += m) {
                 const R *w = W + 18 * (size_t)o;
                 const double *da = dpa + 6 * (size_t)__ldg(obs_cam + o);

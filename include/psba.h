@@ -173,6 +173,14 @@ int psba_trust_region(psba_handle *h, const psba_opts *opts, int *itno, psba_res
 /* The LM <-> TR alternation of PSBA/main.cpp:193-208, from itno = 0. */
 int psba_solve_hybrid(psba_handle *h, const psba_opts *opts, psba_result *res);
 
+/* Bound of the handle's device-side waits: the dense factor's waits on its
+ * task flags and the Y kernel's wait for its bulk copies, in polls (0: the
+ * default, 2^22, about half a second).  A wait that runs out ends its kernel
+ * with a status the driver reads; the solve then returns PSBA_ERR_STATE and
+ * the handle stays usable.  No reference counterpart: the reference's
+ * device-side enqueue chain has no waits of its own (CL_files/SPD_inv.cl:165-179). */
+int psba_set_wait_limit(psba_handle *h, long long polls);
+
 /* ---- stage evaluation (parity checks; reference layouts, host buffers) -- */
 
 /* Precision used by the psba_eval_* calls (PSBA_PREC_*); the drivers take it
@@ -210,6 +218,22 @@ int psba_eval_jmultiply(psba_handle *h, const double *x, double *out);
  * and the diagonal correction to E.  Runs on the device; n % 3 == 0. */
 int psba_eval_cholmod(int n, double *S, double *E);
 
+/* The reduced-camera solve of psba_eval_step (Cholesky factor with the
+ * forward solve carried along, then the back solve) on an n x n matrix given
+ * by the caller: S row-major, lower triangle read, 1 <= n <= 4096; x = S^-1 b.
+ * *status is 0 when S was factored, 1 when a pivot was not positive, finite
+ * and normal (the reference's failure test, SPD_inv.cl:66-107; subnormal
+ * pivots count as failures here), 2 when a device-side wait ran out.
+ * Replaces SPDinv + matVec_mul (PSBA/cl_spdinv.cpp:18-40,
+ * PSBA/cl_linearalg.cpp:19-55) for parity checks at any size. */
+int psba_eval_dense_solve(int n, const double *S, const double *b, double *x, int *status);
+
+/* The dense factor's pivot reciprocal (the hardware's approximate reciprocal
+ * refined by one order-3 Householder step) applied to n values on the
+ * device, for accuracy checks against the correctly rounded 1.0 / x.  No
+ * reference counterpart: the reference divides (SPD_inv.cl:60-111). */
+int psba_eval_pivot_reciprocal(int n, const double *x, double *y);
+
 /* ---- measurement (no reference counterpart: the reference only keeps
  * host clock() totals, PSBA/main.cpp:22-37,220-227) ---------------------- */
 
@@ -234,7 +258,9 @@ int psba_transfer_bytes(psba_handle *h, size_t *h2d, size_t *d2h);
 /* Kernels launched by this library in the process so far. */
 long long psba_kernel_launches(void);
 
-/* FMA throughput of the current device in TFLOP/s: which = 0 FP64, 1 FP32. */
+/* Throughput of the current device in TFLOP/s: which = 0 FP64 FMA, 1 FP32
+ * FMA, 2 FP64 tensor cores (mma.sync m8n8k4), 3 FP64 tensor cores (mma.sync
+ * m16n8k16).  Eight independent chains per thread or warp. */
 int psba_measure_peak(int which, double *tflops);
 
 /* ---- batches of independent problems ------------------------------------ */
@@ -304,7 +330,9 @@ typedef struct psba_server_opts {
     int large_lanes;         /* large-lane host threads, each solving one request at a time (default 4) */
     double large_share;      /* share of hbm_budget_bytes reserved for the large lane (default 0.25) */
     int large_obs;           /* ... and so do requests with more observations (default 20000; 0: no limit) */
-    int reserved;
+    int fp64_intrinsics;     /* 1: requests with 11/16-parameter cameras are solved in FP64 even when the
+                                server's precision is mixed (default 1: with FP32 Jacobian columns for the
+                                intrinsics, LM converges slowly or stalls short of the FP64 minimum) */
 } psba_server_opts;
 
 typedef struct psba_request_result {
@@ -346,24 +374,29 @@ int psba_server_destroy(psba_server *s);
 
 /* ---- cost evaluation without device allocation ------------------------ */
 
-/* Sum of squared reprojection residuals (what psba_eval_residual returns in
- * *cost) for callers that cannot allocate device memory when they need it:
- * code running while a CUDA stream is being captured into a graph (cudaMalloc
- * is not allowed then), a serving loop held to a fixed HBM budget, or a host
- * framework that owns all device memory.  No counterpart in the reference.
+/* Sum of squared reprojection residuals of an unweighted problem with
+ * 6-parameter cameras and fixed K (for such a problem, what
+ * psba_eval_residual returns in *cost; it takes no covariances and no 11/16-
+ * parameter cameras), for callers that cannot allocate device memory when
+ * they need it: code running while a CUDA stream is being captured into a
+ * graph (cudaMalloc is not allowed then), a serving loop held to a fixed HBM
+ * budget, or a host framework that owns all device memory.  No counterpart
+ * in the reference.
  *
  * Every pointer is a device pointer the caller owns, in this header's layout
  * (K 5, q0 4, cams 6 per camera; pts 3 per point; meas 2 per observation;
  * obs_pt, obs_cam per observation); *cost (device) receives the result on
- * `stream` (a cudaStream_t, NULL for the default stream).  Nothing is
- * allocated: the scratch (camera tables and block sums) is a fixed 1 MiB
- * array inside the library, held by every GPU that loads it until the
- * process exits.  Limits: n_cams <= 1024, n_obs <= 16,777,216; larger sizes
- * return PSBA_ERR_ARG.  The first call on a device looks up the array's
+ * `stream` (a cudaStream_t, NULL for the default stream).  The indices are
+ * checked on the device: an observation whose point index is outside
+ * 0..n_pts-1 or camera index outside 0..n_cams-1 is skipped and makes *cost
+ * NaN.  Nothing is allocated: the scratch (camera tables and block sums) is a
+ * fixed 1 MiB array inside the library, held by every GPU that loads it until
+ * the process exits.  Limits: n_cams <= 1024, n_obs <= 16,777,216; larger
+ * sizes return PSBA_ERR_ARG.  The first call on a device looks up the array's
  * device address (no allocation); make that first call before any stream
  * capture begins.  All calls on a device share the array and keep the last
  * call's contents, so calls that overlap on the GPU race: order them. */
-int psba_cost_noalloc(int n_cams, int n_obs, const double *K, const double *q0, const double *cams,
+int psba_cost_noalloc(int n_cams, int n_pts, int n_obs, const double *K, const double *q0, const double *cams,
                       const double *pts, const double *meas, const int *obs_pt, const int *obs_cam,
                       double *cost, void *stream);
 

@@ -64,10 +64,11 @@ TRACE_DTYPE = np.dtype([("itno", np.int32), ("kind", np.int32), ("accepted", np.
 
 # every entry point declared in include/psba.h
 EXPORTS = ("psba_default_opts", "psba_create", "psba_destroy", "psba_get_params", "psba_set_params",
-           "psba_reset_params", "psba_set_precision",
+           "psba_reset_params", "psba_set_precision", "psba_set_wait_limit",
            "psba_levmar", "psba_trust_region", "psba_solve_hybrid", "psba_eval_residual",
            "psba_eval_jacobian", "psba_eval_normal", "psba_eval_reduced", "psba_eval_step",
-           "psba_eval_jmultiply", "psba_eval_cholmod", "psba_last_error", "psba_stream",
+           "psba_eval_jmultiply", "psba_eval_cholmod", "psba_eval_dense_solve", "psba_eval_pivot_reciprocal",
+           "psba_last_error", "psba_stream",
            "psba_device_bytes", "psba_version", "psba_set_stage_timing", "psba_set_stage_mask", "psba_get_stage_timing",
            "psba_transfer_bytes", "psba_kernel_launches", "psba_measure_peak", "psba_cost_noalloc",
            "psba_batch_create", "psba_batch_destroy", "psba_batch_levmar", "psba_batch_get_params",
@@ -104,6 +105,7 @@ def lib():
         L.psba_set_params.argtypes = [C.c_void_p, _dp, _dp]
         L.psba_reset_params.argtypes = [C.c_void_p]
         L.psba_set_precision.argtypes = [C.c_void_p, C.c_int]
+        L.psba_set_wait_limit.argtypes = [C.c_void_p, C.c_longlong]
         for f in ("psba_levmar", "psba_trust_region"):
             getattr(L, f).argtypes = [C.c_void_p, C.POINTER(Opts), _ip, C.POINTER(Result)]
         L.psba_solve_hybrid.argtypes = [C.c_void_p, C.POINTER(Opts), C.POINTER(Result)]
@@ -114,6 +116,8 @@ def lib():
         L.psba_eval_step.argtypes = [C.c_void_p, _dp, _ip]
         L.psba_eval_jmultiply.argtypes = [C.c_void_p, _dp, _dp]
         L.psba_eval_cholmod.argtypes = [C.c_int, _dp, _dp]
+        L.psba_eval_dense_solve.argtypes = [C.c_int, _dp, _dp, _dp, _ip]
+        L.psba_eval_pivot_reciprocal.argtypes = [C.c_int, _dp, _dp]
         L.psba_last_error.restype = C.c_char_p
         L.psba_stream.argtypes = [C.c_void_p]
         L.psba_stream.restype = C.c_void_p
@@ -263,6 +267,10 @@ class Solver:
         """Precision of the eval_* stages: PREC_FP64 or PREC_MIXED."""
         _check(lib().psba_set_precision(self.h, int(precision)))
 
+    def set_wait_limit(self, polls=0):
+        """Polls per device-side wait before it reports a stall (0: default)."""
+        _check(lib().psba_set_wait_limit(self.h, int(polls)))
+
     def reset_params(self):
         """Back to the initial estimate given at creation (device-side copy)."""
         _check(lib().psba_reset_params(self.h))
@@ -339,6 +347,27 @@ def cholmod(S):
     return S, E
 
 
+def dense_solve(S, b):
+    """The solver's dense reduced-camera solve on the device: (status, x)
+    with x = S^-1 b (S's lower triangle read); status 0 factored, 1 a pivot
+    not positive/finite/normal, 2 a device-side wait ran out."""
+    S = np.ascontiguousarray(S, dtype=np.float64)
+    n = S.shape[0]
+    b = _f64(b)
+    x = np.full(n, np.nan)
+    st = C.c_int(-1)
+    _check(lib().psba_eval_dense_solve(n, _d(S), _d(b), _d(x), C.byref(st)))
+    return st.value, x
+
+
+def pivot_reciprocal(x):
+    """The dense factor's pivot reciprocal, evaluated on the device."""
+    x = _f64(x).ravel()
+    y = np.empty_like(x)
+    _check(lib().psba_eval_pivot_reciprocal(x.size, _d(x), _d(y)))
+    return y
+
+
 def version():
     return lib().psba_version().decode()
 
@@ -347,7 +376,12 @@ def kernel_launches():
     return int(lib().psba_kernel_launches())
 
 
+PEAK_KINDS = {"fp64": 0, "fp32": 1, "dmma_m8n8k4": 2, "dmma_m16n8k16": 3}
+
+
 def measure_peak(which="fp64"):
+    """Measured throughput in TFLOP/s of the current device: "fp64" / "fp32"
+    FMA chains, or the FP64 tensor cores ("dmma_m8n8k4", "dmma_m16n8k16")."""
     t = C.c_double()
-    _check(lib().psba_measure_peak(0 if which == "fp64" else 1, C.byref(t)))
+    _check(lib().psba_measure_peak(PEAK_KINDS[which], C.byref(t)))
     return t.value

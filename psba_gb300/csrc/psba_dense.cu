@@ -20,6 +20,7 @@
 // iteration budget sets status 2 and the kernel completes.
 #include <cfloat>
 #include <cooperative_groups.h>
+#include <mutex>
 #include <vector>
 
 #include "psba_internal.h"
@@ -45,36 +46,13 @@ constexpr int TT = TILE * TILE;
 #define PSBA_CHOL_PER_SM 1  // the panel's FP64 chain runs alone on its SM
 #endif
 constexpr int CF_THREADS = PSBA_CHOL_THREADS;
-constexpr long long SPIN_LIMIT = 1LL << 22;  // ~0.5 s of polling with 64 ns sleeps
+// Polls per wait (each poll an acquire load and a 64 ns sleep; the default,
+// 2^22, is ~0.5 s) come from the launch: a handle can shorten the bound
+// (psba_set_wait_limit).  Thread 0 of each CTA stores it here at entry.
+__shared__ long long s_spin_limit;
 constexpr int BJ = PSBA_CHOL_BJ;             // update steps staged per batch in a tile task
 static_assert(BJ >= 2, "the diagonal factor reuses two staging tiles");
 
-#ifdef PSBA_CHOL_TRACE
-// Timing probe (off in the library): per task, the global timer at its
-// start, after its updates, after its factor / triangular solve, at its end.
-__device__ long long g_chol_trace[4 * 65536];
-__device__ __forceinline__ void trace_mark(int t, int k)
-{
-    if (threadIdx.x == 0 && t < 65536) {
-        long long v;
-        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(v));
-        g_chol_trace[4 * t + k] = v;
-    }
-}
-#define CHOL_MARK(t, k) trace_mark(t, k)
-// back-solve step K of the cluster solve, on the step's owner: clock64 into
-// shared memory (a global store before the barrier's release would delay it),
-// copied out after the solve
-#define TRI_TRACE_STEPS 128
-#define TRI_MARK(K, k)                                                                                       \
-    do {                                                                                                     \
-        if (threadIdx.x == 0 && (K) % 8 == (int)cg::this_cluster().block_rank() && (K) < TRI_TRACE_STEPS) \
-            tri_tr[(K)][(k)] = clock64();                                                                    \
-    } while (0)
-#else
-#define CHOL_MARK(t, k)
-#define TRI_MARK(K, k)
-#endif
 
 __device__ __forceinline__ int ld_acquire(const int *p)
 {
@@ -95,7 +73,8 @@ __device__ bool block_wait(const int *flag, int epoch, int *status)
     __shared__ int ok;
     if (threadIdx.x == 0) {
         int good = 0;
-        for (long long it = 0; it < SPIN_LIMIT; ++it) {
+        const long long limit = s_spin_limit;
+        for (long long it = 0; it < limit; ++it) {
             if (ld_acquire(flag) == epoch) {
                 good = 1;
                 break;
@@ -712,7 +691,8 @@ struct PanelSide {
         }
         if (!want) return;
         bool up = false;
-        for (long long it = 0; it < SPIN_LIMIT; ++it) {
+        const long long limit = s_spin_limit;
+        for (long long it = 0; it < limit; ++it) {
             // every lane acquires the flags itself, so its own loads below are ordered after them
             up = (fa == nullptr || ld_acquire(fa) == epoch) && (fb == nullptr || ld_acquire(fb) == epoch);
             if (up || *(const volatile int *)fdone) break;
@@ -759,7 +739,7 @@ __global__ void __launch_bounds__(CF_THREADS, 1) k_chol_dataflow(int Np, int nb,
                                                               double *__restrict__ rhs,
                                                               double *__restrict__ pre,
                                                               int *__restrict__ flags, int epoch,
-                                                              int *__restrict__ status)
+                                                              int *__restrict__ status, long long spin_limit)
 {
     static_assert(BJ >= 6, "the panel keeps six tiles in the staging area");
     static_assert(LowerUpdate<true>::PART <= BJ * T * (T + 1), "update_lower's partial sums fit in the staging area");
@@ -770,6 +750,8 @@ __global__ void __launch_bounds__(CF_THREADS, 1) k_chol_dataflow(int Np, int nb,
     const int n_fact = nb * (nb + 1) / 2;
     const int tid = threadIdx.x;
     double *part = &bk[0][0][0];
+    if (tid == 0) s_spin_limit = spin_limit;
+    __syncthreads();
     if (blockIdx.x == 0) {
         // ---- panel.  Step I: warp 4 stores step I-1's outputs (L_{I-1,I-1},
         // its inverse, y_{I-1}, L_{I,I-1}) and raises their flags while the
@@ -798,7 +780,6 @@ __global__ void __launch_bounds__(CF_THREADS, 1) k_chol_dataflow(int Np, int nb,
         __syncthreads();
         for (int I = 0; I < nb; ++I) {
             const int td = tile_task(I, I, nb);
-            CHOL_MARK(td, 0);
             if (I >= 1) {
                 // warp 4 stores step I-1's outputs and raises their flags (its
                 // release waits for the stores, off the pivot chain) while the
@@ -823,7 +804,6 @@ __global__ void __launch_bounds__(CF_THREADS, 1) k_chol_dataflow(int Np, int nb,
                     update_lower<true, CF_THREADS - 32>(wa, lsub, W + PW_B, W + PW_Y, part);
                 }
             }
-            CHOL_MARK(td, 1);
             if (tid == 0) pf_done = 0;
             if (!failed) {
                 PanelSide side{nullptr, nullptr,
@@ -838,7 +818,6 @@ __global__ void __launch_bounds__(CF_THREADS, 1) k_chol_dataflow(int Np, int nb,
             } else {
                 __syncthreads();
             }
-            CHOL_MARK(td, 2);
             if (I + 1 < nb) {
                 // the tile and b are free after the factor: the next diagonal tile goes there
                 if (pf_done) {
@@ -858,7 +837,6 @@ __global__ void __launch_bounds__(CF_THREADS, 1) k_chol_dataflow(int Np, int nb,
                 if (!failed) tile_trsm(lsub, asub, wli);
                 __syncthreads();
             }
-            CHOL_MARK(td, 3);
         }
         // the last step's outputs
         if (!failed) {
@@ -875,7 +853,6 @@ __global__ void __launch_bounds__(CF_THREADS, 1) k_chol_dataflow(int Np, int nb,
         const int I = tasks[t].x, K = tasks[t].y;
         const int kind = I - K;  // 0: PD(I), 1: SUB(K), >= 2: tile (I, K)
         const int mark = kind == 0 ? n_fact + I : kind == 1 ? n_fact + nb + K : tile_task(I, K, nb);
-        CHOL_MARK(mark, 0);
         load_tile(a, S, Np, I, K);
         if (kind == 0 && tid < T) bvec[tid] = __ldcg(rhs + I * T + tid);
         __syncthreads();
@@ -963,7 +940,6 @@ __global__ void __launch_bounds__(CF_THREADS, 1) k_chol_dataflow(int Np, int nb,
             for (int e2 = tid; e2 < TT; e2 += CF_THREADS) pre[(size_t)K * TT + e2] = a[e2 / T][e2 % T];
             block_release(flags + n_fact + 2 * nb + K, epoch);
         }
-        CHOL_MARK(mark, 1);
         const bool failed = block_failed(status);
         if (kind == 0) {
             if (!failed) {
@@ -982,9 +958,7 @@ __global__ void __launch_bounds__(CF_THREADS, 1) k_chol_dataflow(int Np, int nb,
                 store_tile(S, Np, I, K, bi[0]);
             }
         }
-        CHOL_MARK(mark, 2);
         block_release(flags + mark, epoch);
-        CHOL_MARK(mark, 3);
         __syncthreads();
     }
 }
@@ -1005,14 +979,27 @@ void chol_task_list(int nb, std::vector<int2> &tasks)
 
 int chol_grid(int n_tasks, int grid_cap)
 {
-    static int per_sm = -1, sms = 0;
-    if (per_sm < 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_chol_dataflow, CF_THREADS, 0);
-        if (per_sm < 1) per_sm = 1;
-        if (PSBA_CHOL_PER_SM > 0 && per_sm > PSBA_CHOL_PER_SM) per_sm = PSBA_CHOL_PER_SM;
+    // CTAs per SM and SMs, per device (handles on several devices and
+    // several host threads share this cache)
+    static std::mutex mu;
+    static int per_sm_dev[MAX_DEVICES], sms_dev[MAX_DEVICES];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= MAX_DEVICES) dev = 0;
+    int per_sm, sms;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (sms_dev[dev] == 0) {
+            int p = 0, n = 0;
+            cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&p, k_chol_dataflow, CF_THREADS, 0);
+            if (p < 1) p = 1;
+            if (PSBA_CHOL_PER_SM > 0 && p > PSBA_CHOL_PER_SM) p = PSBA_CHOL_PER_SM;
+            per_sm_dev[dev] = p;
+            sms_dev[dev] = n > 0 ? n : 1;
+        }
+        per_sm = per_sm_dev[dev];
+        sms = sms_dev[dev];
     }
     int cap = per_sm * sms;
     if (grid_cap > 0 && grid_cap < cap) cap = grid_cap;
@@ -1097,9 +1084,6 @@ __global__ void __launch_bounds__(TC_THREADS) k_tri_cluster(int Np, int nb,
     static_assert(TC_THREADS == TT, "one thread per term of the 16 x 16 diagonal product");
     extern __shared__ double vec[];  // Np; this CTA's blocks are the valid ones
     __shared__ double xb[2][T], xs[2][T];
-#ifdef PSBA_CHOL_TRACE
-    __shared__ long long tri_tr[TRI_TRACE_STEPS][8];
-#endif
     cg::cluster_group cl = cg::this_cluster();
     const int rank = (int)cl.block_rank(), tid = threadIdx.x;
     if (*status != 0) return;  // the same word for every CTA: all leave together
@@ -1151,18 +1135,14 @@ __global__ void __launch_bounds__(TC_THREADS) k_tri_cluster(int Np, int nb,
         int pend = -1;
         auto step = [&](int K, double &pl, double &pln, double (&cf)[4], double (&cfn)[4], double (&df)[4],
                         double (&dfn)[4]) {
-            TRI_MARK(K, 0);
             if (mine(K)) {
                 const double xv = half_warp_sum(pl * vec[K * T + dk]);
                 if (dk == 0) xb[K & 1][dr] = xv;
             }
-            TRI_MARK(K, 1);
             __syncthreads();
             // x_K replaces y_K in the owner's vector (no global store before the release)
             if (mine(K) && tid < T) vec[K * T + tid] = xb[K & 1][tid];
-            TRI_MARK(K, 2);
             cl_arrive();
-            TRI_MARK(K, 3);
             pln = K > 0 ? ldiag(K - 1) : 0.0;
             lcrit(K - 1, cfn);
             ldef(K, dfn);
@@ -1172,15 +1152,11 @@ __global__ void __launch_bounds__(TC_THREADS) k_tri_cluster(int Np, int nb,
                           [&](int r, int c) { return __ldcg(S + (size_t)(P * T + r) * Np + c); },
                           [&](int q) { return entry_between(-1, q); });
             }
-            TRI_MARK(K, 4);
             cl_wait();
-            TRI_MARK(K, 5);
             if (tid < T) xs[K & 1][tid] = cl.map_shared_rank(&xb[K & 1][0], K % TC_CTAS)[tid];
             __syncthreads();
-            TRI_MARK(K, 6);
             if (mine(K - 1)) crit_apply(xs[K & 1], cf, (K - 1) * T + cq);
             __syncthreads();
-            TRI_MARK(K, 7);
             pend = K;
         };
         double plA = ldiag(nb - 1), plB = 0.0, cfA[4], cfB[4], dfA[4] = {0.0, 0.0, 0.0, 0.0}, dfB[4];
@@ -1195,10 +1171,6 @@ __global__ void __launch_bounds__(TC_THREADS) k_tri_cluster(int Np, int nb,
         for (int I = rank; I < nb; I += TC_CTAS)
             if (tid < T) x[I * T + tid] = vec[I * T + tid];
     }
-#ifdef PSBA_CHOL_TRACE
-    for (int K = rank; K < nb && K < TRI_TRACE_STEPS; K += TC_CTAS)
-        if (tid < 8) g_chol_trace[4 * 40000 + 8 * K + tid] = tri_tr[K][tid];
-#endif
 }
 
 void launch_chol_dataflow(const DeviceProblem &d, int epoch, double *x_out, cudaStream_t s)
@@ -1211,7 +1183,8 @@ void launch_chol_dataflow(const DeviceProblem &d, int epoch, double *x_out, cuda
         const int2 *tasks = d.chol_tasks;
         double *S = d.S, *Linv = d.Linv, *rhs = d.rhs, *pre = d.chol_pre;
         int *flags = d.chol_flags, *status = d.status;
-        void *args[] = {&Np, &nb, &n_tasks, (void *)&tasks, &S, &Linv, &rhs, &pre, &flags, &epoch, &status};
+        long long spin = d.wait_limit;
+        void *args[] = {&Np, &nb, &n_tasks, (void *)&tasks, &S, &Linv, &rhs, &pre, &flags, &epoch, &status, &spin};
         cudaMemsetAsync(d.status, 0, 2 * sizeof(int), s);
         cudaLaunchCooperativeKernel((const void *)k_chol_dataflow, dim3(grid), dim3(CF_THREADS), args, 0, s);
         note_launch(1);
@@ -1440,3 +1413,96 @@ void launch_cholmod(double *S, int n, int ld, double *E, double *work, cudaStrea
 }
 
 }  // namespace psba
+
+// ---------------------------------------------------------------------------
+// Diagnostic entry points for the parity tests: the dense solve on a caller
+// matrix, and the pivot chain's reciprocal.
+namespace psba {
+
+__global__ void k_pivot_reciprocal(int n, const double *__restrict__ x, double *__restrict__ y)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = rcp_fast(x[i]);
+}
+
+}  // namespace psba
+
+extern "C" int psba_eval_pivot_reciprocal(int n, const double *x, double *y)
+{
+    using namespace psba;
+    if (n < 0 || (n > 0 && (!x || !y))) return set_error("psba_eval_pivot_reciprocal: bad arguments"), PSBA_ERR_ARG;
+    if (n == 0) return PSBA_OK;
+    double *dx = nullptr, *dy = nullptr;
+    cudaError_t e = cudaMalloc(&dx, sizeof(double) * (size_t)n);
+    if (e == cudaSuccess) e = cudaMalloc(&dy, sizeof(double) * (size_t)n);
+    if (e == cudaSuccess) e = cudaMemcpy(dx, x, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        k_pivot_reciprocal<<<(n + 255) / 256, 256>>>(n, dx, dy);
+        note_launch(1);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(y, dy, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost);
+    cudaFree(dx);
+    cudaFree(dy);
+    if (e != cudaSuccess) return set_error(std::string("CUDA error: ") + cudaGetErrorString(e)), PSBA_ERR_CUDA;
+    return PSBA_OK;
+}
+
+// The handle's dense solve (k_chol_dataflow + the back solve) on an n x n
+// matrix given by the caller: S row-major, lower triangle read; padded to a
+// multiple of TILE with an identity block.
+extern "C" int psba_eval_dense_solve(int n, const double *S, const double *b, double *x, int *status)
+{
+    using namespace psba;
+    if (n <= 0 || n > 4096 || !S || !b || !x || !status)
+        return set_error("psba_eval_dense_solve: n must be in 1..4096 and every pointer set"), PSBA_ERR_ARG;
+    DeviceProblem d;
+    d.Np = ((n + TILE - 1) / TILE) * TILE;
+    const int Np = d.Np, nb = Np / TILE;
+    std::vector<int2> tasks;
+    chol_task_list(nb, tasks);
+    d.chol_n_tasks = (int)tasks.size();
+    d.chol_n_flags = nb * (nb + 1) / 2 + 3 * nb;
+    std::vector<double> hS((size_t)Np * Np, 0.0), hb(Np, 0.0);
+    for (int r = 0; r < Np; ++r)
+        for (int c = 0; c <= r; ++c) hS[(size_t)r * Np + c] = (r < n && c < n) ? S[(size_t)r * n + c] : (r == c ? 1.0 : 0.0);
+    for (int r = 0; r < n; ++r) hb[r] = b[r];
+    cudaStream_t st = nullptr;
+    std::vector<void *> mem;
+    cudaError_t e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    auto get = [&](auto **p, size_t count) {
+        if (e != cudaSuccess) return;
+        e = cudaMalloc((void **)p, sizeof(**p) * (count ? count : 1));
+        if (e == cudaSuccess) mem.push_back((void *)*p);
+    };
+    get(&d.S, (size_t)Np * Np);
+    get(&d.rhs, (size_t)Np);
+    get(&d.xsol, (size_t)Np);
+    get(&d.Linv, (size_t)Np * TILE);
+    get(&d.chol_pre, (size_t)nb * TILE * TILE);
+    get(&d.chol_tasks, tasks.size());
+    get(&d.chol_flags, (size_t)d.chol_n_flags);
+    get(&d.status, 4);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d.S, hS.data(), sizeof(double) * hS.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d.rhs, hb.data(), sizeof(double) * Np, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && !tasks.empty())
+        e = cudaMemcpyAsync(d.chol_tasks, tasks.data(), sizeof(int2) * tasks.size(), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d.chol_flags, 0, sizeof(int) * d.chol_n_flags, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d.status, 0, sizeof(int) * 4, st);
+    if (e == cudaSuccess) {
+        launch_chol_dataflow(d, 1, d.xsol, st);
+        e = cudaGetLastError();
+    }
+    int hst[4] = {0, 0, 0, 0};
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hst, d.status, sizeof(hst), cudaMemcpyDeviceToHost, st);
+    std::vector<double> hx(Np);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hx.data(), d.xsol, sizeof(double) * Np, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    for (void *p : mem) cudaFree(p);
+    if (st) cudaStreamDestroy(st);
+    if (e != cudaSuccess) return set_error(std::string("CUDA error: ") + cudaGetErrorString(e)), PSBA_ERR_CUDA;
+    *status = hst[0];
+    if (hst[0] == 0)
+        for (int r = 0; r < n; ++r) x[r] = hx[r];
+    return PSBA_OK;
+}

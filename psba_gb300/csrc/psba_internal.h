@@ -81,6 +81,10 @@ long long launch_count();
 
 // ---- kernel launchers (psba_kernels.cu) ---------------------------------
 
+// Polls per device-side wait before it gives up and reports status 2 (the
+// dense factor's flag waits sleep 64 ns per poll: ~0.5 s in all).
+constexpr long long DEFAULT_WAIT_LIMIT = 1LL << 22;
+
 struct DeviceProblem {
     int nc = 0, np = 0, no = 0, N = 0, Np = 0;  // N = cnp nc, Np = N padded to TILE
     int cnp = 6;                // parameters per camera: 6, 11 or 16
@@ -150,6 +154,7 @@ struct DeviceProblem {
     int2 *chol_tasks = nullptr;   // helper tasks of the dense factor, in dependency order
     int chol_n_tasks = 0;
     int chol_grid_cap = 0;        // CTAs of the dense factor at most (0: one per SM)
+    long long wait_limit = DEFAULT_WAIT_LIMIT;  // polls per device-side wait (dense factor flags, Y copies)
     double *chol_pre = nullptr;   // second-subdiagonal tiles before their solve (Np / TILE tiles)
     int *chol_flags = nullptr;    // one flag per dataflow task (value = epoch when done)
     int chol_n_flags = 0;
@@ -183,6 +188,10 @@ int residual_blocks(const DeviceProblem &d);
 // Damping trial: V^-1, Y, Schur complement, ea.
 void launch_vinv(const DeviceProblem &d, double mu, cudaStream_t s);
 void launch_yblocks(const DeviceProblem &d, cudaStream_t s);
+// Per-device kernel attributes (dynamic shared-memory opt-ins); call with the
+// device current before the first launch on it.
+constexpr int MAX_DEVICES = 64;
+int prepare_device_kernels();
 void launch_schur(const DeviceProblem &d, double mu, cudaStream_t s);
 void launch_schur_off(const DeviceProblem &d, cudaStream_t s);
 // threads of one resident wave of the 6-parameter off-diagonal Schur kernel on this device

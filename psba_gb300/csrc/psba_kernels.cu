@@ -8,6 +8,8 @@
 //   22); U 36 per camera; g = [ga (6C) | gb (3P)].
 // Every reduction runs in a fixed order (no floating-point atomics), so a
 // solve is bit-for-bit repeatable.
+#include <mutex>
+
 #include "psba_internal.h"
 
 namespace psba {
@@ -646,9 +648,14 @@ __device__ __forceinline__ void vinv_one(const R *Vi, R mu, R *out)
 // is kept in FP64: for a point seen from two nearby cameras V_i is nearly
 // singular, and an FP32 V_i + mu I (which drops mu) or an FP32 V^-1 moves the
 // LM fixed point by ~1e-2 of the cost.
-__global__ void k_vinv(int np, const double *__restrict__ V, double mu, double *__restrict__ Vinv)
+// Each damping trial starts here, so this launch also clears the status word
+// of the trial's bulk copies (status[2], set by k_yblocks_bulk when a wait
+// runs out), which nothing else resets.
+__global__ void k_vinv(int np, const double *__restrict__ V, double mu, double *__restrict__ Vinv,
+                       int *__restrict__ status)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) status[2] = 0;
     if (i >= np) return;
     double vi[6], out[6];
     for (int e = 0; e < 6; ++e) vi[e] = V[6 * (size_t)i + e];
@@ -659,7 +666,7 @@ __global__ void k_vinv(int np, const double *__restrict__ V, double mu, double *
 void launch_vinv(const DeviceProblem &d, double mu, cudaStream_t s)
 {
     if (d.np == 0) return;
-    k_vinv<<<ceil_div(d.np, 128), 128, 0, s>>>(d.np, d.V, mu, d.Vinv);
+    k_vinv<<<ceil_div(d.np, 128), 128, 0, s>>>(d.np, d.V, mu, d.Vinv, d.status);
     note_launch(1);
 }
 
@@ -733,15 +740,19 @@ __device__ __forceinline__ void bulk_s2g(void *dst, const void *src, unsigned by
 // each thread forms its row of Y there (16-byte shared loads at a 144-byte
 // stride: no bank conflicts), and one bulk copy writes the CTA's Y rows
 // back.  Same arithmetic as k_yblocks.  A copy that does not complete within
-// the poll budget sets status[2] (the trial then reports the wait budget
-// exhausted) and the CTA leaves.
+// poll_limit polls sets status[2] (the trial then reports the wait budget
+// exhausted); the CTA then waits for the copy to land in its shared memory
+// (at most YB_DRAIN_LIMIT polls: a bulk copy of 37 KB from this GPU's own
+// memory completes in microseconds) before it leaves.  Should the drain wait
+// also run out, the CTA leaves with the copy possibly still in flight; that
+// needs a copy stalled for the whole drain budget, which no test provokes.
 constexpr int YB_ROWS = 256;
-constexpr long long YB_POLL_LIMIT = 1LL << 22;
+constexpr long long YB_DRAIN_LIMIT = 1LL << 22;
 
 __global__ void __launch_bounds__(YB_ROWS) k_yblocks_bulk(int no, const int *__restrict__ obs_pt,
                                                           const double *__restrict__ W,
                                                           const double *__restrict__ Vinv, double *__restrict__ Y,
-                                                          int *__restrict__ status)
+                                                          int *__restrict__ status, long long poll_limit)
 {
     extern __shared__ __align__(16) double yb_sm[];  // W rows, then Y rows
     __shared__ __align__(8) unsigned long long bar;
@@ -757,9 +768,9 @@ __global__ void __launch_bounds__(YB_ROWS) k_yblocks_bulk(int no, const int *__r
         s00 = __ldg(vi); s01 = __ldg(vi + 1); s02 = __ldg(vi + 2);
         s11 = __ldg(vi + 3); s12 = __ldg(vi + 4); s22 = __ldg(vi + 5);
     }
-    if (!mbar_wait0(&bar, YB_POLL_LIMIT)) {
+    if (!mbar_wait0(&bar, poll_limit)) {
         if (t == 0) atomicExch(status + 2, 2);
-        mbar_wait0(&bar, YB_POLL_LIMIT);  // the copy may still land in this CTA's memory
+        mbar_wait0(&bar, YB_DRAIN_LIMIT);  // the copy may still land in this CTA's memory
         return;
     }
     if (t < rows) {
@@ -787,18 +798,35 @@ __global__ void __launch_bounds__(YB_ROWS) k_yblocks_bulk(int no, const int *__r
     if (t == 0) bulk_s2g(Y + 18 * (size_t)o0, sy, bytes);
 }
 
+// The bulk Y kernel's dynamic shared memory (73,728 B) is above the default
+// 48 KB limit; the opt-in is a per-device attribute, so it is set once for
+// every device a handle is created on, with that device current.
+int prepare_device_kernels()
+{
+    static std::mutex mu;
+    static bool done[MAX_DEVICES] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_error(std::string("cudaGetDevice: ") + cudaGetErrorString(e)), PSBA_ERR_CUDA;
+    if (dev < 0 || dev >= MAX_DEVICES) return set_error("device index out of range"), PSBA_ERR_ARG;
+    std::lock_guard<std::mutex> lk(mu);
+    if (done[dev]) return PSBA_OK;
+    e = cudaFuncSetAttribute(k_yblocks_bulk, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(2 * YB_ROWS * 18 * sizeof(double)));
+    if (e != cudaSuccess)
+        return set_error(std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e)), PSBA_ERR_CUDA;
+    done[dev] = true;
+    return PSBA_OK;
+}
+
 void launch_yblocks(const DeviceProblem &d, cudaStream_t s)
 {
     if (d.cnp != 6) return launch_yblocks_v(d, s);
     if (d.no == 0) return;
     if (d.prec == PSBA_PREC_FP64) {
-        static bool smem_set = false;
         const int smem = (int)(2 * YB_ROWS * 18 * sizeof(double));
-        if (!smem_set) {
-            cudaFuncSetAttribute(k_yblocks_bulk, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-            smem_set = true;
-        }
-        k_yblocks_bulk<<<ceil_div(d.no, YB_ROWS), YB_ROWS, smem, s>>>(d.no, d.obs_pt, d.W, d.Vinv, d.Y, d.status);
+        k_yblocks_bulk<<<ceil_div(d.no, YB_ROWS), YB_ROWS, smem, s>>>(d.no, d.obs_pt, d.W, d.Vinv, d.Y, d.status,
+                                                                      d.wait_limit);
     } else
         k_yblocks<float><<<ceil_div(d.no, 256), 256, 0, s>>>(d.no, d.obs_pt, (const float *)d.W, d.Vinv,
                                                                (float *)d.Y);

@@ -5,10 +5,18 @@
 // (cudaMalloc is not allowed during capture), a serving loop that admits work
 // against a fixed HBM budget and must not grow its footprint per request, or
 // a host framework that owns all device memory and hands out only its own
-// buffers.  This entry point evaluates the same cost as psba_eval_residual
-// (the reference's compute_exQT + compute_L2_sq) on arrays the caller already
+// buffers.  This entry point evaluates the cost psba_eval_residual returns
+// for an unweighted problem with 6-parameter cameras and fixed K (the
+// reference's compute_exQT + compute_L2_sq) on arrays the caller already
 // holds on the device, with its scratch in a fixed array that is part of the
-// library image instead of a cudaMalloc'd buffer.
+// library image instead of a cudaMalloc'd buffer.  It takes no covariances
+// and no 11/16-parameter cameras: for those, psba_eval_residual's cost
+// differs from this one.
+//
+// The observation indices come from caller memory and are not seen by the
+// host, so the kernel checks them: an observation whose point index is
+// outside 0..n_pts-1 or whose camera index is outside 0..n_cams-1 is not
+// read through, and it makes the result NaN.
 //
 // The scratch array is shared by every call on a device and keeps the last
 // call's contents.  Calls that overlap on the GPU (two streams, or two host
@@ -35,13 +43,14 @@ static_assert(SCRATCH_DOUBLES * sizeof(double) <= (1u << 20), "scratch above 1 M
 // Every GPU that loads the library holds this array until the process exits.
 static __device__ __align__(256) double g_scratch[SCRATCH_DOUBLES];
 
-constexpr int MAX_DEVICES = 64;
 static double *g_ptr[MAX_DEVICES];
 static std::mutex g_mu;
 
 // Device address of g_scratch for the current device, looked up once per
 // device with that device current.  Host code only ever passes this address
-// to kernels; g_scratch itself is a host-side stand-in on the host.
+// to kernels; g_scratch itself is a host-side stand-in on the host.  The
+// cached address assumes the device's primary context lives as long as the
+// process (no cudaDeviceReset between calls).
 static int scratch_address(double **out)
 {
     int dev = 0;
@@ -89,8 +98,9 @@ __global__ void k_tables(int nc, const double *__restrict__ K, const double *__r
     o[43] = k[2];
 }
 
-// Squared residuals, one partial sum per block of THREADS observations.
-__global__ void __launch_bounds__(THREADS) k_sq(int no, const int *__restrict__ obs_pt,
+// Squared residuals, one partial sum per block of THREADS observations.  An
+// observation with an index out of range is skipped and contributes NaN.
+__global__ void __launch_bounds__(THREADS) k_sq(int nc, int np, int no, const int *__restrict__ obs_pt,
                                                 const int *__restrict__ obs_cam,
                                                 const double *__restrict__ meas,
                                                 const double *__restrict__ pts,
@@ -102,16 +112,20 @@ __global__ void __launch_bounds__(THREADS) k_sq(int no, const int *__restrict__ 
     double sq = 0.0;
     if (o < no) {
         const int i = obs_pt[o], j = obs_cam[o];
-        const double X0 = pts[3 * i], X1 = pts[3 * i + 1], X2 = pts[3 * i + 2];
-        const double *T = tab + (size_t)CAMTAB * j;
-        const double xc = T[0] * X0 + T[1] * X1 + T[2] * X2 + T[36];
-        const double yc = T[3] * X0 + T[4] * X1 + T[5] * X2 + T[37];
-        const double zc = T[6] * X0 + T[7] * X1 + T[8] * X2 + T[38];
-        const double iz = 1.0 / zc;
-        const double u = (T[39] * xc + T[40] * yc + T[41] * zc) * iz;
-        const double v = (T[42] * yc + T[43] * zc) * iz;
-        const double e0 = meas[2 * (size_t)o] - u, e1 = meas[2 * (size_t)o + 1] - v;
-        sq = e0 * e0 + e1 * e1;
+        if (i < 0 || i >= np || j < 0 || j >= nc) {
+            sq = NAN;
+        } else {
+            const double X0 = pts[3 * i], X1 = pts[3 * i + 1], X2 = pts[3 * i + 2];
+            const double *T = tab + (size_t)CAMTAB * j;
+            const double xc = T[0] * X0 + T[1] * X1 + T[2] * X2 + T[36];
+            const double yc = T[3] * X0 + T[4] * X1 + T[5] * X2 + T[37];
+            const double zc = T[6] * X0 + T[7] * X1 + T[8] * X2 + T[38];
+            const double iz = 1.0 / zc;
+            const double u = (T[39] * xc + T[40] * yc + T[41] * zc) * iz;
+            const double v = (T[42] * yc + T[43] * zc) * iz;
+            const double e0 = meas[2 * (size_t)o] - u, e1 = meas[2 * (size_t)o + 1] - v;
+            sq = e0 * e0 + e1 * e1;
+        }
     }
     red[threadIdx.x] = sq;
     __syncthreads();
@@ -140,7 +154,7 @@ __global__ void k_total(const double *__restrict__ partial, int n, double *__res
 }  // namespace noalloc
 }  // namespace psba
 
-extern "C" int psba_cost_noalloc(int n_cams, int n_obs, const double *K, const double *q0, const double *cams,
+extern "C" int psba_cost_noalloc(int n_cams, int n_pts, int n_obs, const double *K, const double *q0, const double *cams,
                                  const double *pts, const double *meas, const int *obs_pt, const int *obs_cam,
                                  double *cost, void *stream)
 {
@@ -148,6 +162,7 @@ extern "C" int psba_cost_noalloc(int n_cams, int n_obs, const double *K, const d
     using namespace psba::noalloc;
     if (n_cams <= 0 || n_cams > MAX_CAMS)
         return set_error("psba_cost_noalloc: n_cams must be in 1.." + std::to_string(MAX_CAMS)), PSBA_ERR_ARG;
+    if (n_pts < 0) return set_error("psba_cost_noalloc: n_pts must be >= 0"), PSBA_ERR_ARG;
     if (n_obs < 0 || n_obs > MAX_OBS)
         return set_error("psba_cost_noalloc: n_obs must be in 0.." + std::to_string(MAX_OBS)), PSBA_ERR_ARG;
     if (!K || !q0 || !cams || !cost || (n_obs > 0 && (!pts || !meas || !obs_pt || !obs_cam)))
@@ -161,7 +176,7 @@ extern "C" int psba_cost_noalloc(int n_cams, int n_obs, const double *K, const d
     const int nblocks = n_obs > 0 ? (n_obs + THREADS - 1) / THREADS : 1;
     k_tables<<<(n_cams + 127) / 128, 128, 0, s>>>(n_cams, K, q0, cams, tab);
     note_launch(1);
-    k_sq<<<nblocks, THREADS, 0, s>>>(n_obs, obs_pt, obs_cam, meas, pts, tab, partial);
+    k_sq<<<nblocks, THREADS, 0, s>>>(n_cams, n_pts, n_obs, obs_pt, obs_cam, meas, pts, tab, partial);
     note_launch(1);
     k_total<<<1, THREADS, 0, s>>>(partial, nblocks, cost);
     note_launch(1);

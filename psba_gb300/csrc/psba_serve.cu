@@ -394,7 +394,12 @@ void large_main(psba_server *s)
         int rc = psba_create(&desc, &h);
         // the lanes' dense factors run side by side: each takes its share of the SMs
         if (rc == PSBA_OK) set_chol_grid_cap(h, s->large_chol_cap);
-        if (rc == PSBA_OK) rc = psba_levmar(h, &s->lm, &itno, &res);
+        // cameras with intrinsics (11/16 parameters) in FP64 when the server
+        // asks for it: their mixed-form Jacobian columns lose the
+        // ill-conditioned intrinsics directions (slow or stalled convergence)
+        psba_opts lm = s->lm;
+        if (r->cnp != 6 && s->so.fp64_intrinsics) lm.precision = PSBA_PREC_FP64;
+        if (rc == PSBA_OK) rc = psba_levmar(h, &lm, &itno, &res);
         r->cams.resize((size_t)r->cnp * r->nc);
         r->pts.resize(3 * (size_t)r->np);
         if (rc == PSBA_OK) rc = psba_get_params(h, r->cams.data(), r->pts.data());
@@ -472,6 +477,7 @@ void psba_server_default_opts(psba_server_opts *o)
     o->large_lanes = 4;
     o->large_share = 0.25;
     o->large_obs = 20000;
+    o->fp64_intrinsics = 1;
 }
 
 int psba_server_create(const psba_server_opts *so, const psba_opts *lm, psba_server **out)

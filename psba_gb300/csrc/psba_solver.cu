@@ -1190,6 +1190,13 @@ int psba_create(const psba_problem_desc *desc, psba_handle **out)
     psba_handle *h = new (std::nothrow) psba_handle();
     if (!h) return set_error("host allocation failed"), PSBA_ERR_NOMEM;
     keep_pool_memory();
+    {
+        const int r = prepare_device_kernels();
+        if (r != PSBA_OK) {
+            destroy_impl(h);
+            return r;
+        }
+    }
     cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreate(&h->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&h->ev1);
@@ -1470,6 +1477,15 @@ int psba_transfer_bytes(psba_handle *h, size_t *h2d, size_t *d2h)
     if (!h) return set_error("null handle"), PSBA_ERR_ARG;
     if (h2d) *h2d = h->h2d_bytes;
     if (d2h) *d2h = h->d2h_bytes;
+    return PSBA_OK;
+}
+
+int psba_set_wait_limit(psba_handle *h, long long polls)
+{
+    if (!h) return set_error("null handle"), PSBA_ERR_ARG;
+    if (polls < 0) return set_error("psba_set_wait_limit: polls must be >= 0"), PSBA_ERR_ARG;
+    TRY(sync(h));
+    h->d.wait_limit = polls == 0 ? DEFAULT_WAIT_LIMIT : polls;
     return PSBA_OK;
 }
 

@@ -26,7 +26,7 @@ class ServerOpts(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_double), ("max_active", C.c_int), ("slice_iters", C.c_int),
                 ("threads", C.c_int), ("lanes_per_pair", C.c_int), ("large_cams", C.c_int),
                 ("large_lanes", C.c_int), ("large_share", C.c_double), ("large_obs", C.c_int),
-                ("reserved", C.c_int)]
+                ("fp64_intrinsics", C.c_int)]
 
 
 class RequestResult(C.Structure):
@@ -79,7 +79,7 @@ class Request:
 class Server:
     def __init__(self, precision=PREC_FP64, max_iter=15, hbm_budget_bytes=120e9, max_active=1024,
                  slice_iters=1, threads=256, lanes_per_pair=32, large_cams=None, large_lanes=None,
-                 large_share=None, large_obs=None, **lm):
+                 large_share=None, large_obs=None, fp64_intrinsics=None, **lm):
         L = _bind()
         so = ServerOpts()
         L.psba_server_default_opts(C.byref(so))
@@ -96,6 +96,8 @@ class Server:
             so.large_share = float(large_share)
         if large_obs is not None:
             so.large_obs = int(large_obs)
+        if fp64_intrinsics is not None:
+            so.fp64_intrinsics = int(bool(fp64_intrinsics))
         o = default_opts(precision=precision, max_iter=max_iter, allow_switch=0, **lm)
         h = C.c_void_p()
         _check(L.psba_server_create(C.byref(so), C.byref(o), C.byref(h)))

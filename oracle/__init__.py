@@ -136,7 +136,10 @@ class OracleProblem:
 def default_opts(**kw):
     o = Opts()
     lib().orc_default_opts(C.byref(o))
+    names = {f[0] for f in Opts._fields_}
     for k, v in kw.items():
+        if k not in names:
+            raise KeyError(k)
         setattr(o, k, v)
     return o
 

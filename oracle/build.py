@@ -8,6 +8,13 @@
   ``oracle/_ref/libpsba_ref.so``.  It only runs where the reference checkout
   exists; the output is git-ignored and is used to pin the oracle and to
   regenerate ``tests/golden``.
+* ``build_ref_reader()`` compiles the reference's problem-file reader
+  (``PSBA/readparams.cpp`` with ``quat2vec`` from ``PSBA/misc.cpp``, through
+  ``ref_reader_shim.cpp``) into ``oracle/_ref/libpsba_ref_reader.so``, to pin
+  this repository's reader against it.
+
+The reference checkout is taken from ``PSBA_REFERENCE_DIR`` when it is set,
+else from the path where this machine mounts it.
 """
 import os
 import subprocess
@@ -17,6 +24,18 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REFERENCE = os.environ.get("PSBA_REFERENCE_DIR", "/root/reference")
 ORACLE_SO = os.path.join(HERE, "libpsba_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libpsba_ref.so")
+REF_READER_SO = os.path.join(HERE, "_ref", "libpsba_ref_reader.so")
+
+
+def reference_dir():
+    """The reference checkout this recipe reads, or None where it is absent."""
+    return REFERENCE if os.path.isdir(REFERENCE) else None
+
+
+def reference_data_dir():
+    """The reference's example problem files (data/), or None."""
+    d = os.path.join(REFERENCE, "data")
+    return d if os.path.isdir(d) else None
 
 
 def _run(cmd):
@@ -60,6 +79,20 @@ def build_ref(force=False):
     return REF_SO
 
 
+def build_ref_reader(force=False):
+    src = os.path.join(REFERENCE, "PSBA", "readparams.cpp")
+    if not (os.path.isfile(src) and os.path.isfile(os.path.join(REFERENCE, "PSBA", "misc.cpp"))):
+        return None
+    os.makedirs(os.path.dirname(REF_READER_SO), exist_ok=True)
+    shim = os.path.join(HERE, "ref_reader_shim.cpp")
+    if force or _stale(REF_READER_SO, [shim, __file__]):
+        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-w", "-fpermissive",
+              "-I" + os.path.join(REFERENCE, "PSBA"), "-I" + os.path.join(HERE, "ref_stub"),
+              shim, "-o", REF_READER_SO])
+    return REF_READER_SO
+
+
 if __name__ == "__main__":
     print(build_oracle(force="--force" in sys.argv))
     print(build_ref(force="--force" in sys.argv))
+    print(build_ref_reader(force="--force" in sys.argv))

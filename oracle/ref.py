@@ -174,3 +174,46 @@ def matvec(M, v):
     out = np.empty(M.shape[0])
     lib().ref_matVec_mul(M.shape[0], _d(M), _d(_f(v)), _d(out))
     return out
+
+
+# ---------------------------------------------------------------- the reader
+
+_reader = None
+
+
+def reader_available():
+    return _build.build_ref_reader() is not None
+
+
+def read_sba(cams_path, pts_path, cnp=11, filecnp=12):
+    """readInitialSBAEstimate (PSBA/readparams.cpp:444-519) with quat2vec as
+    its input filter, compiled from the reference: returns (motstruct
+    (ncams * cnp + npts * 3), initrot (4 per camera), imgpts (2 per
+    projection, file order), cov (4 per projection) or None, vmask (npts x
+    ncams)), the arrays as the reference's main() receives them
+    (PSBA/main.cpp:102-110)."""
+    global _reader
+    if _reader is None:
+        path = _build.build_ref_reader()
+        if path is None:
+            raise RuntimeError("reference sources are not available on this machine")
+        _reader = C.CDLL(path)
+        _reader.ref_read_sba.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, _ip, _ip, _ip,
+                                         C.POINTER(_dp), C.POINTER(_dp), C.POINTER(_dp), C.POINTER(_dp),
+                                         C.POINTER(C.POINTER(C.c_char))]
+        _reader.ref_reader_free.argtypes = [C.c_void_p]
+    nc, npt, npr = C.c_int(), C.c_int(), C.c_int()
+    ms, ir, ip, cv = _dp(), _dp(), _dp(), _dp()
+    vm = C.POINTER(C.c_char)()
+    _reader.ref_read_sba(str(cams_path).encode(), str(pts_path).encode(), cnp, filecnp, C.byref(nc), C.byref(npt),
+                         C.byref(npr), C.byref(ms), C.byref(ir), C.byref(ip), C.byref(cv), C.byref(vm))
+    n_ms = nc.value * cnp + npt.value * 3
+    out = (np.ctypeslib.as_array(ms, (n_ms,)).copy(), np.ctypeslib.as_array(ir, (4 * nc.value,)).copy(),
+           np.ctypeslib.as_array(ip, (2 * npr.value,)).copy(),
+           np.ctypeslib.as_array(cv, (4 * npr.value,)).copy() if cv else None,
+           np.frombuffer(C.string_at(vm, npt.value * nc.value), dtype=np.int8).reshape(npt.value, nc.value).copy())
+    for p in (ms, ir, ip, cv):
+        if p:
+            _reader.ref_reader_free(C.cast(p, C.c_void_p))
+    _reader.ref_reader_free(C.cast(vm, C.c_void_p))
+    return out

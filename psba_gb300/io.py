@@ -92,7 +92,8 @@ def _quat_in(q):
     mag = np.sqrt((q * q).sum(axis=1))
     sg = np.where(q[:, 0] >= 0.0, 1.0, -1.0)
     v = q[:, 1:] * (sg / mag)[:, None]
-    s = np.sqrt(1.0 - (v * v).sum(axis=1))
+    # the reference's order of operations: 1 - v1^2 - v2^2 - v3^2
+    s = np.sqrt(((1.0 - v[:, 0] * v[:, 0]) - v[:, 1] * v[:, 1]) - v[:, 2] * v[:, 2])
     return np.concatenate([s[:, None], v], axis=1)
 
 

@@ -154,3 +154,18 @@ def test_serve_variable_intrinsics_and_weighted_requests():
     with S.Server(precision=P.PREC_FP64, max_iter=10, hbm_budget_bytes=4e9, large_cams=0) as srv:
         with pytest.raises(P.PSBAError):
             srv.submit(var11)  # no large lane to run it
+
+
+@pytest.mark.parametrize("fp64_intrinsics", [1, 0])
+def test_serve_mixed_server_precision_policy_for_intrinsics(fp64_intrinsics):
+    # a mixed-precision server solves 11-parameter requests in FP64 unless
+    # told otherwise: each result is psba_levmar's in the precision the
+    # policy names
+    var11 = scenes.with_intrinsics(scenes.arc_scene(seed=31, n_cams=8, n_pts=300), 11, seed=32, k_off=0.01)
+    with S.Server(precision=P.PREC_MIXED, max_iter=10, hbm_budget_bytes=4e9,
+                  fp64_intrinsics=fp64_intrinsics) as srv:
+        r = srv.wait(srv.submit(var11))
+    want = P.PREC_FP64 if fp64_intrinsics else P.PREC_MIXED
+    with P.Solver(var11) as s:
+        g = s.levmar(allow_switch=0, max_iter=10, precision=want)
+    assert r.final_cost == g.final_cost and np.array_equal(r.cams, g.cams)

@@ -20,6 +20,7 @@ constexpr int CAMTAB = 56;  // doubles per camera table entry (CamTab)
 constexpr int TILE = 16;    // dense Cholesky tile size
 constexpr int SCHUR_CHUNK = 32;  // pair-list entries per off-diagonal Schur work unit (11/16-parameter cameras)
 constexpr int OFF_MIN_LEN = 8;   // 6-parameter cameras: fewest pair-list entries per off-diagonal chunk
+constexpr int MX_UNIT = 256;     // 6-parameter cameras, FP32 products: pair-list entries per warp unit
 constexpr int DIAG_CHUNK = 16;   // observations per diagonal Schur work unit (11/16-parameter cameras)
 constexpr int SD_THREADS = 128, SD_PER = 8;     // 6-parameter cameras: one CTA per unit, 8 observations a thread
 constexpr int DIAG_SUPER = SD_THREADS * SD_PER;  // observations per diagonal unit, 6-parameter cameras
@@ -116,6 +117,11 @@ struct DeviceProblem {
     // of one resident wave, a slot per pair a chunk touches
     SchurUnit *off_chunks = nullptr;
     int n_off_chunks = 0;
+    // 6-parameter cameras, FP32 products: units of <= MX_UNIT entries of one
+    // pair, one warp and one slot each, longest first
+    SchurUnit *mx_units = nullptr;
+    int n_mx_units = 0;
+    int *mx_unit_start = nullptr;  // per pair: first unit (n_pairs + 1)
     int n_off_chunk_slots = 0;
     int *off_chunk_start = nullptr;  // per pair: first slot (n_pairs + 1)
     int *pair_start = nullptr;       // per pair: first entry (n_pairs + 1)
@@ -199,7 +205,8 @@ int schur_off_wave_threads();
 // off-diagonal partial slots reserved ahead of the diagonal partials (the larger layout)
 inline size_t off_partial_slots(const DeviceProblem &d)
 {
-    return (size_t)(d.n_off_units > d.n_off_chunk_slots ? d.n_off_units : d.n_off_chunk_slots);
+    size_t n = (size_t)(d.n_off_units > d.n_off_chunk_slots ? d.n_off_units : d.n_off_chunk_slots);
+    return n > (size_t)d.n_mx_units ? n : (size_t)d.n_mx_units;
 }
 void launch_schur_diag(const DeviceProblem &d, cudaStream_t s);
 void launch_schur_reduce(const DeviceProblem &d, double mu, cudaStream_t s);

@@ -841,49 +841,6 @@ void launch_yblocks(const DeviceProblem &d, cudaStream_t s)
 // observations, the 21 lower entries plus the 6 ea sums.  The slots are then
 // summed in order (k_schur_reduce).
 //
-// FP32 products: one thread per unit of <= SCHUR_CHUNK entries of one pair,
-// units longest first; FP32 sums of FLUSH products, then FP64.
-template <typename R>
-__device__ __forceinline__ void schur_off_unit(int uid, int n_units, const SchurUnit *__restrict__ units,
-                                               const int *__restrict__ pa, const int *__restrict__ pb,
-                                               const R *__restrict__ Y, const R *__restrict__ W,
-                                               double *__restrict__ partial)
-{
-    if (uid >= n_units) return;
-    const SchurUnit u = units[uid];
-    double acc[36];
-#pragma unroll
-    for (int e = 0; e < 36; ++e) acc[e] = 0.0;
-    static_assert(!is_fp64<R>(), "FP64 products take the chunked kernel");
-    for (int t0 = 0; t0 < u.count; t0 += FLUSH) {
-        R part[36];
-#pragma unroll
-        for (int e = 0; e < 36; ++e) part[e] = (R)0;
-        const int tend = min(u.count, t0 + FLUSH);
-        for (int t = t0; t < tend; ++t) {
-            const int a = __ldg(pa + u.begin + t), b = __ldg(pb + u.begin + t);
-            R w[18], y[18];
-            ldn<R, 18>(W + 18 * (size_t)b, w);
-            ldn<R, 18>(Y + 18 * (size_t)a, y);
-#pragma unroll
-            for (int r = 0; r < 6; ++r)
-#pragma unroll
-                for (int c = 0; c < 6; ++c) {
-                    R s = part[r * 6 + c];
-                    s = fma(y[3 * r], w[3 * c], s);
-                    s = fma(y[3 * r + 1], w[3 * c + 1], s);
-                    s = fma(y[3 * r + 2], w[3 * c + 2], s);
-                    part[r * 6 + c] = s;
-                }
-        }
-#pragma unroll
-        for (int e = 0; e < 36; ++e) acc[e] += (double)part[e];
-    }
-    double *p = partial + (size_t)u.out * 36;
-#pragma unroll
-    for (int e = 0; e < 36; ++e) p[e] = acc[e];
-}
-
 // FP64 products (6-parameter cameras): the pair list cut into equal chunks,
 // one per thread of one resident wave, so that every SM issues the same
 // number of FP64 multiply-adds; a thread writes its sums to the next slot
@@ -978,12 +935,15 @@ __device__ __forceinline__ void diag_products(const R *y, const R *w, double g0,
 // FP32 products over the thread's observations, then one FP64 addition).
 // The CTA then sums its threads' partials in a fixed order (each output by
 // four threads over 32 partials each, then the four) and writes one partial
-// per unit, so a camera has only a handful for k_schur_reduce.
+// per unit, so a camera has only a handful for k_schur_reduce.  In the mixed
+// form the unit's observation and point indices are first gathered into
+// shared memory (sidx, 2 DIAG_SUPER ints) by the whole CTA, so a thread's
+// walk waits for one L2 round trip per observation instead of three.
 template <typename R>
 __device__ __forceinline__ void schur_diag_cta(const SchurUnit u, const int *__restrict__ cam_obs,
                                                const int *__restrict__ obs_pt, const R *__restrict__ Y,
                                                const R *__restrict__ W, const double *__restrict__ gb,
-                                               double *__restrict__ partial)
+                                               double *__restrict__ partial, int *sidx = nullptr)
 {
     static_assert(SD_THREADS == 128 && DIAG_NV * 4 <= SD_THREADS, "four summing threads per output");
     __shared__ double red[DIAG_NV][SD_THREADS + 1];
@@ -1005,12 +965,19 @@ __device__ __forceinline__ void schur_diag_cta(const SchurUnit u, const int *__r
         }
     } else {
         static_assert(SD_PER <= FLUSH, "one FP32 flush per thread");
+        for (int k = t; k < u.count; k += SD_THREADS) {
+            const int a = __ldg(cam_obs + u.begin + k);
+            sidx[k] = a;
+            sidx[DIAG_SUPER + k] = __ldg(obs_pt + a);
+        }
+        __syncthreads();
         R part[21];
 #pragma unroll
         for (int e = 0; e < 21; ++e) part[e] = (R)0;
+#pragma unroll 2
         for (int o = t * SD_PER; o < o1; ++o) {
-            const int a = __ldg(cam_obs + u.begin + o);
-            const int i = __ldg(obs_pt + a);
+            const int a = sidx[o];
+            const int i = sidx[DIAG_SUPER + o];
             R w[18], y[18];
             ldn<R, 18>(W + 18 * (size_t)a, w);
             ldn<R, 18>(Y + 18 * (size_t)a, y);
@@ -1070,10 +1037,85 @@ int schur_off_wave_threads()
     return threads;
 }
 
-// FP32 products: the off-diagonal units (blocks below off_ctas) and the
-// diagonal units (the rest) in one launch, so the diagonal CTAs run in the
-// off-diagonal units' last wave.
-__global__ void __launch_bounds__(128) k_schur_f32(int n_units, int off_ctas, const SchurUnit *__restrict__ units,
+// FP32 products, 6-parameter cameras: one warp per unit of <= MX_UNIT
+// entries of one camera pair.  The warp first copies the unit's two index
+// lists into shared memory (coalesced), so that each step waits for one L2
+// round trip (the rows) instead of two.  Lane 4 s + q then works on the
+// entries s, s + 8, s + 16, ... of the unit (s = 0..7) and on quadrant q of
+// the 6 x 6 block (rows 3 (q >> 1) .. +2, columns 3 (q & 1) .. +2): it loads
+// the nine Y values of its rows and the nine W values of its columns (the
+// four lanes of an entry read two 36-byte halves of each row, so the
+// requests of a warp instruction are eight rows' worth) and keeps nine FP32
+// sums, in two interleaved sets (entries s, s + 16, ... and s + 8, s + 24,
+// ...: two independent chains of at most 16 products each, added in FP32 at
+// the end, so a lane's sum covers at most 32 products).  The eight entry
+// slots are combined in FP64 by a fixed xor tree and the unit's partial goes
+// to its slot; k_schur_reduce sums a pair's units in order, in FP64.  Every
+// sum has a fixed order, so the result does not depend on scheduling.
+__device__ __forceinline__ void mx_quadrant(const float *__restrict__ Y, const float *__restrict__ W, int a, int b,
+                                            int qr, int qc, float *acc)
+{
+    float y[9], w[9];
+    const float *py = Y + 18 * (size_t)a + 9 * qr, *pw = W + 18 * (size_t)b + 9 * qc;
+#pragma unroll
+    for (int e = 0; e < 9; ++e) {
+        y[e] = __ldg(py + e);
+        w[e] = __ldg(pw + e);
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            float s = acc[3 * i + j];
+            s = fmaf(y[3 * i], w[3 * j], s);
+            s = fmaf(y[3 * i + 1], w[3 * j + 1], s);
+            s = fmaf(y[3 * i + 2], w[3 * j + 2], s);
+            acc[3 * i + j] = s;
+        }
+}
+
+__device__ __forceinline__ void schur_off_warp(const SchurUnit u, const int *__restrict__ pa,
+                                               const int *__restrict__ pb, const float *__restrict__ Y,
+                                               const float *__restrict__ W, int *sidx,
+                                               double *__restrict__ partial)
+{
+    const int lane = threadIdx.x & 31, s = lane >> 2, q = lane & 3, qr = q >> 1, qc = q & 1;
+    int *ia = sidx, *ib = sidx + MX_UNIT;
+    for (int t = lane; t < u.count; t += 32) {
+        ia[t] = __ldg(pa + u.begin + t);
+        ib[t] = __ldg(pb + u.begin + t);
+    }
+    __syncwarp();
+    float a0[9], a1[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) a0[e] = a1[e] = 0.0f;
+    for (int t = s; t < u.count; t += 16) {
+        mx_quadrant(Y, W, ia[t], ib[t], qr, qc, a0);
+        if (t + 8 < u.count) mx_quadrant(Y, W, ia[t + 8], ib[t + 8], qr, qc, a1);
+    }
+    double v[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) {
+        double x = (double)(a0[e] + a1[e]);
+        x += __shfl_xor_sync(0xffffffffu, x, 4);
+        x += __shfl_xor_sync(0xffffffffu, x, 8);
+        x += __shfl_xor_sync(0xffffffffu, x, 16);
+        v[e] = x;
+    }
+    if (s == 0) {
+        double *p = partial + (size_t)u.out * 36 + 18 * qr + 3 * qc;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) p[6 * i + j] = v[3 * i + j];
+    }
+}
+
+// FP32 products: the diagonal units first (one CTA each, blocks below
+// n_diag: they walk their observations one after another, so they start
+// early and run beside the off-diagonal units), then the off-diagonal units
+// (four per block, a warp each).
+__global__ void __launch_bounds__(128) k_schur_f32(int n_units, int n_diag, const SchurUnit *__restrict__ units,
                                                    const int *__restrict__ pa, const int *__restrict__ pb,
                                                    const SchurUnit *__restrict__ diag_units,
                                                    const int *__restrict__ cam_obs, const int *__restrict__ obs_pt,
@@ -1081,10 +1123,14 @@ __global__ void __launch_bounds__(128) k_schur_f32(int n_units, int off_ctas, co
                                                    const double *__restrict__ gb, double *__restrict__ off_partial,
                                                    double *__restrict__ diag_partial)
 {
-    if ((int)blockIdx.x < off_ctas)
-        schur_off_unit<float>(blockIdx.x * 128 + threadIdx.x, n_units, units, pa, pb, Y, W, off_partial);
-    else
-        schur_diag_cta<float>(diag_units[blockIdx.x - off_ctas], cam_obs, obs_pt, Y, W, gb, diag_partial);
+    static_assert(4 * 2 * MX_UNIT >= 2 * DIAG_SUPER, "the index buffer holds a diagonal unit's indices");
+    __shared__ int sidx[4][2 * MX_UNIT];
+    if ((int)blockIdx.x < n_diag) {
+        schur_diag_cta<float>(diag_units[blockIdx.x], cam_obs, obs_pt, Y, W, gb, diag_partial, &sidx[0][0]);
+    } else {
+        const int uid = (blockIdx.x - n_diag) * 4 + (threadIdx.x >> 5);
+        if (uid < n_units) schur_off_warp(units[uid], pa, pb, Y, W, sidx[threadIdx.x >> 5], off_partial);
+    }
 }
 
 // Sum unit partials into S (lower) and rhs = ea.
@@ -1149,10 +1195,10 @@ void launch_schur_off(const DeviceProblem &d, cudaStream_t s)
         note_launch(1);
         return;
     }
-    const int off_ctas = ceil_div(d.n_off_units, 128);
+    const int off_ctas = ceil_div(d.n_mx_units, 4);
     if (off_ctas + d.n_diag_units == 0) return;
     k_schur_f32<<<off_ctas + d.n_diag_units, 128, 0, s>>>(
-        d.n_off_units, off_ctas, d.off_units, d.pair_a, d.pair_b, d.diag_units, d.cam_obs, d.obs_pt,
+        d.n_mx_units, d.n_diag_units, d.mx_units, d.pair_a, d.pair_b, d.diag_units, d.cam_obs, d.obs_pt,
         (const float *)d.Y, (const float *)d.W, d.g + d.N, d.schur_partial,
         d.schur_partial + off_partial_slots(d) * 36);
     note_launch(1);
@@ -1179,7 +1225,7 @@ void launch_schur_reduce(const DeviceProblem &d, double mu, cudaStream_t s)
     double *off_partial = d.schur_partial;
     double *diag_partial = d.schur_partial + off_partial_slots(d) * 36;
     const int total = d.n_pairs * 36 + d.nc * DIAG_NV;
-    const int *off_start = d.prec == PSBA_PREC_FP64 ? d.off_chunk_start : d.off_unit_start;
+    const int *off_start = d.prec == PSBA_PREC_FP64 ? d.off_chunk_start : d.mx_unit_start;
     k_schur_reduce<<<ceil_div(total, 128), 128, 0, s>>>(d.n_pairs, d.nc, d.Np, d.pair_kl,
                                                           off_start, off_partial,
                                                           d.diag_unit_start, diag_partial, d.U, d.g,

@@ -909,8 +909,9 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
                      d.pt_start, d_off, d.pair_a, d.pair_b, h->stream);
     TRY(check_launch());
     // Schur work units; execution order longest first
-    std::vector<SchurUnit> off_units, off_chunks, diag_units;
-    std::vector<int> off_start(n_pairs + 1, 0), chunk_start(n_pairs + 1, 0), diag_start(nc + 1, 0);
+    std::vector<SchurUnit> off_units, off_chunks, diag_units, mx_units;
+    std::vector<int> off_start(n_pairs + 1, 0), chunk_start(n_pairs + 1, 0), diag_start(nc + 1, 0),
+        mx_start(n_pairs + 1, 0);
     off_units.reserve((size_t)(n_entries / SCHUR_CHUNK) + (size_t)n_pairs);
     for (int q = 0; q < n_pairs; ++q) {
         for (long long b = pair_start[q]; b < pair_start[q + 1]; b += SCHUR_CHUNK) {
@@ -941,6 +942,15 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
             }
         }
         chunk_start[n_pairs] = n_chunk_slots;
+        // FP32 products: units of <= MX_UNIT entries of one pair, one warp each
+        mx_units.reserve((size_t)(n_entries / MX_UNIT) + (size_t)n_pairs);
+        for (int q = 0; q < n_pairs; ++q) {
+            for (long long b = pair_start[q]; b < pair_start[q + 1]; b += MX_UNIT) {
+                const int cnt = (int)std::min<long long>(MX_UNIT, pair_start[q + 1] - b);
+                mx_units.push_back({q, (int)b, cnt, (int)mx_units.size()});
+            }
+            mx_start[q + 1] = (int)mx_units.size();
+        }
     }
     const int dchunk = d.cnp == 6 ? DIAG_SUPER : DIAG_CHUNK;
     for (int j = 0; j < nc; ++j) {
@@ -960,6 +970,7 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
         u.swap(out);
     };
     sort_by_count(off_units, SCHUR_CHUNK);
+    sort_by_count(mx_units, MX_UNIT);
     sort_by_count(diag_units, dchunk);
     std::vector<CamUnit> cam_units;
     std::vector<int> cam_unit_start(nc + 1, 0);
@@ -974,6 +985,7 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     d.n_off_units = (int)off_units.size();
     d.n_off_chunks = (int)off_chunks.size();
     d.n_off_chunk_slots = n_chunk_slots;
+    d.n_mx_units = (int)mx_units.size();
     d.n_diag_units = (int)diag_units.size();
     d.n_cam_units = (int)cam_units.size();
 
@@ -988,6 +1000,8 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
         TRY(dalloc(h, &d.pair_start, (size_t)n_pairs + 1));
         TRY(dalloc(h, &d.off_chunk_start, (size_t)n_pairs + 1));
         TRY(dalloc(h, &d.off_chunks, off_chunks.size()));
+        TRY(dalloc(h, &d.mx_units, mx_units.size()));
+        TRY(dalloc(h, &d.mx_unit_start, (size_t)n_pairs + 1));
     }
     TRY(dalloc(h, &d.diag_units, diag_units.size()));
     TRY(dalloc(h, &d.diag_unit_start, (size_t)nc + 1));
@@ -1077,6 +1091,8 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
         TRY(upload(h, d.pair_start, ps.data(), ps.size()));
         TRY(upload(h, d.off_chunk_start, chunk_start.data(), chunk_start.size()));
         TRY(upload(h, d.off_chunks, off_chunks.data(), off_chunks.size()));
+        TRY(upload(h, d.mx_units, mx_units.data(), mx_units.size()));
+        TRY(upload(h, d.mx_unit_start, mx_start.data(), mx_start.size()));
     }
     TRY(upload(h, d.diag_units, diag_units.data(), diag_units.size()));
     TRY(upload(h, d.diag_unit_start, diag_start.data(), diag_start.size()));

@@ -54,7 +54,7 @@ def build(force=False, verbose=False, extra=()):
 
     def one(src):
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-        out = _run([nvcc()] + flags + ["-dc" if False else "-c", src, "-o", obj] +
+        out = _run([nvcc()] + flags + ["-c", src, "-o", obj] +
                    (["-Xptxas", "-v"] if verbose else []))
         return obj, out
 

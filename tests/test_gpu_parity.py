@@ -192,7 +192,7 @@ def _tr_envelope(sc, n_iter, max_iter=12):
     |sum E| / N from the modified Cholesky of that singular S, so lambda moves
     by per cent and the early trial costs by ~1e-5 under a 1-ulp change of
     the input, while its LM path moves by 1e-15.  Returns the per-record
-    maximum relative spreads of cost and lambda."""
+    maximum relative spreads of cost and lambda, and that of the final cost."""
     base = oracle.trust_region(sc, max_iter=max_iter)
     runs = []
     for sign in (np.inf, -np.inf):
@@ -201,14 +201,15 @@ def _tr_envelope(sc, n_iter, max_iter=12):
         runs.append(oracle.trust_region(sc2, max_iter=max_iter))
     runs.append(oracle.trust_region(sc, max_iter=max_iter, solve_mode=1))
     t0 = base.trace[base.trace["itno"] < n_iter]
-    ec, el = np.zeros(len(t0)), np.zeros(len(t0))
+    ec, el, ef = np.zeros(len(t0)), np.zeros(len(t0)), 0.0
     for r in runs:
+        ef = max(ef, abs(r.final_cost - base.final_cost) / base.final_cost)
         t = r.trace[r.trace["itno"] < n_iter]
         assert np.array_equal(t["kind"], t0["kind"]) and np.array_equal(t["accepted"], t0["accepted"])
         with np.errstate(invalid="ignore", divide="ignore"):
             ec = np.fmax(ec, np.abs(t["cost"] - t0["cost"]) / t0["cost"])
             el = np.fmax(el, np.abs(t["lambda_"] - t0["lambda_"]) / t0["lambda_"])
-    return base, np.nan_to_num(ec), np.nan_to_num(el)
+    return base, np.nan_to_num(ec), np.nan_to_num(el), ef
 
 
 @pytest.mark.parametrize("name", ["arc0", "arc1", "arc2", "circle24"])
@@ -218,10 +219,11 @@ def test_trust_region_trace_matches_oracle(name):
     Cholesky, trust_region.cpp:341-371), the accept decisions
     (trust_region.cpp:223-246) and the trust radius exactly; each trial's
     cost and lambda within ten times the oracle's own spread under 1-ulp
-    input changes (plus 1e-9); the final cost to 1e-9."""
+    input changes (plus 1e-9); the final cost likewise (1e-9 where the
+    oracle's spread is below that)."""
     sc = scenes.circle_scene(seed=1, n_cams=24, n_pts=3000, name="circle24") if name == "circle24" \
         else scenes.small_lm_scene(int(name[-1]))
-    o, env_cost, env_lam = _tr_envelope(sc, 10)
+    o, env_cost, env_lam, env_final = _tr_envelope(sc, 10)
     with P.Solver(sc) as s:
         g = s.trust_region(max_iter=12)
     to, tg = o.trace[o.trace["itno"] < 10], g.trace[g.trace["itno"] < 10]
@@ -238,7 +240,7 @@ def test_trust_region_trace_matches_oracle(name):
     dl = np.abs(tg["lambda_"][lam] - to["lambda_"][lam]) / to["lambda_"][lam]
     assert np.all(dl <= 10 * env_lam[lam] + 1e-9), (dl, env_lam[lam])
     assert g.status == o.status and g.iterations == o.iterations
-    assert abs(g.final_cost - o.final_cost) <= 1e-9 * o.final_cost
+    assert abs(g.final_cost - o.final_cost) <= (10 * env_final + 1e-9) * o.final_cost
 
 
 def test_hybrid_matched_final_cost():

@@ -99,6 +99,7 @@ def parse():
     ap.add_argument("--serve-pool", type=int, default=32, help="distinct request scenes (cycled)")
     ap.add_argument("--serve-large-lanes", type=int, default=None, help="server large_lanes (default: library's)")
     ap.add_argument("--serve-large-obs", type=int, default=None, help="server large_obs (default: library's)")
+    ap.add_argument("--serve-large-cams", type=int, default=None, help="server large_cams (default: library's)")
     return ap.parse_args()
 
 
@@ -472,7 +473,7 @@ def serving_leg(P, args):
                        "6-param cameras, FP64 for 11-param; 120 GB HBM budget" % (len(pool), cap),
            "mean_observations": float(np.mean([sc.n_obs for sc in pool])), "rates": []}
     rel_all = []
-    with S.Server(precision=P.PREC_MIXED, max_iter=cap, hbm_budget_bytes=120e9,
+    with S.Server(precision=P.PREC_MIXED, max_iter=cap, hbm_budget_bytes=120e9, large_cams=args.serve_large_cams,
                   large_lanes=args.serve_large_lanes, large_obs=args.serve_large_obs) as srv:
         S.run_poisson(srv, pool[:4], rate=1000.0, n_requests=4, seed=1)
         for rate in rates:

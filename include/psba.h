@@ -87,9 +87,10 @@ typedef struct {
      * 11: followed by the intrinsics fx, cx, cy, aspect, skew (the sba
      * variable-K camera files, data/7camsvarK.txt).  16: followed further by
      * the distortion k1, k2, p1, p2, k3 (data/54camsvarKD.txt).  The 11- and
-     * 16-parameter models have no reference kernels; the trust-region entry
-     * points and psba_batch_* take 6-parameter cameras (the server runs the
-     * others on its large lane). */
+     * 16-parameter models have no reference kernels; psba_batch_* takes
+     * 6-parameter cameras (the server runs the others on its large lane).
+     * With them the trust-region driver's lambda fallback runs its 3x3-block
+     * modified Cholesky on S padded to a multiple of 3 by an identity block. */
     int cnp;
     /* Optional (NULL: unweighted): per observation the 2x2 covariance of the
      * image measurement, row-major (4 values, symmetric positive definite),

@@ -1304,10 +1304,25 @@ static int compute_pb(orc_ws *w, const orc_opts *o, double *lambda)
     ea_ix(p, &w->ix, w->Y, w->g, w->ea);
     if (reduced_solve(w, o->solve_mode, w->dp)) {
         if (*lambda == 0.0) {
-            memcpy(w->S, w->Saux, sizeof(double) * (size_t)N * N);
-            orc_cholmod(N, w->S, w->E);
             double sum = 0.0;
-            for (int i = 0; i < N; ++i) sum += w->E[i];
+            if (N % 3 == 0) {
+                memcpy(w->S, w->Saux, sizeof(double) * (size_t)N * N);
+                orc_cholmod(N, w->S, w->E);
+                for (int i = 0; i < N; ++i) sum += w->E[i];
+            } else {
+                /* 11/16-parameter cameras (no reference counterpart): the
+                 * 3x3-block modified Cholesky on S padded to a multiple of 3
+                 * with an identity block; lambda from the first N corrections */
+                const int n3 = N + (3 - N % 3);
+                double *Sp = (double *)calloc((size_t)n3 * n3, sizeof(double));
+                double *Ep = (double *)malloc(sizeof(double) * (size_t)n3);
+                for (int r = 0; r < N; ++r) memcpy(Sp + (size_t)r * n3, w->Saux + (size_t)r * N, sizeof(double) * N);
+                for (int r = N; r < n3; ++r) Sp[(size_t)r * n3 + r] = 1.0;
+                orc_cholmod(n3, Sp, Ep);
+                for (int i = 0; i < N; ++i) sum += Ep[i];
+                free(Sp);
+                free(Ep);
+            }
             *lambda = fabs(sum) / N;
             return 0;
         }
@@ -1391,7 +1406,7 @@ static int trust_region_ws(orc_ws *w, double *cams, double *pts, const orc_opts 
         /* the U/V/W of coeff 2 are the negatives of coeff -2 */
         for (int k = 0; k < w->cnp * w->cnp * w->nc; ++k) w->U[k] = -w->U[k];
         for (int k = 0; k < 9 * w->np; ++k) w->V[k] = -w->V[k];
-        for (long long k = 0; k < 18LL * w->no; ++k) w->W[k] = -w->W[k];
+        for (long long k = 0; k < 3LL * w->cnp * w->no; ++k) w->W[k] = -w->W[k];
         for (int k = 0; k < nt; ++k) w->UVdiag[k] = -w->UVdiag[k];
         orc_jmultiply(p, w->JA, w->JB, w->g, w->Jx1);
         gtBg = 2 * dotp(no2, w->Jx1, w->Jx1);

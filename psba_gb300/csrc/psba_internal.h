@@ -151,7 +151,10 @@ struct DeviceProblem {
     double *Y = nullptr;          // 18 per obs
     double *schur_partial = nullptr;  // off-diagonal slots (off_partial_slots), then the diagonal units'
     double *S = nullptr;          // Np x Np (lower)
-    double *Ssave = nullptr;      // copy of S (trust-region modified-Cholesky fallback)
+    double *Ssave = nullptr;      // copy of S (trust-region modified-Cholesky fallback), Nm3 x Nm3
+    // the fallback's matrix size: Np, or (N not a multiple of 3: 11/16-parameter
+    // cameras) Np rounded up to a multiple of 3, the rows past Np identity
+    int Nm3 = 0;
     double *rhs = nullptr;        // Np (ea on entry, y after the forward solve)
     double *xsol = nullptr;       // Np
     double *Linv = nullptr;       // (Np / TILE) * TILE * TILE inverses of the diagonal blocks

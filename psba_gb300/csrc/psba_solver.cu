@@ -451,8 +451,7 @@ int levmar_impl(psba_handle *h, const psba_opts *o, int *itno, psba_result *res,
                     trace_push(res, *itno, PSBA_TRACE_LM_TRIAL, 1, mu_used, rho, new_ex_L2, 0);
                     if (std::fabs(rho - 1) < (1.0 / 5.0)) {
                         gooditer_cnt++;
-                        // the trust-region driver takes 6-parameter cameras only
-                        if (gooditer_cnt >= 5 && o->allow_switch && h->d.cnp == 6) {
+                        if (gooditer_cnt >= 5 && o->allow_switch) {
                             iter_flag = PSBA_ITER_TURN_TO_TR;
                             break;
                         }
@@ -501,8 +500,12 @@ int compute_pb(psba_handle *h, double *lambda, int *solved)
     DeviceProblem &d = h->d;
     const long long nt = d.N + 3LL * d.np;
     enqueue_reduced(h, *lambda);
-    PSBA_CUDA_TRY(cudaMemcpyAsync(d.Ssave, d.S, sizeof(double) * (size_t)d.Np * d.Np,
-                                  cudaMemcpyDeviceToDevice, h->stream));
+    if (d.Nm3 == d.Np)
+        PSBA_CUDA_TRY(cudaMemcpyAsync(d.Ssave, d.S, sizeof(double) * (size_t)d.Np * d.Np,
+                                      cudaMemcpyDeviceToDevice, h->stream));
+    else
+        PSBA_CUDA_TRY(cudaMemcpy2DAsync(d.Ssave, sizeof(double) * d.Nm3, d.S, sizeof(double) * d.Np,
+                                        sizeof(double) * d.Np, d.Np, cudaMemcpyDeviceToDevice, h->stream));
     enqueue_step(h, *lambda);
     TRY(check_launch());
     TrialScalars ts;
@@ -511,8 +514,11 @@ int compute_pb(psba_handle *h, double *lambda, int *solved)
         return set_error("dense solver wait budget exhausted (device dataflow stalled)"), PSBA_ERR_STATE;
     if (ts.chol_status != 0) {
         if (*lambda == 0.0) {
-            // modified Cholesky of the saved S (lower, N x N inside the padded Np)
-            launch_cholmod(d.Ssave, d.N, d.Np, d.E, d.red_partial, h->stream);
+            // modified Cholesky of the saved S (lower, N x N inside the padded
+            // Np; N not a multiple of 3: the 3x3-block form runs on S padded
+            // to one with its identity rows, lambda from the first N entries)
+            const int n3 = d.N % 3 == 0 ? d.N : d.N + (3 - d.N % 3);
+            launch_cholmod(d.Ssave, n3, d.Nm3, d.E, d.red_partial, h->stream);
             TRY(check_launch());
             std::vector<double> E(d.N);
             PSBA_CUDA_TRY(cudaMemcpyAsync(E.data(), d.E, sizeof(double) * d.N, cudaMemcpyDeviceToHost,
@@ -1029,7 +1035,8 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     TRY(dalloc(h, &d.Y, 3 * cnp * (size_t)no));
     TRY(dalloc(h, &d.schur_partial, cnp * cnp * off_partial_slots(d) + diag_nv * diag_units.size()));
     TRY(dalloc(h, &d.S, (size_t)d.Np * d.Np));
-    TRY(dalloc(h, &d.Ssave, (size_t)d.Np * d.Np));
+    d.Nm3 = d.N % 3 == 0 ? d.Np : ((d.Np + 2) / 3) * 3;
+    TRY(dalloc(h, &d.Ssave, (size_t)d.Nm3 * d.Nm3));
     TRY(dalloc(h, &d.rhs, (size_t)d.Np));
     TRY(dalloc(h, &d.xsol, (size_t)d.Np));
     TRY(dalloc(h, &d.Linv, (size_t)d.Np * TILE));
@@ -1051,7 +1058,7 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     TRY(dalloc(h, &d.eb, 3 * (size_t)np));
     h->nred = 512;
     const int res_blocks = residual_blocks(d), ebb = eb_blocks(d);
-    d.red_partial_cap = std::max<int>({2 * ebb + 8 + res_blocks, h->nred + 8, 5 * d.Np + 8});
+    d.red_partial_cap = std::max<int>({2 * ebb + 8 + res_blocks, h->nred + 8, 5 * d.Nm3 + 8});
     TRY(dalloc(h, &d.red_partial, (size_t)d.red_partial_cap));
     TRY(dalloc(h, &d.scal, 1));
     TRY(dalloc(h, &h->scratch, 64));
@@ -1060,7 +1067,14 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     TRY(dalloc(h, &d.vecP, nt));
     TRY(dalloc(h, &d.jx1, 2 * (size_t)no));
     TRY(dalloc(h, &d.jx2, 2 * (size_t)no));
-    TRY(dalloc(h, &d.E, (size_t)d.Np));
+    TRY(dalloc(h, &d.E, (size_t)d.Nm3));
+    if (d.Nm3 > d.Np) {
+        // the rows and columns past Np stay an identity block: the fallback's
+        // copies of S fill only the leading Np x Np part
+        std::vector<double> pad((size_t)d.Nm3 * d.Nm3, 0.0);
+        for (int r = d.Np; r < d.Nm3; ++r) pad[(size_t)r * d.Nm3 + r] = 1.0;
+        TRY(upload(h, d.Ssave, pad.data(), pad.size()));
+    }
     TRY(dalloc(h, &d.tmp9, 9 * (size_t)np));
     d.scal_host = static_cast<TrialScalars *>(pinned_get(sizeof(TrialScalars)));
     h->host_scalars = static_cast<double *>(pinned_get(64 * sizeof(double)));
@@ -1292,10 +1306,6 @@ int psba_levmar(psba_handle *h, const psba_opts *opts, int *itno, psba_result *r
 int psba_trust_region(psba_handle *h, const psba_opts *opts, int *itno, psba_result *res)
 {
     if (!h || !itno) return set_error("null argument"), PSBA_ERR_ARG;
-    if (h->d.cnp != 6)
-        return set_error("psba_trust_region: 6-parameter cameras only (its modified-Cholesky fallback "
-                         "works on 3x3 blocks)"),
-               PSBA_ERR_ARG;
     TRY(check_opts(opts));
     h->d.prec = opts->precision;
     reset_result(res);

@@ -14,6 +14,7 @@ import pytest
 import oracle
 import psba_gb300 as P
 from psba_gb300 import scenes
+from tr_envelope import tr_envelope, assert_tr_trace_close
 
 pytestmark = pytest.mark.gpu
 
@@ -183,35 +184,6 @@ def test_levmar_power_law_scene():
     assert abs(g.final_cost - o.final_cost) <= 1e-9 * o.final_cost
 
 
-def _tr_envelope(sc, n_iter, max_iter=12):
-    """The oracle's own spread over its trust-region trace when its inputs
-    move by one ulp (points nudged up, points nudged down) or it solves
-    instead of inverting S.  The reference's dogleg is ill-conditioned on
-    these problems: its first Gauss-Newton step solves S + lambda I with S
-    the singular lambda = 0 system (7 gauge directions) and lambda =
-    |sum E| / N from the modified Cholesky of that singular S, so lambda moves
-    by per cent and the early trial costs by ~1e-5 under a 1-ulp change of
-    the input, while its LM path moves by 1e-15.  Returns the per-record
-    maximum relative spreads of cost and lambda, and that of the final cost."""
-    base = oracle.trust_region(sc, max_iter=max_iter)
-    runs = []
-    for sign in (np.inf, -np.inf):
-        sc2 = sc.copy()
-        sc2.pts = np.nextafter(sc.pts, sign)
-        runs.append(oracle.trust_region(sc2, max_iter=max_iter))
-    runs.append(oracle.trust_region(sc, max_iter=max_iter, solve_mode=1))
-    t0 = base.trace[base.trace["itno"] < n_iter]
-    ec, el, ef = np.zeros(len(t0)), np.zeros(len(t0)), 0.0
-    for r in runs:
-        ef = max(ef, abs(r.final_cost - base.final_cost) / base.final_cost)
-        t = r.trace[r.trace["itno"] < n_iter]
-        assert np.array_equal(t["kind"], t0["kind"]) and np.array_equal(t["accepted"], t0["accepted"])
-        with np.errstate(invalid="ignore", divide="ignore"):
-            ec = np.fmax(ec, np.abs(t["cost"] - t0["cost"]) / t0["cost"])
-            el = np.fmax(el, np.abs(t["lambda_"] - t0["lambda_"]) / t0["lambda_"])
-    return base, np.nan_to_num(ec), np.nan_to_num(el), ef
-
-
 @pytest.mark.parametrize("name", ["arc0", "arc1", "arc2", "circle24"])
 def test_trust_region_trace_matches_oracle(name):
     """TR traces over the first 10 iterations: the record kinds (TR trials
@@ -223,24 +195,11 @@ def test_trust_region_trace_matches_oracle(name):
     oracle's spread is below that)."""
     sc = scenes.circle_scene(seed=1, n_cams=24, n_pts=3000, name="circle24") if name == "circle24" \
         else scenes.small_lm_scene(int(name[-1]))
-    o, env_cost, env_lam, env_final = _tr_envelope(sc, 10)
+    o, n, env = tr_envelope(sc, 10)
+    assert n == 10
     with P.Solver(sc) as s:
         g = s.trust_region(max_iter=12)
-    to, tg = o.trace[o.trace["itno"] < 10], g.trace[g.trace["itno"] < 10]
-    assert len(to) == len(tg)
-    assert np.array_equal(to["itno"], tg["itno"])
-    assert np.array_equal(to["kind"], tg["kind"]) and np.array_equal(to["accepted"], tg["accepted"])
-    assert np.array_equal(to["damping"], tg["damping"])
-    assert np.any(to["kind"] == P.TRACE_TR_PB_FAIL)  # the modified-Cholesky lambda path ran
-    c = np.isfinite(to["cost"])
-    assert np.array_equal(c, np.isfinite(tg["cost"]))
-    dc = np.abs(tg["cost"][c] - to["cost"][c]) / to["cost"][c]
-    assert np.all(dc <= 10 * env_cost[c] + 1e-9), (dc, env_cost[c])
-    lam = to["lambda_"] > 0
-    dl = np.abs(tg["lambda_"][lam] - to["lambda_"][lam]) / to["lambda_"][lam]
-    assert np.all(dl <= 10 * env_lam[lam] + 1e-9), (dl, env_lam[lam])
-    assert g.status == o.status and g.iterations == o.iterations
-    assert abs(g.final_cost - o.final_cost) <= (10 * env_final + 1e-9) * o.final_cost
+    assert_tr_trace_close(o, g, n, env)
 
 
 def test_hybrid_matched_final_cost():

@@ -619,6 +619,41 @@ __device__ void update_lower(double (*a)[T + 1], const double (*L)[T + 1], doubl
     sync();
 }
 
+// The panel's last update of the diagonal tile and of b, a -= L L^T and
+// b -= L y over the lower triangle, one output per thread (152 outputs, 224
+// threads on named barrier 1): sixteen multiply-adds in two interleaved
+// chains of eight, then one subtraction.  One pass, where update_lower's
+// even deal of the products needs partial sums, a barrier and a second pass.
+__device__ void update_lower_panel(double (*a)[T + 1], const double (*L)[T + 1], double *b, const double *y)
+{
+    constexpr int NT = CF_THREADS - 32, NTRI = T * (T + 1) / 2, NE = NTRI + T;
+    static_assert(NE <= NT, "one output per thread");
+    const int tid = (int)threadIdx.x - ((int)threadIdx.x >= 160 ? 32 : 0);
+    if (tid < NE) {
+        int r = 0, c = 0;
+        const double *xr, *yr;
+        double *dst;
+        if (tid < NTRI) {
+            tri_of(tid, r, c);
+            xr = L[r];
+            yr = L[c];
+            dst = &a[r][c];
+        } else {
+            xr = L[tid - NTRI];
+            yr = y;
+            dst = b + (tid - NTRI);
+        }
+        double s0 = 0.0, s1 = 0.0;
+#pragma unroll
+        for (int k = 0; k < T; k += 2) {
+            s0 = fma(xr[k], yr[k], s0);
+            s1 = fma(xr[k + 1], yr[k + 1], s1);
+        }
+        *dst -= s0 + s1;
+    }
+    asm volatile("bar.sync 1, %0;" ::"n"(NT) : "memory");
+}
+
 // out = A Linv^T restricted to the lower triangle of Linv (out[r][c] =
 // sum_{k <= c} A[r][k] Linv[c][k]): columns c and T-1-c of a row go to one
 // thread, T + 1 products each.
@@ -801,7 +836,7 @@ __global__ void __launch_bounds__(CF_THREADS, 1) k_chol_dataflow(int Np, int nb,
                         st_release(flags + tile_task(I, I - 1, nb), epoch);
                     }
                 } else if (!failed) {
-                    update_lower<true, CF_THREADS - 32>(wa, lsub, W + PW_B, W + PW_Y, part);
+                    update_lower_panel(wa, lsub, W + PW_B, W + PW_Y);
                 }
             }
             if (tid == 0) pf_done = 0;

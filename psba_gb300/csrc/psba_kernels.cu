@@ -1052,16 +1052,34 @@ int schur_off_wave_threads()
 // slots are combined in FP64 by a fixed xor tree and the unit's partial goes
 // to its slot; k_schur_reduce sums a pair's units in order, in FP64.  Every
 // sum has a fixed order, so the result does not depend on scheduling.
+// Nine consecutive floats of a row half: the half starts at float 9 h of a
+// 72-byte row (row start 8-byte aligned), so it is one scalar and four
+// 8-byte pairs -- the scalar last for h = 0, first for h = 1 -- five loads
+// instead of nine (the L1 is what bounds this kernel).
+__device__ __forceinline__ void ld_half(const float *__restrict__ row, int h, float (&v)[9])
+{
+    const float *p = row + 9 * h;
+    const float single = __ldg(p + (h ? 0 : 8));
+    const float2 *q = reinterpret_cast<const float2 *>(p + (h ? 1 : 0));
+    float pr[8];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float2 t = __ldg(q + k);
+        pr[2 * k] = t.x;
+        pr[2 * k + 1] = t.y;
+    }
+    v[0] = h ? single : pr[0];
+#pragma unroll
+    for (int e = 1; e < 8; ++e) v[e] = h ? pr[e - 1] : pr[e];
+    v[8] = h ? pr[7] : single;
+}
+
 __device__ __forceinline__ void mx_quadrant(const float *__restrict__ Y, const float *__restrict__ W, int a, int b,
                                             int qr, int qc, float *acc)
 {
     float y[9], w[9];
-    const float *py = Y + 18 * (size_t)a + 9 * qr, *pw = W + 18 * (size_t)b + 9 * qc;
-#pragma unroll
-    for (int e = 0; e < 9; ++e) {
-        y[e] = __ldg(py + e);
-        w[e] = __ldg(pw + e);
-    }
+    ld_half(Y + 18 * (size_t)a, qr, y);
+    ld_half(W + 18 * (size_t)b, qc, w);
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll

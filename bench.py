@@ -23,12 +23,21 @@ estimate.  The metric is LM iterations per second.
   FP64 FMA rate.  roofline_chol: the dense solve (k_chol_dataflow +
   k_tri_cluster); roofline_mixed: the mixed form's Schur products
   (k_schur_f32) against the FP32 FMA rate and HBM.
-* matched_cost: solves at matched final cost.  The FP64 form runs to the
+* matched_cost: solves at matched final cost, on the bench problem and
+  more seeded problems of the same shape.  The FP64 form runs to the
   reference's own stopping rule (levmar.cpp:157-179, 247-248) from the
   initial estimate; its cost C* is the target.  Each form (FP64, mixed) is
   then timed to the first iteration whose cost is within 1e-6 of C* (the
   same trajectory cut at that iteration), and the mixed form's own
-  converged endpoint is reported with an FP64 polish from it.
+  converged endpoint is reported with an FP64 polish from it.  LM on these
+  problems (2% outliers) is chaotic past ~20 iterations, so which of
+  several minima a trajectory ends in changes with its last bits; a
+  problem where the mixed form ends in another minimum (certified by the
+  polish) has no matched time, and the summary counts both kinds.  The
+  control: the FP64 form from the initial estimate with the points moved by
+  one ulp, and whether it ends in the same minimum as unmoved.
+* refine: one FP64 solve of the same budget with the refinement step of
+  the reduced solve on (psba_opts.refine), its dense-solve stage timed.
 * variable_intrinsics: 52 cameras x 64,053 points with 11- and
   16-parameter cameras, the same matched-cost protocol.
 * batched: 1,024 small problems in one persistent launch, every problem
@@ -85,6 +94,9 @@ def parse():
                     help="iteration cap of the solves to the stopping rule (matched-cost legs)")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-form and matched-cost legs")
     ap.add_argument("--no-matched", action="store_true", help="skip the matched-cost leg")
+    ap.add_argument("--matched-seeds", default="0,1,2,3",
+                    help="problem seeds of the matched-cost leg (0: the bench problem)")
+    ap.add_argument("--no-refine", action="store_true", help="skip the refinement-step leg")
     ap.add_argument("--tr-iters", type=int, default=50, help="trust-region leg iterations (0: skip)")
     ap.add_argument("--varcam", action="store_true", default=True)
     ap.add_argument("--no-varcam", dest="varcam", action="store_false", help="skip the variable-intrinsics leg")
@@ -292,20 +304,10 @@ def first_iteration_at(trace, target):
     return int(hit["itno"][0]) + 1 if len(hit) else None
 
 
-def time_to_target(P, torch, flush, solver, precision, target, cap, reps):
-    """The form's solve from the initial estimate cut at the first iteration
-    whose cost is <= target: (iterations, trials, device ms (median of
-    reps), cost there), plus the form's run to the stopping rule (cap
-    iterations at most)."""
-    solver.reset_params()
-    full = solver.levmar(P.default_opts(allow_switch=0, max_iter=cap, precision=precision), fetch=True,
-                         trace_cap=50000)
-    out = {"to_stopping_rule": {"status": full.status_name, "iterations": full.iterations,
-                                "trials": full.n_trials, "final_cost": full.final_cost, "ms": full.device_ms}}
-    k = first_iteration_at(full.trace, target)
-    out["reached"] = k is not None
-    if k is None:
-        return out, full
+def timed_cut(P, torch, flush, solver, precision, k, reps):
+    """The form's solve from the initial estimate cut at iteration k (the
+    same trajectory as its full run, which is deterministic): device ms
+    (median of reps), trials and cost there."""
     o = P.default_opts(allow_switch=0, max_iter=k, precision=precision)
     ms = []
     for _ in range(max(1, reps)):
@@ -313,43 +315,139 @@ def time_to_target(P, torch, flush, solver, precision, target, cap, reps):
         flush_l2(torch, flush)
         r = solver.levmar(o, fetch=False, trace_cap=0)
         ms.append(r.device_ms)
-    out.update({"iterations": k, "trials": r.n_trials, "cost": r.final_cost, "ms": float(np.median(ms)),
-                "solves_per_s": 1e3 / float(np.median(ms)), "iterations_per_s": k / (float(np.median(ms)) / 1e3)})
-    return out, full
+    m = float(np.median(ms))
+    return {"iterations": k, "trials": r.n_trials, "cost": r.final_cost, "ms": m, "solves_per_s": 1e3 / m,
+            "iterations_per_s": k / (m / 1e3)}
+
+
+def cost_by_iteration(trace):
+    """cost[k] = the cost after k outer iterations (accepted steps only
+    change it), from a trace; cost[0] is not recorded and stays NaN."""
+    acc = trace[trace["accepted"] == 1]
+    n = int(trace["itno"].max()) + 2 if len(trace) else 1
+    c = np.full(n, np.nan)
+    for it, cost in zip(acc["itno"], acc["cost"]):
+        c[int(it) + 1] = cost
+    for k in range(1, n):  # an iteration without an accepted step keeps the cost
+        if np.isnan(c[k]) and k > 1:
+            c[k] = c[k - 1]
+    return c
 
 
 def matched_cost_leg(P, torch, flush, sc, args, reps, solver=None):
-    """Both forms on one problem at matched final cost.  The FP64 form's run
-    to the reference's stopping rule gives the target C*; each form is
-    timed to its first iteration within MATCH_TOL of C*; the mixed form's
-    own converged endpoint is reported with an FP64 polish from it (FP64 LM
-    restarted there: how much lower it gets)."""
+    """Both forms on one problem at matched cost.  The FP64 form's run to the
+    reference's stopping rule gives C*; the same run with the points moved by
+    one ulp is the control.  Two targets:
+      converged: within MATCH_TOL of C*; each form timed to its first
+        iteration there (its trajectory cut at that iteration), the mixed
+        form's own endpoint reported with an FP64 polish from it (FP64 LM
+        restarted there: how much lower it gets);
+      horizon: the FP64 cost at the last iteration where the FP64 run and its
+        control still agree to MATCH_TOL (past it the trajectories' chaos,
+        not their precision, decides where they go), each form timed to its
+        first iteration within MATCH_TOL of it."""
     own = solver is None
     solver = solver or P.Solver(sc)
     try:
-        solver.reset_params()
-        ref = solver.levmar(P.default_opts(allow_switch=0, max_iter=args.converge_cap), fetch=False,
-                            trace_cap=50000)
+        cap = args.converge_cap
+        runs = {}
+        for tag, prec, nudge in (("fp64", P.PREC_FP64, False), ("mixed", P.PREC_MIXED, False),
+                                 ("fp64_1ulp", P.PREC_FP64, True)):
+            solver.reset_params()
+            if nudge:
+                cams0, pts0 = solver.get_params()
+                solver.set_params(cams0, np.nextafter(pts0, np.inf))
+            runs[tag] = solver.levmar(P.default_opts(allow_switch=0, max_iter=cap, precision=prec),
+                                      fetch=(tag == "mixed"), trace_cap=50000)
+        ref, mix, nud = runs["fp64"], runs["mixed"], runs["fp64_1ulp"]
         cstar = ref.final_cost
-        target = cstar * (1.0 + MATCH_TOL)
         out = {"target": {"cost": cstar, "tolerance": MATCH_TOL, "fp64_status": ref.status_name,
-                          "fp64_iterations": ref.iterations, "cap": args.converge_cap}}
+                          "fp64_iterations": ref.iterations, "cap": cap}}
         for tag, prec in (("fp64", P.PREC_FP64), ("mixed", P.PREC_MIXED)):
-            res, full = time_to_target(P, torch, flush, solver, prec, target, args.converge_cap, reps)
-            if tag == "mixed":
-                res["to_stopping_rule"]["rel_vs_fp64"] = (full.final_cost - cstar) / cstar
-                solver.set_params(full.cams, full.pts)
-                pol = solver.levmar(P.default_opts(allow_switch=0, max_iter=100), fetch=False, trace_cap=0)
-                res["to_stopping_rule"]["fp64_polish_rel_decrease"] = (full.final_cost - pol.final_cost) / \
-                    pol.final_cost
+            full = runs[tag]
+            res = {"to_stopping_rule": {"status": full.status_name, "iterations": full.iterations,
+                                        "trials": full.n_trials, "final_cost": full.final_cost, "ms": full.device_ms}}
+            k = first_iteration_at(full.trace, cstar * (1.0 + MATCH_TOL))
+            res["reached"] = k is not None
+            if k is not None:
+                res.update(timed_cut(P, torch, flush, solver, prec, k, reps))
             out[tag] = res
+        out["mixed"]["to_stopping_rule"]["rel_vs_fp64"] = (mix.final_cost - cstar) / cstar
+        solver.set_params(mix.cams, mix.pts)
+        pol = solver.levmar(P.default_opts(allow_switch=0, max_iter=100), fetch=False, trace_cap=0)
+        out["mixed"]["to_stopping_rule"]["fp64_polish_rel_decrease"] = (mix.final_cost - pol.final_cost) / \
+            pol.final_cost
         if out["fp64"]["reached"] and out["mixed"]["reached"]:
             out["speedup_mixed_vs_fp64"] = out["fp64"]["ms"] / out["mixed"]["ms"]
+        out["fp64_points_1ulp"] = {"status": nud.status_name, "iterations": nud.iterations,
+                                   "final_cost_rel_vs_fp64": (nud.final_cost - cstar) / cstar,
+                                   "same_minimum": bool(abs(nud.final_cost - cstar) <= MATCH_TOL * cstar)}
+        # the predictability horizon and the cost target there
+        cr, cn = cost_by_iteration(ref.trace), cost_by_iteration(nud.trace)
+        n = min(len(cr), len(cn))
+        kh = 0
+        for k in range(1, n):
+            if not abs(cr[k] - cn[k]) <= MATCH_TOL * cr[k]:
+                break
+            kh = k
+        if kh > 0:
+            th = cr[kh]
+            hz = {"iteration": kh, "cost": th}
+            for tag, prec in (("fp64", P.PREC_FP64), ("mixed", P.PREC_MIXED)):
+                k = first_iteration_at(runs[tag].trace, th * (1.0 + MATCH_TOL))
+                hz[tag] = {"reached": k is not None}
+                if k is not None:
+                    hz[tag].update(timed_cut(P, torch, flush, solver, prec, k, reps))
+            if hz["fp64"]["reached"] and hz["mixed"]["reached"]:
+                hz["speedup_mixed_vs_fp64"] = hz["fp64"]["ms"] / hz["mixed"]["ms"]
+            out["horizon"] = hz
         solver.reset_params()
         return out
     finally:
         if own:
             solver.close()
+
+
+def matched_cost_instances(P, torch, flush, scenes, args, reps, solver):
+    """The matched-cost protocol on several seeded problems of the bench's
+    shape (seed 0 is the bench problem, on its solver): each problem's
+    record, and a summary over the problems where both forms reached the
+    FP64 target."""
+    recs = []
+    for seed in [int(x) for x in args.matched_seeds.split(",") if x.strip()]:
+        if seed == 0:
+            r = matched_cost_leg(P, torch, flush, None, args, reps, solver=solver)
+        else:
+            sc = scenes.circle_scene(seed=seed, n_cams=args.cams, n_pts=args.points, name="circle")
+            r = matched_cost_leg(P, torch, flush, sc, args, reps)
+        r["seed"] = seed
+        recs.append(r)
+    both = [r for r in recs if r["fp64"]["reached"] and r["mixed"]["reached"]]
+    other = [r for r in recs if not r["mixed"]["reached"]]
+    hz = [r["horizon"] for r in recs if "horizon" in r and "speedup_mixed_vs_fp64" in r["horizon"]]
+    summary = {"problems": len(recs), "mixed_reached_fp64_minimum": len(both),
+               "mixed_ended_in_another_minimum": len(other),
+               "fp64_points_1ulp_same_minimum": sum(bool(r["fp64_points_1ulp"]["same_minimum"]) for r in recs)}
+    if both:
+        sp = [r["fp64"]["ms"] / r["mixed"]["ms"] for r in both]
+        summary.update({
+            "speedup_mixed_vs_fp64_geomean": float(np.exp(np.mean(np.log(sp)))),
+            "speedup_mixed_vs_fp64_min": float(min(sp)), "speedup_mixed_vs_fp64_max": float(max(sp)),
+            "fp64_ms_total": sum(r["fp64"]["ms"] for r in both),
+            "mixed_ms_total": sum(r["mixed"]["ms"] for r in both)})
+    if hz:
+        sp = [h["speedup_mixed_vs_fp64"] for h in hz]
+        summary["horizon"] = {
+            "problems_reached": len(hz), "iterations": [h["iteration"] for h in hz],
+            "speedup_mixed_vs_fp64_geomean": float(np.exp(np.mean(np.log(sp)))),
+            "speedup_mixed_vs_fp64_min": float(min(sp)), "speedup_mixed_vs_fp64_max": float(max(sp)),
+            "fp64_ms_total": sum(h["fp64"]["ms"] for h in hz), "mixed_ms_total": sum(h["mixed"]["ms"] for h in hz)}
+    if other:
+        summary["other_minima"] = [{"seed": r["seed"], "rel_vs_fp64": r["mixed"]["to_stopping_rule"]["rel_vs_fp64"],
+                                    "fp64_polish_rel_decrease":
+                                        r["mixed"]["to_stopping_rule"]["fp64_polish_rel_decrease"]}
+                                   for r in other]
+    return {"summary": summary, "problems": recs}
 
 
 def batched_leg(P, args):
@@ -570,6 +668,24 @@ def main():
     total_dev_s, wall, iters_all = aggregate_replicas(torch, dist, sum(dev_ms) / 1e3, wall, iters, "cuda")
     value = iters_all / total_dev_s
 
+    # ---- the reduced solve with its refinement step (opts.refine): one FP64
+    # solve of the same budget, the dense-solve stage timed
+    refine = None
+    if not args.no_refine:
+        ropts = P.default_opts(allow_switch=0, max_iter=args.max_iter, refine=1)
+        solver.set_stage_timing(True, stages=("cholesky",))
+        solver.reset_params()
+        flush_l2(torch, flush)
+        r = solver.levmar(ropts, fetch=False, trace_cap=0)
+        rs = solver.stage_timing()["cholesky"]
+        solver.set_stage_timing(False)
+        refine = {"value": r.iterations / (r.device_ms / 1e3), "unit": UNIT, "ms_per_step": r.device_ms,
+                  "dense_solve_ms_per_trial": rs[0] / max(rs[1], 1),
+                  "plain_dense_solve_ms_per_trial": live["cholesky"][0] / max(live["cholesky"][1], 1),
+                  "final_cost": r.final_cost, "final_cost_rel_vs_plain": (r.final_cost - costs[-1]) / costs[-1],
+                  "note": "residual as an accurate dot product against a copy of S, then both triangular "
+                          "solves; FP64 form, same iteration budget"}
+
     # ---- the mixed FP32/FP64 form at the same iteration budget (same
     # protocol), with its Schur products (k_schur_f32) timed live
     mixed = None
@@ -603,7 +719,7 @@ def main():
     # ---- matched final cost: each form to within MATCH_TOL of the FP64 converged cost
     matched = None
     if not args.no_mixed and not args.no_matched:
-        matched = matched_cost_leg(P, torch, flush, sc, args, min(args.steps, 3), solver=solver)
+        matched = matched_cost_instances(P, torch, flush, scenes, args, min(args.steps, 3), solver)
 
     # ---- trust region (dogleg) on the same workload, FP64, same protocol
     tr = None
@@ -718,7 +834,7 @@ def main():
                                    "frac": achieved_gbs / peak_gbs, "algorithmic_bytes": schur_bytes(sc),
                                    "peak_source": peak_kind}},
         "roofline_mixed": roofline_mixed, "dmma_tflops": dmma,
-        "stage_ms": stage_ms, "mixed": mixed, "matched_cost": matched, "trust_region": tr,
+        "stage_ms": stage_ms, "mixed": mixed, "matched_cost": matched, "trust_region": tr, "refine": refine,
         "stage_share": {k: (v[0] / total_stage if total_stage else 0.0) for k, v in stages.items()},
         "clocks": clk, "gpu_launches": int(launches),
     }

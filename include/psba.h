@@ -111,7 +111,12 @@ typedef struct {
     int max_iter;       /* shared iteration budget, 50 (levmar.cpp:100) */
     int allow_switch;   /* 1: LM hands over to TR after 5 good steps (levmar.cpp:215-219) */
     int precision;      /* PSBA_PREC_* */
-    int reserved;
+    int refine;         /* 1: one step of iterative refinement after each reduced solve:
+                           r = ea - S dpa against a copy of S, formed as an accurate dot
+                           product (twice the working precision), then both triangular solves
+                           with the factor, added into dpa; the forward error of dpa falls
+                           from ~cond(S) eps to ~eps.  Per-handle solver only (the batched
+                           and serving engines refuse it); default 0 */
 } psba_opts;
 
 typedef struct {
@@ -188,6 +193,12 @@ int psba_set_wait_limit(psba_handle *h, long long polls);
  * from their options.  No reference counterpart: the reference is FP64 only
  * (CL_files/PSBA.cl:2). */
 int psba_set_precision(psba_handle *h, int precision);
+
+/* Refinement step of the psba_eval_step calls (0 or 1, see psba_opts.refine);
+ * the drivers take it from their options.  No reference counterpart: the
+ * reference inverts S explicitly (SPD_inv.cl) and multiplies once
+ * (matVec_mul, cl_linearalg.cpp:19). */
+int psba_set_refine(psba_handle *h, int refine);
 
 /* compute_exQT (sba_func.cpp:81-145): ex = meas - projection; *cost = sum ex^2. */
 int psba_eval_residual(psba_handle *h, double *ex, double *cost);

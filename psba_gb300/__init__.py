@@ -42,7 +42,7 @@ class ProblemDesc(C.Structure):
 class Opts(C.Structure):
     _fields_ = [("tau", C.c_double), ("stop_thresh", C.c_double), ("eps", C.c_double),
                 ("eps2", C.c_double), ("max_iter", C.c_int), ("allow_switch", C.c_int),
-                ("precision", C.c_int), ("reserved", C.c_int)]
+                ("precision", C.c_int), ("refine", C.c_int)]
 
 
 class TraceEntry(C.Structure):
@@ -64,7 +64,7 @@ TRACE_DTYPE = np.dtype([("itno", np.int32), ("kind", np.int32), ("accepted", np.
 
 # every entry point declared in include/psba.h
 EXPORTS = ("psba_default_opts", "psba_create", "psba_destroy", "psba_get_params", "psba_set_params",
-           "psba_reset_params", "psba_set_precision", "psba_set_wait_limit",
+           "psba_reset_params", "psba_set_precision", "psba_set_refine", "psba_set_wait_limit",
            "psba_levmar", "psba_trust_region", "psba_solve_hybrid", "psba_eval_residual",
            "psba_eval_jacobian", "psba_eval_normal", "psba_eval_reduced", "psba_eval_step",
            "psba_eval_jmultiply", "psba_eval_cholmod", "psba_eval_dense_solve", "psba_eval_pivot_reciprocal",
@@ -105,6 +105,7 @@ def lib():
         L.psba_set_params.argtypes = [C.c_void_p, _dp, _dp]
         L.psba_reset_params.argtypes = [C.c_void_p]
         L.psba_set_precision.argtypes = [C.c_void_p, C.c_int]
+        L.psba_set_refine.argtypes = [C.c_void_p, C.c_int]
         L.psba_set_wait_limit.argtypes = [C.c_void_p, C.c_longlong]
         for f in ("psba_levmar", "psba_trust_region"):
             getattr(L, f).argtypes = [C.c_void_p, C.POINTER(Opts), _ip, C.POINTER(Result)]
@@ -266,6 +267,11 @@ class Solver:
     def set_precision(self, precision):
         """Precision of the eval_* stages: PREC_FP64 or PREC_MIXED."""
         _check(lib().psba_set_precision(self.h, int(precision)))
+
+    def set_refine(self, refine):
+        """1: one step of iterative refinement after each reduced solve of the
+        eval_* stages (the solves take it from their options)."""
+        _check(lib().psba_set_refine(self.h, int(refine)))
 
     def set_wait_limit(self, polls=0):
         """Polls per device-side wait before it reports a stall (0: default)."""

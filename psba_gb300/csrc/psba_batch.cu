@@ -1000,6 +1000,7 @@ int psba_batch_reset_params(psba_batch *b)
 int psba_batch_levmar(psba_batch *b, const psba_opts *opts, psba_batch_result *results, double *device_ms)
 {
     if (!b || !opts) return set_error("null argument"), PSBA_ERR_ARG;
+    if (opts->refine != 0) return set_error("psba_batch_levmar: refine is for the per-handle solver"), PSBA_ERR_ARG;
     HostBatch &h = b->hb;
     BatchOpts o;
     o.tau = opts->tau;

@@ -10,7 +10,10 @@
 // inverses, in a fixed dependency order; waits are bounded spins on per-task
 // flags in global memory (acquire/release).  After the factor, the back
 // solve L^T x = y runs on a thread-block cluster (k_tri_cluster; k_tri_solve,
-// one CTA, when PSBA_TRI_CLUSTER is 0).
+// one CTA, when PSBA_TRI_CLUSTER is 0).  On request one step of iterative
+// refinement follows: r = b - S x in FP64 against a copy of S taken before
+// the factor (k_refine_residual), then both triangular solves of r with the
+// factor, added into x (the same kernels with their forward part on).
 //
 // This replaces the reference's explicit inverse (SPD_inv.cl: 3x3-block
 // Cholesky chain, kern_trigMat_inv, kern_trigMat_mul, then matVec_mul) with
@@ -474,10 +477,41 @@ __device__ __forceinline__ double half_warp_sum(double p)
     return p;
 }
 
+// forward: b <- L^-1 b (right-looking: y_K = Linv_K b_K, then b_I -= L_IK y_K)
+__device__ void cta_forward(int Np, int nb, const double *__restrict__ S, const double *__restrict__ Linv,
+                            double *bs, double *tmp)
+{
+    const int tid = threadIdx.x;
+    for (int K = 0; K < nb; ++K) {
+        if (tid < T) {
+            const double *Li = Linv + (size_t)K * TT + tid * T;
+            double y = 0.0;
+#pragma unroll
+            for (int k = 0; k < T; ++k) y = fma(k <= tid ? __ldcg(Li + k) : 0.0, bs[K * T + k], y);
+            tmp[tid] = y;
+        }
+        __syncthreads();
+        if (tid < T) bs[K * T + tid] = tmp[tid];
+        for (int i = (K + 1) * T + tid; i < Np; i += blockDim.x) {
+            const double2 *row = reinterpret_cast<const double2 *>(S + (size_t)i * Np + K * T);
+            double s = 0.0;
+#pragma unroll
+            for (int c = 0; c < T / 2; ++c) {
+                const double2 v = __ldcg(row + c);
+                s = fma(v.x, tmp[2 * c], s);
+                s = fma(v.y, tmp[2 * c + 1], s);
+            }
+            bs[i] -= s;
+        }
+        __syncthreads();
+    }
+}
+
 // back: x <- L^-T y (right-looking over the columns of L^T: x_K = Linv_K^T y_K,
-// then y_I -= L_KI^T x_K for I < K, reading rows K*T..K*T+T-1 of L).
+// then y_I -= L_KI^T x_K for I < K, reading rows K*T..K*T+T-1 of L); acc: x
+// += the solution instead.
 __device__ void cta_back(int Np, int nb, const double *__restrict__ S, const double *__restrict__ Linv,
-                         double *ys, double *xs, double *__restrict__ x)
+                         double *ys, double *xs, double *__restrict__ x, bool acc)
 {
     const int tid = threadIdx.x, nthr = blockDim.x;
     const int dc = tid / T, dk = tid % T;  // diagonal product: output column, term
@@ -503,7 +537,7 @@ __device__ void cta_back(int Np, int nb, const double *__restrict__ S, const dou
             const double v = half_warp_sum(curL * ys[K * T + dk]);
             if (dk == 0) {
                 xs[dc] = v;
-                x[K * T + dc] = v;
+                x[K * T + dc] = acc ? x[K * T + dc] + v : v;
             }
         }
         __syncthreads();
@@ -1044,10 +1078,11 @@ int chol_grid(int n_tasks, int grid_cap)
 
 // The back solve L^T x = rhs in one CTA of TS_THREADS threads with the
 // right-hand side in shared memory (the factor's diagonal tasks already
-// applied L^-1 to rhs).  A failed factor (status != 0) leaves x untouched.
+// applied L^-1 to rhs); refine = 1: both solves of rhs, added into x.  A
+// failed factor (status != 0) leaves x untouched.
 constexpr int TS_THREADS = 512;
 
-__global__ void __launch_bounds__(TS_THREADS) k_tri_solve(int Np, int nb, const double *__restrict__ S,
+__global__ void __launch_bounds__(TS_THREADS) k_tri_solve(int refine, int Np, int nb, const double *__restrict__ S,
                                                            const double *__restrict__ Linv,
                                                            const double *__restrict__ rhs, double *__restrict__ x,
                                                            const int *__restrict__ status)
@@ -1057,12 +1092,14 @@ __global__ void __launch_bounds__(TS_THREADS) k_tri_solve(int Np, int nb, const 
     if (*status != 0) return;
     for (int i = threadIdx.x; i < Np; i += blockDim.x) vec[i] = rhs[i];
     __syncthreads();
-    cta_back(Np, nb, S, Linv, vec, tmp, x);
+    if (refine) cta_forward(Np, nb, S, Linv, vec, tmp);
+    cta_back(Np, nb, S, Linv, vec, tmp, x, refine != 0);
 }
 
 // ---------------------------------------------------------------------------
-// The back solve on a thread-block cluster of TC_CTAS CTAs (one SM
-// each).  One SM's FP64 rate bounds a one-CTA solve (N^2 / 2 multiply-adds);
+// The triangular solves on a thread-block cluster of TC_CTAS CTAs (one SM
+// each): the back solve after the factor, or (refine = 1) both solves of a
+// refinement residual, added into x.  One SM's FP64 rate bounds a one-CTA solve (N^2 / 2 multiply-adds);
 // the cluster spreads the updates over TC_CTAS SMs and passes each step's
 // solved block through distributed shared memory with one cluster barrier
 // per step (~400 cycles on GB300, against 1-2 us for a flag in L2).
@@ -1074,14 +1111,15 @@ __global__ void __launch_bounds__(TS_THREADS) k_tri_solve(int Np, int nb, const 
 // K from the owner and first updates the block the next step needs (if it
 // owns it), so the next owner can solve and arrive at once.  The diagonal
 // inverse entries and the coefficients of both updates are loaded a step
-// ahead, after the arrive.  Each vector entry takes its updates in step order: results
-// do not depend on timing.
+// ahead, after the arrive.  The forward solve runs the same steps in the
+// other direction over the rows of L.  Each vector entry takes its updates
+// in step order: results do not depend on timing.
 constexpr int TC_CTAS = 8, TC_THREADS = 256;
 
 __device__ __forceinline__ void cl_arrive() { asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory"); }
 __device__ __forceinline__ void cl_wait() { asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory"); }
 
-// v[c] -= sum_r P(r, c) xs[r] for the columns listed
+// v[c] -= sum_r P(r, c) xs[r] for the columns (back) or rows (forward) listed
 // by idx(q), q < n: four threads per entry, four terms each, fixed tree.  The
 // first pass (q < TC_THREADS / 4) takes its four coefficients from first[],
 // loaded by the caller a step ahead; later passes load them here.
@@ -1110,7 +1148,7 @@ __device__ __forceinline__ void cl_update(double *v, const double *xs, int n, co
     }
 }
 
-__global__ void __launch_bounds__(TC_THREADS) k_tri_cluster(int Np, int nb,
+__global__ void __launch_bounds__(TC_THREADS) k_tri_cluster(int refine, int Np, int nb,
                                                             const double *__restrict__ S,
                                                             const double *__restrict__ Linv,
                                                             const double *__restrict__ rhs,
@@ -1150,6 +1188,60 @@ __global__ void __launch_bounds__(TC_THREADS) k_tri_cluster(int Np, int nb,
     // ping-pong pair (the loop is unrolled by two), so nothing waits for a
     // load until the step that uses it; all loads are issued after the
     // arrive (a load in flight at the arrive would hold up its release).
+    if (refine) {
+        // L y = b: step K solves y_K = Linv_K b_K, then b_I -= L_IK y_K for I > K
+        auto ldiag = [&](int K) {
+            return mine(K) && dk <= dr ? __ldcg(Linv + (size_t)K * TT + dr * T + dk) : 0.0;
+        };
+        auto lcrit = [&](int K, double (&cf)[4]) {  // rows of block K+1, columns of block K
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                cf[j] = (cq < T && mine(K + 1)) ? __ldcg(S + (size_t)((K + 1) * T + cq) * Np + K * T + 4 * cg4 + j)
+                                                : 0.0;
+        };
+        auto ldef = [&](int P, double (&df)[4]) {  // rows of my blocks above P + 1, columns of block P
+            const int n = n_between(P + 1, nb);
+            const int i = cq < n ? entry_between(P + 1, cq) : 0;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) df[j] = cq < n ? __ldcg(S + (size_t)i * Np + P * T + 4 * cg4 + j) : 0.0;
+        };
+        int pend = -1;
+        auto step = [&](int K, double &pl, double &pln, double (&cf)[4], double (&cfn)[4], double (&df)[4],
+                        double (&dfn)[4]) {
+            if (mine(K)) {
+                const double yv = half_warp_sum(pl * vec[K * T + dk]);
+                if (dk == 0) xb[K & 1][dr] = yv;
+            }
+            __syncthreads();
+            if (mine(K) && tid < T) vec[K * T + tid] = xb[K & 1][tid];
+            cl_arrive();
+            pln = K + 1 < nb ? ldiag(K + 1) : 0.0;
+            lcrit(K + 1, cfn);
+            ldef(K, dfn);
+            if (pend >= 0) {  // the previous step's block, applied to my blocks above pend + 1
+                const int P = pend;
+                cl_update(vec, xs[P & 1], n_between(P + 1, nb), df,
+                          [&](int r, int i) { return __ldcg(S + (size_t)i * Np + P * T + r); },
+                          [&](int q) { return entry_between(P + 1, q); });
+            }
+            cl_wait();
+            if (tid < T) xs[K & 1][tid] = cl.map_shared_rank(&xb[K & 1][0], K % TC_CTAS)[tid];
+            __syncthreads();
+            if (mine(K + 1)) crit_apply(xs[K & 1], cf, (K + 1) * T + cq);
+            __syncthreads();
+            pend = K;
+        };
+        double plA = ldiag(0), plB = 0.0, cfA[4], cfB[4], dfA[4] = {0.0, 0.0, 0.0, 0.0}, dfB[4];
+        lcrit(0, cfA);
+        for (int K = 0; K < nb; K += 2) {
+            step(K, plA, plB, cfA, cfB, dfA, dfB);
+            if (K + 1 < nb) step(K + 1, plB, plA, cfB, cfA, dfB, dfA);
+        }
+        // the last step's block reaches no block above it; every CTA has read
+        // it before the back solve's first step rewrites its buffer
+        cl_arrive();
+        cl_wait();
+    }
     {
         // L^T x = y: step K solves x_K = Linv_K^T y_K, then y_I -= L_KI^T x_K for I < K
         auto ldiag = [&](int K) {
@@ -1204,8 +1296,34 @@ __global__ void __launch_bounds__(TC_THREADS) k_tri_cluster(int Np, int nb,
         cl_arrive();
         cl_wait();
         for (int I = rank; I < nb; I += TC_CTAS)
-            if (tid < T) x[I * T + tid] = vec[I * T + tid];
+            if (tid < T) x[I * T + tid] = refine ? x[I * T + tid] + vec[I * T + tid] : vec[I * T + tid];
     }
+}
+
+// The triangular solves after the factor: the back solve of d.rhs into x
+// (refine = 0), or both solves of d.rhs added into x (refine = 1).
+void launch_tri(const DeviceProblem &d, int refine, double *x, cudaStream_t s)
+{
+    const int nb = d.Np / T, Np = d.Np;
+#if PSBA_TRI_CLUSTER
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(TC_CTAS);
+    cfg.blockDim = dim3(TC_THREADS);
+    cfg.dynamicSmemBytes = sizeof(double) * Np;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = TC_CTAS;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const double *S = d.S, *Linv = d.Linv, *rhs = d.rhs;
+    cudaLaunchKernelEx(&cfg, k_tri_cluster, refine, Np, nb, S, Linv, rhs, x, (const int *)d.status);
+#else
+    k_tri_solve<<<1, TS_THREADS, sizeof(double) * Np, s>>>(refine, Np, nb, d.S, d.Linv, d.rhs, x, d.status);
+#endif
+    note_launch(1);
 }
 
 void launch_chol_dataflow(const DeviceProblem &d, int epoch, double *x_out, cudaStream_t s)
@@ -1224,28 +1342,76 @@ void launch_chol_dataflow(const DeviceProblem &d, int epoch, double *x_out, cuda
         cudaLaunchCooperativeKernel((const void *)k_chol_dataflow, dim3(grid), dim3(CF_THREADS), args, 0, s);
         note_launch(1);
     }
-#if PSBA_TRI_CLUSTER
-    {
-        cudaLaunchConfig_t cfg = {};
-        cfg.gridDim = dim3(TC_CTAS);
-        cfg.blockDim = dim3(TC_THREADS);
-        cfg.dynamicSmemBytes = sizeof(double) * Np;
-        cfg.stream = s;
-        cudaLaunchAttribute attr[1];
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = TC_CTAS;
-        attr[0].val.clusterDim.y = 1;
-        attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-        const double *S = d.S, *Linv = d.Linv, *rhs = d.rhs;
-        cudaLaunchKernelEx(&cfg, k_tri_cluster, Np, nb, S, Linv, rhs, x_out,
-                           (const int *)d.status);
+    launch_tri(d, 0, x_out, s);
+}
+
+// r = b - S x over the Np rows (S symmetric, its lower triangle in Sc with
+// leading dimension ld), each row's sum as Dot2 of Ogita, Rump and Oishi
+// ("Accurate sum and dot product", SIAM J. Sci. Comput. 26(6), 2005): every
+// product split exactly by an FMA, the running sum carried with Knuth's
+// TwoSum and the rounding errors summed beside it, so the residual is as
+// accurate as if S x were formed in twice the working precision.  A residual
+// formed in plain FP64 is mostly the rounding of S x (S x matches b to the
+// last bits after a backward-stable solve), so a refinement step on it
+// leaves the forward error where it was; on this one it falls from ~cond(S)
+// eps to ~eps.  One warp a row: the row's part left of the diagonal and the
+// column's part below it, each lane's terms in order, then a fixed xor tree
+// of the (sum, error) pairs.  A failed factor (status != 0) leaves r
+// untouched.
+constexpr int RR_THREADS = 256;
+
+// s + e = a + b exactly (Knuth's TwoSum)
+__device__ __forceinline__ void two_sum(double a, double b, double &s, double &e)
+{
+    s = __dadd_rn(a, b);
+    const double z = __dsub_rn(s, a);
+    e = __dadd_rn(__dsub_rn(a, __dsub_rn(s, z)), __dsub_rn(b, z));
+}
+
+// (hi, lo) += a x
+__device__ __forceinline__ void dot2_add(double a, double x, double &hi, double &lo)
+{
+    const double p = __dmul_rn(a, x);
+    const double pe = fma(a, x, -p);  // a x - p exactly
+    double t;
+    two_sum(hi, p, hi, t);
+    lo = __dadd_rn(lo, __dadd_rn(t, pe));
+}
+
+__global__ void __launch_bounds__(RR_THREADS) k_refine_residual(int Np, const double *__restrict__ Sc, int ld,
+                                                                 const double *__restrict__ b,
+                                                                 const double *__restrict__ x, double *__restrict__ r,
+                                                                 const int *__restrict__ status)
+{
+    const int i = (int)((blockIdx.x * (size_t)RR_THREADS + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (i >= Np || *status != 0) return;
+    const double *row = Sc + (size_t)i * ld;
+    double hi = 0.0, lo = 0.0;
+    for (int j = lane; j <= i; j += 32) dot2_add(row[j], x[j], hi, lo);
+    for (int j = i + 1 + lane; j < Np; j += 32) dot2_add(Sc[(size_t)j * ld + i], x[j], hi, lo);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const double oh = __shfl_xor_sync(0xffffffffu, hi, off), ol = __shfl_xor_sync(0xffffffffu, lo, off);
+        double t;
+        two_sum(hi, oh, hi, t);
+        lo = __dadd_rn(__dadd_rn(lo, ol), t);
     }
-#else
-    k_tri_solve<<<1, TS_THREADS, sizeof(double) * Np, s>>>(Np, nb, d.S, d.Linv, d.rhs, x_out, d.status);
-#endif
+    if (lane == 0) {
+        double s, t;
+        two_sum(b[i], -hi, s, t);
+        r[i] = __dadd_rn(s, __dsub_rn(t, lo));
+    }
+}
+
+// One refinement step of the solve x of S x = b just made: S and b were saved
+// (Sc with leading dimension ld, bc) before the factor overwrote them; the
+// residual goes to d.rhs, and its solve is added into x.
+void launch_refine(const DeviceProblem &d, const double *Sc, int ld, const double *bc, double *x, cudaStream_t s)
+{
+    const int blocks = (int)(((size_t)d.Np * 32 + RR_THREADS - 1) / RR_THREADS);
+    k_refine_residual<<<blocks, RR_THREADS, 0, s>>>(d.Np, Sc, ld, bc, x, d.rhs, d.status);
     note_launch(1);
+    launch_tri(d, 1, x, s);
 }
 
 // ---------------------------------------------------------------------------

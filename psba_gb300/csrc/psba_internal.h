@@ -148,15 +148,18 @@ struct DeviceProblem {
     double *cam_partial = nullptr;  // n_cam_units * 27
     // per-trial
     double *Vinv = nullptr;       // 6 per point
+    float *Vinv2f = nullptr;      // 12 per point: V^-1 as FP32 pairs hi + lo (the mixed form's Y)
+    float *gb32 = nullptr;        // 3 per point: gb rounded to FP32 (the mixed form's ea sums)
     double *Y = nullptr;          // 18 per obs
     double *schur_partial = nullptr;  // off-diagonal slots (off_partial_slots), then the diagonal units'
     double *S = nullptr;          // Np x Np (lower)
-    double *Ssave = nullptr;      // copy of S (trust-region modified-Cholesky fallback), Nm3 x Nm3
+    double *Ssave = nullptr;      // copy of S (trust-region modified-Cholesky fallback, refinement), Nm3 x Nm3
     // the fallback's matrix size: Np, or (N not a multiple of 3: 11/16-parameter
     // cameras) Np rounded up to a multiple of 3, the rows past Np identity
     int Nm3 = 0;
     double *rhs = nullptr;        // Np (ea on entry, y after the forward solve)
     double *xsol = nullptr;       // Np
+    double *rsave = nullptr;      // Np: ea saved before the factor (refinement)
     double *Linv = nullptr;       // (Np / TILE) * TILE * TILE inverses of the diagonal blocks
     int *status = nullptr;        // Cholesky status word (0 ok, 1 not SPD, 2 wait budget exhausted)
     int *tickets = nullptr;       // 2 words, zero between launches: last-block tickets (eb/dpb, residual)
@@ -237,6 +240,7 @@ void launch_scale(double *out, const double *x, const double *num, const double 
 // launch), then the back solve into x_out; epoch must increase from launch
 // to launch.
 void launch_chol_dataflow(const DeviceProblem &d, int epoch, double *x_out, cudaStream_t s);
+void launch_refine(const DeviceProblem &d, const double *Sc, int ld, const double *bc, double *x, cudaStream_t s);
 // at most cap CTAs for a handle's dense factor (0: one per SM); for callers
 // that run several handles side by side
 void set_chol_grid_cap(psba_handle *h, int cap);

@@ -400,7 +400,8 @@ __global__ void __launch_bounds__(256) k_point_blocks(int np, int ncp, const int
                                                       const int *__restrict__ pt_start,
                                                       const int *__restrict__ pt_order, const R *__restrict__ B,
                                                       const R *__restrict__ ex, R coeff, double *__restrict__ V,
-                                                      double *__restrict__ g, double *__restrict__ uvdiag)
+                                                      double *__restrict__ g, double *__restrict__ uvdiag,
+                                                      float *__restrict__ gb32)
 {
     // the eb/dpb warp schedule (points in pt_order, 3 m lanes a point): lane
     // r of a point sums its observations r, r + L, r + 2L, ... (L = 3 m), so
@@ -461,6 +462,11 @@ __global__ void __launch_bounds__(256) k_point_blocks(int np, int ncp, const int
     g[ncp + 3 * (size_t)i] = cf * s[6];
     g[ncp + 3 * (size_t)i + 1] = cf * s[7];
     g[ncp + 3 * (size_t)i + 2] = cf * s[8];
+    if (gb32) {  // the mixed form's ea sums take gb in FP32
+        gb32[3 * (size_t)i] = (float)(cf * s[6]);
+        gb32[3 * (size_t)i + 1] = (float)(cf * s[7]);
+        gb32[3 * (size_t)i + 2] = (float)(cf * s[8]);
+    }
 }
 
 void launch_point_blocks(const DeviceProblem &d, double coeff, cudaStream_t s)
@@ -468,11 +474,11 @@ void launch_point_blocks(const DeviceProblem &d, double coeff, cudaStream_t s)
     if (d.np == 0) return;
     if (d.prec == PSBA_PREC_FP64)
         k_point_blocks<double><<<eb_blocks(d), 256, 0, s>>>(d.np, d.N, d.eb_warps, d.pt_start, d.pt_order, d.B,
-                                                              d.ex, coeff, d.V, d.g, d.uvdiag);
+                                                              d.ex, coeff, d.V, d.g, d.uvdiag, nullptr);
     else
         k_point_blocks<float><<<eb_blocks(d), 256, 0, s>>>(d.np, d.N, d.eb_warps, d.pt_start, d.pt_order,
                                                              (const float *)d.B, (const float *)d.ex, (float)coeff,
-                                                             d.V, d.g, d.uvdiag);
+                                                             d.V, d.g, d.uvdiag, d.cnp == 6 ? d.gb32 : nullptr);
     note_launch(1);
 }
 
@@ -652,46 +658,91 @@ __device__ __forceinline__ void vinv_one(const R *Vi, R mu, R *out)
 // of the trial's bulk copies (status[2], set by k_yblocks_bulk when a wait
 // runs out), which nothing else resets.
 __global__ void k_vinv(int np, const double *__restrict__ V, double mu, double *__restrict__ Vinv,
-                       int *__restrict__ status)
+                       float *__restrict__ Vinv2f, int *__restrict__ status)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) status[2] = 0;
     if (i >= np) return;
     double vi[6], out[6];
+#pragma unroll
     for (int e = 0; e < 6; ++e) vi[e] = V[6 * (size_t)i + e];
     vinv_one<double>(vi, mu, out);
+#pragma unroll
     for (int e = 0; e < 6; ++e) Vinv[6 * (size_t)i + e] = out[e];
+    if (Vinv2f) {  // hi = fl32(v), lo = fl32(v - hi): v to ~2^-48
+        float2 *dst = reinterpret_cast<float2 *>(Vinv2f + 12 * (size_t)i);
+#pragma unroll
+        for (int e = 0; e < 6; ++e) {
+            const float hi = (float)out[e];
+            dst[e] = make_float2(hi, (float)(out[e] - (double)hi));
+        }
+    }
 }
 
 void launch_vinv(const DeviceProblem &d, double mu, cudaStream_t s)
 {
     if (d.np == 0) return;
-    k_vinv<<<ceil_div(d.np, 128), 128, 0, s>>>(d.np, d.V, mu, d.Vinv, d.status);
+    k_vinv<<<ceil_div(d.np, 128), 128, 0, s>>>(d.np, d.V, mu, d.Vinv,
+                                               d.prec == PSBA_PREC_MIXED && d.cnp == 6 ? d.Vinv2f : nullptr,
+                                               d.status);
     note_launch(1);
 }
 
-// Y = W V^-1 (compute_Yblks.cl:26-37), one thread per observation.
-// Y = W V^-1 evaluated in FP64 (V^-1 is FP64), stored in R.
-template <typename R>
+// s + e = a + b exactly (Knuth's TwoSum), FP32
+__device__ __forceinline__ void two_sum_f(float a, float b, float &s, float &e)
+{
+    s = __fadd_rn(a, b);
+    const float z = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, z)), __fsub_rn(b, z));
+}
+
+// w0 v0 + w1 v1 + w2 v2 with each v = hi + lo (two FP32 values), rounded
+// once to FP32: the products w hi split exactly by an FMA, the w lo products
+// and the errors summed beside a TwoSum chain, so the result is the FP32
+// rounding of the sum computed to ~2^-44 of its terms (double-float
+// arithmetic), as if formed in FP64 and rounded on store.
+__device__ __forceinline__ float dot3_df(float w0, float w1, float w2, float2 v0, float2 v1, float2 v2)
+{
+    const float p0 = __fmul_rn(w0, v0.x), p1 = __fmul_rn(w1, v1.x), p2 = __fmul_rn(w2, v2.x);
+    float lo = fmaf(w0, v0.x, -p0) + fmaf(w1, v1.x, -p1) + fmaf(w2, v2.x, -p2);
+    lo = fmaf(w0, v0.y, lo);
+    lo = fmaf(w1, v1.y, lo);
+    lo = fmaf(w2, v2.y, lo);
+    float s1, t1, s2, t2;
+    two_sum_f(p0, p1, s1, t1);
+    two_sum_f(s1, p2, s2, t2);
+    return __fadd_rn(s2, (t1 + t2) + lo);
+}
+
+// Y = W V^-1 (compute_Yblks.cl:26-37), one thread per observation, the
+// mixed form: W in FP32, V^-1 inverted in FP64 and carried as FP32 pairs
+// (hi + lo, split once per point), each Y entry formed in double-float
+// arithmetic and rounded to FP32.  No value passes through the FP64 pipe (on
+// GB300 a conversion between FP32 and FP64 issues there), and Y keeps the
+// accuracy of an FP64 product: a V^-1 rounded to FP32 instead breaks it for
+// points seen from nearby cameras (V nearly singular, V^-1 with large entries
+// of both signs), which sent LM to minima ~3% higher.  The FP64 form is
+// k_yblocks_bulk.
 __global__ void __launch_bounds__(256) k_yblocks(int no, const int *__restrict__ obs_pt,
-                                                 const R *__restrict__ W, const double *__restrict__ Vinv,
-                                                 R *__restrict__ Y)
+                                                 const float *__restrict__ W, const float *__restrict__ Vinv2f,
+                                                 float *__restrict__ Y)
 {
     int o = blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= no) return;
-    const double *vi = Vinv + 6 * (size_t)__ldg(obs_pt + o);
-    const double s00 = __ldg(vi), s01 = __ldg(vi + 1), s02 = __ldg(vi + 2), s11 = __ldg(vi + 3),
-                 s12 = __ldg(vi + 4), s22 = __ldg(vi + 5);
-    R w[18], y[18];
-    ldn<R, 18>(W + 18 * (size_t)o, w);
+    const float4 *vi = reinterpret_cast<const float4 *>(Vinv2f + 12 * (size_t)__ldg(obs_pt + o));
+    const float4 a = __ldg(vi), b = __ldg(vi + 1), c = __ldg(vi + 2);
+    const float2 s00 = make_float2(a.x, a.y), s01 = make_float2(a.z, a.w), s02 = make_float2(b.x, b.y),
+                 s11 = make_float2(b.z, b.w), s12 = make_float2(c.x, c.y), s22 = make_float2(c.z, c.w);
+    float w[18], y[18];
+    ldn<float, 18>(W + 18 * (size_t)o, w);
 #pragma unroll
     for (int r = 0; r < 6; ++r) {
-        const double w0 = w[3 * r], w1 = w[3 * r + 1], w2 = w[3 * r + 2];
-        y[3 * r + 0] = (R)(w0 * s00 + w1 * s01 + w2 * s02);
-        y[3 * r + 1] = (R)(w0 * s01 + w1 * s11 + w2 * s12);
-        y[3 * r + 2] = (R)(w0 * s02 + w1 * s12 + w2 * s22);
+        const float w0 = w[3 * r], w1 = w[3 * r + 1], w2 = w[3 * r + 2];
+        y[3 * r + 0] = dot3_df(w0, w1, w2, s00, s01, s02);
+        y[3 * r + 1] = dot3_df(w0, w1, w2, s01, s11, s12);
+        y[3 * r + 2] = dot3_df(w0, w1, w2, s02, s12, s22);
     }
-    stn<R, 18>(Y + 18 * (size_t)o, y);
+    stn<float, 18>(Y + 18 * (size_t)o, y);
 }
 
 // Bulk asynchronous copies between global and shared memory (the copy
@@ -739,13 +790,14 @@ __device__ __forceinline__ void bulk_s2g(void *dst, const void *src, unsigned by
 // rows (contiguous, 144 bytes each) come into shared memory by one bulk copy,
 // each thread forms its row of Y there (16-byte shared loads at a 144-byte
 // stride: no bank conflicts), and one bulk copy writes the CTA's Y rows
-// back.  Same arithmetic as k_yblocks.  A copy that does not complete within
-// poll_limit polls sets status[2] (the trial then reports the wait budget
-// exhausted); the CTA then waits for the copy to land in its shared memory
-// (at most YB_DRAIN_LIMIT polls: a bulk copy of 37 KB from this GPU's own
-// memory completes in microseconds) before it leaves.  Should the drain wait
-// also run out, the CTA leaves with the copy possibly still in flight; that
-// needs a copy stalled for the whole drain budget, which no test provokes.
+// back (the products of compute_Yblks.cl:26-37).  A copy that does not
+// complete within poll_limit polls sets status[2] (the trial then reports
+// the wait budget exhausted); the CTA then waits for the copy to land in
+// its shared memory (at most YB_DRAIN_LIMIT polls: a bulk copy of 37 KB from
+// this GPU's own memory completes in microseconds) before it leaves.  Should
+// the drain wait also run out, the CTA leaves with the copy possibly still
+// in flight; that needs a copy stalled for the whole drain budget, which no
+// test provokes.
 constexpr int YB_ROWS = 256;
 constexpr long long YB_DRAIN_LIMIT = 1LL << 22;
 
@@ -828,8 +880,7 @@ void launch_yblocks(const DeviceProblem &d, cudaStream_t s)
         k_yblocks_bulk<<<ceil_div(d.no, YB_ROWS), YB_ROWS, smem, s>>>(d.no, d.obs_pt, d.W, d.Vinv, d.Y, d.status,
                                                                       d.wait_limit);
     } else
-        k_yblocks<float><<<ceil_div(d.no, 256), 256, 0, s>>>(d.no, d.obs_pt, (const float *)d.W, d.Vinv,
-                                                               (float *)d.Y);
+        k_yblocks<<<ceil_div(d.no, 256), 256, 0, s>>>(d.no, d.obs_pt, (const float *)d.W, d.Vinv2f, (float *)d.Y);
     note_launch(1);
 }
 
@@ -929,6 +980,32 @@ __device__ __forceinline__ void diag_products(const R *y, const R *w, double g0,
     }
 }
 
+// The mixed form's diagonal products: the 21 block sums and the 6 ea sums
+// (y . gb) of one observation, all in FP32.
+__device__ __forceinline__ void diag_products_f32(const float *y, const float *w, float g0, float g1, float g2,
+                                                  float *acc)
+{
+    int v = 0;
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int c = 0; c <= r; ++c, ++v) {
+            float s = acc[v];
+            s = fmaf(y[3 * r], w[3 * c], s);
+            s = fmaf(y[3 * r + 1], w[3 * c + 1], s);
+            s = fmaf(y[3 * r + 2], w[3 * c + 2], s);
+            acc[v] = s;
+        }
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+        float s = acc[21 + r];
+        s = fmaf(y[3 * r], g0, s);
+        s = fmaf(y[3 * r + 1], g1, s);
+        s = fmaf(y[3 * r + 2], g2, s);
+        acc[21 + r] = s;
+    }
+}
+
 // Diagonal blocks U_k - sum Y W^T (lower 21) and the ea sums (6): one CTA of
 // SD_THREADS per unit of <= DIAG_SUPER observations of one camera, SD_PER
 // consecutive observations per thread (FP64: accumulated directly; mixed:
@@ -939,14 +1016,20 @@ __device__ __forceinline__ void diag_products(const R *y, const R *w, double g0,
 // form the unit's observation and point indices are first gathered into
 // shared memory (sidx, 2 DIAG_SUPER ints) by the whole CTA, so a thread's
 // walk waits for one L2 round trip per observation instead of three.
+// The mixed form's CTA reduction is narrower (two xor-shuffle levels first,
+// then 32 partials per output in shared memory): its shared buffer is also
+// the off-diagonal warps' index buffer, and a smaller one leaves the L1 more
+// room for the rows those warps gather.
+constexpr int SD_RED_MX = SD_THREADS / 4;
+
 template <typename R>
 __device__ __forceinline__ void schur_diag_cta(const SchurUnit u, const int *__restrict__ cam_obs,
                                                const int *__restrict__ obs_pt, const R *__restrict__ Y,
-                                               const R *__restrict__ W, const double *__restrict__ gb,
-                                               double *__restrict__ partial, int *sidx = nullptr)
+                                               const R *__restrict__ W, const R *__restrict__ gb,
+                                               double *__restrict__ partial, double *red_buf,
+                                               int *sidx = nullptr)
 {
     static_assert(SD_THREADS == 128 && DIAG_NV * 4 <= SD_THREADS, "four summing threads per output");
-    __shared__ double red[DIAG_NV][SD_THREADS + 1];
     const int t = threadIdx.x;
     double acc[DIAG_NV];
 #pragma unroll
@@ -971,31 +1054,50 @@ __device__ __forceinline__ void schur_diag_cta(const SchurUnit u, const int *__r
             sidx[DIAG_SUPER + k] = __ldg(obs_pt + a);
         }
         __syncthreads();
-        R part[21];
+        // the block and the ea sums alike: FP32 products summed over the
+        // thread's observations (gb rounded to FP32 once per point), then FP64
+        float part[DIAG_NV];
 #pragma unroll
-        for (int e = 0; e < 21; ++e) part[e] = (R)0;
+        for (int e = 0; e < DIAG_NV; ++e) part[e] = 0.0f;
 #pragma unroll 2
         for (int o = t * SD_PER; o < o1; ++o) {
             const int a = sidx[o];
             const int i = sidx[DIAG_SUPER + o];
-            R w[18], y[18];
-            ldn<R, 18>(W + 18 * (size_t)a, w);
-            ldn<R, 18>(Y + 18 * (size_t)a, y);
-            const double g0 = __ldg(gb + 3 * (size_t)i), g1 = __ldg(gb + 3 * (size_t)i + 1),
-                         g2 = __ldg(gb + 3 * (size_t)i + 2);
-            diag_products<R>(y, w, g0, g1, g2, part, acc + 21);
+            float w[18], y[18];
+            ldn<float, 18>(W + 18 * (size_t)a, w);
+            ldn<float, 18>(Y + 18 * (size_t)a, y);
+            const float g0 = __ldg(gb + 3 * (size_t)i), g1 = __ldg(gb + 3 * (size_t)i + 1),
+                        g2 = __ldg(gb + 3 * (size_t)i + 2);
+            diag_products_f32(y, w, g0, g1, g2, part);
         }
+        __syncthreads();  // the walk's indices are read: red may overlay them
 #pragma unroll
-        for (int e = 0; e < 21; ++e) acc[e] = (double)part[e];
+        for (int e = 0; e < DIAG_NV; ++e) acc[e] = (double)part[e];
     }
+    // fixed-order CTA sum: each output by four threads over W partials
+    // each, then the four (W = 32: one per thread; mixed form, W = 8 per
+    // warp after two xor levels over lanes l, l + 8, l + 16, l + 24)
+    constexpr int NP = is_fp64<R>() ? SD_THREADS : SD_RED_MX;
+    double(*red)[NP + 1] = reinterpret_cast<double(*)[NP + 1]>(red_buf);
+    if constexpr (is_fp64<R>()) {
 #pragma unroll
-    for (int e = 0; e < DIAG_NV; ++e) red[e][t] = acc[e];
+        for (int e = 0; e < DIAG_NV; ++e) red[e][t] = acc[e];
+    } else {
+        const int lane = t & 31;
+#pragma unroll
+        for (int e = 0; e < DIAG_NV; ++e) {
+            double x = acc[e];
+            x += __shfl_xor_sync(0xffffffffu, x, 16);
+            x += __shfl_xor_sync(0xffffffffu, x, 8);
+            if (lane < 8) red[e][(t >> 5) * 8 + lane] = x;
+        }
+    }
     __syncthreads();
     double s = 0.0;
     const int v = t >> 2, g = t & 3;
     if (v < DIAG_NV) {
 #pragma unroll 8
-        for (int q = 0; q < SD_THREADS / 4; ++q) s += red[v][g * (SD_THREADS / 4) + q];
+        for (int q = 0; q < NP / 4; ++q) s += red[v][g * (NP / 4) + q];
     }
     __syncthreads();
     if (v < DIAG_NV) red[v][g] = s;
@@ -1017,11 +1119,12 @@ __global__ void __launch_bounds__(128) k_schur(int n_chunks, int off_ctas, const
                                                double *__restrict__ diag_partial)
 {
     static_assert(SD_THREADS == 128, "one block size for both parts");
+    __shared__ double red[DIAG_NV][SD_THREADS + 1];
     if ((int)blockIdx.x < off_ctas)
         schur_off_chunk<double>(blockIdx.x * 128 + threadIdx.x, n_chunks, chunks, pair_start, pa, pb, Y, W,
                                 off_partial);
     else
-        schur_diag_cta<double>(diag_units[blockIdx.x - off_ctas], cam_obs, obs_pt, Y, W, gb, diag_partial);
+        schur_diag_cta<double>(diag_units[blockIdx.x - off_ctas], cam_obs, obs_pt, Y, W, gb, diag_partial, &red[0][0]);
 }
 
 int schur_off_wave_threads()
@@ -1138,16 +1241,21 @@ __global__ void __launch_bounds__(128) k_schur_f32(int n_units, int n_diag, cons
                                                    const SchurUnit *__restrict__ diag_units,
                                                    const int *__restrict__ cam_obs, const int *__restrict__ obs_pt,
                                                    const float *__restrict__ Y, const float *__restrict__ W,
-                                                   const double *__restrict__ gb, double *__restrict__ off_partial,
+                                                   const float *__restrict__ gb32, double *__restrict__ off_partial,
                                                    double *__restrict__ diag_partial)
 {
-    static_assert(4 * 2 * MX_UNIT >= 2 * DIAG_SUPER, "the index buffer holds a diagonal unit's indices");
-    __shared__ int sidx[4][2 * MX_UNIT];
+    // one shared buffer: a diagonal unit's indices, then its reduction
+    // (after a barrier), or the four warps' index lists
+    constexpr int RED_WORDS = DIAG_NV * (SD_RED_MX + 1) * 2, IDX_WORDS = 4 * 2 * MX_UNIT;
+    static_assert(IDX_WORDS >= 2 * DIAG_SUPER, "the index buffer holds a diagonal unit's indices");
+    __shared__ __align__(16) int buf[RED_WORDS > IDX_WORDS ? RED_WORDS : IDX_WORDS];
     if ((int)blockIdx.x < n_diag) {
-        schur_diag_cta<float>(diag_units[blockIdx.x], cam_obs, obs_pt, Y, W, gb, diag_partial, &sidx[0][0]);
+        schur_diag_cta<float>(diag_units[blockIdx.x], cam_obs, obs_pt, Y, W, gb32, diag_partial,
+                              reinterpret_cast<double *>(buf), buf);
     } else {
         const int uid = (blockIdx.x - n_diag) * 4 + (threadIdx.x >> 5);
-        if (uid < n_units) schur_off_warp(units[uid], pa, pb, Y, W, sidx[threadIdx.x >> 5], off_partial);
+        if (uid < n_units) schur_off_warp(units[uid], pa, pb, Y, W, buf + (threadIdx.x >> 5) * 2 * MX_UNIT,
+                                          off_partial);
     }
 }
 
@@ -1217,7 +1325,7 @@ void launch_schur_off(const DeviceProblem &d, cudaStream_t s)
     if (off_ctas + d.n_diag_units == 0) return;
     k_schur_f32<<<off_ctas + d.n_diag_units, 128, 0, s>>>(
         d.n_mx_units, d.n_diag_units, d.mx_units, d.pair_a, d.pair_b, d.diag_units, d.cam_obs, d.obs_pt,
-        (const float *)d.Y, (const float *)d.W, d.g + d.N, d.schur_partial,
+        (const float *)d.Y, (const float *)d.W, d.gb32, d.schur_partial,
         d.schur_partial + off_partial_slots(d) * 36);
     note_launch(1);
 }

@@ -489,7 +489,8 @@ int psba_server_create(const psba_server_opts *so, const psba_opts *lm, psba_ser
         (so->lanes_per_pair != 8 && so->lanes_per_pair != 16 && so->lanes_per_pair != 32) || so->large_cams < 0 ||
         so->large_lanes < 0 || so->large_lanes > 16 || !(so->large_share >= 0.0 && so->large_share < 1.0) ||
         so->large_obs < 0 ||
-        (lm->precision != PSBA_PREC_FP64 && lm->precision != PSBA_PREC_MIXED) || lm->max_iter < 0)
+        (lm->precision != PSBA_PREC_FP64 && lm->precision != PSBA_PREC_MIXED) || lm->max_iter < 0 ||
+        lm->refine != 0)
         return set_error("psba_server_create: bad options"), PSBA_ERR_ARG;
     psba_server *s = new psba_server();
     s->so = *so;

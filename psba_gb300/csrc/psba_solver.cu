@@ -77,6 +77,7 @@ struct psba_handle {
     double last_mu = 0.0;
     double *host_scalars = nullptr;  // pinned, 64 doubles
     int chol_epoch = 0;              // increases with every dense-solver launch
+    int refine = 0;                  // 1: one refinement step after each reduced solve
 };
 
 namespace {
@@ -341,7 +342,13 @@ void enqueue_step(psba_handle *h, double mu)
     DeviceProblem &d = h->d;
     {
         StageScope sc(h, ST_CHOL);
+        if (h->refine) {  // the factor overwrites S and ea: keep copies for the residual
+            cudaMemcpy2DAsync(d.Ssave, sizeof(double) * d.Nm3, d.S, sizeof(double) * d.Np, sizeof(double) * d.Np,
+                              d.Np, cudaMemcpyDeviceToDevice, h->stream);
+            cudaMemcpyAsync(d.rsave, d.rhs, sizeof(double) * d.Np, cudaMemcpyDeviceToDevice, h->stream);
+        }
         launch_chol_dataflow(d, ++h->chol_epoch, d.xsol, h->stream);
+        if (h->refine) launch_refine(d, d.Ssave, d.Nm3, d.rsave, d.xsol, h->stream);
         cudaMemcpyAsync(d.dp, d.xsol, sizeof(double) * d.N, cudaMemcpyDeviceToDevice, h->stream);
     }
     {
@@ -1032,12 +1039,15 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     TRY(dalloc(h, &d.uvdiag, nt));
     TRY(dalloc(h, &d.cam_partial, cam_nv * cam_units.size()));
     TRY(dalloc(h, &d.Vinv, 6 * (size_t)np));
+    TRY(dalloc(h, &d.Vinv2f, 12 * (size_t)np));
+    TRY(dalloc(h, &d.gb32, 3 * (size_t)np));
     TRY(dalloc(h, &d.Y, 3 * cnp * (size_t)no));
     TRY(dalloc(h, &d.schur_partial, cnp * cnp * off_partial_slots(d) + diag_nv * diag_units.size()));
     TRY(dalloc(h, &d.S, (size_t)d.Np * d.Np));
     d.Nm3 = d.N % 3 == 0 ? d.Np : ((d.Np + 2) / 3) * 3;
     TRY(dalloc(h, &d.Ssave, (size_t)d.Nm3 * d.Nm3));
     TRY(dalloc(h, &d.rhs, (size_t)d.Np));
+    TRY(dalloc(h, &d.rsave, (size_t)d.Np));
     TRY(dalloc(h, &d.xsol, (size_t)d.Np));
     TRY(dalloc(h, &d.Linv, (size_t)d.Np * TILE));
     TRY(dalloc(h, &d.status, 4));
@@ -1192,6 +1202,7 @@ int check_opts(const psba_opts *o)
     if (!o) return set_error("null options"), PSBA_ERR_ARG;
     if (o->precision != PSBA_PREC_FP64 && o->precision != PSBA_PREC_MIXED)
         return set_error("unknown precision"), PSBA_ERR_ARG;
+    if (o->refine != 0 && o->refine != 1) return set_error("refine must be 0 or 1"), PSBA_ERR_ARG;
     return PSBA_OK;
 }
 
@@ -1209,7 +1220,7 @@ void psba_default_opts(psba_opts *o)
     o->max_iter = 50;
     o->allow_switch = 1;
     o->precision = PSBA_PREC_FP64;
-    o->reserved = 0;
+    o->refine = 0;
 }
 
 int psba_create(const psba_problem_desc *desc, psba_handle **out)
@@ -1295,6 +1306,7 @@ int psba_levmar(psba_handle *h, const psba_opts *opts, int *itno, psba_result *r
     if (!h || !itno) return set_error("null argument"), PSBA_ERR_ARG;
     TRY(check_opts(opts));
     h->d.prec = opts->precision;
+    h->refine = opts->refine;
     reset_result(res);
     TRY(timed_begin(h));
     int flag = 0;
@@ -1308,6 +1320,7 @@ int psba_trust_region(psba_handle *h, const psba_opts *opts, int *itno, psba_res
     if (!h || !itno) return set_error("null argument"), PSBA_ERR_ARG;
     TRY(check_opts(opts));
     h->d.prec = opts->precision;
+    h->refine = opts->refine;
     reset_result(res);
     TRY(timed_begin(h));
     int flag = 0;
@@ -1321,6 +1334,7 @@ int psba_solve_hybrid(psba_handle *h, const psba_opts *opts, psba_result *res)
     if (!h) return set_error("null argument"), PSBA_ERR_ARG;
     TRY(check_opts(opts));
     h->d.prec = opts->precision;
+    h->refine = opts->refine;
     reset_result(res);
     TRY(timed_begin(h));
     int itno = 0, flag = 0;
@@ -1523,6 +1537,15 @@ int psba_set_precision(psba_handle *h, int precision)
     TRY(sync(h));
     h->d.prec = precision;
     h->linearized = 0;
+    return PSBA_OK;
+}
+
+int psba_set_refine(psba_handle *h, int refine)
+{
+    if (!h) return set_error("null handle"), PSBA_ERR_ARG;
+    if (refine != 0 && refine != 1) return set_error("refine must be 0 or 1"), PSBA_ERR_ARG;
+    TRY(sync(h));
+    h->refine = refine;
     return PSBA_OK;
 }
 

@@ -41,6 +41,15 @@ def test_default_opts_are_reference_constants(L):
     o = psba_gb300.default_opts()
     assert o.tau == 1e-3 and o.stop_thresh == 1e-12 and o.eps == 1e-12 and o.eps2 == 1e-12
     assert o.max_iter == 50 and o.allow_switch == 1 and o.precision == psba_gb300.PREC_FP64
+    assert o.refine == 0
+
+
+def test_server_refuses_refine(L):
+    # the refinement step is for the per-handle solver; the server's options
+    # are checked before anything touches the device
+    from psba_gb300.serve import Server
+    with pytest.raises(psba_gb300.PSBAError):
+        Server(refine=1)
 
 
 def test_version_string(L):

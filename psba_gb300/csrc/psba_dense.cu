@@ -477,6 +477,14 @@ __device__ __forceinline__ double half_warp_sum(double p)
     return p;
 }
 
+// x as two FP32 values hi + lo (x to ~2^-48): the mixed form's eb sums take
+// dpa in this form, so that their products need no FP64 instruction
+__device__ __forceinline__ float2 split2f(double x)
+{
+    const float hi = (float)x;
+    return make_float2(hi, (float)(x - (double)hi));
+}
+
 // forward: b <- L^-1 b (right-looking: y_K = Linv_K b_K, then b_I -= L_IK y_K)
 __device__ void cta_forward(int Np, int nb, const double *__restrict__ S, const double *__restrict__ Linv,
                             double *bs, double *tmp)
@@ -511,7 +519,7 @@ __device__ void cta_forward(int Np, int nb, const double *__restrict__ S, const 
 // then y_I -= L_KI^T x_K for I < K, reading rows K*T..K*T+T-1 of L); acc: x
 // += the solution instead.
 __device__ void cta_back(int Np, int nb, const double *__restrict__ S, const double *__restrict__ Linv,
-                         double *ys, double *xs, double *__restrict__ x, bool acc)
+                         double *ys, double *xs, double *__restrict__ x, bool acc, float2 *__restrict__ x2)
 {
     const int tid = threadIdx.x, nthr = blockDim.x;
     const int dc = tid / T, dk = tid % T;  // diagonal product: output column, term
@@ -537,7 +545,9 @@ __device__ void cta_back(int Np, int nb, const double *__restrict__ S, const dou
             const double v = half_warp_sum(curL * ys[K * T + dk]);
             if (dk == 0) {
                 xs[dc] = v;
-                x[K * T + dc] = acc ? x[K * T + dc] + v : v;
+                const double xv = acc ? x[K * T + dc] + v : v;
+                x[K * T + dc] = xv;
+                if (x2) x2[K * T + dc] = split2f(xv);
             }
         }
         __syncthreads();
@@ -1085,7 +1095,7 @@ constexpr int TS_THREADS = 512;
 __global__ void __launch_bounds__(TS_THREADS) k_tri_solve(int refine, int Np, int nb, const double *__restrict__ S,
                                                            const double *__restrict__ Linv,
                                                            const double *__restrict__ rhs, double *__restrict__ x,
-                                                           const int *__restrict__ status)
+                                                           float2 *__restrict__ x2, const int *__restrict__ status)
 {
     extern __shared__ double vec[];  // Np
     __shared__ double tmp[T];
@@ -1093,7 +1103,7 @@ __global__ void __launch_bounds__(TS_THREADS) k_tri_solve(int refine, int Np, in
     for (int i = threadIdx.x; i < Np; i += blockDim.x) vec[i] = rhs[i];
     __syncthreads();
     if (refine) cta_forward(Np, nb, S, Linv, vec, tmp);
-    cta_back(Np, nb, S, Linv, vec, tmp, x, refine != 0);
+    cta_back(Np, nb, S, Linv, vec, tmp, x, refine != 0, x2);
 }
 
 // ---------------------------------------------------------------------------
@@ -1152,7 +1162,8 @@ __global__ void __launch_bounds__(TC_THREADS) k_tri_cluster(int refine, int Np, 
                                                             const double *__restrict__ S,
                                                             const double *__restrict__ Linv,
                                                             const double *__restrict__ rhs,
-                                                            double *__restrict__ x, const int *__restrict__ status)
+                                                            double *__restrict__ x, float2 *__restrict__ x2,
+                                                            const int *__restrict__ status)
 {
     static_assert(TC_THREADS == TT, "one thread per term of the 16 x 16 diagonal product");
     extern __shared__ double vec[];  // Np; this CTA's blocks are the valid ones
@@ -1296,7 +1307,11 @@ __global__ void __launch_bounds__(TC_THREADS) k_tri_cluster(int refine, int Np, 
         cl_arrive();
         cl_wait();
         for (int I = rank; I < nb; I += TC_CTAS)
-            if (tid < T) x[I * T + tid] = refine ? x[I * T + tid] + vec[I * T + tid] : vec[I * T + tid];
+            if (tid < T) {
+                const double xv = refine ? x[I * T + tid] + vec[I * T + tid] : vec[I * T + tid];
+                x[I * T + tid] = xv;
+                if (x2) x2[I * T + tid] = split2f(xv);
+            }
     }
 }
 
@@ -1305,6 +1320,9 @@ __global__ void __launch_bounds__(TC_THREADS) k_tri_cluster(int refine, int Np, 
 void launch_tri(const DeviceProblem &d, int refine, double *x, cudaStream_t s)
 {
     const int nb = d.Np / T, Np = d.Np;
+    // the solution also as FP32 pairs for the mixed form's eb sums (x is dpa
+    // on every path that reaches them)
+    float2 *x2 = d.prec == PSBA_PREC_MIXED && d.cnp == 6 ? d.dpa2f : nullptr;
 #if PSBA_TRI_CLUSTER
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(TC_CTAS);
@@ -1319,9 +1337,9 @@ void launch_tri(const DeviceProblem &d, int refine, double *x, cudaStream_t s)
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     const double *S = d.S, *Linv = d.Linv, *rhs = d.rhs;
-    cudaLaunchKernelEx(&cfg, k_tri_cluster, refine, Np, nb, S, Linv, rhs, x, (const int *)d.status);
+    cudaLaunchKernelEx(&cfg, k_tri_cluster, refine, Np, nb, S, Linv, rhs, x, x2, (const int *)d.status);
 #else
-    k_tri_solve<<<1, TS_THREADS, sizeof(double) * Np, s>>>(refine, Np, nb, d.S, d.Linv, d.rhs, x, d.status);
+    k_tri_solve<<<1, TS_THREADS, sizeof(double) * Np, s>>>(refine, Np, nb, d.S, d.Linv, d.rhs, x, x2, d.status);
 #endif
     note_launch(1);
 }

@@ -17,6 +17,7 @@ constexpr int CNP = 6;   // camera parameters (rotation vector part + translatio
 constexpr int PNP = 3;   // point parameters
 constexpr int MNP = 2;   // image coordinates
 constexpr int CAMTAB = 56;  // doubles per camera table entry (CamTab)
+constexpr int CAMTAB32 = 40;  // floats per FP32 camera table entry: M, D, fx, sk, fy (the mixed Jacobian)
 constexpr int TILE = 16;    // dense Cholesky tile size
 constexpr int SCHUR_CHUNK = 32;  // pair-list entries per off-diagonal Schur work unit (11/16-parameter cameras)
 constexpr int OFF_MIN_LEN = 8;   // 6-parameter cameras: fewest pair-list entries per off-diagonal chunk
@@ -150,6 +151,7 @@ struct DeviceProblem {
     double *Vinv = nullptr;       // 6 per point
     float *Vinv2f = nullptr;      // 12 per point: V^-1 as FP32 pairs hi + lo (the mixed form's Y)
     float *gb32 = nullptr;        // 3 per point: gb rounded to FP32 (the mixed form's ea sums)
+    float *camtab32 = nullptr;    // CAMTAB32 per camera: the table's M, D, fx, sk, fy in FP32 (mixed J)
     double *Y = nullptr;          // 18 per obs
     double *schur_partial = nullptr;  // off-diagonal slots (off_partial_slots), then the diagonal units'
     double *S = nullptr;          // Np x Np (lower)
@@ -160,6 +162,7 @@ struct DeviceProblem {
     double *rhs = nullptr;        // Np (ea on entry, y after the forward solve)
     double *xsol = nullptr;       // Np
     double *rsave = nullptr;      // Np: ea saved before the factor (refinement)
+    float2 *dpa2f = nullptr;      // Np: dpa as FP32 pairs hi + lo (the mixed form's eb sums)
     double *Linv = nullptr;       // (Np / TILE) * TILE * TILE inverses of the diagonal blocks
     int *status = nullptr;        // Cholesky status word (0 ok, 1 not SPD, 2 wait budget exhausted)
     int *tickets = nullptr;       // 2 words, zero between launches: last-block tickets (eb/dpb, residual)
@@ -185,7 +188,7 @@ struct DeviceProblem {
 
 // Linearization: camera tables, residual, Jacobian, W, V, gb, U, ga.
 void launch_cam_tables(const DeviceProblem &d, const double *cams, const double *dpa,
-                       double *tab, cudaStream_t s);
+                       double *tab, cudaStream_t s, float *tab32 = nullptr);
 void launch_linearize(const DeviceProblem &d, double coeff, cudaStream_t s);
 void launch_point_blocks(const DeviceProblem &d, double coeff, cudaStream_t s);
 void launch_camera_blocks(const DeviceProblem &d, double coeff, cudaStream_t s);

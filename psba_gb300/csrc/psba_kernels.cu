@@ -104,7 +104,8 @@ __device__ void sum_partials_block(const double *partial, int n, double *dst)
 // warp 0 writes M, t and the intrinsics, warp 1 + m writes D[m].
 __global__ void __launch_bounds__(128) k_cam_tables(int nc, int cnp, const double *__restrict__ K,
                                                     const double *__restrict__ q0, const double *__restrict__ cams,
-                                                    const double *__restrict__ dpa, double *__restrict__ tab)
+                                                    const double *__restrict__ dpa, double *__restrict__ tab,
+                                                    float *__restrict__ tab32)
 {
     const int role = threadIdx.x >> 5;
     const int j = blockIdx.x * 32 + (threadIdx.x & 31);
@@ -125,6 +126,11 @@ __global__ void __launch_bounds__(128) k_cam_tables(int nc, int cnp, const doubl
         T->M[0] = d + 2 * a * a;      T->M[1] = 2 * (a * b - s * c); T->M[2] = 2 * (a * c + s * b);
         T->M[3] = 2 * (a * b + s * c); T->M[4] = d + 2 * b * b;      T->M[5] = 2 * (b * c - s * a);
         T->M[6] = 2 * (a * c - s * b); T->M[7] = 2 * (b * c + s * a); T->M[8] = d + 2 * c * c;
+        if (tab32) {  // the mixed Jacobian's operands, rounded once per camera
+            float *F = tab32 + (size_t)CAMTAB32 * j;
+#pragma unroll
+            for (int e = 0; e < 9; ++e) F[e] = (float)T->M[e];
+        }
         for (int m = 0; m < 3; ++m) T->t[m] = dj ? cj[3 + m] + dj[3 + m] : cj[3 + m];
         double kk[5], kc[5] = {0, 0, 0, 0, 0};
         if (cnp > 6) {
@@ -135,6 +141,13 @@ __global__ void __launch_bounds__(128) k_cam_tables(int nc, int cnp, const doubl
             for (int m = 0; m < 5; ++m) kk[m] = K[5 * j + m];
         }
         T->fx = kk[0]; T->cx = kk[1]; T->cy = kk[2]; T->fy = kk[0] * kk[3]; T->sk = kk[4];
+        if (tab32) {
+            float *F = tab32 + (size_t)CAMTAB32 * j;
+            F[36] = (float)T->fx;
+            F[37] = (float)T->sk;
+            F[38] = (float)T->fy;
+            F[39] = 0.0f;
+        }
         T->ar = kk[3];
         for (int m = 0; m < 5; ++m) T->kc[m] = kc[m];
         for (int m = 0; m < 6; ++m) T->pad[m] = 0.0;
@@ -161,12 +174,17 @@ __global__ void __launch_bounds__(128) k_cam_tables(int nc, int cnp, const doubl
     double *D = T->D + 9 * m;
 #pragma unroll
     for (int e = 0; e < 9; ++e) D[e] = dS[e] * dq0 + dA[e] * dq1 + dB[e] * dq2 + dC[e] * dq3;
+    if (tab32) {
+        float *F = tab32 + (size_t)CAMTAB32 * j + 9 + 9 * m;
+#pragma unroll
+        for (int e = 0; e < 9; ++e) F[e] = (float)D[e];
+    }
 }
 
 void launch_cam_tables(const DeviceProblem &d, const double *cams, const double *dpa, double *tab,
-                       cudaStream_t s)
+                       cudaStream_t s, float *tab32)
 {
-    k_cam_tables<<<ceil_div(d.nc, 32), 128, 0, s>>>(d.nc, d.cnp, d.K, d.q0, cams, dpa, tab);
+    k_cam_tables<<<ceil_div(d.nc, 32), 128, 0, s>>>(d.nc, d.cnp, d.K, d.q0, cams, dpa, tab, tab32);
     note_launch(1);
 }
 
@@ -183,7 +201,8 @@ __global__ void __launch_bounds__(256) k_linearize(int no, const int *__restrict
                                                    const double *__restrict__ tab, R coeff,
                                                    const double *__restrict__ wt,
                                                    R *__restrict__ ex, R *__restrict__ A,
-                                                   R *__restrict__ B, R *__restrict__ W)
+                                                   R *__restrict__ B, R *__restrict__ W,
+                                                   const float *__restrict__ tab32)
 {
     int o = blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= no) return;
@@ -218,10 +237,15 @@ __global__ void __launch_bounds__(256) k_linearize(int no, const int *__restrict
     }
     st2<R>(ex + 2 * (size_t)o, (R)e0, (R)e1);
     const R X0 = (R)Xd0, X1 = (R)Xd1, X2 = (R)Xd2;
+    // the mixed form takes the table's FP32 copy (the same values, rounded
+    // once per camera instead of once per observation on the FP64 pipe)
+    const float *F = is_fp64<R>() ? nullptr : tab32 + (size_t)CAMTAB32 * j;
     R M[9];
 #pragma unroll
-    for (int e = 0; e < 9; ++e) M[e] = (R)Md[e];
-    const R yc = (R)ycd, iz = (R)izd, nu = (R)nud, fx = (R)fxd, sk = (R)skd, fy = (R)fyd;
+    for (int e = 0; e < 9; ++e) M[e] = is_fp64<R>() ? (R)Md[e] : (R)__ldg(F + e);
+    const R yc = (R)ycd, iz = (R)izd, nu = (R)nud;
+    const R fx = is_fp64<R>() ? (R)fxd : (R)__ldg(F + 36), sk = is_fp64<R>() ? (R)skd : (R)__ldg(F + 37),
+            fy = is_fp64<R>() ? (R)fyd : (R)__ldg(F + 38);
     // d(x,y)/dXc
     const R p00 = fx * iz, p01 = sk * iz, p02 = -nu * iz * iz;
     const R p11 = fy * iz, p12 = -fy * yc * iz * iz;
@@ -229,10 +253,17 @@ __global__ void __launch_bounds__(256) k_linearize(int no, const int *__restrict
     R a[12];
 #pragma unroll
     for (int m = 0; m < 3; ++m) {
-        const double *Dm = T + 9 + 9 * m;
-        const R g0 = (R)__ldg(Dm + 0) * X0 + (R)__ldg(Dm + 1) * X1 + (R)__ldg(Dm + 2) * X2;
-        const R g1 = (R)__ldg(Dm + 3) * X0 + (R)__ldg(Dm + 4) * X1 + (R)__ldg(Dm + 5) * X2;
-        const R g2 = (R)__ldg(Dm + 6) * X0 + (R)__ldg(Dm + 7) * X1 + (R)__ldg(Dm + 8) * X2;
+        R Dm[9];
+        if constexpr (is_fp64<R>()) {
+#pragma unroll
+            for (int e = 0; e < 9; ++e) Dm[e] = __ldg(T + 9 + 9 * m + e);
+        } else {
+#pragma unroll
+            for (int e = 0; e < 9; ++e) Dm[e] = __ldg(F + 9 + 9 * m + e);
+        }
+        const R g0 = Dm[0] * X0 + Dm[1] * X1 + Dm[2] * X2;
+        const R g1 = Dm[3] * X0 + Dm[4] * X1 + Dm[5] * X2;
+        const R g2 = Dm[6] * X0 + Dm[7] * X1 + Dm[8] * X2;
         a[m] = p00 * g0 + p01 * g1 + p02 * g2;
         a[6 + m] = p11 * g1 + p12 * g2;
     }
@@ -282,11 +313,12 @@ void launch_linearize(const DeviceProblem &d, double coeff, cudaStream_t s)
     if (d.no == 0) return;
     if (d.prec == PSBA_PREC_FP64) {
         k_linearize<double><<<ceil_div(d.no, 256), 256, 0, s>>>(d.no, d.obs_pt, d.obs_cam, d.meas, d.pts,
-                                                                  d.camtab, coeff, d.wt, d.ex, d.A, d.B, d.W);
+                                                                  d.camtab, coeff, d.wt, d.ex, d.A, d.B, d.W,
+                                                                  nullptr);
     } else {
         k_linearize<float><<<ceil_div(d.no, 256), 256, 0, s>>>(
             d.no, d.obs_pt, d.obs_cam, d.meas, d.pts, d.camtab, (float)coeff, d.wt, (float *)d.ex, (float *)d.A,
-            (float *)d.B, (float *)d.W);
+            (float *)d.B, (float *)d.W, d.camtab32);
     }
     note_launch(1);
 }
@@ -386,15 +418,24 @@ void launch_residual(const DeviceProblem &d, const double *tab, const double *pt
     note_launch(1);
 }
 
+// s + e = a + b exactly (Knuth's TwoSum), FP32
+__device__ __forceinline__ void two_sum_f(float a, float b, float &s, float &e)
+{
+    s = __fadd_rn(a, b);
+    const float z = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, z)), __fsub_rn(b, z));
+}
+
 // ---------------------------------------------------------------------------
 // Per-point sums: V_i = coeff sum B^T B (compute_V.cl:24-37) and
 // gb_i = coeff sum B^T e (compute_g.cl:42-57): 3 m lanes a point, each
 // summing every (3 m)-th observation in ascending camera order, then the
 // lanes' sums added in a fixed order.
-// V is accumulated in FP64 in both forms (in the mixed form from FP32
-// products): an FP32 running sum of B^T B can turn the nearly singular V of a
-// point seen from two close cameras indefinite, which moved the mixed form's
-// LM fixed point by 7e-3 of the cost on a 24-camera power-law scene.
+// V is accumulated to FP64 accuracy in both forms (in the mixed form from
+// FP32 products, in double-float FP32 arithmetic: ~2^-44 of the terms): an
+// FP32 running sum of B^T B can turn the nearly singular V of a point seen
+// from two close cameras indefinite, which moved the mixed form's LM fixed
+// point by 7e-3 of the cost on a 24-camera power-law scene.
 template <typename R>
 __global__ void __launch_bounds__(256) k_point_blocks(int np, int ncp, const int2 *__restrict__ eb_warps,
                                                       const int *__restrict__ pt_start,
@@ -413,35 +454,65 @@ __global__ void __launch_bounds__(256) k_point_blocks(int np, int ncp, const int
     const int L = 3 * wi.y, pw = lane / L, r = lane - L * pw;
     const bool live = pw < npw;
     const int i = live ? pt_order[wi.x + pw] : 0;
-    double a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // v00 v01 v02 v11 v12 v22, then the gradient (FP64 sums of exact products in both forms)
-    if (live) {
-        const int e = pt_start[i + 1];
+    double a[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // v00 v01 v02 v11 v12 v22, then the gradient
+    if constexpr (is_fp64<R>()) {
+        if (live) {
+            const int e = pt_start[i + 1];
 #pragma unroll 2
-        for (int o = pt_start[i] + r; o < e; o += L) {
-            R b[6], ee[2];
-            ldn<R, 6>(B + 6 * (size_t)o, b);
-            ld2<R>(ex + 2 * (size_t)o, ee[0], ee[1]);
-            const R b0 = b[0], b1 = b[1], b2 = b[2], c0 = b[3], c1 = b[4], c2 = b[5];
-            const R e0 = ee[0], e1 = ee[1];
-            if constexpr (is_fp64<R>()) {
+            for (int o = pt_start[i] + r; o < e; o += L) {
+                R b[6], ee[2];
+                ldn<R, 6>(B + 6 * (size_t)o, b);
+                ld2<R>(ex + 2 * (size_t)o, ee[0], ee[1]);
+                const R b0 = b[0], b1 = b[1], b2 = b[2], c0 = b[3], c1 = b[4], c2 = b[5];
+                const R e0 = ee[0], e1 = ee[1];
                 a[0] = a[0] + b0 * b0 + c0 * c0;
                 a[1] = a[1] + b0 * b1 + c0 * c1;
                 a[2] = a[2] + b0 * b2 + c0 * c2;
                 a[3] = a[3] + b1 * b1 + c1 * c1;
                 a[4] = a[4] + b1 * b2 + c1 * c2;
                 a[5] = a[5] + b2 * b2 + c2 * c2;
-            } else {
-                a[0] += (double)(b0 * b0 + c0 * c0);
-                a[1] += (double)(b0 * b1 + c0 * c1);
-                a[2] += (double)(b0 * b2 + c0 * c2);
-                a[3] += (double)(b1 * b1 + c1 * c1);
-                a[4] += (double)(b1 * b2 + c1 * c2);
-                a[5] += (double)(b2 * b2 + c2 * c2);
+                a[6] = a[6] + b0 * e0 + c0 * e1;
+                a[7] = a[7] + b1 * e0 + c1 * e1;
+                a[8] = a[8] + b2 * e0 + c2 * e1;
             }
-            a[6] = a[6] + (double)b0 * (double)e0 + (double)c0 * (double)e1;
-            a[7] = a[7] + (double)b1 * (double)e0 + (double)c1 * (double)e1;
-            a[8] = a[8] + (double)b2 * (double)e0 + (double)c2 * (double)e1;
         }
+    } else {
+        // the mixed form in double-float FP32 arithmetic (hi, lo pairs,
+        // TwoSum), converted to FP64 once per lane: V sums the FP32 products
+        // b_k b_l + c_k c_l, the gradient the exact products b e (each split
+        // by an FMA), so the sums are those of FP64 to ~2^-44 without an FP64
+        // instruction per observation
+        float h[9], l[9];
+#pragma unroll
+        for (int v = 0; v < 9; ++v) h[v] = l[v] = 0.0f;
+        if (live) {
+            const int e = pt_start[i + 1];
+            for (int o = pt_start[i] + r; o < e; o += L) {
+                float b[6], e0, e1;
+                ldn<float, 6>(reinterpret_cast<const float *>(B) + 6 * (size_t)o, b);
+                ld2<float>(reinterpret_cast<const float *>(ex) + 2 * (size_t)o, e0, e1);
+                const float vv[6] = {fmaf(b[0], b[0], b[3] * b[3]), fmaf(b[0], b[1], b[3] * b[4]),
+                                     fmaf(b[0], b[2], b[3] * b[5]), fmaf(b[1], b[1], b[4] * b[4]),
+                                     fmaf(b[1], b[2], b[4] * b[5]), fmaf(b[2], b[2], b[5] * b[5])};
+#pragma unroll
+                for (int v = 0; v < 6; ++v) {
+                    float t;
+                    two_sum_f(h[v], vv[v], h[v], t);
+                    l[v] += t;
+                }
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const float p0 = __fmul_rn(b[k], e0), p1 = __fmul_rn(b[3 + k], e1);
+                    const float q = fmaf(b[k], e0, -p0) + fmaf(b[3 + k], e1, -p1);
+                    float t0, t1;
+                    two_sum_f(h[6 + k], p0, h[6 + k], t0);
+                    two_sum_f(h[6 + k], p1, h[6 + k], t1);
+                    l[6 + k] += (t0 + t1) + q;
+                }
+            }
+        }
+#pragma unroll
+        for (int v = 0; v < 9; ++v) a[v] = (double)h[v] + (double)l[v];
     }
     double s[9];
 #pragma unroll
@@ -513,6 +584,9 @@ __global__ void __launch_bounds__(CAM_THREADS) k_camera_partial(const CamUnit *_
     R part[21];
 #pragma unroll
     for (int v = 0; v < 21; ++v) part[v] = (R)0;
+    float gh[6], gl[6];  // mixed form: the gradient sums as double-float pairs
+#pragma unroll
+    for (int q = 0; q < 6; ++q) gh[q] = gl[q] = 0.0f;
     const int k1 = min(u.count, (t + 1) * CAM_PER);
     for (int kk = t * CAM_PER; kk < k1; ++kk) {
         const int o = __ldg(cam_obs + u.begin + kk);
@@ -531,15 +605,30 @@ __global__ void __launch_bounds__(CAM_THREADS) k_camera_partial(const CamUnit *_
 #pragma unroll
                 for (int c = r; c < 6; ++c, ++v) part[v] = part[v] + a[r] * a[c] + a[6 + r] * a[6 + c];
         }
-        // the gradient sets the LM fixed point: FP64 sums of the exact
-        // products of the stored values in both forms
+        // the gradient sets the LM fixed point: sums of the exact products
+        // of the stored values, in FP64 (FP64 form) or in double-float FP32
+        // arithmetic (mixed form: each product split by an FMA, TwoSum, to
+        // ~2^-44 of the terms, converted to FP64 once per thread)
+        if constexpr (is_fp64<R>()) {
 #pragma unroll
-        for (int q = 0; q < 6; ++q)
-            acc[21 + q] = acc[21 + q] + (double)a[q] * (double)e2[0] + (double)a[6 + q] * (double)e2[1];
+            for (int q = 0; q < 6; ++q) acc[21 + q] = acc[21 + q] + a[q] * e2[0] + a[6 + q] * e2[1];
+        } else {
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+                const float p0 = __fmul_rn(a[q], e2[0]), p1 = __fmul_rn(a[6 + q], e2[1]);
+                const float r = fmaf(a[q], e2[0], -p0) + fmaf(a[6 + q], e2[1], -p1);
+                float t0, t1;
+                two_sum_f(gh[q], p0, gh[q], t0);
+                two_sum_f(gh[q], p1, gh[q], t1);
+                gl[q] += (t0 + t1) + r;
+            }
+        }
     }
     if constexpr (!is_fp64<R>()) {
 #pragma unroll
         for (int v = 0; v < 21; ++v) acc[v] = (double)part[v];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) acc[21 + q] = (double)gh[q] + (double)gl[q];
     }
 #pragma unroll
     for (int v = 0; v < CAM_NV; ++v) red[v][t] = acc[v];
@@ -688,13 +777,6 @@ void launch_vinv(const DeviceProblem &d, double mu, cudaStream_t s)
     note_launch(1);
 }
 
-// s + e = a + b exactly (Knuth's TwoSum), FP32
-__device__ __forceinline__ void two_sum_f(float a, float b, float &s, float &e)
-{
-    s = __fadd_rn(a, b);
-    const float z = __fsub_rn(s, a);
-    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, z)), __fsub_rn(b, z));
-}
 
 // w0 v0 + w1 v1 + w2 v2 with each v = hi + lo (two FP32 values), rounded
 // once to FP32: the products w hi split exactly by an FMA, the w lo products
@@ -1419,17 +1501,25 @@ __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int2 *__r
                                                 double *__restrict__ dp, double *__restrict__ eb,
                                                 double *__restrict__ partial, int stage,
                                                 const int *__restrict__ status, int *__restrict__ ticket,
-                                                TrialScalars *__restrict__ out)
+                                                TrialScalars *__restrict__ out, const float2 *__restrict__ dpa2f)
 {
     static_assert(EB_WARPS == 8, "eight warps a block");
     __shared__ double s_sum[EB_PPB][3];
     __shared__ double r0[EB_WARPS], r1[EB_WARPS];
     extern __shared__ double s_dpa[];  // the camera part of dp (ncp doubles) when staged
+    // the mixed form, staged: dpa as FP32 pairs (hi, lo), the products in
+    // double-float arithmetic, so no FP64 instruction per observation
+    constexpr bool DF = !is_fp64<R>();
+    float2 *s_dpa2 = reinterpret_cast<float2 *>(s_dpa);
     if (stage) {
-        for (int e = threadIdx.x; e < ncp; e += blockDim.x) s_dpa[e] = dp[e];
+        if (DF && dpa2f)
+            for (int e = threadIdx.x; e < ncp; e += blockDim.x) s_dpa2[e] = dpa2f[e];
+        else
+            for (int e = threadIdx.x; e < ncp; e += blockDim.x) s_dpa[e] = dp[e];
         __syncthreads();
     }
     const double *dpa = stage ? s_dpa : dp;
+    const bool df = DF && stage && dpa2f;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int first = eb_warps[blockIdx.x * EB_WARPS].x;  // the block's points: [first, last) in pt_order
     const int last = eb_warps[(blockIdx.x + 1) * EB_WARPS].x;
@@ -1439,20 +1529,53 @@ __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int2 *__r
         const int2 wi = eb_warps[blockIdx.x * EB_WARPS + warp];
         const int npw = eb_warps[blockIdx.x * EB_WARPS + warp + 1].x - wi.x, m = wi.y;
         const int lpp = 3 * m, pw = lane / lpp, r = lane - lpp * pw, s = r / 3, c = r - 3 * s;
-        // one accumulator per camera parameter: six short chains
-        double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-        if (pw < npw) {
-            const int i = pt_order[wi.x + pw];
-            const int end = pt_start[i + 1];
-#pragma unroll 4
-            for (int o = pt_start[i] + s; o < end; o += m) {
-                const R *w = W + 18 * (size_t)o;
-                const double *da = dpa + 6 * (size_t)__ldg(obs_cam + o);
+        double part = 0.0;
+        if (df) {
+            // two double-float accumulators (hi, lo): w dpa_hi split exactly
+            // by an FMA, the sum carried by TwoSum, w dpa_lo and the errors
+            // summed in lo; converted to FP64 once per lane
+            float h0 = 0.0f, l0 = 0.0f, h1 = 0.0f, l1 = 0.0f;
+            if (pw < npw) {
+                const int i = pt_order[wi.x + pw];
+                const int end = pt_start[i + 1];
+#pragma unroll 2
+                for (int o = pt_start[i] + s; o < end; o += m) {
+                    const float *w = reinterpret_cast<const float *>(W) + 18 * (size_t)o;
+                    const float2 *da = s_dpa2 + 6 * (size_t)__ldg(obs_cam + o);
 #pragma unroll
-                for (int k = 0; k < 6; ++k) acc[k] = fma((double)w[3 * k + c], da[k], acc[k]);
+                    for (int k = 0; k < 6; ++k) {
+                        const float wv = w[3 * k + c];
+                        const float2 d2 = da[k];
+                        const float p = __fmul_rn(wv, d2.x);
+                        const float pe = fmaf(wv, d2.x, -p);
+                        float t;
+                        if (k & 1) {
+                            two_sum_f(h1, p, h1, t);
+                            l1 = fmaf(wv, d2.y, l1 + (t + pe));
+                        } else {
+                            two_sum_f(h0, p, h0, t);
+                            l0 = fmaf(wv, d2.y, l0 + (t + pe));
+                        }
+                    }
+                }
             }
+            part = ((double)h0 + (double)l0) + ((double)h1 + (double)l1);
+        } else {
+            // one accumulator per camera parameter: six short chains
+            double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+            if (pw < npw) {
+                const int i = pt_order[wi.x + pw];
+                const int end = pt_start[i + 1];
+#pragma unroll 4
+                for (int o = pt_start[i] + s; o < end; o += m) {
+                    const R *w = W + 18 * (size_t)o;
+                    const double *da = dpa + 6 * (size_t)__ldg(obs_cam + o);
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) acc[k] = fma((double)w[3 * k + c], da[k], acc[k]);
+                }
+            }
+            part = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + (acc[4] + acc[5]);
         }
-        const double part = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + (acc[4] + acc[5]);
         // the m partial sums of a component, in order of s (each lane's own
         // partial is what is exchanged, not a running sum)
         double e = part;
@@ -1534,11 +1657,12 @@ void launch_eb_dpb(const DeviceProblem &d, double mu, cudaStream_t s)
     if (d.prec == PSBA_PREC_FP64)
         k_eb_dpb<double><<<eb_blocks(d), 256, smem, s>>>(d.np, d.N, d.eb_warps, d.pt_start, d.pt_order, d.obs_cam,
                                                            d.W, d.Vinv, d.g, mu, d.dp, d.eb, d.red_partial, stage,
-                                                           d.status, d.tickets, d.scal);
+                                                           d.status, d.tickets, d.scal, nullptr);
     else
         k_eb_dpb<float><<<eb_blocks(d), 256, smem, s>>>(d.np, d.N, d.eb_warps, d.pt_start, d.pt_order, d.obs_cam,
                                                           (const float *)d.W, d.Vinv, d.g, mu, d.dp, d.eb,
-                                                          d.red_partial, stage, d.status, d.tickets, d.scal);
+                                                          d.red_partial, stage, d.status, d.tickets, d.scal,
+                                                          d.dpa2f);
     note_launch(1);
 }
 

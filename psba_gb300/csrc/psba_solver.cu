@@ -297,7 +297,8 @@ void enqueue_linearize(psba_handle *h, double coeff)
     DeviceProblem &d = h->d;
     {
         StageScope sc(h, ST_LINEARIZE);
-        launch_cam_tables(d, d.cams, nullptr, d.camtab, h->stream);
+        launch_cam_tables(d, d.cams, nullptr, d.camtab, h->stream,
+                          d.prec == PSBA_PREC_MIXED && d.cnp == 6 ? d.camtab32 : nullptr);
         launch_linearize(d, coeff, h->stream);
     }
     {
@@ -1026,6 +1027,7 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     TRY(dalloc(h, &d.pts0, 3 * (size_t)np));
     TRY(dalloc(h, &d.camtab, (size_t)CAMTAB * nc));
     TRY(dalloc(h, &d.camtab_new, (size_t)CAMTAB * nc));
+    TRY(dalloc(h, &d.camtab32, (size_t)CAMTAB32 * nc));
     TRY(dalloc(h, &d.ex, 2 * (size_t)no));
     const size_t cnp = (size_t)d.cnp;
     const size_t cam_nv = d.cnp == 6 ? 27 : varcam_cam_partial(d.cnp);
@@ -1048,6 +1050,7 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     TRY(dalloc(h, &d.Ssave, (size_t)d.Nm3 * d.Nm3));
     TRY(dalloc(h, &d.rhs, (size_t)d.Np));
     TRY(dalloc(h, &d.rsave, (size_t)d.Np));
+    TRY(dalloc(h, &d.dpa2f, (size_t)d.Np));
     TRY(dalloc(h, &d.xsol, (size_t)d.Np));
     TRY(dalloc(h, &d.Linv, (size_t)d.Np * TILE));
     TRY(dalloc(h, &d.status, 4));

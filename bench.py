@@ -758,6 +758,7 @@ def main():
     # the FP64 tensor cores (mma.sync m8n8k4 / m16n8k16) against the FP64 FMA
     # rate: on GB300 they are slower, so no FP64 stage here uses them
     dmma = {"m8n8k4": P.measure_peak("dmma_m8n8k4"), "m16n8k16": P.measure_peak("dmma_m16n8k16"),
+            "m8n8k4_and_fp64_fma_side_by_side": P.measure_peak("dmma_and_fp64"),
             "fp64_fma": fp64_peak, "unit": "TFLOP/s"}
     schur_ms = sum(stages[k][0] for k in ("schur_off", "schur_diag", "schur_reduce"))
     schur_n = max(stages["schur_off"][1], 1)

@@ -272,7 +272,8 @@ long long psba_kernel_launches(void);
 
 /* Throughput of the current device in TFLOP/s: which = 0 FP64 FMA, 1 FP32
  * FMA, 2 FP64 tensor cores (mma.sync m8n8k4), 3 FP64 tensor cores (mma.sync
- * m16n8k16).  Eight independent chains per thread or warp. */
+ * m16n8k16), 4 both FP64 paths at once (half the warps m8n8k4, half FMA,
+ * equal flops).  Eight independent chains per thread or warp. */
 int psba_measure_peak(int which, double *tflops);
 
 /* ---- batches of independent problems ------------------------------------ */

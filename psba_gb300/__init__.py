@@ -382,7 +382,7 @@ def kernel_launches():
     return int(lib().psba_kernel_launches())
 
 
-PEAK_KINDS = {"fp64": 0, "fp32": 1, "dmma_m8n8k4": 2, "dmma_m16n8k16": 3}
+PEAK_KINDS = {"fp64": 0, "fp32": 1, "dmma_m8n8k4": 2, "dmma_m16n8k16": 3, "dmma_and_fp64": 4}
 
 
 def measure_peak(which="fp64"):

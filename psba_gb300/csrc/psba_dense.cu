@@ -1437,49 +1437,77 @@ void launch_refine(const DeviceProblem &d, const double *Sc, int ld, const doubl
 // with get_delta_beta (cl_cholmod.cpp:109-165) and kern_cholmod_E: block
 // columns of 3 are factored as plain 3x3 blocks when the pivots are positive
 // and every entry below is <= beta; otherwise their columns are redone one
-// at a time with d = max(|c|, delta) and the theta/beta bound.  One block of
-// threads; this path runs at most a few times per solve.
-constexpr int CM_THREADS = 1024;
+// at a time with d = max(|c|, delta) and the theta/beta bound.
+//
+// One cooperative launch over CM_CTAS CTAs (grid-wide barriers), right-
+// looking: step j factors the 3x3 diagonal block of the already updated
+// matrix (every CTA redundantly, the same arithmetic), writes the panel
+// below it (a 3x3 block per thread) and, after a grid barrier that also
+// combines the "entry above beta" flags, updates the trailing lower triangle
+// with the rank-3 product of the panel (rows dealt to CTAs, columns to
+// threads).  Each entry thus takes the same sequence of 3-term subtractions,
+// in the same block order, as the reference's left-looking sums, so the plain
+// path rounds as before; the column-at-a-time path subtracts the earlier
+// blocks in those 3-term groups and the block's own columns one at a time.
+// The work per step is spread over the GPU instead of one block of threads
+// (at N = 528: ~33 ms on one CTA, where a step had at most 175 threads busy).
+constexpr int CM_THREADS = 256;
 
-__device__ double block_max(double v, double *red)
+__device__ double cta_max(double v, double *red)
 {
-    red[threadIdx.x] = v;
+    for (int off = 16; off > 0; off >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, off));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
     __syncthreads();
-    for (int st = CM_THREADS / 2; st > 0; st >>= 1) {
-        if (threadIdx.x < st) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + st]);
-        __syncthreads();
-    }
-    const double r = red[0];
+    double r = red[0];
+    for (int w = 1; w < CM_THREADS / 32; ++w) r = fmax(r, red[w]);
     __syncthreads();
     return r;
 }
 
-__device__ int block_or(int v, int *red)
+__device__ int cta_or(int v, int *red)
 {
-    red[threadIdx.x] = v;
+    v = __any_sync(0xffffffffu, v) ? 1 : 0;
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
     __syncthreads();
-    for (int st = CM_THREADS / 2; st > 0; st >>= 1) {
-        if (threadIdx.x < st) red[threadIdx.x] = red[threadIdx.x] | red[threadIdx.x + st];
-        __syncthreads();
-    }
-    const int r = red[0];
+    int r = 0;
+    for (int w = 0; w < CM_THREADS / 32; ++w) r |= red[w];
     __syncthreads();
     return r;
 }
 
+// work: diag (n), orig (3 n), C (n), then gmax[2 G] and gflag[G] (doubles)
 __global__ void __launch_bounds__(CM_THREADS) k_cholmod(double *S, int n, int ld, double *E, double *work)
 {
-    __shared__ double dred[CM_THREADS];
-    __shared__ int ired[CM_THREADS];
-    __shared__ double sh_T[9], sh_L[6], sh_Li[9];
+    cg::grid_group grid = cg::this_grid();
+    __shared__ double dred[CM_THREADS / 32];
+    __shared__ int ired[CM_THREADS / 32];
+    __shared__ double sh_L[6], sh_Li[9], sh_lxx;
     __shared__ int sh_fail;
-    double *diag = work;          // n
-    double *orig = work + n;      // 3 n
-    double *C = work + 4 * n;     // n
-    const int tid = threadIdx.x;
+    const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x;
+    const long long gtid = (long long)b * CM_THREADS + tid, gsize = (long long)G * CM_THREADS;
+    double *diag = work, *orig = work + n, *C = work + 4 * n, *gmax = work + 5 * n, *gflag = gmax + 2 * G;
+    // a grid-wide OR / max through per-CTA slots (after a grid barrier every
+    // CTA reads them all, in the same order)
+    auto grid_or = [&](int v) {
+        v = cta_or(v, ired);
+        if (tid == 0) gflag[b] = v ? 1.0 : 0.0;
+        grid.sync();
+        int r = 0;
+        for (int q = 0; q < G; ++q) r |= gflag[q] != 0.0;
+        grid.sync();  // the slots are reused
+        return r;
+    };
+    auto grid_max = [&](double v, int slot) {
+        v = cta_max(v, dred);
+        if (tid == 0) gmax[2 * b + slot] = v;
+        grid.sync();
+        double r = 0.0;
+        for (int q = 0; q < G; ++q) r = fmax(r, gmax[2 * q + slot]);
+        return r;
+    };
     // xi = max |offdiag|, gamma = max |diag| over the symmetric matrix (lower read)
     double xi = 0.0, gam = 0.0;
-    for (long long e = tid; e < (long long)n * n; e += CM_THREADS) {
+    for (long long e = gtid; e < (long long)n * n; e += gsize) {
         const int r = (int)(e / n), k = (int)(e % n);
         if (r == k) {
             gam = fmax(gam, fabs(S[(size_t)r * ld + r]));
@@ -1488,33 +1516,35 @@ __global__ void __launch_bounds__(CM_THREADS) k_cholmod(double *S, int n, int ld
             xi = fmax(xi, fabs(S[(size_t)hi * ld + lo]));
         }
     }
-    xi = block_max(xi, dred);
-    gam = block_max(gam, dred);
+    for (long long r = gtid; r < n; r += gsize) diag[r] = S[(size_t)r * ld + r];
+    xi = cta_max(xi, dred);
+    gam = cta_max(gam, dred);
+    if (tid == 0) {
+        gmax[2 * b] = xi;
+        gmax[2 * b + 1] = gam;
+    }
+    grid.sync();
+    xi = 0.0;
+    gam = 0.0;
+    for (int q = 0; q < G; ++q) {
+        xi = fmax(xi, gmax[2 * q]);
+        gam = fmax(gam, gmax[2 * q + 1]);
+    }
+    grid.sync();
     const double delta = 1e-15 * fmax(xi + gam, 1.0);
     double beta = fmax(gam, 1e-15);
     beta = fmax(beta, xi / sqrt((double)(n * n - 1)));
     beta = sqrt(beta);
-    for (int r = tid; r < n; r += CM_THREADS) diag[r] = S[(size_t)r * ld + r];
-    __syncthreads();
     const int nb = n / 3;
     for (int j = 0; j < nb; ++j) {
-        for (int e = tid; e < (n - 3 * j) * 3; e += CM_THREADS) {
-            const int r = 3 * j + e / 3, v = e % 3;
-            orig[(size_t)r * 3 + v] = S[(size_t)r * ld + 3 * j + v];
-        }
-        __syncthreads();
-        if (tid < 9) {
-            const int u = tid / 3, v = tid % 3;
-            const int ru = 3 * j + u, rv = 3 * j + v;
-            double sum = v > u ? S[(size_t)rv * ld + ru] : S[(size_t)ru * ld + rv];
-            const double *lu = S + (size_t)ru * ld, *lv = S + (size_t)rv * ld;
-            for (int k = 0; k < j; ++k)
-                sum -= (lu[3 * k] * lv[3 * k] + lu[3 * k + 1] * lv[3 * k + 1] + lu[3 * k + 2] * lv[3 * k + 2]);
-            sh_T[tid] = sum;
-        }
-        __syncthreads();
+        const int j3 = 3 * j;
+        // the diagonal block, already updated by the earlier steps
         if (tid == 0) {
-            const double *Tm = sh_T;
+            double Tm[9];
+            for (int q = 0; q < 9; ++q) {
+                const int u = q / 3, v = q % 3;
+                Tm[q] = v > u ? S[(size_t)(j3 + v) * ld + j3 + u] : S[(size_t)(j3 + u) * ld + j3 + v];
+            }
             int fail = 0;
             const double p0 = Tm[0];
             const double p1 = Tm[4] - Tm[3] * Tm[3] / Tm[0];
@@ -1542,93 +1572,116 @@ __global__ void __launch_bounds__(CM_THREADS) k_cholmod(double *S, int n, int ld
             sh_fail = fail;
         }
         __syncthreads();
-        int fail = sh_fail;
+        const int fail = sh_fail;  // the same in every CTA
+        // keep the column block (rows j3 .. n-1) for the column-at-a-time path
+        for (long long e = gtid; e < (long long)(n - j3) * 3; e += gsize) {
+            const int r = j3 + (int)(e / 3), v = (int)(e % 3);
+            orig[(size_t)r * 3 + v] = S[(size_t)r * ld + j3 + v];
+        }
+        grid.sync();
+        int redo = fail;
         if (!fail) {
-            // write the diagonal block, then the blocks below: T_ij then L_ij = T_ij Li^T
-            if (tid == 0) {
-                double *dd = S + (size_t)(3 * j) * ld + 3 * j;
+            // the diagonal block, then the blocks below: L_ij = T_ij Li^T
+            if (gtid == 0) {
+                double *dd = S + (size_t)j3 * ld + j3;
                 dd[0] = sh_L[0]; dd[1] = 0; dd[2] = 0;
                 dd[ld] = sh_L[1]; dd[ld + 1] = sh_L[2]; dd[ld + 2] = 0;
                 dd[2 * ld] = sh_L[3]; dd[2 * ld + 1] = sh_L[4]; dd[2 * ld + 2] = sh_L[5];
             }
-            __syncthreads();
             int big = 0;
-            for (int blk = j + 1 + tid; blk < nb; blk += CM_THREADS) {
+            for (long long blk = j + 1 + gtid; blk < nb; blk += gsize) {
                 double Tij[9];
-                for (int u = 0; u < 3; ++u)
-                    for (int v = 0; v < 3; ++v) {
-                        const int ri = 3 * blk + u, rj = 3 * j + v;
-                        double sum = S[(size_t)ri * ld + rj];
-                        const double *lu = S + (size_t)ri * ld, *lv = S + (size_t)rj * ld;
-                        for (int k = 0; k < j; ++k)
-                            sum -= (lu[3 * k] * lv[3 * k] + lu[3 * k + 1] * lv[3 * k + 1] +
-                                    lu[3 * k + 2] * lv[3 * k + 2]);
-                        Tij[u * 3 + v] = sum;
-                    }
+                for (int q = 0; q < 9; ++q) Tij[q] = S[(size_t)(3 * blk + q / 3) * ld + j3 + q % 3];
                 for (int u = 0; u < 3; ++u)
                     for (int v = 0; v < 3; ++v) {
                         const double val = (Tij[u * 3] * sh_Li[v * 3] + Tij[u * 3 + 1] * sh_Li[v * 3 + 1] +
                                             Tij[u * 3 + 2] * sh_Li[v * 3 + 2]);
-                        S[(size_t)(3 * blk + u) * ld + 3 * j + v] = val;
-                        S[(size_t)(3 * j + v) * ld + 3 * blk + u] = 0.0;
+                        S[(size_t)(3 * blk + u) * ld + j3 + v] = val;
+                        S[(size_t)(j3 + v) * ld + 3 * blk + u] = 0.0;
                         if (val > beta) big = 1;
                     }
             }
-            fail = block_or(big, ired);
+            redo = grid_or(big);
         }
-        if (!fail) continue;
-        // restore column block j and redo its columns one at a time
-        for (int e = tid; e < (n - 3 * j) * 3; e += CM_THREADS) {
-            const int r = 3 * j + e / 3, v = e % 3;
-            S[(size_t)r * ld + 3 * j + v] = orig[(size_t)r * 3 + v];
-        }
-        __syncthreads();
-        for (int col = 0; col < 3; ++col) {
-            const int x = 3 * j + col;
-            if (tid == 0) {
-                double sum = S[(size_t)x * ld + x];
-                for (int k = 0; k < x; ++k) {
-                    const double l = S[(size_t)x * ld + k];
-                    sum -= l * l;
+        if (redo) {
+            // restore the column block and redo its columns one at a time
+            for (long long e = gtid; e < (long long)(n - j3) * 3; e += gsize) {
+                const int r = j3 + (int)(e / 3), v = (int)(e % 3);
+                S[(size_t)r * ld + j3 + v] = orig[(size_t)r * 3 + v];
+            }
+            grid.sync();
+            for (int col = 0; col < 3; ++col) {
+                const int x = j3 + col;
+                if (tid == 0) {  // every CTA, the same arithmetic
+                    double sum = S[(size_t)x * ld + x];
+                    for (int k = j3; k < x; ++k) {
+                        const double l = S[(size_t)x * ld + k];
+                        sum -= l * l;
+                    }
+                    sum = fabs(sum);
+                    sh_lxx = sqrt(fmax(sum, delta));
                 }
-                sum = fabs(sum);
-                S[(size_t)x * ld + x] = sqrt(fmax(sum, delta));
+                __syncthreads();
+                const double lxx = sh_lxx;
+                int big = 0;
+                for (long long i = x + 1 + gtid; i < n; i += gsize) {
+                    double c = S[(size_t)i * ld + x];
+                    for (int k = j3; k < x; ++k) c = c - (S[(size_t)i * ld + k] * S[(size_t)x * ld + k]);
+                    C[i] = c;
+                    const double l = c / lxx;
+                    S[(size_t)i * ld + x] = l;
+                    S[(size_t)x * ld + i] = 0.0;
+                    if (l > beta) big = 1;
+                }
+                big = grid_or(big);  // also orders the column's writes before the next column
+                if (gtid == 0) S[(size_t)x * ld + x] = lxx;
+                if (big) {
+                    double th = 0.0;
+                    for (long long i = x + 1 + gtid; i < n; i += gsize) th = fmax(th, fabs(C[i]));
+                    th = grid_max(th, 0);
+                    const double nl = th / beta;
+                    if (gtid == 0) S[(size_t)x * ld + x] = nl;
+                    for (long long i = x + 1 + gtid; i < n; i += gsize) S[(size_t)i * ld + x] = C[i] / nl;
+                }
+                grid.sync();
             }
-            __syncthreads();
-            const double lxx = S[(size_t)x * ld + x];
-            int big = 0;
-            for (int i = x + 1 + tid; i < n; i += CM_THREADS) {
-                double c = S[(size_t)i * ld + x];
-                for (int k = 0; k < x; ++k) c = c - (S[(size_t)i * ld + k] * S[(size_t)x * ld + k]);
-                C[i] = c;
-                const double l = c / lxx;
-                S[(size_t)i * ld + x] = l;
-                S[(size_t)x * ld + i] = 0.0;
-                if (l > beta) big = 1;
-            }
-            big = block_or(big, ired);
-            if (big) {
-                double th = 0.0;
-                for (int i = x + 1 + tid; i < n; i += CM_THREADS) th = fmax(th, fabs(C[i]));
-                th = block_max(th, dred);
-                const double nl = th / beta;
-                if (tid == 0) S[(size_t)x * ld + x] = nl;
-                for (int i = x + 1 + tid; i < n; i += CM_THREADS) S[(size_t)i * ld + x] = C[i] / nl;
-            }
-            __syncthreads();
         }
+        // the trailing lower triangle: S_ic -= L_i,j3.. L_c,j3.. (rank 3),
+        // rows i dealt to CTAs, columns c to threads
+        const int t0 = j3 + 3;
+        for (int i = t0 + b; i < n; i += G) {
+            const double *Li_ = S + (size_t)i * ld + j3;
+            const double a0 = Li_[0], a1 = Li_[1], a2 = Li_[2];
+            for (int c = t0 + tid; c <= i; c += CM_THREADS) {
+                const double *Lc = S + (size_t)c * ld + j3;
+                S[(size_t)i * ld + c] -= (a0 * Lc[0] + a1 * Lc[1] + a2 * Lc[2]);
+            }
+        }
+        grid.sync();
     }
-    __syncthreads();
-    for (int i = tid; i < n; i += CM_THREADS) {
+    for (long long i = gtid; i < n; i += gsize) {
         double sum = 0.0;
         for (int k = 0; k <= i; ++k) sum += S[(size_t)i * ld + k] * S[(size_t)i * ld + k];
         E[i] = sum - diag[i];
     }
 }
 
-void launch_cholmod(double *S, int n, int ld, double *E, double *work, cudaStream_t s)
+// doubles of work the modified Cholesky needs at size n
+size_t cholmod_work(int n) { return 5 * (size_t)n + 3 * (size_t)CM_MAX_CTAS + 8; }
+
+void launch_cholmod(double *S, int n, int ld, double *E, double *work, cudaStream_t s, int grid_cap)
 {
-    k_cholmod<<<1, CM_THREADS, 0, s>>>(S, n, ld, E, work); note_launch(1);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int G = sms < CM_MAX_CTAS ? sms : CM_MAX_CTAS;
+    if (grid_cap > 0 && grid_cap < G) G = grid_cap;
+    const int rows = (n + 7) / 8;  // no more CTAs than the trailing rows can use
+    if (rows < G) G = rows;
+    if (G < 1) G = 1;
+    void *args[] = {&S, &n, &ld, &E, &work};
+    cudaLaunchCooperativeKernel((const void *)k_cholmod, dim3(G), dim3(CM_THREADS), args, 0, s);
+    note_launch(1);
 }
 
 }  // namespace psba

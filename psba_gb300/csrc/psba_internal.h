@@ -280,7 +280,9 @@ void launch_jmultiply_v(const DeviceProblem &d, const double *x, double *out, cu
 void launch_residual_dist(const DeviceProblem &d, const double *tab, const double *pts, const double *dpb,
                           double *ex_out, double *partial, int nblocks, cudaStream_t s);
 // Modified Cholesky (trust-region lambda fallback) and its diagonal correction.
-void launch_cholmod(double *S, int n, int ld, double *E, double *work, cudaStream_t s);
+constexpr int CM_MAX_CTAS = 256;  // CTAs of the modified Cholesky's cooperative launch, at most
+size_t cholmod_work(int n);       // doubles of work it needs at size n
+void launch_cholmod(double *S, int n, int ld, double *E, double *work, cudaStream_t s, int grid_cap = 0);
 
 // Copies for the parity interface.
 void launch_expand_V(const DeviceProblem &d, const double *V6, double *V9, cudaStream_t s);

@@ -526,7 +526,7 @@ int compute_pb(psba_handle *h, double *lambda, int *solved)
             // Np; N not a multiple of 3: the 3x3-block form runs on S padded
             // to one with its identity rows, lambda from the first N entries)
             const int n3 = d.N % 3 == 0 ? d.N : d.N + (3 - d.N % 3);
-            launch_cholmod(d.Ssave, n3, d.Nm3, d.E, d.red_partial, h->stream);
+            launch_cholmod(d.Ssave, n3, d.Nm3, d.E, d.red_partial, h->stream, d.chol_grid_cap);
             TRY(check_launch());
             std::vector<double> E(d.N);
             PSBA_CUDA_TRY(cudaMemcpyAsync(E.data(), d.E, sizeof(double) * d.N, cudaMemcpyDeviceToHost,
@@ -1071,7 +1071,7 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     TRY(dalloc(h, &d.eb, 3 * (size_t)np));
     h->nred = 512;
     const int res_blocks = residual_blocks(d), ebb = eb_blocks(d);
-    d.red_partial_cap = std::max<int>({2 * ebb + 8 + res_blocks, h->nred + 8, 5 * d.Nm3 + 8});
+    d.red_partial_cap = std::max<int>({2 * ebb + 8 + res_blocks, h->nred + 8, (int)cholmod_work(d.Nm3)});
     TRY(dalloc(h, &d.red_partial, (size_t)d.red_partial_cap));
     TRY(dalloc(h, &d.scal, 1));
     TRY(dalloc(h, &h->scratch, 64));
@@ -1471,7 +1471,7 @@ int psba_eval_cholmod(int n, double *S, double *E)
     const size_t nn = (size_t)n * n;
     cudaError_t e = cudaMalloc(&dS, nn * sizeof(double));
     if (e == cudaSuccess) e = cudaMalloc(&dE, (size_t)n * sizeof(double));
-    if (e == cudaSuccess) e = cudaMalloc(&dW, 5 * (size_t)n * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&dW, cholmod_work(n) * sizeof(double));
     if (e == cudaSuccess) e = cudaMemcpy(dS, S, nn * sizeof(double), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
         launch_cholmod(dS, n, n, dE, dW, 0);

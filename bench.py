@@ -579,8 +579,9 @@ def serving_leg(P, args):
             got, wall = S.run_poisson(srv, pool, rate, n, seed=int(rate))
             lat = np.array([r.latency_ms for r in got])
             qd = np.array([r.queued_ms for r in got])
+            failed = [(q, r.status, r.error) for q, r in enumerate(got) if r.error is not None]
             rel = np.array([(r.final_cost - pbp_cost[q % len(pool)]) / pbp_cost[q % len(pool)]
-                            for q, r in enumerate(got)])
+                            for q, r in enumerate(got) if r.error is None])
             rel_all.append(rel)
             seq_ms = sum(pbp_ms[q % len(pool)] for q in range(n))
             out["rates"].append({"rate_req_s": rate, "requests": n, "solves_per_s": n / wall,
@@ -588,7 +589,9 @@ def serving_leg(P, args):
                                  "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                                  "queued_p50_ms": float(np.percentile(qd, 50)),
                                  "queued_p99_ms": float(np.percentile(qd, 99)),
-                                 "matched_frac": float((rel <= MATCH_TOL).mean())})
+                                 "matched_frac": float((rel <= MATCH_TOL).sum() / n),
+                                 "failed_requests": len(failed),
+                                 "failures": [{"request": q, "status": st, "error": msg} for q, st, msg in failed[:5]]})
         st = srv.stats()
     rel = np.concatenate(rel_all)
     best = max(out["rates"], key=lambda x: x["solves_per_s"])

@@ -346,6 +346,9 @@ typedef struct psba_server_opts {
     int fp64_intrinsics;     /* 1: requests with 11/16-parameter cameras are solved in FP64 even when the
                                 server's precision is mixed (default 1: with FP32 Jacobian columns for the
                                 intrinsics, LM converges slowly or stalls short of the FP64 minimum) */
+    long long large_wait_limit; /* polls per device-side wait of a large-lane solve (psba_set_wait_limit;
+                                   default 0: the library's); a wait that runs out fails that request
+                                   alone (PSBA_REQUEST_FAILED from psba_batch_poll) */
 } psba_server_opts;
 
 typedef struct psba_request_result {
@@ -367,7 +370,8 @@ typedef struct psba_server_stats {
     double busy_ms; /* GPU time of all slice launches */
 } psba_server_stats;
 
-#define PSBA_PENDING 1 /* psba_batch_poll: not finished yet */
+#define PSBA_PENDING 1        /* psba_batch_poll: not finished yet */
+#define PSBA_REQUEST_FAILED 2 /* psba_batch_poll: the request ended with an error (res->status holds it) */
 
 void psba_server_default_opts(psba_server_opts *o);
 /* lm: tau, thresholds, max_iter and precision for every request. */
@@ -377,8 +381,12 @@ int psba_server_create(const psba_server_opts *so, const psba_opts *lm, psba_ser
 int psba_batch_submit(psba_server *s, const psba_problem_desc *desc, long long *ticket);
 /* PSBA_OK: finished; *res, and cams (6 per camera) / pts (3 per point) when
  * not NULL, are written and the ticket is released.  PSBA_PENDING: not
- * finished within timeout_ms (0: return at once).  PSBA_ERR_ARG: unknown
- * ticket.  PSBA_ERR_CUDA: the server stopped on a device error. */
+ * finished within timeout_ms (0: return at once).  PSBA_REQUEST_FAILED: the
+ * request alone ended with an error (e.g. PSBA_ERR_STATE: a large-lane dense
+ * factor's device wait ran out while other work held the SMs); res->status
+ * holds that error code, psba_last_error() the message, the ticket is
+ * released and the server goes on.  PSBA_ERR_ARG: unknown ticket.
+ * PSBA_ERR_CUDA: the server stopped on a device error. */
 int psba_batch_poll(psba_server *s, long long ticket, int timeout_ms, psba_request_result *res, double *cams,
                     double *pts);
 int psba_server_stats_get(psba_server *s, psba_server_stats *st);

@@ -394,6 +394,7 @@ void large_main(psba_server *s)
         int rc = psba_create(&desc, &h);
         // the lanes' dense factors run side by side: each takes its share of the SMs
         if (rc == PSBA_OK) set_chol_grid_cap(h, s->large_chol_cap);
+        if (rc == PSBA_OK && s->so.large_wait_limit > 0) rc = psba_set_wait_limit(h, s->so.large_wait_limit);
         // cameras with intrinsics (11/16 parameters) in FP64 when the server
         // asks for it: their mixed-form Jacobian columns lose the
         // ill-conditioned intrinsics directions (slow or stalled convergence)
@@ -488,7 +489,7 @@ int psba_server_create(const psba_server_opts *so, const psba_opts *lm, psba_ser
         (so->threads != 128 && so->threads != 256 && so->threads != 512) ||
         (so->lanes_per_pair != 8 && so->lanes_per_pair != 16 && so->lanes_per_pair != 32) || so->large_cams < 0 ||
         so->large_lanes < 0 || so->large_lanes > 16 || !(so->large_share >= 0.0 && so->large_share < 1.0) ||
-        so->large_obs < 0 ||
+        so->large_obs < 0 || so->large_wait_limit < 0 ||
         (lm->precision != PSBA_PREC_FP64 && lm->precision != PSBA_PREC_MIXED) || lm->max_iter < 0 ||
         lm->refine != 0)
         return set_error("psba_server_create: bad options"), PSBA_ERR_ARG;
@@ -624,10 +625,15 @@ int psba_batch_poll(psba_server *s, long long ticket, int timeout_ms, psba_reque
         return PSBA_PENDING;
     }
     if (r->err != PSBA_OK) {
-        const int e = r->err;
         set_error("psba_batch_poll: request failed: " + r->err_msg);
+        if (res) {
+            *res = psba_request_result{};
+            res->status = r->err;
+            res->queued_ms = ms_between(r->t_submit, r->t_admit);
+            res->latency_ms = ms_between(r->t_submit, r->t_done);
+        }
         s->reqs.erase(it);
-        return e;
+        return PSBA_REQUEST_FAILED;
     }
     if (res) {
         res->status = r->st.status;

@@ -20,13 +20,14 @@ import numpy as np
 from . import PREC_FP64, PSBAError, ProblemDesc, _check, _d, _f64, _ip, default_opts, lib, Opts
 
 PSBA_PENDING = 1
+PSBA_REQUEST_FAILED = 2  # psba_batch_poll: the request ended with an error
 
 
 class ServerOpts(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_double), ("max_active", C.c_int), ("slice_iters", C.c_int),
                 ("threads", C.c_int), ("lanes_per_pair", C.c_int), ("large_cams", C.c_int),
                 ("large_lanes", C.c_int), ("large_share", C.c_double), ("large_obs", C.c_int),
-                ("fp64_intrinsics", C.c_int)]
+                ("fp64_intrinsics", C.c_int), ("large_wait_limit", C.c_longlong)]
 
 
 class RequestResult(C.Structure):
@@ -63,7 +64,8 @@ def _bind():
 class Request:
     """A finished request: the solver's result, host-clock timings, parameters."""
 
-    def __init__(self, r, cams, pts):
+    def __init__(self, r, cams, pts, error=None):
+        self.error = error  # None, or the message of a request that ended with an error (status: its code)
         self.status = r.status
         self.iterations = r.iterations
         self.n_trials = r.n_trials
@@ -79,7 +81,7 @@ class Request:
 class Server:
     def __init__(self, precision=PREC_FP64, max_iter=15, hbm_budget_bytes=120e9, max_active=1024,
                  slice_iters=1, threads=256, lanes_per_pair=32, large_cams=None, large_lanes=None,
-                 large_share=None, large_obs=None, fp64_intrinsics=None, **lm):
+                 large_share=None, large_obs=None, fp64_intrinsics=None, large_wait_limit=None, **lm):
         L = _bind()
         so = ServerOpts()
         L.psba_server_default_opts(C.byref(so))
@@ -98,6 +100,8 @@ class Server:
             so.large_obs = int(large_obs)
         if fp64_intrinsics is not None:
             so.fp64_intrinsics = int(bool(fp64_intrinsics))
+        if large_wait_limit is not None:
+            so.large_wait_limit = int(large_wait_limit)
         o = default_opts(precision=precision, max_iter=max_iter, allow_switch=0, **lm)
         h = C.c_void_p()
         _check(L.psba_server_create(C.byref(so), C.byref(o), C.byref(h)))
@@ -131,6 +135,10 @@ class Server:
                                    pts.ctypes.data)
         if rc == PSBA_PENDING:
             return None
+        if rc == PSBA_REQUEST_FAILED:  # this request alone; the server goes on
+            with self._lock:
+                del self._shapes[ticket]
+            return Request(r, None, None, error=lib().psba_last_error().decode())
         _check(rc)
         with self._lock:
             del self._shapes[ticket]

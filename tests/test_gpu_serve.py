@@ -136,6 +136,28 @@ def test_serve_large_lane_in_a_mix(precision):
         assert abs(r.final_cost - o.final_cost) <= (1e-9 if precision == P.PREC_FP64 else 1e-4) * o.final_cost
 
 
+def test_serve_large_request_failure_is_its_own():
+    # a large-lane solve whose device-side waits are cut to one poll gives up
+    # (PSBA_ERR_STATE): poll reports that request as failed, with its error,
+    # and the server goes on serving the batch lane beside it
+    small = probs(3, seed=24)
+    large = scenes.circle_scene(seed=3, n_cams=44, n_pts=2000, name="circle44")
+    with S.Server(precision=P.PREC_FP64, max_iter=8, hbm_budget_bytes=4e9, large_cams=40,
+                  large_wait_limit=1) as srv:
+        tl = srv.submit(large)
+        ts = [srv.submit(sc) for sc in small]
+        r = srv.wait(tl)
+        assert r.error is not None and "wait budget" in r.error
+        assert r.status == P.PSBA_ERR_STATE
+        res = [srv.wait(t) for t in ts]
+        with pytest.raises(KeyError):
+            srv.poll(tl)  # released
+    for sc, got in zip(small, res):
+        assert got.error is None
+        o = oracle.levmar(sc, allow_switch=0, max_iter=8)
+        assert abs(got.final_cost - o.final_cost) <= 1e-9 * o.final_cost
+
+
 def test_serve_variable_intrinsics_and_weighted_requests():
     # 11-parameter cameras and covariance-weighted problems take the large
     # lane; their results are those of psba_levmar on the same problem

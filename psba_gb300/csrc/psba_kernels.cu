@@ -1211,15 +1211,21 @@ __global__ void __launch_bounds__(128) k_schur(int n_chunks, int off_ctas, const
 
 int schur_off_wave_threads()
 {
-    static int threads = 0;
-    if (threads == 0) {
-        int dev = 0, sms = 0, per_sm = 0;
-        cudaGetDevice(&dev);
+    // one resident wave of k_schur, per device (the serving lanes' threads
+    // ask at the same time)
+    static std::mutex mu;
+    static int threads[MAX_DEVICES] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= MAX_DEVICES) dev = 0;
+    std::lock_guard<std::mutex> lk(mu);
+    if (threads[dev] == 0) {
+        int sms = 0, per_sm = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_schur, 128, 0);
-        threads = std::max(1, sms) * std::max(1, per_sm) * 128;
+        threads[dev] = std::max(1, sms) * std::max(1, per_sm) * 128;
     }
-    return threads;
+    return threads[dev];
 }
 
 // FP32 products, 6-parameter cameras: one warp per unit of <= MX_UNIT

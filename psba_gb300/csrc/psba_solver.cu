@@ -91,9 +91,9 @@ namespace {
 void keep_pool_memory()
 {
     static std::mutex mu;
-    static bool done[64] = {};
+    static bool done[MAX_DEVICES] = {};
     int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return;
     std::lock_guard<std::mutex> lk(mu);
     if (done[dev]) return;
     cudaMemPool_t pool;

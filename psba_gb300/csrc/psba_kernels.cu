@@ -1283,9 +1283,23 @@ __device__ __forceinline__ void mx_quadrant(const float *__restrict__ Y, const f
         }
 }
 
+// The rows of one step (sixteen entries: their Y rows and W rows, 288
+// float pairs) are loaded by the whole warp, each lane the same nine
+// (row, pair) slots at every step, and meet the lanes that use them in
+// shared memory: a warp load instruction then covers ~256 contiguous bytes
+// of about four rows instead of fifteen sectors of eight, which cuts the L1
+// wavefronts the gathers cost (the kernel's bound).  The next step's pairs
+// are loaded into registers while the current one is summed.  Lane 4s + q
+// sums entry s of the step into a0 and entry s + 8 into a1 (the order of the
+// per-entry loads it replaced).
+constexpr int MX_STEP = 16;                 // entries per step
+constexpr int MX_PAIRS = 2 * MX_STEP * 9;   // float pairs of one step's rows
+constexpr int MX_ROWF = 2 * MX_PAIRS;       // their floats in shared memory
+constexpr int MX_SLOTS = MX_PAIRS / 32 + (MX_PAIRS % 32 != 0);  // pairs a lane loads per step
+
 __device__ __forceinline__ void schur_off_warp(const SchurUnit u, const int *__restrict__ pa,
                                                const int *__restrict__ pb, const float *__restrict__ Y,
-                                               const float *__restrict__ W, int *sidx,
+                                               const float *__restrict__ W, int *sidx, float *rowf,
                                                double *__restrict__ partial)
 {
     const int lane = threadIdx.x & 31, s = lane >> 2, q = lane & 3, qr = q >> 1, qc = q & 1;
@@ -1295,12 +1309,52 @@ __device__ __forceinline__ void schur_off_warp(const SchurUnit u, const int *__r
         ib[t] = __ldg(pb + u.begin + t);
     }
     __syncwarp();
+    // this lane's slots: pair k = lane + 32 m of the step's; row r = k / 9
+    // (0-15: Y of entry r, 16-31: W of entry r - 16), pair k % 9 of the row
+    auto load_step = [&](int t0, float2 (&v)[MX_SLOTS]) {
+#pragma unroll
+        for (int m = 0; m < MX_SLOTS; ++m) {
+            const int kk = lane + 32 * m, r = kk / 9, t = t0 + (r & (MX_STEP - 1));
+            if (kk < MX_PAIRS && t < u.count) {
+                const float *row = r < MX_STEP ? Y + 18 * (size_t)ia[t] : W + 18 * (size_t)ib[t];
+                v[m] = __ldg(reinterpret_cast<const float2 *>(row) + (kk - 9 * r));
+            }
+        }
+    };
     float a0[9], a1[9];
 #pragma unroll
     for (int e = 0; e < 9; ++e) a0[e] = a1[e] = 0.0f;
-    for (int t = s; t < u.count; t += 16) {
-        mx_quadrant(Y, W, ia[t], ib[t], qr, qc, a0);
-        if (t + 8 < u.count) mx_quadrant(Y, W, ia[t + 8], ib[t + 8], qr, qc, a1);
+    auto prod = [&](const float *yrow, const float *wrow, float (&acc)[9]) {
+        float y[9], w[9];
+#pragma unroll
+        for (int e = 0; e < 9; ++e) {
+            y[e] = yrow[e];
+            w[e] = wrow[e];
+        }
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                float sm = acc[3 * i + j];
+                sm = fmaf(y[3 * i], w[3 * j], sm);
+                sm = fmaf(y[3 * i + 1], w[3 * j + 1], sm);
+                sm = fmaf(y[3 * i + 2], w[3 * j + 2], sm);
+                acc[3 * i + j] = sm;
+            }
+    };
+    float2 nxt[MX_SLOTS];
+    load_step(0, nxt);
+    for (int t0 = 0; t0 < u.count; t0 += MX_STEP) {
+        __syncwarp();  // the previous step's rows are read
+#pragma unroll
+        for (int m = 0; m < MX_SLOTS; ++m)
+            if (lane + 32 * m < MX_PAIRS) reinterpret_cast<float2 *>(rowf)[lane + 32 * m] = nxt[m];
+        __syncwarp();
+        if (t0 + MX_STEP < u.count) load_step(t0 + MX_STEP, nxt);
+        if (t0 + s < u.count)
+            prod(rowf + 18 * s + 9 * qr, rowf + 18 * (MX_STEP + s) + 9 * qc, a0);
+        if (t0 + 8 + s < u.count)
+            prod(rowf + 18 * (8 + s) + 9 * qr, rowf + 18 * (MX_STEP + 8 + s) + 9 * qc, a1);
     }
     double v[9];
 #pragma unroll
@@ -1324,7 +1378,10 @@ __device__ __forceinline__ void schur_off_warp(const SchurUnit u, const int *__r
 // n_diag: they walk their observations one after another, so they start
 // early and run beside the off-diagonal units), then the off-diagonal units
 // (four per block, a warp each).
-__global__ void __launch_bounds__(128) k_schur_f32(int n_units, int n_diag, const SchurUnit *__restrict__ units,
+#ifndef PSBA_SF32_MINB
+#define PSBA_SF32_MINB 6  // blocks per SM that k_schur_f32's register budget aims at (tuning knob)
+#endif
+__global__ void __launch_bounds__(128, PSBA_SF32_MINB) k_schur_f32(int n_units, int n_diag, const SchurUnit *__restrict__ units,
                                                    const int *__restrict__ pa, const int *__restrict__ pb,
                                                    const SchurUnit *__restrict__ diag_units,
                                                    const int *__restrict__ cam_obs, const int *__restrict__ obs_pt,
@@ -1335,14 +1392,16 @@ __global__ void __launch_bounds__(128) k_schur_f32(int n_units, int n_diag, cons
     // one shared buffer: a diagonal unit's indices, then its reduction
     // (after a barrier), or the four warps' index lists
     constexpr int RED_WORDS = DIAG_NV * (SD_RED_MX + 1) * 2, IDX_WORDS = 4 * 2 * MX_UNIT;
+    constexpr int OFF_WORDS = IDX_WORDS + 4 * MX_ROWF;  // + each warp's step rows
     static_assert(IDX_WORDS >= 2 * DIAG_SUPER, "the index buffer holds a diagonal unit's indices");
-    __shared__ __align__(16) int buf[RED_WORDS > IDX_WORDS ? RED_WORDS : IDX_WORDS];
+    __shared__ __align__(16) int buf[RED_WORDS > OFF_WORDS ? RED_WORDS : OFF_WORDS];
     if ((int)blockIdx.x < n_diag) {
         schur_diag_cta<float>(diag_units[blockIdx.x], cam_obs, obs_pt, Y, W, gb32, diag_partial,
                               reinterpret_cast<double *>(buf), buf);
     } else {
         const int uid = (blockIdx.x - n_diag) * 4 + (threadIdx.x >> 5);
         if (uid < n_units) schur_off_warp(units[uid], pa, pb, Y, W, buf + (threadIdx.x >> 5) * 2 * MX_UNIT,
+                                          reinterpret_cast<float *>(buf + IDX_WORDS) + (threadIdx.x >> 5) * MX_ROWF,
                                           off_partial);
     }
 }

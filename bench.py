@@ -112,6 +112,8 @@ def parse():
     ap.add_argument("--serve-large-lanes", type=int, default=None, help="server large_lanes (default: library's)")
     ap.add_argument("--serve-large-obs", type=int, default=None, help="server large_obs (default: library's)")
     ap.add_argument("--serve-large-cams", type=int, default=None, help="server large_cams (default: library's)")
+    ap.add_argument("--serve-large-chol", type=int, default=None,
+                    help="server large_chol_ctas (default: library's)")
     return ap.parse_args()
 
 
@@ -572,7 +574,8 @@ def serving_leg(P, args):
            "mean_observations": float(np.mean([sc.n_obs for sc in pool])), "rates": []}
     rel_all = []
     with S.Server(precision=P.PREC_MIXED, max_iter=cap, hbm_budget_bytes=120e9, large_cams=args.serve_large_cams,
-                  large_lanes=args.serve_large_lanes, large_obs=args.serve_large_obs) as srv:
+                  large_lanes=args.serve_large_lanes, large_obs=args.serve_large_obs,
+                  large_chol_ctas=args.serve_large_chol) as srv:
         S.run_poisson(srv, pool[:4], rate=1000.0, n_requests=4, seed=1)
         for rate in rates:
             n = int(min(max(rate * args.serve_seconds, 20), args.serve_max))

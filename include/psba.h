@@ -346,6 +346,8 @@ typedef struct psba_server_opts {
     int fp64_intrinsics;     /* 1: requests with 11/16-parameter cameras are solved in FP64 even when the
                                 server's precision is mixed (default 1: with FP32 Jacobian columns for the
                                 intrinsics, LM converges slowly or stalls short of the FP64 minimum) */
+    int large_chol_ctas;     /* CTAs of each large-lane solve's dense factor (default 0: the SMs divided by
+                                large_lanes, so the lanes' factors run side by side) */
     long long large_wait_limit; /* polls per device-side wait of a large-lane solve (psba_set_wait_limit;
                                    default 0: the library's); a wait that runs out fails that request
                                    alone (PSBA_REQUEST_FAILED from psba_batch_poll) */

@@ -489,7 +489,7 @@ int psba_server_create(const psba_server_opts *so, const psba_opts *lm, psba_ser
         (so->threads != 128 && so->threads != 256 && so->threads != 512) ||
         (so->lanes_per_pair != 8 && so->lanes_per_pair != 16 && so->lanes_per_pair != 32) || so->large_cams < 0 ||
         so->large_lanes < 0 || so->large_lanes > 16 || !(so->large_share >= 0.0 && so->large_share < 1.0) ||
-        so->large_obs < 0 || so->large_wait_limit < 0 ||
+        so->large_obs < 0 || so->large_wait_limit < 0 || so->large_chol_ctas < 0 ||
         (lm->precision != PSBA_PREC_FP64 && lm->precision != PSBA_PREC_MIXED) || lm->max_iter < 0 ||
         lm->refine != 0)
         return set_error("psba_server_create: bad options"), PSBA_ERR_ARG;
@@ -532,7 +532,9 @@ int psba_server_create(const psba_server_opts *so, const psba_opts *lm, psba_ser
     }
     std::memset(s->h_probs, 0, sizeof(BatchProblem) * M);
     s->grid_cap = batch_blocks_per_sm(s->precision, so->threads) * sms;
-    if (with_large) s->large_chol_cap = std::max(2, sms / so->large_lanes);
+    if (with_large)
+        s->large_chol_cap = so->large_chol_ctas > 0 ? std::min(so->large_chol_ctas, sms)
+                                                    : std::max(2, sms / so->large_lanes);
     s->alloc.reset(s->pool_size);
     s->slots.assign(M, nullptr);
     s->worker = std::thread(worker_main, s);

@@ -27,7 +27,7 @@ class ServerOpts(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_double), ("max_active", C.c_int), ("slice_iters", C.c_int),
                 ("threads", C.c_int), ("lanes_per_pair", C.c_int), ("large_cams", C.c_int),
                 ("large_lanes", C.c_int), ("large_share", C.c_double), ("large_obs", C.c_int),
-                ("fp64_intrinsics", C.c_int), ("large_wait_limit", C.c_longlong)]
+                ("fp64_intrinsics", C.c_int), ("large_chol_ctas", C.c_int), ("large_wait_limit", C.c_longlong)]
 
 
 class RequestResult(C.Structure):
@@ -81,7 +81,8 @@ class Request:
 class Server:
     def __init__(self, precision=PREC_FP64, max_iter=15, hbm_budget_bytes=120e9, max_active=1024,
                  slice_iters=1, threads=256, lanes_per_pair=32, large_cams=None, large_lanes=None,
-                 large_share=None, large_obs=None, fp64_intrinsics=None, large_wait_limit=None, **lm):
+                 large_share=None, large_obs=None, fp64_intrinsics=None, large_wait_limit=None,
+                 large_chol_ctas=None, **lm):
         L = _bind()
         so = ServerOpts()
         L.psba_server_default_opts(C.byref(so))
@@ -102,6 +103,8 @@ class Server:
             so.fp64_intrinsics = int(bool(fp64_intrinsics))
         if large_wait_limit is not None:
             so.large_wait_limit = int(large_wait_limit)
+        if large_chol_ctas is not None:
+            so.large_chol_ctas = int(large_chol_ctas)
         o = default_opts(precision=precision, max_iter=max_iter, allow_switch=0, **lm)
         h = C.c_void_p()
         _check(L.psba_server_create(C.byref(so), C.byref(o), C.byref(h)))

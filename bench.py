@@ -206,6 +206,44 @@ def schur_flops(cfg):
     return 2 * 108 * cfg["pair_entries"] + 2 * 81 * cfg["observations"]
 
 
+def stage_rooflines(sc, cfg, stage_ms, real_bytes, peak_gbs, fp64_peak, fp32_peak=None):
+    """Every per-trial or per-iteration stage against HBM and its compute
+    pipe: algorithmic bytes of the stage's defined inputs and outputs (the
+    scope table's formulas with the run's O, P, C and c = 6; real_bytes 8 for
+    the FP64 form, 4 for the mixed form's FP32 arrays; the stages this design
+    adds or splits -- V^-1, eb/dpb, the trial cost -- by the same rule) and
+    its approximate FMA count (from the kernel's arithmetic), over the
+    stage's CUDA-event time."""
+    O, P, C, c, s = sc.n_obs, sc.n_pts, sc.n_cams, 6, real_bytes
+    pairs = cfg["pair_entries"]
+    st = {
+        # J: the residual and the chain-rule Jacobian (k_cam_tables, k_linearize)
+        "linearize": (O * (16 + 8) + P * 24 + C * (c + 9) * 8 + O * (2 * c + 6 + 2) * s, 110 * O),
+        # U/V/W/g: W is written by the linearization here, so it is counted there
+        "point_blocks": (O * (6 + 2) * s + O * 8 + P * 9 * 8 + 3 * P * 8, 18 * O),
+        "camera_blocks": (O * (12 + 2) * s + O * 4 + C * c * c * 8 + C * c * 8, 54 * O),
+        "vinv": (P * 6 * 8 * 2, 40 * P),
+        "yblocks": (2 * O * 3 * c * s + P * 9 * s + O * 4, 54 * O),
+        "schur_off": (2 * O * 3 * c * s + O * 4 + (C * c) ** 2 * 8, 108 * pairs + 81 * O),
+        "eb_dpb": (O * 3 * c * s + O * 4 + (C * c + 3 * P) * 8 * 3 + P * 6 * 8, 18 * O + 9 * P),
+        "trial_cost": (O * (16 + 8) + P * 24 * 2 + C * 17 * 8, 30 * O),
+    }
+    out = {}
+    for k, (nbytes, fma) in st.items():
+        t = stage_ms.get(k, 0.0)
+        if t <= 0:
+            continue
+        gbs = nbytes / (t * 1e-3) / 1e9
+        tf = 2 * fma / (t * 1e-3) / 1e12
+        out[k] = {"ms": t, "algorithmic_bytes": int(nbytes), "hbm_gbs": gbs, "hbm_frac": gbs / peak_gbs,
+                  "fma": int(fma), "tflops": tf}
+        if fp32_peak:  # the mixed form: its products are FP32
+            out[k]["fp32_frac"] = tf / fp32_peak
+        else:
+            out[k]["fp64_frac"] = tf / fp64_peak
+    return out
+
+
 def flush_l2(torch, buf):
     buf.zero_()
     torch.cuda.synchronize()
@@ -785,11 +823,18 @@ def main():
     stage_ms = {k: (v[0] / v[1] if v[1] else 0.0) for k, v in stages.items()}
     total_stage = sum(v[0] for v in stages.values())
 
+    stage_roof = {"fp64": stage_rooflines(sc, cfg, stage_ms, 8, peak_gbs, fp64_peak),
+                  "note": "per stage: the scope table's algorithmic bytes (O, P, C of this run; c = 6) and the "
+                          "stage's approximate FMA count over its CUDA-event time; hbm_frac of the measured copy "
+                          "rate, fp64_frac (FP64 form) or fp32_frac (mixed form) of the measured FMA rate.  Useful "
+                          "FMAs only: a warp instruction costs the FP64 pipe the same with idle lanes, so the "
+                          "pipe itself (ncu: sm__pipe_fp64_cycles_active) is busier than fp64_frac where lanes idle"}
     roofline_mixed = None
     if mixed is not None:
         fp32_peak = P.measure_peak("fp32")
         f32_s = m_live["schur_off"][0] / max(m_live["schur_off"][1], 1) / 1e3
         f32_bytes = 2 * sc.n_obs * 18 * 4 + 2 * 4 * cfg["pair_entries"] + 4 * sc.n_obs
+        stage_roof["mixed"] = stage_rooflines(sc, cfg, mixed["stage_ms"], 4, peak_gbs, fp64_peak, fp32_peak)
         roofline_mixed = {
             "kernel": "k_schur_f32: the mixed form's Schur products (FP32 products, FP64 sums), off-diagonal "
                       "and diagonal units in one launch per LM trial",
@@ -840,7 +885,7 @@ def main():
                            "hbm": {"achieved": achieved_gbs, "peak": peak_gbs, "unit": "GB/s",
                                    "frac": achieved_gbs / peak_gbs, "algorithmic_bytes": schur_bytes(sc),
                                    "peak_source": peak_kind}},
-        "roofline_mixed": roofline_mixed, "dmma_tflops": dmma,
+        "roofline_mixed": roofline_mixed, "stage_rooflines": stage_roof, "dmma_tflops": dmma,
         "stage_ms": stage_ms, "mixed": mixed, "matched_cost": matched, "trust_region": tr, "refine": refine,
         "stage_share": {k: (v[0] / total_stage if total_stage else 0.0) for k, v in stages.items()},
         "clocks": clk, "gpu_launches": int(launches),

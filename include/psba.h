@@ -340,7 +340,7 @@ typedef struct psba_server_opts {
     int threads;             /* CTA size of the persistent launch: 128, 256, 512 (default 256) */
     int lanes_per_pair;      /* lanes per camera pair in the Schur stage: 8, 16, 32 (default 32) */
     int large_cams;          /* requests with more cameras run on the large lane (default 40; 0: no large lane) */
-    int large_lanes;         /* large-lane host threads, each solving one request at a time (default 4) */
+    int large_lanes;         /* large-lane host threads, each solving one request at a time (default 8) */
     double large_share;      /* share of hbm_budget_bytes reserved for the large lane (default 0.25) */
     int large_obs;           /* ... and so do requests with more observations (default 20000; 0: no limit) */
     int fp64_intrinsics;     /* 1: requests with 11/16-parameter cameras are solved in FP64 even when the

@@ -475,7 +475,7 @@ void psba_server_default_opts(psba_server_opts *o)
     o->threads = 256;
     o->lanes_per_pair = 32;
     o->large_cams = 40;
-    o->large_lanes = 4;
+    o->large_lanes = 8;
     o->large_share = 0.25;
     o->large_obs = 20000;
     o->fp64_intrinsics = 1;

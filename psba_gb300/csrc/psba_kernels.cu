@@ -344,14 +344,16 @@ __global__ void __launch_bounds__(256) k_residual(int no, const int *__restrict_
                                                   double *__restrict__ partial, int stage_nc,
                                                   double *__restrict__ sum_dst, int *__restrict__ ticket)
 {
-    __shared__ double red[256];
+    __shared__ double red[256 / 32];
     extern __shared__ double s_tab[];  // stage_nc * RES_TAB
     for (int e = threadIdx.x; e < stage_nc * RES_TAB; e += blockDim.x)
         s_tab[e] = __ldg(tab + (size_t)CAMTAB * (e / RES_TAB) + res_tab_src(e % RES_TAB));
     if (stage_nc > 0) __syncthreads();
-    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    // a few resident blocks per SM, each thread over the observations o, o +
+    // the grid's threads, ...: the table is staged once per block instead of
+    // once per 256 observations; each thread's squares summed in its order
     double sq = 0.0;
-    if (o < no) {
+    for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < no; o += gridDim.x * blockDim.x) {
         const int i = __ldg(obs_pt + o), j = __ldg(obs_cam + o);
         double X[3];
 #pragma unroll
@@ -372,7 +374,7 @@ __global__ void __launch_bounds__(256) k_residual(int no, const int *__restrict_
         const double iz = 1.0 / zc;
         const double u = (Tv[12] * xc + Tv[13] * yc + Tv[14] * zc) * iz;
         const double v = (Tv[15] * yc + Tv[16] * zc) * iz;
-        const double2 m2 = *reinterpret_cast<const double2 *>(meas + 2 * (size_t)o);
+        const double2 m2 = __ldg(reinterpret_cast<const double2 *>(meas + 2 * (size_t)o));
         double e0 = m2.x - u, e1 = m2.y - v;
         if (wt) {
             const double t0 = wt[3 * (size_t)o] * e0 + wt[3 * (size_t)o + 1] * e1;
@@ -380,15 +382,18 @@ __global__ void __launch_bounds__(256) k_residual(int no, const int *__restrict_
             e0 = t0;
         }
         if (ex_out) *reinterpret_cast<double2 *>(ex_out + 2 * (size_t)o) = make_double2(e0, e1);
-        sq = e0 * e0 + e1 * e1;
+        sq = fma(e0, e0, fma(e1, e1, sq));
     }
-    red[threadIdx.x] = sq;
+    // fixed-order block sum: xor tree in each warp, then the warps in order
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, off);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sq;
     __syncthreads();
-    for (int st = 128; st > 0; st >>= 1) {
-        if (threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
-        __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = red[0];
+        for (int w = 1; w < 256 / 32; ++w) a += red[w];
+        partial[blockIdx.x] = a;
     }
-    if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
     if (sum_dst && take_last_ticket(ticket)) {
         sum_partials_block(partial, gridDim.x, sum_dst);
         if (threadIdx.x == 0) *ticket = 0;
@@ -401,7 +406,22 @@ int residual_stage_nc(const DeviceProblem &d)
     return (size_t)d.nc * RES_TAB * sizeof(double) <= 48 * 1024 ? d.nc : 0;
 }
 
-int residual_blocks(const DeviceProblem &d) { return ceil_div(d.no > 0 ? d.no : 1, 256); }
+// k_residual's grid: four blocks of 256 per SM at most (its loop takes the rest)
+int residual_blocks(const DeviceProblem &d)
+{
+    static std::mutex mu;
+    static int sms_dev[MAX_DEVICES] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= MAX_DEVICES) dev = 0;
+    int sms = 0;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (sms_dev[dev] == 0) cudaDeviceGetAttribute(&sms_dev[dev], cudaDevAttrMultiProcessorCount, dev);
+        sms = std::max(1, sms_dev[dev]);
+    }
+    return std::max(1, std::min(ceil_div(d.no > 0 ? d.no : 1, 256), 4 * sms));
+}
 
 void launch_residual(const DeviceProblem &d, const double *tab, const double *pts, const double *dpb,
                      double *ex_out, double *partial, int nblocks, double *sum_dst, cudaStream_t s)

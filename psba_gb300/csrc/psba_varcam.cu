@@ -195,10 +195,11 @@ __global__ void __launch_bounds__(256) k_residual_dist(int no, const int *__rest
                                                        double *__restrict__ ex_out,
                                                        double *__restrict__ partial)
 {
-    __shared__ double red[256];
-    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ double red[256 / 32];
+    // the grid's threads over the observations o, o + grid, ... (the grid of
+    // k_residual: a few blocks per SM), each thread's squares in its order
     double sq = 0.0;
-    if (o < no) {
+    for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < no; o += gridDim.x * blockDim.x) {
         const int i = obs_pt[o], j = obs_cam[o];
         double X[3];
         for (int m = 0; m < 3; ++m) X[m] = dpb ? pts[3 * i + m] + dpb[3 * i + m] : pts[3 * i + m];
@@ -223,15 +224,17 @@ __global__ void __launch_bounds__(256) k_residual_dist(int no, const int *__rest
             ex_out[2 * (size_t)o] = e0;
             ex_out[2 * (size_t)o + 1] = e1;
         }
-        sq = e0 * e0 + e1 * e1;
+        sq = fma(e0, e0, fma(e1, e1, sq));
     }
-    red[threadIdx.x] = sq;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) sq += __shfl_xor_sync(0xffffffffu, sq, off);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = sq;
     __syncthreads();
-    for (int st = 128; st > 0; st >>= 1) {
-        if (threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
-        __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = red[0];
+        for (int w = 1; w < 256 / 32; ++w) a += red[w];
+        partial[blockIdx.x] = a;
     }
-    if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
 }
 
 // ---------------------------------------------------------------------------

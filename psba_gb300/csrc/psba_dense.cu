@@ -300,19 +300,6 @@ __device__ __forceinline__ void pf_step(const PfSlot &q, double &v, double ik2, 
     if (lval) W[q.dofs] = t;
 }
 
-// 1 / x for the pivot chain: the hardware's approximate reciprocal
-// (rcp.approx.ftz.f64, ~2^-20 relative error) and one step of the order-3
-// Householder iteration for f(y) = 1/y - x: with e = 1 - x y,
-// y <- y (1 + e + e^2), cubing the relative error.  Within 1 ulp of 1.0 / x
-// for x in [2^-80, 2^80], in ~200 cycles against ~330 for the division.
-__device__ __forceinline__ double rcp_fast(double x)
-{
-    double y;
-    asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-    const double e = fma(-x, y, 1.0);
-    return fma(y, fma(e, e, e), y);
-}
-
 // Phase S of the whole CTA (see the plan above).
 // The phases synchronise the seven warps with a role (named barrier 1); warp
 // 4 joins the CTA only at the factor's start and end.

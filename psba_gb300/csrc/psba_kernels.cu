@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(256) k_linearize(int no, const int *__restrict
     const double zcd = Md[6] * Xd0 + Md[7] * Xd1 + Md[8] * Xd2 + __ldg(T + 38);
     const double fxd = __ldg(T + 39), skd = __ldg(T + 40), cxd = __ldg(T + 41), fyd = __ldg(T + 42),
                  cyd = __ldg(T + 43);
-    const double izd = 1.0 / zcd;
+    const double izd = rcp_fast(zcd);
     const double2 m2 = __ldg(reinterpret_cast<const double2 *>(meas + 2 * (size_t)o));
     const double nud = fxd * xcd + skd * ycd;
     const double u = (nud + cxd * zcd) * izd;
@@ -371,7 +371,7 @@ __global__ void __launch_bounds__(256) k_residual(int no, const int *__restrict_
         const double xc = Tv[0] * X[0] + Tv[1] * X[1] + Tv[2] * X[2] + Tv[9];
         const double yc = Tv[3] * X[0] + Tv[4] * X[1] + Tv[5] * X[2] + Tv[10];
         const double zc = Tv[6] * X[0] + Tv[7] * X[1] + Tv[8] * X[2] + Tv[11];
-        const double iz = 1.0 / zc;
+        const double iz = rcp_fast(zc);
         const double u = (Tv[12] * xc + Tv[13] * yc + Tv[14] * zc) * iz;
         const double v = (Tv[15] * yc + Tv[16] * zc) * iz;
         const double2 m2 = __ldg(reinterpret_cast<const double2 *>(meas + 2 * (size_t)o));

@@ -213,8 +213,9 @@ def test_hybrid_matched_final_cost():
 
 # ---------------------------------------------------------------- mixed precision
 # Jacobian, residual, W, V and Y in FP32; U, S, ea accumulated in FP64; the
-# damped V^-1, Y's products, Cholesky, the solves, step, cost and gain ratio
-# in FP64.  Stage tolerance:
+# damped V^-1, Cholesky, the solves, step, cost and gain ratio in FP64; Y's
+# products and the V, g and eb sums in double-float FP32 arithmetic (FP64
+# accuracy).  Stage tolerance:
 # 1e-5 of the array's largest magnitude (FP32 rounding of quantities built
 # from a handful of FP32 operations); solves: final cost within 1e-6 of the
 # FP64 oracle's.

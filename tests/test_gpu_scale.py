@@ -1,13 +1,15 @@
 """Parity at the benchmark sizes: the GPU solver against the FP64 oracle on
 the single large problem (88 cameras x 64,298 points, N = 528: 33 diagonal
 tiles of the dense factor, the 8-CTA cluster back solve, pair-list chunks
-that span pairs) and on the variable-intrinsics problem with 16-parameter
-cameras (52 x 64,053, N = 832) and 11-parameter cameras (N = 572).
+that span pairs, the multi-CTA modified Cholesky) and on the
+variable-intrinsics problem with 16-parameter cameras (52 x 64,053,
+N = 832) and 11-parameter cameras (N = 572).
 
 The bar of the small scenes holds here too: the LM accept/reject sequence of
 the first 10 iterations equals the oracle's (levmar.cpp:100-249), and the
-cost after the run is within 1e-9 relative.  The oracle runs on every host
-core (OpenMP, fixed-order partial sums).
+cost after the run is within 1e-9 relative; the trust-region trace as on the
+small scenes, within the oracle's own spread under 1-ulp input changes.  The
+oracle runs on every host core (OpenMP, fixed-order partial sums).
 """
 import os
 
@@ -17,6 +19,7 @@ import pytest
 import oracle
 import psba_gb300 as P
 from psba_gb300 import scenes
+from tr_envelope import tr_envelope, assert_tr_trace_close
 
 pytestmark = pytest.mark.gpu
 
@@ -57,3 +60,16 @@ def test_levmar_variable_intrinsics_full_size_matches_oracle(cnp, iters):
     assert sc.n_cams * cnp == {16: 832, 11: 572}[cnp]
     o, g = _compare(sc, iters)
     assert abs(g.final_cost - o.final_cost) <= 1e-9 * o.final_cost
+
+
+def test_trust_region_single_large_problem_matches_oracle():
+    # the dogleg driver at the benchmark size: its first Gauss-Newton step
+    # fails on the singular lambda = 0 system and lambda comes from the
+    # modified Cholesky of S (N = 528); the decisions over the iterations
+    # where the oracle's nudged runs agree, costs and lambda within its spread
+    sc = scenes.circle_scene(seed=0, name="circle")
+    o, n, env = tr_envelope(sc, 10, max_iter=10, n_threads=os.cpu_count() or 1)
+    assert n >= 3
+    with P.Solver(sc) as s:
+        g = s.trust_region(max_iter=10, fetch=False)
+    assert_tr_trace_close(o, g, n, env, same_end=n == 10)

@@ -7,7 +7,7 @@ import oracle
 import psba_gb300 as P
 
 
-def tr_envelope(sc, n_iter, max_iter=12):
+def tr_envelope(sc, n_iter, max_iter=12, **okw):
     """The oracle's own spread over its trust-region trace when its inputs
     move by one ulp (points nudged up, points nudged down) or it solves
     instead of inverting S.  The reference's dogleg is ill-conditioned on
@@ -18,14 +18,15 @@ def tr_envelope(sc, n_iter, max_iter=12):
     the input, while its LM path moves by 1e-15.  Returns the oracle's run,
     the number of leading iterations (at most n_iter) over which every nudged
     run makes the same decisions, and the per-record maximum relative spreads
-    of cost and lambda over those iterations and that of the final cost."""
-    base = oracle.trust_region(sc, max_iter=max_iter)
+    of cost and lambda over those iterations and that of the final cost.
+    okw: further oracle options (n_threads)."""
+    base = oracle.trust_region(sc, max_iter=max_iter, **okw)
     runs = []
     for sign in (np.inf, -np.inf):
         sc2 = sc.copy()
         sc2.pts = np.nextafter(sc.pts, sign)
-        runs.append(oracle.trust_region(sc2, max_iter=max_iter))
-    runs.append(oracle.trust_region(sc, max_iter=max_iter, solve_mode=1))
+        runs.append(oracle.trust_region(sc2, max_iter=max_iter, **okw))
+    runs.append(oracle.trust_region(sc, max_iter=max_iter, solve_mode=1, **okw))
     n = n_iter
     while n > 0:
         t0 = base.trace[base.trace["itno"] < n]

@@ -103,6 +103,9 @@ def parse():
     ap.add_argument("--batch", type=int, default=1024, help="problems in the batched leg (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--batch-cap", type=int, default=240, help="iteration cap of the batched and serving solves")
+    ap.add_argument("--batch-handoff", type=int, default=48,
+                    help="batched leg: iterations after which an unfinished problem moves to the single-problem "
+                         "solver (0: skip)")
     ap.add_argument("--pbp-sample", type=int, default=64,
                     help="problems solved one by one by the plain FP64 form for the batched comparison")
     ap.add_argument("--serve-rates", default="50,200,1000,2000", help="Poisson rates, req/s ('none' to skip)")
@@ -521,6 +524,24 @@ def batched_leg(P, args):
         res_f, f_ms = timed(b, fo)
         res_15, m15_ms = timed(b, P.default_opts(allow_switch=0, max_iter=15, precision=P.PREC_MIXED))
         res_15f, _ = timed(b, P.default_opts(allow_switch=0, max_iter=15))
+        hand = None
+        if args.batch_handoff > 0:
+            ho_ms, ho = [], None
+            for _ in range(args.batch_steps):
+                b.reset()
+                ho, bms, hms, todo = B.levmar_with_handoff(b, mo, args.batch_handoff)
+                ho_ms.append((bms + hms, bms, hms, len(todo)))
+            tot, bms, hms, nt = sorted(ho_ms)[len(ho_ms) // 2]
+            rel_h = (ho["final_cost"] - res_f["final_cost"]) / res_f["final_cost"]
+            hand = {"cap": args.batch_handoff, "handed_over": nt, "batch_ms": bms, "handoff_host_ms": hms,
+                    "total_ms": tot, "mixed_solves_per_s": args.batch / (tot / 1e3),
+                    "status": {P.STATUS_NAMES.get(int(k), str(k)): int(c)
+                               for k, c in zip(*np.unique(ho["status"], return_counts=True))},
+                    "frac_within_1e-6_of_fp64_converged": float((rel_h <= MATCH_TOL).mean()),
+                    "note": "problems the persistent launch has not finished after `cap` iterations continue on "
+                            "the single-problem solver from the batch's parameters and LM state "
+                            "(psba_levmar_resume), up to 8 at once; batch device time plus the hand-over's "
+                            "host time (handle creation included)"}
         dev_bytes = b.device_bytes()
     # the plain FP64 form, problem by problem (create outside the timing)
     sample = probs[: args.pbp_sample]
@@ -551,6 +572,8 @@ def batched_leg(P, args):
         "fp64_problem_by_problem_solves_per_s": pbp_sps,
         "fp64_problem_by_problem_sample": len(sample),
         "speedup_mixed_batched_vs_fp64_problem_by_problem": m_sps / pbp_sps,
+        "handoff": hand,
+        "speedup_mixed_handoff_vs_fp64_problem_by_problem": (hand["mixed_solves_per_s"] / pbp_sps) if hand else None,
         "matched": {"criterion": "final cost <= (1 + %g) x the FP64 converged cost of the same problem" % MATCH_TOL,
                     "frac_vs_fp64_batched": float((rel <= MATCH_TOL).mean()),
                     "frac_vs_fp64_problem_by_problem": float((rel_pbp <= MATCH_TOL).mean()),

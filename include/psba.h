@@ -179,6 +179,14 @@ int psba_trust_region(psba_handle *h, const psba_opts *opts, int *itno, psba_res
 /* The LM <-> TR alternation of PSBA/main.cpp:193-208, from itno = 0. */
 int psba_solve_hybrid(psba_handle *h, const psba_opts *opts, psba_result *res);
 
+/* levmar() continued from a given LM state (mu, nu, |p|^2 of the current
+ * parameters, e.g. a psba_batch_result of a problem its iteration cap
+ * stopped) at the handle's current parameters and shared iteration count
+ * *itno: the first linearization does not re-initialise mu (levmar.cpp:
+ * 114-120 runs only for a fresh solve); otherwise psba_levmar. */
+int psba_levmar_resume(psba_handle *h, const psba_opts *opts, double mu, int nu, double p_L2, int *itno,
+                       psba_result *res);
+
 /* Bound of the handle's device-side waits: the dense factor's waits on its
  * task flags and the Y kernel's wait for its bulk copies, in polls (0: the
  * default, 2^22, about half a second).  A wait that runs out ends its kernel
@@ -291,6 +299,13 @@ typedef struct {
     int n_linearizations;
     double initial_cost;
     double final_cost;
+    /* LM state at exit (for psba_levmar_resume when the iteration cap ended
+     * the solve): damping mu, its growth factor nu, |p|^2 of the last accepted
+     * parameters (levmar.cpp:73-249) */
+    double mu;
+    double p_L2;
+    int nu;
+    int pad;
 } psba_batch_result;
 
 int psba_batch_create(const psba_problem_desc *problems, int n_problems, psba_batch **out);

@@ -65,7 +65,7 @@ TRACE_DTYPE = np.dtype([("itno", np.int32), ("kind", np.int32), ("accepted", np.
 # every entry point declared in include/psba.h
 EXPORTS = ("psba_default_opts", "psba_create", "psba_destroy", "psba_get_params", "psba_set_params",
            "psba_reset_params", "psba_set_precision", "psba_set_refine", "psba_set_wait_limit",
-           "psba_levmar", "psba_trust_region", "psba_solve_hybrid", "psba_eval_residual",
+           "psba_levmar", "psba_levmar_resume", "psba_trust_region", "psba_solve_hybrid", "psba_eval_residual",
            "psba_eval_jacobian", "psba_eval_normal", "psba_eval_reduced", "psba_eval_step",
            "psba_eval_jmultiply", "psba_eval_cholmod", "psba_eval_dense_solve", "psba_eval_pivot_reciprocal",
            "psba_last_error", "psba_stream",
@@ -110,6 +110,8 @@ def lib():
         for f in ("psba_levmar", "psba_trust_region"):
             getattr(L, f).argtypes = [C.c_void_p, C.POINTER(Opts), _ip, C.POINTER(Result)]
         L.psba_solve_hybrid.argtypes = [C.c_void_p, C.POINTER(Opts), C.POINTER(Result)]
+        L.psba_levmar_resume.argtypes = [C.c_void_p, C.POINTER(Opts), C.c_double, C.c_int, C.c_double, _ip,
+                                         C.POINTER(Result)]
         L.psba_eval_residual.argtypes = [C.c_void_p, _dp, _dp]
         L.psba_eval_jacobian.argtypes = [C.c_void_p, _dp, _dp]
         L.psba_eval_normal.argtypes = [C.c_void_p, C.c_double, _dp, _dp, _dp, _dp]
@@ -297,6 +299,20 @@ class Solver:
 
     def levmar(self, opts=None, itno=0, trace_cap=4096, fetch=True, **kw):
         return self._run("psba_levmar", opts or default_opts(**kw), itno, trace_cap, fetch)
+
+    def levmar_resume(self, opts, mu, nu, p_L2, itno=0, trace_cap=4096, fetch=True):
+        """levmar() continued from an LM state (mu, nu, |p|^2) at the current
+        parameters, e.g. a batch problem its iteration cap stopped."""
+        tr = np.zeros(max(trace_cap, 1), dtype=TRACE_DTYPE)
+        res = Result()
+        res.trace_cap = trace_cap
+        res.trace = tr.ctypes.data_as(C.POINTER(TraceEntry)) if trace_cap else None
+        it = C.c_int(itno)
+        _check(lib().psba_levmar_resume(self.h, C.byref(opts), float(mu), int(nu), float(p_L2), C.byref(it),
+                                        C.byref(res)))
+        n = min(res.n_trace, trace_cap)
+        cams, pts = self.get_params() if fetch else (None, None)
+        return SolveResult(res, tr[:n].copy(), cams, pts)
 
     def trust_region(self, opts=None, itno=0, trace_cap=4096, fetch=True, **kw):
         return self._run("psba_trust_region", opts or default_opts(**kw), itno, trace_cap, fetch)

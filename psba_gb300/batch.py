@@ -18,12 +18,14 @@ from . import (Opts, PSBAError, ProblemDesc, PREC_FP64, PREC_MIXED, _check, _d, 
 
 class BatchResult(C.Structure):
     _fields_ = [("status", C.c_int), ("iterations", C.c_int), ("n_trials", C.c_int),
-                ("n_linearizations", C.c_int), ("initial_cost", C.c_double), ("final_cost", C.c_double)]
+                ("n_linearizations", C.c_int), ("initial_cost", C.c_double), ("final_cost", C.c_double),
+                ("mu", C.c_double), ("p_L2", C.c_double), ("nu", C.c_int), ("pad", C.c_int)]
 
 
 RESULT_DTYPE = np.dtype([("status", np.int32), ("iterations", np.int32), ("n_trials", np.int32),
                          ("n_linearizations", np.int32), ("initial_cost", np.float64),
-                         ("final_cost", np.float64)])
+                         ("final_cost", np.float64), ("mu", np.float64), ("p_L2", np.float64),
+                         ("nu", np.int32), ("pad", np.int32)])
 
 _bound = False
 
@@ -123,6 +125,45 @@ class Batch:
         pts = np.empty((sc.n_pts, 3))
         _check(lib().psba_batch_get_params(self.h, int(q), cams.ctypes.data, pts.ctypes.data))
         return cams, pts
+
+
+def levmar_with_handoff(batch, opts, cap, workers=8):
+    """The batch solved to opts.max_iter, with the problems the persistent
+    launch has not finished after `cap` iterations handed over to the
+    single-problem solver (all SMs per problem, one host thread and stream
+    each, up to `workers` at once).  A problem runs LM in one CTA of the
+    batched launch, so one that needs many iterations holds the whole launch
+    while the other SMs idle; the single-problem solver continues it from
+    the batch's parameters and LM state (psba_levmar_resume).  Returns the
+    results (the batch's, with the continued problems' replaced), the batch's
+    device ms and the hand-over's host ms (handle creation included)."""
+    import concurrent.futures as cf
+    from . import ITER_CONTINUE, Solver
+    o1 = Opts.from_buffer_copy(opts)
+    o1.max_iter = min(int(cap), int(opts.max_iter))
+    res, batch_ms = batch.levmar(o1)
+    todo = [int(q) for q in np.nonzero((res["status"] == ITER_CONTINUE) & (res["iterations"] < opts.max_iter))[0]]
+
+    def one(q):
+        cams, pts = batch.get_params(q)
+        with Solver(batch.scenes[q]) as s:
+            s.set_params(cams, pts)
+            r = s.levmar_resume(opts, float(res["mu"][q]), int(res["nu"][q]), float(res["p_L2"][q]),
+                                itno=int(res["iterations"][q]), fetch=False, trace_cap=0)
+        return q, r
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=max(1, workers)) as ex:
+        done = list(ex.map(one, todo))
+    hand_ms = 1e3 * (time.perf_counter() - t0) if todo else 0.0
+    out = res.copy()
+    for q, r in done:
+        out["status"][q] = r.status
+        out["iterations"][q] = r.iterations
+        out["n_trials"][q] += r.n_trials
+        out["n_linearizations"][q] += r.n_linearizations
+        out["final_cost"][q] = r.final_cost
+    return out, batch_ms, hand_ms, todo
 
 
 def autotune(batch, precision=PREC_MIXED, n_buckets=3, lane_options=(8, 16, 32), thread_options=(128, 256, 512),

@@ -1059,6 +1059,10 @@ int psba_batch_levmar(psba_batch *b, const psba_opts *opts, psba_batch_result *r
             results[q].n_linearizations = r[q].linearizations;
             results[q].initial_cost = r[q].initial_cost;
             results[q].final_cost = r[q].final_cost;
+            results[q].mu = r[q].mu;
+            results[q].p_L2 = r[q].p_L2;
+            results[q].nu = r[q].nu;
+            results[q].pad = 0;
         }
     }
     return PSBA_OK;

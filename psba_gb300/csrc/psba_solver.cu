@@ -387,7 +387,14 @@ void trace_push(psba_result *res, int itno, int kind, int acc, double damping, d
 // ---------------------------------------------------------------------------
 // levmar(), PSBA/levmar.cpp:45-256
 
-int levmar_impl(psba_handle *h, const psba_opts *o, int *itno, psba_result *res, int *flag_out)
+// An LM state to continue from (psba_levmar_resume).
+struct LmState {
+    double mu, p_L2;
+    int nu;
+};
+
+int levmar_impl(psba_handle *h, const psba_opts *o, int *itno, psba_result *res, int *flag_out,
+                const LmState *from = nullptr)
 {
     DeviceProblem &d = h->d;
     const double tau = o->tau;
@@ -395,6 +402,12 @@ int levmar_impl(psba_handle *h, const psba_opts *o, int *itno, psba_result *res,
     int nu = 2, gooditer_cnt = 0;
     bool first = true;
     double sc[64];
+    if (from) {
+        mu = from->mu;
+        p_L2 = from->p_L2;
+        nu = from->nu;
+        first = false;
+    }
 
     enqueue_cost_current(h, nullptr);
     TRY(check_launch());
@@ -1314,6 +1327,24 @@ int psba_levmar(psba_handle *h, const psba_opts *opts, int *itno, psba_result *r
     TRY(timed_begin(h));
     int flag = 0;
     TRY(levmar_impl(h, opts, itno, res, &flag));
+    TRY(timed_end(h, res));
+    return PSBA_OK;
+}
+
+int psba_levmar_resume(psba_handle *h, const psba_opts *opts, double mu, int nu, double p_L2, int *itno,
+                       psba_result *res)
+{
+    if (!h || !itno) return set_error("null argument"), PSBA_ERR_ARG;
+    TRY(check_opts(opts));
+    if (!(mu > 0.0) || !std::isfinite(mu) || nu < 2 || !(p_L2 >= 0.0) || !std::isfinite(p_L2))
+        return set_error("psba_levmar_resume: mu > 0, nu >= 2 and a finite p_L2 >= 0 are needed"), PSBA_ERR_ARG;
+    h->d.prec = opts->precision;
+    h->refine = opts->refine;
+    reset_result(res);
+    TRY(timed_begin(h));
+    int flag = 0;
+    const LmState st{mu, p_L2, nu};
+    TRY(levmar_impl(h, opts, itno, res, &flag, &st));
     TRY(timed_end(h, res));
     return PSBA_OK;
 }

@@ -87,3 +87,51 @@ def test_autotune_returns_a_valid_choice():
         assert all(v in (8, 16, 32, None) for v in choice["lanes_per_bucket"].values())
         res, _ = b.levmar(allow_switch=0, max_iter=5, precision=P.PREC_MIXED)
         assert np.all(res["final_cost"] < res["initial_cost"])
+
+
+def test_levmar_resume_continues_a_batch_problem():
+    # the batch stopped at 6 iterations hands its parameters and LM state
+    # (mu, nu, |p|^2) to the single-problem solver, which continues to 15:
+    # the same decisions and cost as the oracle's uninterrupted 15 iterations
+    probs = small_batch(3, seed=5)
+    with B.Batch(probs) as b:
+        res, _ = b.levmar(allow_switch=0, max_iter=6)
+        for q, sc in enumerate(probs):
+            o = oracle.levmar(sc, allow_switch=0, max_iter=15)
+            if res["status"][q] != P.ITER_CONTINUE:
+                continue  # converged within the cap: nothing to hand over
+            cams, pts = b.get_params(q)
+            with P.Solver(sc) as s:
+                s.set_params(cams, pts)
+                g = s.levmar_resume(P.default_opts(allow_switch=0, max_iter=15), res["mu"][q], res["nu"][q],
+                                    res["p_L2"][q], itno=int(res["iterations"][q]))
+            assert g.status == o.status and g.iterations == o.iterations, q
+            assert abs(g.final_cost - o.final_cost) <= 1e-9 * o.final_cost, q
+            to = o.trace[o.trace["itno"] >= 6]
+            assert np.array_equal(to["accepted"], g.trace["accepted"]), q
+
+
+def test_levmar_resume_rejects_a_bad_state():
+    sc = small_batch(1, seed=6)[0]
+    with P.Solver(sc) as s:
+        for mu, nu, pl2 in ((0.0, 2, 1.0), (1.0, 1, 1.0), (1.0, 2, float("nan"))):
+            with pytest.raises(P.PSBAError):
+                s.levmar_resume(P.default_opts(max_iter=3), mu, nu, pl2)
+
+
+@pytest.mark.parametrize("precision", [P.PREC_FP64, P.PREC_MIXED])
+def test_batch_handoff_matches_the_batch_alone(precision):
+    # a low cap hands most problems over; every problem still ends at the
+    # cost of the batch run to the stopping rule (FP64: to 1e-9; mixed: the
+    # two engines' FP32 products differ, to 1e-6)
+    probs = small_batch(12, seed=7)
+    opts = P.default_opts(allow_switch=0, max_iter=240, precision=precision)
+    with B.Batch(probs) as b:
+        full, _ = b.levmar(opts)
+        b.reset()
+        got, batch_ms, hand_ms, todo = B.levmar_with_handoff(b, opts, cap=4, workers=4)
+    assert len(todo) > 0 and batch_ms > 0 and hand_ms > 0
+    assert np.all(got["status"] != P.ITER_CONTINUE)
+    tol = 1e-9 if precision == P.PREC_FP64 else 1e-6
+    rel = np.abs(got["final_cost"] - full["final_cost"]) / full["final_cost"]
+    assert np.all(rel <= tol), rel

@@ -353,6 +353,7 @@ __global__ void __launch_bounds__(256) k_residual(int no, const int *__restrict_
     // the grid's threads, ...: the table is staged once per block instead of
     // once per 256 observations; each thread's squares summed in its order
     double sq = 0.0;
+#pragma unroll 2
     for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < no; o += gridDim.x * blockDim.x) {
         const int i = __ldg(obs_pt + o), j = __ldg(obs_cam + o);
         double X[3];

@@ -1523,8 +1523,12 @@ void launch_schur_reduce(const DeviceProblem &d, double mu, cudaStream_t s)
     k_schur_reduce<<<ceil_div(total, 128), 128, 0, s>>>(d.n_pairs, d.nc, d.Np, d.pair_kl,
                                                           off_start, off_partial,
                                                           d.diag_unit_start, diag_partial, d.U, d.g,
-                                                          mu, d.S, d.rhs); note_launch(1);
-    if (d.Np > d.N) k_pad_identity<<<1, TILE, 0, s>>>(d.N, d.Np, d.S, d.rhs); note_launch(1);
+                                                          mu, d.S, d.rhs);
+    note_launch(1);
+    if (d.Np > d.N) {
+        k_pad_identity<<<1, TILE, 0, s>>>(d.N, d.Np, d.S, d.rhs);
+        note_launch(1);
+    }
 }
 
 void launch_schur(const DeviceProblem &d, double mu, cudaStream_t s)

@@ -464,14 +464,6 @@ __device__ __forceinline__ double half_warp_sum(double p)
     return p;
 }
 
-// x as two FP32 values hi + lo (x to ~2^-48): the mixed form's eb sums take
-// dpa in this form, so that their products need no FP64 instruction
-__device__ __forceinline__ float2 split2f(double x)
-{
-    const float hi = (float)x;
-    return make_float2(hi, (float)(x - (double)hi));
-}
-
 // forward: b <- L^-1 b (right-looking: y_K = Linv_K b_K, then b_I -= L_IK y_K)
 __device__ void cta_forward(int Np, int nb, const double *__restrict__ S, const double *__restrict__ Linv,
                             double *bs, double *tmp)

@@ -27,6 +27,14 @@ __device__ __forceinline__ double rcp_fast(double x)
     const double e = fma(-x, y, 1.0);
     return fma(y, fma(e, e, e), y);
 }
+
+// x as two FP32 values hi + lo (x to ~2^-48): the mixed form's double-float
+// sums take their FP64 operands in this form, split once where they are made
+__device__ __forceinline__ float2 split2f(double x)
+{
+    const float hi = (float)x;
+    return make_float2(hi, (float)(x - (double)hi));
+}
 #endif
 
 constexpr int CNP = 6;   // camera parameters (rotation vector part + translation)
@@ -34,6 +42,7 @@ constexpr int PNP = 3;   // point parameters
 constexpr int MNP = 2;   // image coordinates
 constexpr int CAMTAB = 56;  // doubles per camera table entry (CamTab)
 constexpr int CAMTAB32 = 40;  // floats per FP32 camera table entry: M, D, fx, sk, fy (the mixed Jacobian)
+constexpr int RES_TAB2F = 17;  // FP32 pairs per camera of the mixed trial cost: M, t, fx sk cx fy cy
 constexpr int TILE = 16;    // dense Cholesky tile size
 constexpr int SCHUR_CHUNK = 32;  // pair-list entries per off-diagonal Schur work unit (11/16-parameter cameras)
 constexpr int OFF_MIN_LEN = 8;   // 6-parameter cameras: fewest pair-list entries per off-diagonal chunk
@@ -179,6 +188,9 @@ struct DeviceProblem {
     double *xsol = nullptr;       // Np
     double *rsave = nullptr;      // Np: ea saved before the factor (refinement)
     float2 *dpa2f = nullptr;      // Np: dpa as FP32 pairs hi + lo (the mixed form's eb sums)
+    float2 *meas2f = nullptr;     // 2 per obs: the measurements as FP32 pairs (the mixed trial cost)
+    float2 *x2f = nullptr;        // 3 per point: the trial point pts + dpb as FP32 pairs (the mixed trial cost)
+    float2 *tab2f = nullptr;      // RES_TAB2F per camera: the trial camera table's projection values as FP32 pairs
     double *Linv = nullptr;       // (Np / TILE) * TILE * TILE inverses of the diagonal blocks
     int *status = nullptr;        // Cholesky status word (0 ok, 1 not SPD, 2 wait budget exhausted)
     int *tickets = nullptr;       // 2 words, zero between launches: last-block tickets (eb/dpb, residual)
@@ -204,7 +216,9 @@ struct DeviceProblem {
 
 // Linearization: camera tables, residual, Jacobian, W, V, gb, U, ga.
 void launch_cam_tables(const DeviceProblem &d, const double *cams, const double *dpa,
-                       double *tab, cudaStream_t s, float *tab32 = nullptr);
+                       double *tab, cudaStream_t s, float *tab32 = nullptr, float2 *tab2f = nullptr);
+void launch_residual_df(const DeviceProblem &d, double *partial, int nblocks, double *sum_dst, cudaStream_t s);
+void launch_split2f(const double *x, float2 *out, long long n, cudaStream_t s);
 void launch_linearize(const DeviceProblem &d, double coeff, cudaStream_t s);
 void launch_point_blocks(const DeviceProblem &d, double coeff, cudaStream_t s);
 void launch_camera_blocks(const DeviceProblem &d, double coeff, cudaStream_t s);

@@ -105,7 +105,7 @@ __device__ void sum_partials_block(const double *partial, int n, double *dst)
 __global__ void __launch_bounds__(128) k_cam_tables(int nc, int cnp, const double *__restrict__ K,
                                                     const double *__restrict__ q0, const double *__restrict__ cams,
                                                     const double *__restrict__ dpa, double *__restrict__ tab,
-                                                    float *__restrict__ tab32)
+                                                    float *__restrict__ tab32, float2 *__restrict__ tab2f)
 {
     const int role = threadIdx.x >> 5;
     const int j = blockIdx.x * 32 + (threadIdx.x & 31);
@@ -148,6 +148,18 @@ __global__ void __launch_bounds__(128) k_cam_tables(int nc, int cnp, const doubl
             F[38] = (float)T->fy;
             F[39] = 0.0f;
         }
+        if (tab2f) {  // the projection's values as FP32 pairs: M, t, fx sk cx fy cy
+            float2 *F = tab2f + (size_t)RES_TAB2F * j;
+#pragma unroll
+            for (int e = 0; e < 9; ++e) F[e] = split2f(T->M[e]);
+#pragma unroll
+            for (int e = 0; e < 3; ++e) F[9 + e] = split2f(T->t[e]);
+            F[12] = split2f(T->fx);
+            F[13] = split2f(T->sk);
+            F[14] = split2f(T->cx);
+            F[15] = split2f(T->fy);
+            F[16] = split2f(T->cy);
+        }
         T->ar = kk[3];
         for (int m = 0; m < 5; ++m) T->kc[m] = kc[m];
         for (int m = 0; m < 6; ++m) T->pad[m] = 0.0;
@@ -182,9 +194,9 @@ __global__ void __launch_bounds__(128) k_cam_tables(int nc, int cnp, const doubl
 }
 
 void launch_cam_tables(const DeviceProblem &d, const double *cams, const double *dpa, double *tab,
-                       cudaStream_t s, float *tab32)
+                       cudaStream_t s, float *tab32, float2 *tab2f)
 {
-    k_cam_tables<<<ceil_div(d.nc, 32), 128, 0, s>>>(d.nc, d.cnp, d.K, d.q0, cams, dpa, tab, tab32);
+    k_cam_tables<<<ceil_div(d.nc, 32), 128, 0, s>>>(d.nc, d.cnp, d.K, d.q0, cams, dpa, tab, tab32, tab2f);
     note_launch(1);
 }
 
@@ -399,6 +411,118 @@ __global__ void __launch_bounds__(256) k_residual(int no, const int *__restrict_
         sum_partials_block(partial, gridDim.x, sum_dst);
         if (threadIdx.x == 0) *ticket = 0;
     }
+}
+
+// Double-float arithmetic: a value is an unevaluated sum hi + lo of two
+// FP32 numbers (Dekker, "A floating-point technique for extending the
+// available precision", Numer. Math. 18, 1971; Knuth's TwoSum): products
+// split exactly by an FMA, sums carried with TwoSum, each result renormalised,
+// ~2^-44 relative per operation.
+struct df {
+    float hi, lo;
+};
+__device__ __forceinline__ df df_of(float2 v) { return df{v.x, v.y}; }
+__device__ __forceinline__ df df_renorm(float s, float e)  // |s| >= |e|
+{
+    const float h = __fadd_rn(s, e);
+    return df{h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+__device__ __forceinline__ df df_add(df x, df y)
+{
+    const float s = __fadd_rn(x.hi, y.hi), z = __fsub_rn(s, x.hi);
+    const float e = __fadd_rn(__fsub_rn(x.hi, __fsub_rn(s, z)), __fsub_rn(y.hi, z));
+    return df_renorm(s, e + (x.lo + y.lo));
+}
+__device__ __forceinline__ df df_neg(df x) { return df{-x.hi, -x.lo}; }
+__device__ __forceinline__ df df_mul(df x, df y)
+{
+    const float p = __fmul_rn(x.hi, y.hi);
+    const float e = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, fmaf(x.hi, y.hi, -p)));
+    return df_renorm(p, e);
+}
+// 1 / x: the FP32 reciprocal, then one Newton step r + r (1 - x r) in
+// double-float (doubling its ~24 correct bits)
+__device__ __forceinline__ df df_rcp(df x)
+{
+    const float r = __frcp_rn(x.hi);
+    const df xr = df_mul(x, df{r, 0.0f});
+    const df e = df_add(df{1.0f, 0.0f}, df_neg(xr));
+    return df_add(df{r, 0.0f}, df_mul(df{r, 0.0f}, e));
+}
+
+// The mixed form's trial cost (unweighted, 6-parameter cameras): the same
+// projection and sum of squares as k_residual, in double-float FP32
+// arithmetic from the trial camera table and trial points split once into
+// FP32 pairs (k_cam_tables, k_eb_dpb) and the measurements split once per
+// handle.  The residual e = m - pi(X) of ~1 px is a difference of ~1e3 px
+// values; its double-float error is ~1e3 * 2^-44 px, far below what the gain
+// ratio resolves, and no FP64 instruction is issued per observation (each
+// thread converts its sum once).
+__global__ void __launch_bounds__(256) k_residual_df(int no, int nc, const int *__restrict__ obs_pt,
+                                                     const int *__restrict__ obs_cam,
+                                                     const float2 *__restrict__ meas2f,
+                                                     const float2 *__restrict__ x2f,
+                                                     const float2 *__restrict__ tab2f, double *__restrict__ partial,
+                                                     double *__restrict__ sum_dst, int *__restrict__ ticket)
+{
+    __shared__ double red[256 / 32];
+    extern __shared__ float2 s_tab2[];  // nc * RES_TAB2F
+    for (int e = threadIdx.x; e < nc * RES_TAB2F; e += blockDim.x) s_tab2[e] = tab2f[e];
+    __syncthreads();
+    df sq{0.0f, 0.0f};
+    for (int o = blockIdx.x * blockDim.x + threadIdx.x; o < no; o += gridDim.x * blockDim.x) {
+        const int i = __ldg(obs_pt + o), j = __ldg(obs_cam + o);
+        const float2 *T = s_tab2 + RES_TAB2F * j;
+        const df X0 = df_of(__ldg(x2f + 3 * (size_t)i)), X1 = df_of(__ldg(x2f + 3 * (size_t)i + 1)),
+                 X2 = df_of(__ldg(x2f + 3 * (size_t)i + 2));
+        const df xc = df_add(df_add(df_mul(df_of(T[0]), X0), df_mul(df_of(T[1]), X1)),
+                             df_add(df_mul(df_of(T[2]), X2), df_of(T[9])));
+        const df yc = df_add(df_add(df_mul(df_of(T[3]), X0), df_mul(df_of(T[4]), X1)),
+                             df_add(df_mul(df_of(T[5]), X2), df_of(T[10])));
+        const df zc = df_add(df_add(df_mul(df_of(T[6]), X0), df_mul(df_of(T[7]), X1)),
+                             df_add(df_mul(df_of(T[8]), X2), df_of(T[11])));
+        const df iz = df_rcp(zc);
+        const df un = df_add(df_add(df_mul(df_of(T[12]), xc), df_mul(df_of(T[13]), yc)), df_mul(df_of(T[14]), zc));
+        const df vn = df_add(df_mul(df_of(T[15]), yc), df_mul(df_of(T[16]), zc));
+        const df e0 = df_add(df_of(__ldg(meas2f + 2 * (size_t)o)), df_neg(df_mul(un, iz)));
+        const df e1 = df_add(df_of(__ldg(meas2f + 2 * (size_t)o + 1)), df_neg(df_mul(vn, iz)));
+        sq = df_add(sq, df_add(df_mul(e0, e0), df_mul(e1, e1)));
+    }
+    double x = (double)sq.hi + (double)sq.lo;
+    // fixed-order block sum: xor tree in each warp, then the warps in order
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = x;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = red[0];
+        for (int w = 1; w < 256 / 32; ++w) a += red[w];
+        partial[blockIdx.x] = a;
+    }
+    if (take_last_ticket(ticket)) {
+        sum_partials_block(partial, gridDim.x, sum_dst);
+        if (threadIdx.x == 0) *ticket = 0;
+    }
+}
+
+void launch_residual_df(const DeviceProblem &d, double *partial, int nblocks, double *sum_dst, cudaStream_t s)
+{
+    k_residual_df<<<nblocks, 256, sizeof(float2) * RES_TAB2F * d.nc, s>>>(
+        d.no, d.nc, d.obs_pt, d.obs_cam, d.meas2f, d.x2f, d.tab2f, partial, sum_dst, d.tickets + 1);
+    note_launch(1);
+}
+
+__global__ void k_split2f(const double *__restrict__ x, float2 *__restrict__ out, long long n)
+{
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = split2f(x[i]);
+}
+
+void launch_split2f(const double *x, float2 *out, long long n, cudaStream_t s)
+{
+    if (n <= 0) return;
+    k_split2f<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, out, n);
+    note_launch(1);
 }
 
 // cameras whose residual-table values a block stages (0: read the table)
@@ -1591,7 +1715,8 @@ __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int2 *__r
                                                 double *__restrict__ dp, double *__restrict__ eb,
                                                 double *__restrict__ partial, int stage,
                                                 const int *__restrict__ status, int *__restrict__ ticket,
-                                                TrialScalars *__restrict__ out, const float2 *__restrict__ dpa2f)
+                                                TrialScalars *__restrict__ out, const float2 *__restrict__ dpa2f,
+                                                const double *__restrict__ pts, float2 *__restrict__ x2f)
 {
     static_assert(EB_WARPS == 8, "eight warps a block");
     __shared__ double s_sum[EB_PPB][3];
@@ -1697,6 +1822,12 @@ __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int2 *__r
         db[0] = d0;
         db[1] = d1;
         db[2] = d2;
+        if (x2f) {  // the mixed trial cost's point, pts + dpb as FP32 pairs
+            const double *X = pts + 3 * (size_t)i;
+            x2f[3 * (size_t)i] = split2f(X[0] + d0);
+            x2f[3 * (size_t)i + 1] = split2f(X[1] + d1);
+            x2f[3 * (size_t)i + 2] = split2f(X[2] + d2);
+        }
         s_sq = d0 * d0 + d1 * d1 + d2 * d2;
         s_rho = d0 * (mu * d0 + gb[0]) + d1 * (mu * d1 + gb[1]) + d2 * (mu * d2 + gb[2]);
     }
@@ -1747,12 +1878,12 @@ void launch_eb_dpb(const DeviceProblem &d, double mu, cudaStream_t s)
     if (d.prec == PSBA_PREC_FP64)
         k_eb_dpb<double><<<eb_blocks(d), 256, smem, s>>>(d.np, d.N, d.eb_warps, d.pt_start, d.pt_order, d.obs_cam,
                                                            d.W, d.Vinv, d.g, mu, d.dp, d.eb, d.red_partial, stage,
-                                                           d.status, d.tickets, d.scal, nullptr);
+                                                           d.status, d.tickets, d.scal, nullptr, nullptr, nullptr);
     else
         k_eb_dpb<float><<<eb_blocks(d), 256, smem, s>>>(d.np, d.N, d.eb_warps, d.pt_start, d.pt_order, d.obs_cam,
                                                           (const float *)d.W, d.Vinv, d.g, mu, d.dp, d.eb,
                                                           d.red_partial, stage, d.status, d.tickets, d.scal,
-                                                          d.dpa2f);
+                                                          d.dpa2f, d.pts, d.wt ? nullptr : d.x2f);
     note_launch(1);
 }
 

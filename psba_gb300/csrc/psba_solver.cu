@@ -280,15 +280,26 @@ void enqueue_cost_current(psba_handle *h, double *ex_out)
 }
 
 // Cost at p + step (into scal->new_cost).
+#ifndef PSBA_MIXED_DF_COST
+#define PSBA_MIXED_DF_COST 1  // the mixed form's LM trial cost in double-float FP32 arithmetic (else FP64)
+#endif
+
 void enqueue_cost_trial(psba_handle *h, const double *step)
 {
     DeviceProblem &d = h->d;
     StageScope sc(h, ST_COST);
-    launch_cam_tables(d, d.cams, step, d.camtab_new, h->stream);
     const int nb = residual_blocks(d);
     // partials after the eb partials region so they do not collide
     double *part = d.red_partial + 2 * eb_blocks(d) + 8;
-    launch_residual(d, d.camtab_new, d.pts, step + d.N, nullptr, part, nb, &d.scal->new_cost, h->stream);
+    // the mixed form's LM trial (its step d.dp, whose trial points k_eb_dpb
+    // has just split into FP32 pairs): the double-float cost
+    const bool df = PSBA_MIXED_DF_COST && d.prec == PSBA_PREC_MIXED && d.cnp == 6 && !d.wt && step == d.dp &&
+                    (size_t)d.nc * RES_TAB2F * sizeof(float2) <= 48 * 1024;
+    launch_cam_tables(d, d.cams, step, d.camtab_new, h->stream, nullptr, df ? d.tab2f : nullptr);
+    if (df)
+        launch_residual_df(d, part, nb, &d.scal->new_cost, h->stream);
+    else
+        launch_residual(d, d.camtab_new, d.pts, step + d.N, nullptr, part, nb, &d.scal->new_cost, h->stream);
 }
 
 // Jacobian, U, V, W, g with factor coeff at the current parameters.
@@ -1021,6 +1032,7 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     TRY(dalloc(h, &d.K, 5 * (size_t)nc));
     TRY(dalloc(h, &d.q0, 4 * (size_t)nc));
     TRY(dalloc(h, &d.meas, 2 * (size_t)no));
+    TRY(dalloc(h, &d.meas2f, 2 * (size_t)no));
     TRY(dalloc(h, &d.off_units, off_units.size()));
     TRY(dalloc(h, &d.off_unit_start, (size_t)n_pairs + 1));
     if (d.cnp == 6) {
@@ -1064,6 +1076,8 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     TRY(dalloc(h, &d.rhs, (size_t)d.Np));
     TRY(dalloc(h, &d.rsave, (size_t)d.Np));
     TRY(dalloc(h, &d.dpa2f, (size_t)d.Np));
+    TRY(dalloc(h, &d.x2f, 3 * (size_t)np));
+    TRY(dalloc(h, &d.tab2f, (size_t)RES_TAB2F * nc));
     TRY(dalloc(h, &d.xsol, (size_t)d.Np));
     TRY(dalloc(h, &d.Linv, (size_t)d.Np * TILE));
     TRY(dalloc(h, &d.status, 4));
@@ -1109,6 +1123,7 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     if (d.cnp == 6) TRY(upload(h, d.K, p->K, 5 * (size_t)nc));
     TRY(upload(h, d.q0, p->q0, 4 * (size_t)nc));
     TRY(upload(h, d.meas, p->meas, 2 * (size_t)no));
+    launch_split2f(d.meas, d.meas2f, 2LL * no, h->stream);  // the mixed trial cost's measurements
     if (p->cov && no) {
         // whitening L (upper, L^T L = cov^-1) per observation
         std::vector<double> w(3 * (size_t)no);

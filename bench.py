@@ -75,6 +75,7 @@ UNIT = "iterations/s"
 # one ncu capture of this workload's kernels.
 SCHUR_TRAFFIC = 250.1e6
 CHOL_TRAFFIC = 1.30e6  # S (2.2 MB) stays in L2 between the Schur stage and the factor
+SCHUR_F32_TRAFFIC = 83.1e6  # k_schur_f32, mixed form: 79.8 MB read + 3.3 MB written
 MATCH_TOL = 1e-6  # matched final cost: within 1e-6 relative of the FP64 converged cost
 
 
@@ -861,7 +862,9 @@ def main():
         roofline_mixed = {
             "kernel": "k_schur_f32: the mixed form's Schur products (FP32 products, FP64 sums), off-diagonal "
                       "and diagonal units in one launch per LM trial",
-            "bound": "latency", "avg_ms": f32_s * 1e3, "algorithmic_flops": soff_flops,
+            "bound": "l1", "avg_ms": f32_s * 1e3, "algorithmic_flops": soff_flops,
+            "bound_note": "the L1 / shared-memory pipe (ncu: 87% of peak), not the FP32 pipe or HBM",
+            "traffic": SCHUR_F32_TRAFFIC, "traffic_kernel": "k_schur_f32",
             "fp32": {"achieved": soff_flops / f32_s / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": soff_flops / f32_s / 1e12 / fp32_peak,
                      "peak_source": "measured FP32 FMA rate (psba_measure_peak)"},

@@ -42,7 +42,7 @@ constexpr int PNP = 3;   // point parameters
 constexpr int MNP = 2;   // image coordinates
 constexpr int CAMTAB = 56;  // doubles per camera table entry (CamTab)
 constexpr int CAMTAB32 = 40;  // floats per FP32 camera table entry: M, D, fx, sk, fy (the mixed Jacobian)
-constexpr int RES_TAB2F = 17;  // FP32 pairs per camera of the mixed trial cost: M, t, fx sk cx fy cy
+constexpr int RES_TAB2F = 18;  // FP32 pairs per camera of the mixed projection: M, t, fx sk cx fy cy, a pad (16-byte rows)
 constexpr int TILE = 16;    // dense Cholesky tile size
 constexpr int SCHUR_CHUNK = 32;  // pair-list entries per off-diagonal Schur work unit (11/16-parameter cameras)
 constexpr int OFF_MIN_LEN = 8;   // 6-parameter cameras: fewest pair-list entries per off-diagonal chunk
@@ -220,6 +220,9 @@ void launch_cam_tables(const DeviceProblem &d, const double *cams, const double 
 void launch_residual_df(const DeviceProblem &d, double *partial, int nblocks, double *sum_dst, cudaStream_t s);
 void launch_split2f(const double *x, float2 *out, long long n, cudaStream_t s);
 void launch_linearize(const DeviceProblem &d, double coeff, cudaStream_t s);
+// the mixed form's linearization projects in double-float FP32 arithmetic
+// (6-parameter cameras, unweighted): its camera table split by k_cam_tables
+inline bool linearize_df(const DeviceProblem &d) { return d.prec == PSBA_PREC_MIXED && d.cnp == 6 && !d.wt; }
 void launch_point_blocks(const DeviceProblem &d, double coeff, cudaStream_t s);
 void launch_camera_blocks(const DeviceProblem &d, double coeff, cudaStream_t s);
 // Residual only (ex, when ex_out is set) at the parameters given by tab,

@@ -159,6 +159,7 @@ __global__ void __launch_bounds__(128) k_cam_tables(int nc, int cnp, const doubl
             F[14] = split2f(T->cx);
             F[15] = split2f(T->fy);
             F[16] = split2f(T->cy);
+            F[17] = make_float2(0.0f, 0.0f);
         }
         T->ar = kk[3];
         for (int m = 0; m < 5; ++m) T->kc[m] = kc[m];
@@ -200,6 +201,43 @@ void launch_cam_tables(const DeviceProblem &d, const double *cams, const double 
     note_launch(1);
 }
 
+// Double-float arithmetic: a value is an unevaluated sum hi + lo of two
+// FP32 numbers (Dekker, "A floating-point technique for extending the
+// available precision", Numer. Math. 18, 1971; Knuth's TwoSum): products
+// split exactly by an FMA, sums carried with TwoSum, each result renormalised,
+// ~2^-44 relative per operation.
+struct df {
+    float hi, lo;
+};
+__device__ __forceinline__ df df_of(float2 v) { return df{v.x, v.y}; }
+__device__ __forceinline__ df df_renorm(float s, float e)  // |s| >= |e|
+{
+    const float h = __fadd_rn(s, e);
+    return df{h, __fsub_rn(e, __fsub_rn(h, s))};
+}
+__device__ __forceinline__ df df_add(df x, df y)
+{
+    const float s = __fadd_rn(x.hi, y.hi), z = __fsub_rn(s, x.hi);
+    const float e = __fadd_rn(__fsub_rn(x.hi, __fsub_rn(s, z)), __fsub_rn(y.hi, z));
+    return df_renorm(s, e + (x.lo + y.lo));
+}
+__device__ __forceinline__ df df_neg(df x) { return df{-x.hi, -x.lo}; }
+__device__ __forceinline__ df df_mul(df x, df y)
+{
+    const float p = __fmul_rn(x.hi, y.hi);
+    const float e = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, fmaf(x.hi, y.hi, -p)));
+    return df_renorm(p, e);
+}
+// 1 / x: the FP32 reciprocal, then one Newton step r + r (1 - x r) in
+// double-float (doubling its ~24 correct bits)
+__device__ __forceinline__ df df_rcp(df x)
+{
+    const float r = __frcp_rn(x.hi);
+    const df xr = df_mul(x, df{r, 0.0f});
+    const df e = df_add(df{1.0f, 0.0f}, df_neg(xr));
+    return df_add(df{r, 0.0f}, df_mul(df{r, 0.0f}, e));
+}
+
 // ---------------------------------------------------------------------------
 // Linearization, one thread per observation: residual (compute_exQT.cl),
 // Jacobian blocks A = d(x,y)/d(v,t), B = d(x,y)/dX (compute_jacobiQT.cl) by
@@ -214,50 +252,106 @@ __global__ void __launch_bounds__(256) k_linearize(int no, const int *__restrict
                                                    const double *__restrict__ wt,
                                                    R *__restrict__ ex, R *__restrict__ A,
                                                    R *__restrict__ B, R *__restrict__ W,
-                                                   const float *__restrict__ tab32)
+                                                   const float *__restrict__ tab32,
+                                                   const float2 *__restrict__ meas2f,
+                                                   const float2 *__restrict__ tab2f)
 {
     int o = blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= no) return;
     const int i = __ldg(obs_pt + o), j = __ldg(obs_cam + o);
     const double *T = tab + (size_t)CAMTAB * j;
-    // The projection and the residual are FP64 in both forms: e = m - pi(X) is
-    // a small difference of ~1e3 px quantities, and its error moves the
-    // gradient and with it the LM fixed point.  Only the stored e, J and W are
-    // rounded to R.
-    const double Xd0 = __ldg(pts + 3 * i), Xd1 = __ldg(pts + 3 * i + 1), Xd2 = __ldg(pts + 3 * i + 2);
-    double Md[9];
+    // e = m - pi(X) is a small difference of ~1e3 px quantities, and its error
+    // moves the gradient and with it the LM fixed point, so the projection is
+    // FP64 (the FP64 form, and the mixed form with covariance weights) or
+    // double-float FP32 (the mixed form, unweighted: the point split here,
+    // the measurements and camera table split into FP32 pairs once, ~2^-44
+    // relative).  Only the stored e, J and W are rounded to R.  The mixed
+    // form's table rows come in as 16-byte loads (the kernel is bound by the
+    // issue of its global loads and stores, not by arithmetic).
+    R X0, X1, X2, yc, iz, nu;
+    double e0 = 0.0, e1 = 0.0, wa = 1.0, wb = 0.0, wc = 1.0;
+    float e0f = 0.0f, e1f = 0.0f;
+    const bool dfp = !is_fp64<R>() && tab2f != nullptr;
+    if (dfp) {
+        float2 Tf[RES_TAB2F];
+        const float4 *T4 = reinterpret_cast<const float4 *>(tab2f + (size_t)RES_TAB2F * j);
 #pragma unroll
-    for (int e = 0; e < 9; ++e) Md[e] = __ldg(T + e);
-    const double xcd = Md[0] * Xd0 + Md[1] * Xd1 + Md[2] * Xd2 + __ldg(T + 36);
-    const double ycd = Md[3] * Xd0 + Md[4] * Xd1 + Md[5] * Xd2 + __ldg(T + 37);
-    const double zcd = Md[6] * Xd0 + Md[7] * Xd1 + Md[8] * Xd2 + __ldg(T + 38);
-    const double fxd = __ldg(T + 39), skd = __ldg(T + 40), cxd = __ldg(T + 41), fyd = __ldg(T + 42),
-                 cyd = __ldg(T + 43);
-    const double izd = rcp_fast(zcd);
-    const double2 m2 = __ldg(reinterpret_cast<const double2 *>(meas + 2 * (size_t)o));
-    const double nud = fxd * xcd + skd * ycd;
-    const double u = (nud + cxd * zcd) * izd;
-    const double v = (fyd * ycd + cyd * zcd) * izd;
-    double e0 = m2.x - u, e1 = m2.y - v, wa = 1.0, wb = 0.0, wc = 1.0;
-    if (wt) {  // whitening: e <- L e, J rows <- L J
-        wa = __ldg(wt + 3 * (size_t)o);
-        wb = __ldg(wt + 3 * (size_t)o + 1);
-        wc = __ldg(wt + 3 * (size_t)o + 2);
-        const double t0 = wa * e0 + wb * e1;
-        e1 = wc * e1;
-        e0 = t0;
+        for (int k = 0; k < RES_TAB2F / 2; ++k) {
+            const float4 q = __ldg(T4 + k);
+            Tf[2 * k] = make_float2(q.x, q.y);
+            Tf[2 * k + 1] = make_float2(q.z, q.w);
+        }
+        const df Xa = df_of(split2f(__ldg(pts + 3 * i))), Xb = df_of(split2f(__ldg(pts + 3 * i + 1))),
+                 Xc = df_of(split2f(__ldg(pts + 3 * i + 2)));
+        const df xc = df_add(df_add(df_mul(df_of(Tf[0]), Xa), df_mul(df_of(Tf[1]), Xb)),
+                             df_add(df_mul(df_of(Tf[2]), Xc), df_of(Tf[9])));
+        const df ycv = df_add(df_add(df_mul(df_of(Tf[3]), Xa), df_mul(df_of(Tf[4]), Xb)),
+                              df_add(df_mul(df_of(Tf[5]), Xc), df_of(Tf[10])));
+        const df zc = df_add(df_add(df_mul(df_of(Tf[6]), Xa), df_mul(df_of(Tf[7]), Xb)),
+                             df_add(df_mul(df_of(Tf[8]), Xc), df_of(Tf[11])));
+        const df izv = df_rcp(zc);
+        const df nuv = df_add(df_mul(df_of(Tf[12]), xc), df_mul(df_of(Tf[13]), ycv));
+        const df un = df_add(nuv, df_mul(df_of(Tf[14]), zc));
+        const df vn = df_add(df_mul(df_of(Tf[15]), ycv), df_mul(df_of(Tf[16]), zc));
+        const float4 m4 = __ldg(reinterpret_cast<const float4 *>(meas2f) + o);
+        const df ea = df_add(df{m4.x, m4.y}, df_neg(df_mul(un, izv)));
+        const df eb = df_add(df{m4.z, m4.w}, df_neg(df_mul(vn, izv)));
+        e0f = __fadd_rn(ea.hi, ea.lo);
+        e1f = __fadd_rn(eb.hi, eb.lo);
+        X0 = (R)Xa.hi; X1 = (R)Xb.hi; X2 = (R)Xc.hi;
+        yc = (R)__fadd_rn(ycv.hi, ycv.lo);
+        iz = (R)__fadd_rn(izv.hi, izv.lo);
+        nu = (R)__fadd_rn(nuv.hi, nuv.lo);
+        st2<R>(ex + 2 * (size_t)o, (R)e0f, (R)e1f);
+    } else {
+        const double Xd0 = __ldg(pts + 3 * i), Xd1 = __ldg(pts + 3 * i + 1), Xd2 = __ldg(pts + 3 * i + 2);
+        double Md[9];
+#pragma unroll
+        for (int e = 0; e < 9; ++e) Md[e] = __ldg(T + e);
+        const double xcd = Md[0] * Xd0 + Md[1] * Xd1 + Md[2] * Xd2 + __ldg(T + 36);
+        const double ycd = Md[3] * Xd0 + Md[4] * Xd1 + Md[5] * Xd2 + __ldg(T + 37);
+        const double zcd = Md[6] * Xd0 + Md[7] * Xd1 + Md[8] * Xd2 + __ldg(T + 38);
+        const double fxd = __ldg(T + 39), skd = __ldg(T + 40), cxd = __ldg(T + 41), fyd = __ldg(T + 42),
+                     cyd = __ldg(T + 43);
+        const double izd = rcp_fast(zcd);
+        const double2 m2 = __ldg(reinterpret_cast<const double2 *>(meas + 2 * (size_t)o));
+        const double nud = fxd * xcd + skd * ycd;
+        const double u = (nud + cxd * zcd) * izd;
+        const double v = (fyd * ycd + cyd * zcd) * izd;
+        e0 = m2.x - u;
+        e1 = m2.y - v;
+        if (wt) {  // whitening: e <- L e, J rows <- L J
+            wa = __ldg(wt + 3 * (size_t)o);
+            wb = __ldg(wt + 3 * (size_t)o + 1);
+            wc = __ldg(wt + 3 * (size_t)o + 2);
+            const double t0 = wa * e0 + wb * e1;
+            e1 = wc * e1;
+            e0 = t0;
+        }
+        st2<R>(ex + 2 * (size_t)o, (R)e0, (R)e1);
+        X0 = (R)Xd0; X1 = (R)Xd1; X2 = (R)Xd2;
+        yc = (R)ycd; iz = (R)izd; nu = (R)nud;
     }
-    st2<R>(ex + 2 * (size_t)o, (R)e0, (R)e1);
-    const R X0 = (R)Xd0, X1 = (R)Xd1, X2 = (R)Xd2;
     // the mixed form takes the table's FP32 copy (the same values, rounded
-    // once per camera instead of once per observation on the FP64 pipe)
-    const float *F = is_fp64<R>() ? nullptr : tab32 + (size_t)CAMTAB32 * j;
+    // once per camera instead of once per observation on the FP64 pipe),
+    // its 160-byte row in ten 16-byte loads
+    float F[CAMTAB32];
+    if constexpr (!is_fp64<R>()) {
+        const float4 *F4 = reinterpret_cast<const float4 *>(tab32 + (size_t)CAMTAB32 * j);
+#pragma unroll
+        for (int k = 0; k < CAMTAB32 / 4; ++k) {
+            const float4 q = __ldg(F4 + k);
+            F[4 * k] = q.x;
+            F[4 * k + 1] = q.y;
+            F[4 * k + 2] = q.z;
+            F[4 * k + 3] = q.w;
+        }
+    }
     R M[9];
 #pragma unroll
-    for (int e = 0; e < 9; ++e) M[e] = is_fp64<R>() ? (R)Md[e] : (R)__ldg(F + e);
-    const R yc = (R)ycd, iz = (R)izd, nu = (R)nud;
-    const R fx = is_fp64<R>() ? (R)fxd : (R)__ldg(F + 36), sk = is_fp64<R>() ? (R)skd : (R)__ldg(F + 37),
-            fy = is_fp64<R>() ? (R)fyd : (R)__ldg(F + 38);
+    for (int e = 0; e < 9; ++e) M[e] = is_fp64<R>() ? (R)__ldg(T + e) : (R)F[e];
+    const R fx = is_fp64<R>() ? (R)__ldg(T + 39) : (R)F[36], sk = is_fp64<R>() ? (R)__ldg(T + 40) : (R)F[37],
+            fy = is_fp64<R>() ? (R)__ldg(T + 42) : (R)F[38];
     // d(x,y)/dXc
     const R p00 = fx * iz, p01 = sk * iz, p02 = -nu * iz * iz;
     const R p11 = fy * iz, p12 = -fy * yc * iz * iz;
@@ -271,7 +365,7 @@ __global__ void __launch_bounds__(256) k_linearize(int no, const int *__restrict
             for (int e = 0; e < 9; ++e) Dm[e] = __ldg(T + 9 + 9 * m + e);
         } else {
 #pragma unroll
-            for (int e = 0; e < 9; ++e) Dm[e] = __ldg(F + 9 + 9 * m + e);
+            for (int e = 0; e < 9; ++e) Dm[e] = F[9 + 9 * m + e];
         }
         const R g0 = Dm[0] * X0 + Dm[1] * X1 + Dm[2] * X2;
         const R g1 = Dm[3] * X0 + Dm[4] * X1 + Dm[5] * X2;
@@ -302,7 +396,13 @@ __global__ void __launch_bounds__(256) k_linearize(int no, const int *__restrict
             bb[3 + m] = rc * b1;
         }
     }
-    stn<R, 12>(A + 12 * (size_t)o, a);
+    if constexpr (is_fp64<R>()) {
+        stn<R, 12>(A + 12 * (size_t)o, a);
+    } else {  // a 48-byte row: three 16-byte stores
+        float4 *A4 = reinterpret_cast<float4 *>(A + 12 * (size_t)o);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) A4[k] = make_float4(a[4 * k], a[4 * k + 1], a[4 * k + 2], a[4 * k + 3]);
+    }
     stn<R, 6>(B + 6 * (size_t)o, bb);
     // W with coeff folded into a copy of B: the solver's coeff is 1 or 2, a
     // power of two, so coeff (a b + a' b') and a (coeff b) + a' (coeff b') are
@@ -326,11 +426,14 @@ void launch_linearize(const DeviceProblem &d, double coeff, cudaStream_t s)
     if (d.prec == PSBA_PREC_FP64) {
         k_linearize<double><<<ceil_div(d.no, 256), 256, 0, s>>>(d.no, d.obs_pt, d.obs_cam, d.meas, d.pts,
                                                                   d.camtab, coeff, d.wt, d.ex, d.A, d.B, d.W,
-                                                                  nullptr);
+                                                                  nullptr, nullptr, nullptr);
     } else {
+        // unweighted: the double-float projection from the table's split
+        // (k_cam_tables of this linearization)
+        const bool dfp = linearize_df(d);
         k_linearize<float><<<ceil_div(d.no, 256), 256, 0, s>>>(
             d.no, d.obs_pt, d.obs_cam, d.meas, d.pts, d.camtab, (float)coeff, d.wt, (float *)d.ex, (float *)d.A,
-            (float *)d.B, (float *)d.W, d.camtab32);
+            (float *)d.B, (float *)d.W, d.camtab32, dfp ? d.meas2f : nullptr, dfp ? d.tab2f : nullptr);
     }
     note_launch(1);
 }
@@ -411,43 +514,6 @@ __global__ void __launch_bounds__(256) k_residual(int no, const int *__restrict_
         sum_partials_block(partial, gridDim.x, sum_dst);
         if (threadIdx.x == 0) *ticket = 0;
     }
-}
-
-// Double-float arithmetic: a value is an unevaluated sum hi + lo of two
-// FP32 numbers (Dekker, "A floating-point technique for extending the
-// available precision", Numer. Math. 18, 1971; Knuth's TwoSum): products
-// split exactly by an FMA, sums carried with TwoSum, each result renormalised,
-// ~2^-44 relative per operation.
-struct df {
-    float hi, lo;
-};
-__device__ __forceinline__ df df_of(float2 v) { return df{v.x, v.y}; }
-__device__ __forceinline__ df df_renorm(float s, float e)  // |s| >= |e|
-{
-    const float h = __fadd_rn(s, e);
-    return df{h, __fsub_rn(e, __fsub_rn(h, s))};
-}
-__device__ __forceinline__ df df_add(df x, df y)
-{
-    const float s = __fadd_rn(x.hi, y.hi), z = __fsub_rn(s, x.hi);
-    const float e = __fadd_rn(__fsub_rn(x.hi, __fsub_rn(s, z)), __fsub_rn(y.hi, z));
-    return df_renorm(s, e + (x.lo + y.lo));
-}
-__device__ __forceinline__ df df_neg(df x) { return df{-x.hi, -x.lo}; }
-__device__ __forceinline__ df df_mul(df x, df y)
-{
-    const float p = __fmul_rn(x.hi, y.hi);
-    const float e = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, fmaf(x.hi, y.hi, -p)));
-    return df_renorm(p, e);
-}
-// 1 / x: the FP32 reciprocal, then one Newton step r + r (1 - x r) in
-// double-float (doubling its ~24 correct bits)
-__device__ __forceinline__ df df_rcp(df x)
-{
-    const float r = __frcp_rn(x.hi);
-    const df xr = df_mul(x, df{r, 0.0f});
-    const df e = df_add(df{1.0f, 0.0f}, df_neg(xr));
-    return df_add(df{r, 0.0f}, df_mul(df{r, 0.0f}, e));
 }
 
 // The mixed form's trial cost (unweighted, 6-parameter cameras): the same
@@ -656,32 +722,78 @@ __global__ void __launch_bounds__(256) k_point_blocks(int np, int ncp, const int
                 }
             }
         }
+        // the L lanes' sums meet in double-float too, in order of r (lane 0
+        // of the point collects), and the nine totals are converted to FP64
+        // by the point's L lanes, a few each: FP64 work per warp ~3 x 4
+        // instructions instead of ~9 L
+        // (each lane's own sums are what is exchanged, not running sums)
+        float sh[9], sl[9];
 #pragma unroll
-        for (int v = 0; v < 9; ++v) a[v] = (double)h[v] + (double)l[v];
+        for (int v = 0; v < 9; ++v) {
+            sh[v] = h[v];
+            sl[v] = l[v];
+        }
+        for (int q = 1; q < L; ++q) {
+            const int src = min(L * pw + q, 31);
+#pragma unroll
+            for (int v = 0; v < 9; ++v) {
+                const float oh = __shfl_sync(0xffffffffu, h[v], src);
+                const float ol = __shfl_sync(0xffffffffu, l[v], src);
+                float t;
+                two_sum_f(sh[v], oh, sh[v], t);
+                sl[v] += ol + t;
+            }
+        }
+        const int head = min(L * pw, 31);
+#pragma unroll
+        for (int v = 0; v < 9; ++v) {
+            h[v] = __shfl_sync(0xffffffffu, sh[v], head);
+            l[v] = __shfl_sync(0xffffffffu, sl[v], head);
+        }
+        if (!live) return;
+        const double cf = (double)coeff;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {  // L >= 3: value r + j L
+            const int v = r + j * L;
+            if (v >= 9) break;
+            float hv = h[0], lv = l[0];
+#pragma unroll
+            for (int u = 1; u < 9; ++u)
+                if (u == v) {
+                    hv = h[u];
+                    lv = l[u];
+                }
+            const double x = cf * ((double)hv + (double)lv);
+            if (v < 6) {
+                V[6 * (size_t)i + v] = x;
+                if (v == 0 || v == 3 || v == 5) uvdiag[ncp + 3 * (size_t)i + (v == 0 ? 0 : v == 3 ? 1 : 2)] = x;
+            } else {
+                g[ncp + 3 * (size_t)i + (v - 6)] = x;
+                if (gb32) gb32[3 * (size_t)i + (v - 6)] = (float)x;  // the mixed form's ea sums take gb in FP32
+            }
+        }
+        return;
     }
-    double s[9];
+    if constexpr (is_fp64<R>()) {
+        double s[9];
 #pragma unroll
-    for (int v = 0; v < 9; ++v) s[v] = a[v];
-    for (int q = 1; q < L; ++q) {  // L is the same for the whole warp
-        const int src = min(L * pw + q, 31);
+        for (int v = 0; v < 9; ++v) s[v] = a[v];
+        for (int q = 1; q < L; ++q) {  // L is the same for the whole warp
+            const int src = min(L * pw + q, 31);
 #pragma unroll
-        for (int v = 0; v < 9; ++v) s[v] += __shfl_sync(0xffffffffu, a[v], src);
-    }
-    if (!live || r != 0) return;
-    const double cf = (double)coeff;
-    double *Vi = V + 6 * (size_t)i;
-    Vi[0] = cf * s[0]; Vi[1] = cf * s[1]; Vi[2] = cf * s[2];
-    Vi[3] = cf * s[3]; Vi[4] = cf * s[4]; Vi[5] = cf * s[5];
-    uvdiag[ncp + 3 * (size_t)i] = Vi[0];
-    uvdiag[ncp + 3 * (size_t)i + 1] = Vi[3];
-    uvdiag[ncp + 3 * (size_t)i + 2] = Vi[5];
-    g[ncp + 3 * (size_t)i] = cf * s[6];
-    g[ncp + 3 * (size_t)i + 1] = cf * s[7];
-    g[ncp + 3 * (size_t)i + 2] = cf * s[8];
-    if (gb32) {  // the mixed form's ea sums take gb in FP32
-        gb32[3 * (size_t)i] = (float)(cf * s[6]);
-        gb32[3 * (size_t)i + 1] = (float)(cf * s[7]);
-        gb32[3 * (size_t)i + 2] = (float)(cf * s[8]);
+            for (int v = 0; v < 9; ++v) s[v] += __shfl_sync(0xffffffffu, a[v], src);
+        }
+        if (!live || r != 0) return;
+        const double cf = (double)coeff;
+        double *Vi = V + 6 * (size_t)i;
+        Vi[0] = cf * s[0]; Vi[1] = cf * s[1]; Vi[2] = cf * s[2];
+        Vi[3] = cf * s[3]; Vi[4] = cf * s[4]; Vi[5] = cf * s[5];
+        uvdiag[ncp + 3 * (size_t)i] = Vi[0];
+        uvdiag[ncp + 3 * (size_t)i + 1] = Vi[3];
+        uvdiag[ncp + 3 * (size_t)i + 2] = Vi[5];
+        g[ncp + 3 * (size_t)i] = cf * s[6];
+        g[ncp + 3 * (size_t)i + 1] = cf * s[7];
+        g[ncp + 3 * (size_t)i + 2] = cf * s[8];
     }
 }
 
@@ -713,7 +825,7 @@ static_assert(CAM_SUPER == CAM_THREADS * CAM_PER, "camera unit size");
 // the CTA then sums its threads' partials in a fixed order, each output by
 // four threads over 32 partials, then the four.
 template <typename R>
-__global__ void __launch_bounds__(CAM_THREADS) k_camera_partial(const CamUnit *__restrict__ units,
+__global__ void __launch_bounds__(CAM_THREADS, 1) k_camera_partial(const CamUnit *__restrict__ units,
                                                                 const int *__restrict__ cam_obs,
                                                                 const R *__restrict__ A,
                                                                 const R *__restrict__ ex,
@@ -732,62 +844,122 @@ __global__ void __launch_bounds__(CAM_THREADS) k_camera_partial(const CamUnit *_
     float gh[6], gl[6];  // mixed form: the gradient sums as double-float pairs
 #pragma unroll
     for (int q = 0; q < 6; ++q) gh[q] = gl[q] = 0.0f;
-    const int k1 = min(u.count, (t + 1) * CAM_PER);
-    for (int kk = t * CAM_PER; kk < k1; ++kk) {
-        const int o = __ldg(cam_obs + u.begin + kk);
-        R a[12], e2[2];
-        ldn<R, 12>(A + 12 * (size_t)o, a);
-        ld2<R>(ex + 2 * (size_t)o, e2[0], e2[1]);
-        int v = 0;
-        if constexpr (is_fp64<R>()) {
+    const int k0 = t * CAM_PER, k1 = min(u.count, k0 + CAM_PER);
+    if constexpr (is_fp64<R>()) {
+        for (int kk = k0; kk < k1; ++kk) {
+            const int o = __ldg(cam_obs + u.begin + kk);
+            R a[12], e2[2];
+            ldn<R, 12>(A + 12 * (size_t)o, a);
+            ld2<R>(ex + 2 * (size_t)o, e2[0], e2[1]);
+            int v = 0;
 #pragma unroll
             for (int r = 0; r < 6; ++r)
 #pragma unroll
                 for (int c = r; c < 6; ++c, ++v) acc[v] = acc[v] + a[r] * a[c] + a[6 + r] * a[6 + c];
-        } else {
-#pragma unroll
-            for (int r = 0; r < 6; ++r)
-#pragma unroll
-                for (int c = r; c < 6; ++c, ++v) part[v] = part[v] + a[r] * a[c] + a[6 + r] * a[6 + c];
-        }
-        // the gradient sets the LM fixed point: sums of the exact products
-        // of the stored values, in FP64 (FP64 form) or in double-float FP32
-        // arithmetic (mixed form: each product split by an FMA, TwoSum, to
-        // ~2^-44 of the terms, converted to FP64 once per thread)
-        if constexpr (is_fp64<R>()) {
+            // the gradient sets the LM fixed point: sums of the exact
+            // products of the stored values
 #pragma unroll
             for (int q = 0; q < 6; ++q) acc[21 + q] = acc[21 + q] + a[q] * e2[0] + a[6 + q] * e2[1];
-        } else {
+        }
+    } else {
+        // the mixed form: the thread's indices first, then its rows four at
+        // a time (48-byte A rows as three 16-byte loads), so that up to four
+        // gathered rows are in flight at once; summed in the same order
+        int oo[CAM_PER];
 #pragma unroll
-            for (int q = 0; q < 6; ++q) {
-                const float p0 = __fmul_rn(a[q], e2[0]), p1 = __fmul_rn(a[6 + q], e2[1]);
-                const float r = fmaf(a[q], e2[0], -p0) + fmaf(a[6 + q], e2[1], -p1);
-                float t0, t1;
-                two_sum_f(gh[q], p0, gh[q], t0);
-                two_sum_f(gh[q], p1, gh[q], t1);
-                gl[q] += (t0 + t1) + r;
+        for (int q = 0; q < CAM_PER; ++q) oo[q] = k0 + q < k1 ? __ldg(cam_obs + u.begin + k0 + q) : -1;
+#pragma unroll
+        for (int q0 = 0; q0 < CAM_PER; q0 += 4) {
+            float a4[4][12], e4[4][2];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (oo[q0 + q] < 0) continue;
+                const float4 *A4 = reinterpret_cast<const float4 *>(A + 12 * (size_t)oo[q0 + q]);
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const float4 x = __ldg(A4 + k);
+                    a4[q][4 * k] = x.x;
+                    a4[q][4 * k + 1] = x.y;
+                    a4[q][4 * k + 2] = x.z;
+                    a4[q][4 * k + 3] = x.w;
+                }
+                ld2<float>(ex + 2 * (size_t)oo[q0 + q], e4[q][0], e4[q][1]);
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (oo[q0 + q] < 0) continue;
+                const float *a = a4[q];
+                int v = 0;
+#pragma unroll
+                for (int r = 0; r < 6; ++r)
+#pragma unroll
+                    for (int c = r; c < 6; ++c, ++v) part[v] = part[v] + a[r] * a[c] + a[6 + r] * a[6 + c];
+                // the gradient sets the LM fixed point: sums of the exact
+                // products of the stored values in double-float FP32
+                // arithmetic (each product split by an FMA, TwoSum, to ~2^-44
+                // of the terms)
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    const float p0 = __fmul_rn(a[k], e4[q][0]), p1 = __fmul_rn(a[6 + k], e4[q][1]);
+                    const float r = fmaf(a[k], e4[q][0], -p0) + fmaf(a[6 + k], e4[q][1], -p1);
+                    float t0, t1;
+                    two_sum_f(gh[k], p0, gh[k], t0);
+                    two_sum_f(gh[k], p1, gh[k], t1);
+                    gl[k] += (t0 + t1) + r;
+                }
             }
         }
     }
     if constexpr (!is_fp64<R>()) {
+        // the mixed form sums the threads' values in double-float FP32
+        // arithmetic too (the same fixed order), converting only the 27
+        // totals: no FP64 instruction per thread
+        float2(*red2)[CAM_THREADS + 1] = reinterpret_cast<float2(*)[CAM_THREADS + 1]>(red);
 #pragma unroll
-        for (int v = 0; v < 21; ++v) acc[v] = (double)part[v];
+        for (int v = 0; v < 21; ++v) red2[v][t] = make_float2(part[v], 0.0f);
 #pragma unroll
-        for (int q = 0; q < 6; ++q) acc[21 + q] = (double)gh[q] + (double)gl[q];
-    }
-#pragma unroll
-    for (int v = 0; v < CAM_NV; ++v) red[v][t] = acc[v];
-    __syncthreads();
-    double s = 0.0;
-    const int v = t >> 2, g = t & 3;
-    if (v < CAM_NV) {
+        for (int q = 0; q < 6; ++q) red2[21 + q][t] = make_float2(gh[q], gl[q]);
+        __syncthreads();
+        float sh = 0.0f, sl = 0.0f;
+        const int v = t >> 2, g = t & 3;
+        if (v < CAM_NV) {
 #pragma unroll 8
-        for (int q = 0; q < CAM_THREADS / 4; ++q) s += red[v][g * (CAM_THREADS / 4) + q];
+            for (int q = 0; q < CAM_THREADS / 4; ++q) {
+                const float2 x = red2[v][g * (CAM_THREADS / 4) + q];
+                float e;
+                two_sum_f(sh, x.x, sh, e);
+                sl += x.y + e;
+            }
+        }
+        __syncthreads();
+        if (v < CAM_NV) red2[v][g] = make_float2(sh, sl);
+        __syncthreads();
+        if (t < CAM_NV) {
+            float h = red2[t][0].x, l = red2[t][0].y;
+#pragma unroll
+            for (int q = 1; q < 4; ++q) {
+                float e;
+                two_sum_f(h, red2[t][q].x, h, e);
+                l += red2[t][q].y + e;
+            }
+            partial[(size_t)blockIdx.x * CAM_NV + t] = (double)h + (double)l;
+        }
+    } else {
+#pragma unroll
+        for (int v = 0; v < CAM_NV; ++v) red[v][t] = acc[v];
+        __syncthreads();
+        double s = 0.0;
+        const int v = t >> 2, g = t & 3;
+        if (v < CAM_NV) {
+#pragma unroll 8
+            for (int q = 0; q < CAM_THREADS / 4; ++q) s += red[v][g * (CAM_THREADS / 4) + q];
+        }
+        __syncthreads();
+        if (v < CAM_NV) red[v][g] = s;
+        __syncthreads();
+        if (t < CAM_NV)
+            partial[(size_t)blockIdx.x * CAM_NV + t] = (red[t][0] + red[t][1]) + (red[t][2] + red[t][3]);
     }
-    __syncthreads();
-    if (v < CAM_NV) red[v][g] = s;
-    __syncthreads();
-    if (t < CAM_NV) partial[(size_t)blockIdx.x * CAM_NV + t] = (red[t][0] + red[t][1]) + (red[t][2] + red[t][3]);
 }
 
 __global__ void k_camera_finish(int nc, const int *__restrict__ unit_start,
@@ -840,7 +1012,7 @@ void launch_camera_blocks(const DeviceProblem &d, double coeff, cudaStream_t s)
 // V_i^-1 of the damped V_i + mu I by cofactors (compute_Vinv.cl:29-86); the
 // near-singular branch (|T| < 1e-16, :31-73) restates the reference's pivoted
 // elimination on the symmetric matrix.
-template <typename R>
+template <typename R, bool FAST = false>
 __device__ __forceinline__ void vinv_one(const R *Vi, R mu, R *out)
 {
     const R a11 = Vi[0] + mu, a12 = Vi[1], a13 = Vi[2], a22 = Vi[3] + mu, a23 = Vi[4],
@@ -876,6 +1048,20 @@ __device__ __forceinline__ void vinv_one(const R *Vi, R mu, R *out)
         out[5] = (a11 * a22 - a12 * a21) / T;
         return;
     }
+    if constexpr (FAST) {
+        // the mixed form: one reciprocal (within 1 ulp of 1 / T in this
+        // range) and six products instead of six divisions
+        if (fabs(T) > 0x1p-80 && fabs(T) < 0x1p80) {
+            const R iT = -rcp_fast(T);
+            out[0] = (-a23 * a23 + a22 * a33) * iT;
+            out[1] = (a13 * a23 - a12 * a33) * iT;
+            out[2] = (a12 * a23 - a13 * a22) * iT;
+            out[3] = (-a13 * a13 + a11 * a33) * iT;
+            out[4] = (a12 * a13 - a11 * a23) * iT;
+            out[5] = (-a12 * a12 + a11 * a22) * iT;
+            return;
+        }
+    }
     out[0] = -(-a23 * a23 + a22 * a33) / T;
     out[1] = -(a13 * a23 - a12 * a33) / T;
     out[2] = -(a12 * a23 - a13 * a22) / T;
@@ -884,7 +1070,9 @@ __device__ __forceinline__ void vinv_one(const R *Vi, R mu, R *out)
     out[5] = -(-a12 * a12 + a11 * a22) / T;
 }
 
-// The damping is added and the inverse taken in FP64 in both forms, and V^-1
+// The damping is added and the inverse taken in FP64 in both forms (the mixed
+// form multiplies by one reciprocal of the determinant where the FP64 form,
+// like the reference, divides six times), and V^-1
 // is kept in FP64: for a point seen from two nearby cameras V_i is nearly
 // singular, and an FP32 V_i + mu I (which drops mu) or an FP32 V^-1 moves the
 // LM fixed point by ~1e-2 of the cost.
@@ -900,7 +1088,10 @@ __global__ void k_vinv(int np, const double *__restrict__ V, double mu, double *
     double vi[6], out[6];
 #pragma unroll
     for (int e = 0; e < 6; ++e) vi[e] = V[6 * (size_t)i + e];
-    vinv_one<double>(vi, mu, out);
+    if (Vinv2f)
+        vinv_one<double, true>(vi, mu, out);
+    else
+        vinv_one<double>(vi, mu, out);
 #pragma unroll
     for (int e = 0; e < 6; ++e) Vinv[6 * (size_t)i + e] = out[e];
     if (Vinv2f) {  // hi = fl32(v), lo = fl32(v - hi): v to ~2^-48
@@ -954,22 +1145,49 @@ __global__ void __launch_bounds__(256) k_yblocks(int no, const int *__restrict__
                                                  const float *__restrict__ W, const float *__restrict__ Vinv2f,
                                                  float *__restrict__ Y)
 {
-    int o = blockIdx.x * blockDim.x + threadIdx.x;
-    if (o >= no) return;
-    const float4 *vi = reinterpret_cast<const float4 *>(Vinv2f + 12 * (size_t)__ldg(obs_pt + o));
-    const float4 a = __ldg(vi), b = __ldg(vi + 1), c = __ldg(vi + 2);
-    const float2 s00 = make_float2(a.x, a.y), s01 = make_float2(a.z, a.w), s02 = make_float2(b.x, b.y),
-                 s11 = make_float2(b.z, b.w), s12 = make_float2(c.x, c.y), s22 = make_float2(c.z, c.w);
-    float w[18], y[18];
-    ldn<float, 18>(W + 18 * (size_t)o, w);
+    // a warp's 32 rows (2,304 contiguous bytes of W, then of Y) move between
+    // global and shared memory as coalesced 8-byte words; each lane then
+    // takes its own row from shared memory (rows 72 bytes apart: no bank
+    // conflicts within a half-warp)
+    __shared__ float2 rows_s[256 / 32][32 * 9];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int base = (blockIdx.x * (256 / 32) + warp) * 32;
+    if (base >= no) return;  // the whole warp
+    const int nrow = min(32, no - base);
+    float2 *b = rows_s[warp];
+    const float2 *src = reinterpret_cast<const float2 *>(W + 18 * (size_t)base);
+    for (int k = lane; k < 9 * nrow; k += 32) b[k] = __ldg(src + k);
+    __syncwarp();
+    float y[18];
+    if (lane < nrow) {
+        const int o = base + lane;
+        const float4 *vi = reinterpret_cast<const float4 *>(Vinv2f + 12 * (size_t)__ldg(obs_pt + o));
+        const float4 a = __ldg(vi), bb = __ldg(vi + 1), c = __ldg(vi + 2);
+        const float2 s00 = make_float2(a.x, a.y), s01 = make_float2(a.z, a.w), s02 = make_float2(bb.x, bb.y),
+                     s11 = make_float2(bb.z, bb.w), s12 = make_float2(c.x, c.y), s22 = make_float2(c.z, c.w);
+        float w[18];
 #pragma unroll
-    for (int r = 0; r < 6; ++r) {
-        const float w0 = w[3 * r], w1 = w[3 * r + 1], w2 = w[3 * r + 2];
-        y[3 * r + 0] = dot3_df(w0, w1, w2, s00, s01, s02);
-        y[3 * r + 1] = dot3_df(w0, w1, w2, s01, s11, s12);
-        y[3 * r + 2] = dot3_df(w0, w1, w2, s02, s12, s22);
+        for (int k = 0; k < 9; ++k) {
+            const float2 v = b[9 * lane + k];
+            w[2 * k] = v.x;
+            w[2 * k + 1] = v.y;
+        }
+#pragma unroll
+        for (int r = 0; r < 6; ++r) {
+            const float w0 = w[3 * r], w1 = w[3 * r + 1], w2 = w[3 * r + 2];
+            y[3 * r + 0] = dot3_df(w0, w1, w2, s00, s01, s02);
+            y[3 * r + 1] = dot3_df(w0, w1, w2, s01, s11, s12);
+            y[3 * r + 2] = dot3_df(w0, w1, w2, s02, s12, s22);
+        }
     }
-    stn<float, 18>(Y + 18 * (size_t)o, y);
+    __syncwarp();
+    if (lane < nrow) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) b[9 * lane + k] = make_float2(y[2 * k], y[2 * k + 1]);
+    }
+    __syncwarp();
+    float2 *dst = reinterpret_cast<float2 *>(Y + 18 * (size_t)base);
+    for (int k = lane; k < 9 * nrow; k += 32) dst[k] = b[k];
 }
 
 // Bulk asynchronous copies between global and shared memory (the copy
@@ -1774,7 +1992,24 @@ __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int2 *__r
                     }
                 }
             }
-            part = ((double)h0 + (double)l0) + ((double)h1 + (double)l1);
+            // the two accumulators and then the m lanes of a component
+            // meet in double-float as well (in order of s), converted once
+            // (each lane's own partial is what is exchanged, not a running sum)
+            float hp, t;
+            two_sum_f(h0, h1, hp, t);
+            const float lp = (l0 + l1) + t;
+            float hs = hp, ls = lp;
+#pragma unroll
+            for (int q = 1; q < 4; ++q) {
+                const int src = min(lpp * pw + 3 * q + c, 31);
+                const float oh = __shfl_sync(0xffffffffu, hp, src);
+                const float ol = __shfl_sync(0xffffffffu, lp, src);
+                if (q < m) {
+                    two_sum_f(hs, oh, hs, t);
+                    ls += ol + t;
+                }
+            }
+            if (pw < npw && s == 0) s_sum[wi.x + pw - first][c] = (double)hs + (double)ls;
         } else {
             // one accumulator per camera parameter: six short chains
             double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
@@ -1790,16 +2025,16 @@ __global__ void __launch_bounds__(256) k_eb_dpb(int np, int ncp, const int2 *__r
                 }
             }
             part = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + (acc[4] + acc[5]);
-        }
-        // the m partial sums of a component, in order of s (each lane's own
-        // partial is what is exchanged, not a running sum)
-        double e = part;
+            // the m partial sums of a component, in order of s (each lane's
+            // own partial is what is exchanged, not a running sum)
+            double e = part;
 #pragma unroll
-        for (int q = 1; q < 4; ++q) {
-            const double v = __shfl_sync(0xffffffffu, part, min(lpp * pw + 3 * q + c, 31));
-            if (q < m) e += v;
+            for (int q = 1; q < 4; ++q) {
+                const double v = __shfl_sync(0xffffffffu, part, min(lpp * pw + 3 * q + c, 31));
+                if (q < m) e += v;
+            }
+            if (pw < npw && s == 0) s_sum[wi.x + pw - first][c] = e;
         }
-        if (pw < npw && s == 0) s_sum[wi.x + pw - first][c] = e;
     }
     __syncthreads();
     // one thread per point finishes it: eb = gb - W^T dpa, dpb = V^-1 eb

@@ -309,7 +309,8 @@ void enqueue_linearize(psba_handle *h, double coeff)
     {
         StageScope sc(h, ST_LINEARIZE);
         launch_cam_tables(d, d.cams, nullptr, d.camtab, h->stream,
-                          d.prec == PSBA_PREC_MIXED && d.cnp == 6 ? d.camtab32 : nullptr);
+                          d.prec == PSBA_PREC_MIXED && d.cnp == 6 ? d.camtab32 : nullptr,
+                          linearize_df(d) ? d.tab2f : nullptr);
         launch_linearize(d, coeff, h->stream);
     }
     {

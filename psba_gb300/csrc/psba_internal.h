@@ -193,7 +193,7 @@ struct DeviceProblem {
     float2 *tab2f = nullptr;      // RES_TAB2F per camera: the trial camera table's projection values as FP32 pairs
     double *Linv = nullptr;       // (Np / TILE) * TILE * TILE inverses of the diagonal blocks
     int *status = nullptr;        // Cholesky status word (0 ok, 1 not SPD, 2 wait budget exhausted)
-    int *tickets = nullptr;       // 2 words, zero between launches: last-block tickets (eb/dpb, residual)
+    int *tickets = nullptr;       // 3 words, zero between launches: last-block tickets (eb/dpb, residual, |p|^2)
     int2 *chol_tasks = nullptr;   // helper tasks of the dense factor, in dependency order
     int chol_n_tasks = 0;
     int chol_grid_cap = 0;        // CTAs of the dense factor at most (0: one per SM)
@@ -215,8 +215,10 @@ struct DeviceProblem {
 };
 
 // Linearization: camera tables, residual, Jacobian, W, V, gb, U, ga.
+// (with_d: the derivative tables D as well, which only the linearization reads)
 void launch_cam_tables(const DeviceProblem &d, const double *cams, const double *dpa,
-                       double *tab, cudaStream_t s, float *tab32 = nullptr, float2 *tab2f = nullptr);
+                       double *tab, cudaStream_t s, float *tab32 = nullptr, float2 *tab2f = nullptr,
+                       int with_d = 0);
 void launch_residual_df(const DeviceProblem &d, double *partial, int nblocks, double *sum_dst, cudaStream_t s);
 void launch_split2f(const double *x, float2 *out, long long n, cudaStream_t s);
 void launch_linearize(const DeviceProblem &d, double coeff, cudaStream_t s);
@@ -259,10 +261,12 @@ void launch_update_params(const DeviceProblem &d, cudaStream_t s);
 
 // Deterministic reductions and vector helpers.
 void launch_sum_partials(const double *partial, int n, double *dst, cudaStream_t s);
+// |cams|^2 and |pts|^2 (into dst_cams, dst_pts) in one launch: nred blocks over the points, one over the
+// cameras, the last block summing the points' partials in index order
+void launch_param_norm(const DeviceProblem &d, int nred, double *partial, double *dst_cams, double *dst_pts,
+                       cudaStream_t s);
 void launch_finish_trial(const DeviceProblem &d, double mu, cudaStream_t s);
 void launch_max_uvdiag(const DeviceProblem &d, double *dst, cudaStream_t s);
-void launch_sumsq(const double *x, long long n, double *partial, int nblocks, double *dst,
-                  cudaStream_t s);
 void launch_dot(const double *x, const double *y, long long n, double *partial, int nblocks,
                 double *dst, cudaStream_t s);
 void launch_jmultiply(const DeviceProblem &d, const double *x, double *out, cudaStream_t s);

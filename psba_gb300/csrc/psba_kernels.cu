@@ -98,20 +98,53 @@ __device__ void sum_partials_block(const double *partial, int n, double *dst)
 // With cnp > 6 the intrinsics (fx, cx, cy, ar, skew) and, for cnp 16, the
 // distortion (k1, k2, p1, p2, k3) are parameters 6.. of the camera, moved by
 // dpa like the pose; with cnp 6 they come from the fixed K array.
-// One lane per camera, four warps per block by role, so that no warp issues
+// One lane per camera, six warps per block by role, so that no warp issues
 // the whole table's FP64 instructions one after another (a warp issues one
 // FP64 instruction per ~64 cycles): every warp forms q = q(v) (x) q0, then
-// warp 0 writes M, t and the intrinsics, warp 1 + m writes D[m].
-__global__ void __launch_bounds__(128) k_cam_tables(int nc, int cnp, const double *__restrict__ K,
-                                                    const double *__restrict__ q0, const double *__restrict__ cams,
-                                                    const double *__restrict__ dpa, double *__restrict__ tab,
-                                                    float *__restrict__ tab32, float2 *__restrict__ tab2f)
+// warp 0 writes M, t and the intrinsics (and their FP32 copy), warp 1 + m
+// writes D[m] (only where the Jacobian is formed from the table: with_d),
+// and warps 4 and 5 write the FP32-pair split of M and of t and the
+// intrinsics (tab2f).
+constexpr int CT_THREADS = 192;
+__global__ void __launch_bounds__(CT_THREADS) k_cam_tables(int nc, int cnp, const double *__restrict__ K,
+                                                           const double *__restrict__ q0,
+                                                           const double *__restrict__ cams,
+                                                           const double *__restrict__ dpa, double *__restrict__ tab,
+                                                           float *__restrict__ tab32, float2 *__restrict__ tab2f,
+                                                           int with_d)
 {
     const int role = threadIdx.x >> 5;
     const int j = blockIdx.x * 32 + (threadIdx.x & 31);
     if (j >= nc) return;
+    if ((role >= 1 && role <= 3 && !with_d) || (role >= 4 && !tab2f)) return;
     const double *cj = cams + (size_t)cnp * j;
     const double *dj = dpa ? dpa + (size_t)cnp * j : nullptr;
+    // the translation and the intrinsics (roles 0 and 5)
+    auto tk = [&](double (&t)[3], double (&kk)[5], double (&kc)[5]) {
+        for (int m = 0; m < 3; ++m) t[m] = dj ? cj[3 + m] + dj[3 + m] : cj[3 + m];
+        for (int m = 0; m < 5; ++m) kc[m] = 0.0;
+        if (cnp > 6) {
+            for (int m = 0; m < 5; ++m) kk[m] = dj ? cj[6 + m] + dj[6 + m] : cj[6 + m];
+            if (cnp == 16)
+                for (int m = 0; m < 5; ++m) kc[m] = dj ? cj[11 + m] + dj[11 + m] : cj[11 + m];
+        } else {
+            for (int m = 0; m < 5; ++m) kk[m] = K[5 * j + m];
+        }
+    };
+    if (role == 5) {
+        double t[3], kk[5], kc[5];
+        tk(t, kk, kc);
+        float2 *F = tab2f + (size_t)RES_TAB2F * j;
+#pragma unroll
+        for (int e = 0; e < 3; ++e) F[9 + e] = split2f(t[e]);
+        F[12] = split2f(kk[0]);          // fx
+        F[13] = split2f(kk[4]);          // sk
+        F[14] = split2f(kk[1]);          // cx
+        F[15] = split2f(kk[0] * kk[3]);  // fy
+        F[16] = split2f(kk[2]);          // cy
+        F[17] = make_float2(0.0f, 0.0f);
+        return;
+    }
     double vl[3];
     for (int m = 0; m < 3; ++m) vl[m] = dj ? cj[m] + dj[m] : cj[m];
     const double s0 = q0[4 * j], a1 = q0[4 * j + 1], a2 = q0[4 * j + 2], a3 = q0[4 * j + 3];
@@ -121,25 +154,27 @@ __global__ void __launch_bounds__(128) k_cam_tables(int nc, int cnp, const doubl
     const double b = s0 * vl[1] + sl * a2 + a1 * vl[2] - a3 * vl[0];
     const double c = s0 * vl[2] + sl * a3 + a2 * vl[0] - a1 * vl[1];
     CamTab *T = reinterpret_cast<CamTab *>(tab + (size_t)CAMTAB * j);
-    if (role == 0) {
+    if (role == 0 || role == 4) {
         const double d = s * s - (a * a + b * b + c * c);
-        T->M[0] = d + 2 * a * a;      T->M[1] = 2 * (a * b - s * c); T->M[2] = 2 * (a * c + s * b);
-        T->M[3] = 2 * (a * b + s * c); T->M[4] = d + 2 * b * b;      T->M[5] = 2 * (b * c - s * a);
-        T->M[6] = 2 * (a * c - s * b); T->M[7] = 2 * (b * c + s * a); T->M[8] = d + 2 * c * c;
+        const double M[9] = {d + 2 * a * a,       2 * (a * b - s * c), 2 * (a * c + s * b),
+                             2 * (a * b + s * c), d + 2 * b * b,       2 * (b * c - s * a),
+                             2 * (a * c - s * b), 2 * (b * c + s * a), d + 2 * c * c};
+        if (role == 4) {  // the projection's rotation as FP32 pairs
+            float2 *F = tab2f + (size_t)RES_TAB2F * j;
+#pragma unroll
+            for (int e = 0; e < 9; ++e) F[e] = split2f(M[e]);
+            return;
+        }
+#pragma unroll
+        for (int e = 0; e < 9; ++e) T->M[e] = M[e];
         if (tab32) {  // the mixed Jacobian's operands, rounded once per camera
             float *F = tab32 + (size_t)CAMTAB32 * j;
 #pragma unroll
-            for (int e = 0; e < 9; ++e) F[e] = (float)T->M[e];
+            for (int e = 0; e < 9; ++e) F[e] = (float)M[e];
         }
-        for (int m = 0; m < 3; ++m) T->t[m] = dj ? cj[3 + m] + dj[3 + m] : cj[3 + m];
-        double kk[5], kc[5] = {0, 0, 0, 0, 0};
-        if (cnp > 6) {
-            for (int m = 0; m < 5; ++m) kk[m] = dj ? cj[6 + m] + dj[6 + m] : cj[6 + m];
-            if (cnp == 16)
-                for (int m = 0; m < 5; ++m) kc[m] = dj ? cj[11 + m] + dj[11 + m] : cj[11 + m];
-        } else {
-            for (int m = 0; m < 5; ++m) kk[m] = K[5 * j + m];
-        }
+        double t[3], kk[5], kc[5];
+        tk(t, kk, kc);
+        for (int m = 0; m < 3; ++m) T->t[m] = t[m];
         T->fx = kk[0]; T->cx = kk[1]; T->cy = kk[2]; T->fy = kk[0] * kk[3]; T->sk = kk[4];
         if (tab32) {
             float *F = tab32 + (size_t)CAMTAB32 * j;
@@ -147,19 +182,6 @@ __global__ void __launch_bounds__(128) k_cam_tables(int nc, int cnp, const doubl
             F[37] = (float)T->sk;
             F[38] = (float)T->fy;
             F[39] = 0.0f;
-        }
-        if (tab2f) {  // the projection's values as FP32 pairs: M, t, fx sk cx fy cy
-            float2 *F = tab2f + (size_t)RES_TAB2F * j;
-#pragma unroll
-            for (int e = 0; e < 9; ++e) F[e] = split2f(T->M[e]);
-#pragma unroll
-            for (int e = 0; e < 3; ++e) F[9 + e] = split2f(T->t[e]);
-            F[12] = split2f(T->fx);
-            F[13] = split2f(T->sk);
-            F[14] = split2f(T->cx);
-            F[15] = split2f(T->fy);
-            F[16] = split2f(T->cy);
-            F[17] = make_float2(0.0f, 0.0f);
         }
         T->ar = kk[3];
         for (int m = 0; m < 5; ++m) T->kc[m] = kc[m];
@@ -195,9 +217,10 @@ __global__ void __launch_bounds__(128) k_cam_tables(int nc, int cnp, const doubl
 }
 
 void launch_cam_tables(const DeviceProblem &d, const double *cams, const double *dpa, double *tab,
-                       cudaStream_t s, float *tab32, float2 *tab2f)
+                       cudaStream_t s, float *tab32, float2 *tab2f, int with_d)
 {
-    k_cam_tables<<<ceil_div(d.nc, 32), 128, 0, s>>>(d.nc, d.cnp, d.K, d.q0, cams, dpa, tab, tab32, tab2f);
+    k_cam_tables<<<ceil_div(d.nc, 32), CT_THREADS, 0, s>>>(d.nc, d.cnp, d.K, d.q0, cams, dpa, tab, tab32, tab2f,
+                                                           with_d);
     note_launch(1);
 }
 
@@ -2205,11 +2228,44 @@ __global__ void k_sumsq_partial(const double *__restrict__ x, const double *__re
     if (threadIdx.x == 0) partial[blockIdx.x] = r[0];
 }
 
-void launch_sumsq(const double *x, long long n, double *partial, int nblocks, double *dst,
-                  cudaStream_t s)
+// The parameters' squared norms for the LM stop test (levmar.cpp:150-152):
+// blocks below nred stride over the points' coordinates, block nred over
+// the cameras' parameters; fixed-order sums in every block and in the last.
+__global__ void __launch_bounds__(256) k_param_norm(const double *__restrict__ cams, int ncv,
+                                                    const double *__restrict__ pts, long long npv, int nred,
+                                                    double *__restrict__ partial, int *__restrict__ ticket,
+                                                    double *__restrict__ dst_cams, double *__restrict__ dst_pts)
 {
-    k_sumsq_partial<<<nblocks, 256, 0, s>>>(x, nullptr, n, partial); note_launch(1);
-    k_sum_partials<<<1, 256, 0, s>>>(partial, nblocks, dst); note_launch(1);
+    __shared__ double r[256];
+    double a = 0.0;
+    if ((int)blockIdx.x < nred) {
+        const long long stride = (long long)nred * 256;
+        for (long long k = (long long)blockIdx.x * 256 + threadIdx.x; k < npv; k += stride) a = fma(pts[k], pts[k], a);
+    } else {
+        for (int k = threadIdx.x; k < ncv; k += 256) a = fma(cams[k], cams[k], a);
+    }
+    r[threadIdx.x] = a;
+    __syncthreads();
+    for (int st = 128; st > 0; st >>= 1) {
+        if (threadIdx.x < st) r[threadIdx.x] += r[threadIdx.x + st];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = r[0];
+    if (take_last_ticket(ticket)) {
+        sum_partials_block(partial, nred, dst_pts);
+        if (threadIdx.x == 0) {
+            *dst_cams = __ldcg(partial + nred);
+            *ticket = 0;
+        }
+    }
+}
+
+void launch_param_norm(const DeviceProblem &d, int nred, double *partial, double *dst_cams, double *dst_pts,
+                       cudaStream_t s)
+{
+    k_param_norm<<<nred + 1, 256, 0, s>>>(d.cams, d.N, d.pts, 3LL * d.np, nred, partial, d.tickets + 2, dst_cams,
+                                          dst_pts);
+    note_launch(1);
 }
 
 void launch_dot(const double *x, const double *y, long long n, double *partial, int nblocks,

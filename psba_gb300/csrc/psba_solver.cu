@@ -310,7 +310,7 @@ void enqueue_linearize(psba_handle *h, double coeff)
         StageScope sc(h, ST_LINEARIZE);
         launch_cam_tables(d, d.cams, nullptr, d.camtab, h->stream,
                           d.prec == PSBA_PREC_MIXED && d.cnp == 6 ? d.camtab32 : nullptr,
-                          linearize_df(d) ? d.tab2f : nullptr);
+                          linearize_df(d) ? d.tab2f : nullptr, 1);
         launch_linearize(d, coeff, h->stream);
     }
     {
@@ -374,8 +374,7 @@ void enqueue_step(psba_handle *h, double mu)
 void enqueue_param_norm(psba_handle *h)
 {
     DeviceProblem &d = h->d;
-    launch_sumsq(d.cams, d.N, d.red_partial, 1, h->scratch + SC_PL2A, h->stream);
-    launch_sumsq(d.pts, 3LL * d.np, d.red_partial + 4, h->nred, h->scratch + SC_PL2B, h->stream);
+    launch_param_norm(d, h->nred, d.red_partial + 4, h->scratch + SC_PL2A, h->scratch + SC_PL2B, h->stream);
 }
 
 void trace_push(psba_result *res, int itno, int kind, int acc, double damping, double rho, double cost,
@@ -1082,7 +1081,7 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     TRY(dalloc(h, &d.xsol, (size_t)d.Np));
     TRY(dalloc(h, &d.Linv, (size_t)d.Np * TILE));
     TRY(dalloc(h, &d.status, 4));
-    TRY(dalloc(h, &d.tickets, 2));
+    TRY(dalloc(h, &d.tickets, 3));
     {
         const int nb = d.Np / TILE;
         std::vector<int2> tasks;
@@ -1160,7 +1159,7 @@ int create_impl(const psba_problem_desc *p, psba_handle *h)
     PSBA_CUDA_TRY(cudaMemcpyAsync(d.pts0, d.pts, sizeof(double) * 3 * (size_t)np, cudaMemcpyDeviceToDevice,
                                   h->stream));
     PSBA_CUDA_TRY(cudaMemsetAsync(d.status, 0, 4 * sizeof(int), h->stream));
-    PSBA_CUDA_TRY(cudaMemsetAsync(d.tickets, 0, 2 * sizeof(int), h->stream));
+    PSBA_CUDA_TRY(cudaMemsetAsync(d.tickets, 0, 3 * sizeof(int), h->stream));
     PSBA_CUDA_TRY(cudaMemsetAsync(d.scal, 0, sizeof(TrialScalars), h->stream));
     PSBA_CUDA_TRY(cudaMemsetAsync(h->scratch, 0, 64 * sizeof(double), h->stream));
     return sync(h);  // host vectors go out of scope after the copies complete

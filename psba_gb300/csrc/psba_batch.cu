@@ -498,6 +498,512 @@ __device__ void stage_back(const BatchProblem &p, const Arenas<R> &ar, double mu
     out[1] = cta_sum(s_rho, sh);
 }
 
+// ---------------------------------------------------------------- mixed form
+// The mixed form's stages (R = float): no FP64 instruction per observation,
+// as in the single-problem kernels.  On GB300 a conversion between FP32 and
+// FP64 issues on the FP64 pipe, so FP32 products added into FP64 sums cost
+// the FP64 rate per term; instead the sums are double-float (two FP32 values
+// hi + lo, TwoSum, ~2^-44 of the terms) or FP32 chains of at most eight
+// observations flushed into double-float, converted to FP64 once per output.
+// The projections (linearization, trial cost) run in double-float from the
+// camera tables, points and measurements split into FP32 pairs once; Y takes
+// V^-1 split once per point; eb takes the camera step split once.
+
+__device__ __forceinline__ float2 *rf2(const Arenas<float> &ar, long long off)
+{
+    return reinterpret_cast<float2 *>(ar.r + off);
+}
+
+// df accumulator: h + l += x (x an FP32 value)
+__device__ __forceinline__ void dacc(float &h, float &l, float x)
+{
+    float t;
+    two_sum_f(h, x, h, t);
+    l += t;
+}
+
+// fixed-order df sum over a warp (shuffle-down tree, as warp_sum): lane 0
+__device__ __forceinline__ void warp_sum_df(float &h, float &l)
+{
+    for (int off = 16; off > 0; off >>= 1) {
+        const float oh = __shfl_down_sync(0xffffffffu, h, off), ol = __shfl_down_sync(0xffffffffu, l, off);
+        float t;
+        two_sum_f(h, oh, h, t);
+        l += ol + t;
+    }
+}
+
+// camera tables plus the FP32 Jacobian copy (tab32, optional) and the
+// projection's FP32-pair split (tab2f)
+__device__ void stage_tables_mx(const BatchProblem &p, const Arenas<float> &ar, const double *dpa, double *tab,
+                                float *tab32, float2 *tab2f)
+{
+    for (int j = threadIdx.x; j < p.nc; j += blockDim.x) {
+        double *o = tab + (size_t)CAMTAB * j;
+        cam_table(ar.d + p.d_K + 5 * j, ar.d + p.d_q0 + 4 * j, ar.d + p.d_cams + 6 * j, dpa ? dpa + 6 * j : nullptr,
+                  o);
+        if (tab32) {
+            float *F = tab32 + (size_t)CAMTAB32 * j;
+            for (int e = 0; e < 36; ++e) F[e] = (float)o[e];
+            F[36] = (float)o[39];
+            F[37] = (float)o[40];
+            F[38] = (float)o[42];
+            F[39] = 0.0f;
+        }
+        float2 *F2 = tab2f + (size_t)RES_TAB2F * j;
+        for (int e = 0; e < 9; ++e) F2[e] = split2f(o[e]);
+        for (int e = 0; e < 3; ++e) F2[9 + e] = split2f(o[36 + e]);
+        for (int e = 0; e < 5; ++e) F2[12 + e] = split2f(o[39 + e]);  // fx sk cx fy cy
+        F2[17] = make_float2(0.0f, 0.0f);
+    }
+}
+
+// one observation's residual in double-float: m - pi(X) at a split table row
+__device__ __forceinline__ void proj_df(const float2 *T, df X0, df X1, df X2, float4 m, df &e0, df &e1, df &ycv,
+                                        df &izv, df &nuv)
+{
+    const df xc = df_add(df_add(df_mul(df_of(T[0]), X0), df_mul(df_of(T[1]), X1)),
+                         df_add(df_mul(df_of(T[2]), X2), df_of(T[9])));
+    ycv = df_add(df_add(df_mul(df_of(T[3]), X0), df_mul(df_of(T[4]), X1)), df_add(df_mul(df_of(T[5]), X2), df_of(T[10])));
+    const df zc = df_add(df_add(df_mul(df_of(T[6]), X0), df_mul(df_of(T[7]), X1)),
+                         df_add(df_mul(df_of(T[8]), X2), df_of(T[11])));
+    izv = df_rcp(zc);
+    nuv = df_add(df_mul(df_of(T[12]), xc), df_mul(df_of(T[13]), ycv));
+    const df un = df_add(nuv, df_mul(df_of(T[14]), zc));
+    const df vn = df_add(df_mul(df_of(T[15]), ycv), df_mul(df_of(T[16]), zc));
+    e0 = df_add(df{m.x, m.y}, df_neg(df_mul(un, izv)));
+    e1 = df_add(df{m.z, m.w}, df_neg(df_mul(vn, izv)));
+}
+
+// the measurements (once per launch) or the current points split into pairs
+__device__ void split_into(const double *x, float2 *out, long long n)
+{
+    for (long long k = threadIdx.x; k < n; k += blockDim.x) out[k] = split2f(x[k]);
+}
+
+__device__ void stage_linearize_mx(const BatchProblem &p, const Arenas<float> &ar)
+{
+    const int *opt = ar.i + p.i_obs_pt, *ocam = ar.i + p.i_obs_cam;
+    const float2 *T2 = rf2(ar, p.r_tab2f), *X2 = rf2(ar, p.r_pts2f);
+    const float4 *M4 = reinterpret_cast<const float4 *>(ar.r + p.r_meas2f);
+    const float *T32 = ar.r + p.r_tab32;
+    float *ex = ar.r + p.r_ex, *A = ar.r + p.r_A, *B = ar.r + p.r_B, *W = ar.r + p.r_W;
+    for (int o = threadIdx.x; o < p.no; o += blockDim.x) {
+        const int i = opt[o], j = ocam[o];
+        const df Xa = df_of(X2[3 * i]), Xb = df_of(X2[3 * i + 1]), Xc = df_of(X2[3 * i + 2]);
+        df e0, e1, ycv, izv, nuv;
+        proj_df(T2 + (size_t)RES_TAB2F * j, Xa, Xb, Xc, M4[o], e0, e1, ycv, izv, nuv);
+        ex[2 * (size_t)o] = __fadd_rn(e0.hi, e0.lo);
+        ex[2 * (size_t)o + 1] = __fadd_rn(e1.hi, e1.lo);
+        const float X0 = Xa.hi, X1 = Xb.hi, X2v = Xc.hi;
+        const float yc = __fadd_rn(ycv.hi, ycv.lo), iz = __fadd_rn(izv.hi, izv.lo), nu = __fadd_rn(nuv.hi, nuv.lo);
+        const float *F = T32 + (size_t)CAMTAB32 * j;
+        const float fx = F[36], sk = F[37], fy = F[38];
+        const float p00 = fx * iz, p01 = sk * iz, p02 = -nu * iz * iz, p11 = fy * iz, p12 = -fy * yc * iz * iz;
+        float a[12], bb[6];
+        for (int m = 0; m < 3; ++m) {
+            const float *Dm = F + 9 + 9 * m;
+            const float g0 = Dm[0] * X0 + Dm[1] * X1 + Dm[2] * X2v;
+            const float g1 = Dm[3] * X0 + Dm[4] * X1 + Dm[5] * X2v;
+            const float g2 = Dm[6] * X0 + Dm[7] * X1 + Dm[8] * X2v;
+            a[m] = p00 * g0 + p01 * g1 + p02 * g2;
+            a[6 + m] = p11 * g1 + p12 * g2;
+            bb[m] = p00 * F[m] + p01 * F[3 + m] + p02 * F[6 + m];
+            bb[3 + m] = p11 * F[3 + m] + p12 * F[6 + m];
+        }
+        a[3] = p00; a[4] = p01; a[5] = p02;
+        a[9] = 0.0f; a[10] = p11; a[11] = p12;
+        float *Ao = A + 12 * (size_t)o, *Bo = B + 6 * (size_t)o, *Wo = W + 18 * (size_t)o;
+        for (int e = 0; e < 12; ++e) Ao[e] = a[e];
+        for (int e = 0; e < 6; ++e) Bo[e] = bb[e];
+        for (int r = 0; r < 6; ++r)
+            for (int c = 0; c < 3; ++c) Wo[r * 3 + c] = a[r] * bb[c] + a[6 + r] * bb[3 + c];
+    }
+}
+
+// V and gb per point: the FP32 products of V and the exact products of gb
+// in double-float, one conversion per value (gb also rounded to FP32 for the
+// ea sums)
+__device__ void stage_points_mx(const BatchProblem &p, const Arenas<float> &ar)
+{
+    const int *ps = ar.i + p.i_pt_start;
+    const float *B = ar.r + p.r_B, *ex = ar.r + p.r_ex;
+    double *V = ar.d + p.d_V, *g = ar.d + p.d_g, *uvd = ar.d + p.d_uvdiag;
+    float *gb32 = ar.r + p.r_gb32;
+    for (int i = threadIdx.x; i < p.np; i += blockDim.x) {
+        float h[9], l[9];
+        for (int v = 0; v < 9; ++v) h[v] = l[v] = 0.0f;
+        for (int o = ps[i]; o < ps[i + 1]; ++o) {
+            const float *b = B + 6 * (size_t)o;
+            const float e0 = ex[2 * (size_t)o], e1 = ex[2 * (size_t)o + 1];
+            dacc(h[0], l[0], fmaf(b[0], b[0], b[3] * b[3]));
+            dacc(h[1], l[1], fmaf(b[0], b[1], b[3] * b[4]));
+            dacc(h[2], l[2], fmaf(b[0], b[2], b[3] * b[5]));
+            dacc(h[3], l[3], fmaf(b[1], b[1], b[4] * b[4]));
+            dacc(h[4], l[4], fmaf(b[1], b[2], b[4] * b[5]));
+            dacc(h[5], l[5], fmaf(b[2], b[2], b[5] * b[5]));
+            for (int k = 0; k < 3; ++k) {
+                const float p0 = __fmul_rn(b[k], e0), p1 = __fmul_rn(b[3 + k], e1);
+                const float q = fmaf(b[k], e0, -p0) + fmaf(b[3 + k], e1, -p1);
+                float t0, t1;
+                two_sum_f(h[6 + k], p0, h[6 + k], t0);
+                two_sum_f(h[6 + k], p1, h[6 + k], t1);
+                l[6 + k] += (t0 + t1) + q;
+            }
+        }
+        for (int e = 0; e < 6; ++e) V[6 * (size_t)i + e] = (double)h[e] + (double)l[e];
+        uvd[p.N + 3 * i] = V[6 * (size_t)i];
+        uvd[p.N + 3 * i + 1] = V[6 * (size_t)i + 3];
+        uvd[p.N + 3 * i + 2] = V[6 * (size_t)i + 5];
+        for (int k = 0; k < 3; ++k) {
+            g[p.N + 3 * i + k] = (double)h[6 + k] + (double)l[6 + k];
+            gb32[4 * i + k] = __fadd_rn(h[6 + k], l[6 + k]);
+        }
+    }
+}
+
+// xor-tree df sum over the lanes of equal lane & 3 (offsets 4, 8, 16):
+// lanes 0..3 hold the totals
+__device__ __forceinline__ void slot_sum_df(float &h, float &l)
+{
+    for (int off = 4; off < 32; off <<= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, h, off), ol = __shfl_xor_sync(0xffffffffu, l, off);
+        float t;
+        two_sum_f(h, oh, h, t);
+        l += ol + t;
+    }
+}
+
+// U and ga, one warp per camera: lane 4 s + q takes the camera's
+// observations s, s + 8, ... and quadrant q of U (q = 0: rows and columns
+// 0-2; 1: rows 0-2, columns 3-5; 3: rows and columns 3-5) or, for q = 2, the
+// six sums of ga.  U's FP32 products are summed over eight of the lane's
+// observations at a time, then into double-float; ga's exact products in
+// double-float; the eight slots meet in a fixed xor tree.
+__device__ void stage_cameras_mx(const BatchProblem &p, const Arenas<float> &ar)
+{
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32, nw = blockDim.x / 32;
+    const int q = lane & 3, s = lane >> 2, r0 = q == 3 ? 3 : 0, c0 = q == 0 ? 0 : 3;
+    const int *cs = ar.i + p.i_cam_start, *co = ar.i + p.i_cam_obs;
+    const float *A = ar.r + p.r_A, *ex = ar.r + p.r_ex;
+    double *U = ar.d + p.d_U, *g = ar.d + p.d_g, *uvd = ar.d + p.d_uvdiag;
+    for (int j = warp; j < p.nc; j += nw) {
+        float h[9], l[9], part[9];
+#pragma unroll
+        for (int v = 0; v < 9; ++v) h[v] = l[v] = part[v] = 0.0f;
+        int n = 0;
+        for (int t = cs[j] + s; t < cs[j + 1]; t += 8) {
+            const int o = co[t];
+            float a[12];
+#pragma unroll
+            for (int e = 0; e < 12; ++e) a[e] = A[12 * (size_t)o + e];
+            if (q == 2) {
+                const float e0 = ex[2 * (size_t)o], e1 = ex[2 * (size_t)o + 1];
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    const float p0 = __fmul_rn(a[k], e0), p1 = __fmul_rn(a[6 + k], e1);
+                    const float qq = fmaf(a[k], e0, -p0) + fmaf(a[6 + k], e1, -p1);
+                    float t0, t1;
+                    two_sum_f(h[k], p0, h[k], t0);
+                    two_sum_f(h[k], p1, h[k], t1);
+                    l[k] += (t0 + t1) + qq;
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+#pragma unroll
+                    for (int c = 0; c < 3; ++c)
+                        part[3 * r + c] = part[3 * r + c] + a[r0 + r] * a[c0 + c] + a[6 + r0 + r] * a[6 + c0 + c];
+                if (++n == 8) {
+#pragma unroll
+                    for (int v = 0; v < 9; ++v) {
+                        dacc(h[v], l[v], part[v]);
+                        part[v] = 0.0f;
+                    }
+                    n = 0;
+                }
+            }
+        }
+#pragma unroll
+        for (int v = 0; v < 9; ++v) {
+            dacc(h[v], l[v], part[v]);
+            slot_sum_df(h[v], l[v]);
+        }
+        if (s == 0) {
+            if (q == 2) {
+#pragma unroll
+                for (int k = 0; k < 6; ++k) g[6 * j + k] = (double)h[k] + (double)l[k];
+            } else {
+#pragma unroll
+                for (int r = 0; r < 3; ++r)
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const int R = r0 + r, C = c0 + c;
+                        if (R > C) continue;  // the upper triangle, mirrored
+                        const double x = (double)h[3 * r + c] + (double)l[3 * r + c];
+                        U[36 * j + R * 6 + C] = x;
+                        U[36 * j + C * 6 + R] = x;
+                        if (R == C) uvd[6 * j + R] = x;
+                    }
+            }
+        }
+    }
+}
+
+// V^-1 in FP64 per point (split once into pairs), then Y = W V^-1 in
+// double-float per observation
+__device__ void stage_vinv_y_mx(const BatchProblem &p, const Arenas<float> &ar, double mu)
+{
+    const double *V = ar.d + p.d_V;
+    double *Vi = ar.d + p.d_Vinv;
+    float2 *vs = rf2(ar, p.r_vinv2f);
+    for (int i = threadIdx.x; i < p.np; i += blockDim.x) {
+        double out[6];
+        vinv3(V + 6 * (size_t)i, mu, out);
+        for (int e = 0; e < 6; ++e) {
+            Vi[6 * (size_t)i + e] = out[e];
+            vs[6 * (size_t)i + e] = split2f(out[e]);
+        }
+    }
+    __syncthreads();
+    const int *opt = ar.i + p.i_obs_pt;
+    const float *W = ar.r + p.r_W;
+    float *Y = ar.r + p.r_Y;
+    for (int o = threadIdx.x; o < p.no; o += blockDim.x) {
+        const float2 *s = vs + 6 * (size_t)opt[o];
+        const float2 s00 = s[0], s01 = s[1], s02 = s[2], s11 = s[3], s12 = s[4], s22 = s[5];
+        const float *w = W + 18 * (size_t)o;
+        float *y = Y + 18 * (size_t)o;
+        for (int r = 0; r < 6; ++r) {
+            const float w0 = w[3 * r], w1 = w[3 * r + 1], w2 = w[3 * r + 2];
+            y[3 * r] = dot3_df(w0, w1, w2, s00, s01, s02);
+            y[3 * r + 1] = dot3_df(w0, w1, w2, s01, s11, s12);
+            y[3 * r + 2] = dot3_df(w0, w1, w2, s02, s12, s22);
+        }
+    }
+}
+
+// S and ea.  Diagonal blocks: a warp per camera, lanes strided over its
+// observations, FP32 products (ea with gb in FP32) over eight observations
+// at a time, then double-float.  Off-diagonal blocks: lpp lanes per camera
+// pair, lane 4 s + q on quadrant q of the 6 x 6 block (rows 3 (q >> 1) ..,
+// columns 3 (q & 1) ..) and on the pair's common points s, s + lpp / 4, ...,
+// FP32 over eight of them at a time, then double-float, the slots combined
+// by a fixed xor tree.
+__device__ void stage_schur_mx(const BatchProblem &p, const Arenas<float> &ar, double mu)
+{
+    const int N = p.N;
+    double *S = ar.d + p.d_S, *rhs = ar.d + p.d_rhs;
+    for (long long e = threadIdx.x; e < (long long)N * N; e += blockDim.x) S[e] = 0.0;
+    __syncthreads();
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32, nw = blockDim.x / 32;
+    const float *Y = ar.r + p.r_Y, *W = ar.r + p.r_W, *gb32 = ar.r + p.r_gb32;
+    const double *U = ar.d + p.d_U, *g = ar.d + p.d_g;
+    const int *opt = ar.i + p.i_obs_pt, *cs = ar.i + p.i_cam_start, *co = ar.i + p.i_cam_obs;
+    {
+        // diagonal blocks: lane 4 s + q on the camera's observations s, s + 8,
+        // ... and quadrant q of the lower block (0: rows and columns 0-2; 2:
+        // rows 3-5, columns 0-2; 3: rows and columns 3-5) or, for q = 1, the
+        // six ea sums
+        const int qd = lane & 3, sd = lane >> 2, r0 = qd >= 2 ? 3 : 0, c0 = qd == 3 ? 3 : 0;
+        for (int k = warp; k < p.nc; k += nw) {
+            float h[9], l[9], part[9];
+#pragma unroll
+            for (int v = 0; v < 9; ++v) h[v] = l[v] = part[v] = 0.0f;
+            int n = 0;
+            for (int t = cs[k] + sd; t < cs[k + 1]; t += 8) {
+                const int a = co[t];
+                const float *y = Y + 18 * (size_t)a, *w = W + 18 * (size_t)a;
+                if (qd == 1) {
+                    const float *gb = gb32 + 4 * (size_t)opt[a];
+                    const float g0 = gb[0], g1 = gb[1], g2 = gb[2];
+#pragma unroll
+                    for (int r = 0; r < 6; ++r) {
+                        float sm = part[r];
+                        sm = fmaf(y[3 * r], g0, sm);
+                        sm = fmaf(y[3 * r + 1], g1, sm);
+                        sm = fmaf(y[3 * r + 2], g2, sm);
+                        part[r] = sm;
+                    }
+                } else {
+                    float yv[9], wv[9];
+#pragma unroll
+                    for (int e = 0; e < 9; ++e) {
+                        yv[e] = y[9 * (r0 / 3) + e];
+                        wv[e] = w[9 * (c0 / 3) + e];
+                    }
+#pragma unroll
+                    for (int r = 0; r < 3; ++r)
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) {
+                            float sm = part[3 * r + c];
+                            sm = fmaf(yv[3 * r], wv[3 * c], sm);
+                            sm = fmaf(yv[3 * r + 1], wv[3 * c + 1], sm);
+                            sm = fmaf(yv[3 * r + 2], wv[3 * c + 2], sm);
+                            part[3 * r + c] = sm;
+                        }
+                }
+                if (++n == 8) {
+#pragma unroll
+                    for (int v = 0; v < 9; ++v) {
+                        dacc(h[v], l[v], part[v]);
+                        part[v] = 0.0f;
+                    }
+                    n = 0;
+                }
+            }
+#pragma unroll
+            for (int v = 0; v < 9; ++v) {
+                dacc(h[v], l[v], part[v]);
+                slot_sum_df(h[v], l[v]);
+            }
+            if (sd == 0) {
+                if (qd == 1) {
+#pragma unroll
+                    for (int r = 0; r < 6; ++r) rhs[6 * k + r] = g[6 * k + r] - ((double)h[r] + (double)l[r]);
+                } else {
+#pragma unroll
+                    for (int r = 0; r < 3; ++r)
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) {
+                            const int R = r0 + r, C = c0 + c;
+                            if (C > R) continue;  // the lower triangle
+                            const double uu = U[36 * k + R * 6 + C];
+                            S[(size_t)(6 * k + R) * N + 6 * k + C] =
+                                (R == C ? uu + mu : uu) - ((double)h[3 * r + c] + (double)l[3 * r + c]);
+                        }
+                }
+            }
+        }
+    }
+    const int *pst = ar.i + p.i_pair_start, *pkl = ar.i + p.i_pair_kl, *pa = ar.i + p.i_pair_a,
+              *pb = ar.i + p.i_pair_b;
+    const int lpp = (p.flags & 0xff) ? (p.flags & 0xff) : 32;  // 8, 16 or 32
+    const int gpw = 32 / lpp, grp = warp * gpw + lane / lpp, ng = nw * gpw, gl = lane % lpp;
+    const int q4 = gl & 3, s4 = gl >> 2, nslot = lpp >> 2, qr = q4 >> 1, qc = q4 & 1;
+    const int qmax = (p.n_pairs + ng - 1) / ng * ng;  // keep whole warps in the loop for the shuffles
+    for (int q = grp; q < qmax; q += ng) {
+        float h[9], l[9], part[9];
+        for (int v = 0; v < 9; ++v) h[v] = l[v] = part[v] = 0.0f;
+        if (q < p.n_pairs) {
+            int n = 0;
+            for (int t = pst[q] + s4; t < pst[q + 1]; t += nslot) {
+                const float *y = Y + 18 * (size_t)pa[t] + 9 * qr, *w = W + 18 * (size_t)pb[t] + 9 * qc;
+                float yv[9], wv[9];
+                for (int e = 0; e < 9; ++e) {
+                    yv[e] = y[e];
+                    wv[e] = w[e];
+                }
+                for (int r = 0; r < 3; ++r)
+                    for (int c = 0; c < 3; ++c) {
+                        float sm = part[3 * r + c];
+                        sm = fmaf(yv[3 * r], wv[3 * c], sm);
+                        sm = fmaf(yv[3 * r + 1], wv[3 * c + 1], sm);
+                        sm = fmaf(yv[3 * r + 2], wv[3 * c + 2], sm);
+                        part[3 * r + c] = sm;
+                    }
+                if (++n == 8) {
+                    for (int v = 0; v < 9; ++v) {
+                        dacc(h[v], l[v], part[v]);
+                        part[v] = 0.0f;
+                    }
+                    n = 0;
+                }
+            }
+            for (int v = 0; v < 9; ++v) dacc(h[v], l[v], part[v]);
+        }
+        for (int v = 0; v < 9; ++v)
+            for (int off = 4; off < lpp; off <<= 1) {
+                const float oh = __shfl_xor_sync(0xffffffffu, h[v], off), ol = __shfl_xor_sync(0xffffffffu, l[v], off);
+                float t;
+                two_sum_f(h[v], oh, h[v], t);
+                l[v] += ol + t;
+            }
+        if (s4 == 0 && q < p.n_pairs) {
+            const int k = pkl[2 * q], l2 = pkl[2 * q + 1];
+            for (int r = 0; r < 3; ++r)
+                for (int c = 0; c < 3; ++c)
+                    S[(size_t)(6 * k + 3 * qr + r) * N + 6 * l2 + 3 * qc + c] =
+                        -((double)h[3 * r + c] + (double)l[3 * r + c]);
+        }
+    }
+}
+
+// eb = gb - W^T dpa in double-float (dpa split once), dpb = V^-1 eb in
+// FP64 per point; the trial points split for the trial cost
+__device__ void stage_back_mx(const BatchProblem &p, const Arenas<float> &ar, double mu, double *sh, double out[2])
+{
+    const int N = p.N;
+    double *dp = ar.d + p.d_dp;
+    const double *g = ar.d + p.d_g, *Vi = ar.d + p.d_Vinv, *pts = ar.d + p.d_pts;
+    const int *ps = ar.i + p.i_pt_start, *ocam = ar.i + p.i_obs_cam;
+    const float *W = ar.r + p.r_W;
+    float2 *da2 = rf2(ar, p.r_dpa2f), *x2 = rf2(ar, p.r_x2f);
+    double s_sq = 0.0, s_rho = 0.0;
+    for (int k = threadIdx.x; k < N; k += blockDim.x) {
+        const double x = dp[k];
+        da2[k] = split2f(x);
+        s_sq += x * x;
+        s_rho += x * (mu * x + g[k]);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < p.np; i += blockDim.x) {
+        float h[3] = {0.0f, 0.0f, 0.0f}, l[3] = {0.0f, 0.0f, 0.0f};
+        for (int o = ps[i]; o < ps[i + 1]; ++o) {
+            const float *w = W + 18 * (size_t)o;
+            const float2 *da = da2 + 6 * (size_t)ocam[o];
+            for (int k = 0; k < 6; ++k) {
+                const float2 d2 = da[k];
+                for (int c = 0; c < 3; ++c) {
+                    const float wv = w[3 * k + c];
+                    const float pr = __fmul_rn(wv, d2.x);
+                    const float pe = fmaf(wv, d2.x, -pr);
+                    float t;
+                    two_sum_f(h[c], pr, h[c], t);
+                    l[c] = fmaf(wv, d2.y, l[c] + (t + pe));
+                }
+            }
+        }
+        const double *gb = g + N + 3 * (size_t)i;
+        const double e0 = gb[0] - ((double)h[0] + (double)l[0]);
+        const double e1 = gb[1] - ((double)h[1] + (double)l[1]);
+        const double e2 = gb[2] - ((double)h[2] + (double)l[2]);
+        const double *v = Vi + 6 * (size_t)i;
+        const double d0 = v[0] * e0 + v[1] * e1 + v[2] * e2;
+        const double d1 = v[1] * e0 + v[3] * e1 + v[4] * e2;
+        const double d2 = v[2] * e0 + v[4] * e1 + v[5] * e2;
+        double *db = dp + N + 3 * (size_t)i;
+        db[0] = d0;
+        db[1] = d1;
+        db[2] = d2;
+        x2[3 * (size_t)i] = split2f(pts[3 * (size_t)i] + d0);
+        x2[3 * (size_t)i + 1] = split2f(pts[3 * (size_t)i + 1] + d1);
+        x2[3 * (size_t)i + 2] = split2f(pts[3 * (size_t)i + 2] + d2);
+        s_sq += d0 * d0 + d1 * d1 + d2 * d2;
+        s_rho += d0 * (mu * d0 + gb[0]) + d1 * (mu * d1 + gb[1]) + d2 * (mu * d2 + gb[2]);
+    }
+    out[0] = cta_sum(s_sq, sh);
+    out[1] = cta_sum(s_rho, sh);
+}
+
+// the trial cost in double-float: the trial table's split and the trial
+// points' (stage_back_mx), the measurements' pairs
+__device__ double stage_cost_mx(const BatchProblem &p, const Arenas<float> &ar, double *sh)
+{
+    const int *opt = ar.i + p.i_obs_pt, *ocam = ar.i + p.i_obs_cam;
+    const float2 *T2 = rf2(ar, p.r_tab2f2), *X2 = rf2(ar, p.r_x2f);
+    const float4 *M4 = reinterpret_cast<const float4 *>(ar.r + p.r_meas2f);
+    df sq{0.0f, 0.0f};
+    for (int o = threadIdx.x; o < p.no; o += blockDim.x) {
+        const int i = opt[o], j = ocam[o];
+        df e0, e1, ycv, izv, nuv;
+        proj_df(T2 + (size_t)RES_TAB2F * j, df_of(X2[3 * i]), df_of(X2[3 * i + 1]), df_of(X2[3 * i + 2]), M4[o], e0,
+                e1, ycv, izv, nuv);
+        sq = df_add(sq, df_add(df_mul(e0, e0), df_mul(e1, e1)));
+    }
+    return cta_sum((double)sq.hi + (double)sq.lo, sh);
+}
+
 // ---------------------------------------------------------------- one problem
 
 template <typename R>
@@ -536,14 +1042,26 @@ __device__ void solve_problem(const BatchProblem &p, const Arenas<R> &ar, const 
         shi[6] = res->first;
     }
     __syncthreads();
+    constexpr bool MX = sizeof(R) == 4;  // the mixed form
+    if constexpr (MX) split_into(ar.d + p.d_meas, rf2(ar, p.r_meas2f), 2LL * p.no);
     const int slice_end = p.slice > 0 ? shi[3] + p.slice : o.max_iter;
     while (shi[3] < o.max_iter && shi[3] < slice_end && shi[1] == PSBA_ITER_CONTINUE) {
-        stage_tables<R>(p, ar, nullptr, tab);
-        __syncthreads();
-        stage_linearize<R>(p, ar);
-        __syncthreads();
-        stage_points<R>(p, ar);
-        stage_cameras<R>(p, ar);
+        if constexpr (MX) {
+            stage_tables_mx(p, ar, nullptr, tab, ar.r + p.r_tab32, rf2(ar, p.r_tab2f));
+            split_into(pts, rf2(ar, p.r_pts2f), 3LL * p.np);
+            __syncthreads();
+            stage_linearize_mx(p, ar);
+            __syncthreads();
+            stage_points_mx(p, ar);
+            stage_cameras_mx(p, ar);
+        } else {
+            stage_tables<R>(p, ar, nullptr, tab);
+            __syncthreads();
+            stage_linearize<R>(p, ar);
+            __syncthreads();
+            stage_points<R>(p, ar);
+            stage_cameras<R>(p, ar);
+        }
         __syncthreads();
         if (threadIdx.x == 0) shi[5]++;
         if (shi[6]) {
@@ -561,9 +1079,15 @@ __device__ void solve_problem(const BatchProblem &p, const Arenas<R> &ar, const 
         }
         while (true) {
             const double mu = shd[0];
-            stage_vinv_y<R>(p, ar, mu);
-            __syncthreads();
-            stage_schur<R>(p, ar, mu);
+            if constexpr (MX) {
+                stage_vinv_y_mx(p, ar, mu);
+                __syncthreads();
+                stage_schur_mx(p, ar, mu);
+            } else {
+                stage_vinv_y<R>(p, ar, mu);
+                __syncthreads();
+                stage_schur<R>(p, ar, mu);
+            }
             __syncthreads();
             double *S = ar.d + p.d_S, *rhs = ar.d + p.d_rhs, *x = ar.d + p.d_x;
             const int st = stage_cholesky_solve(S, N, rhs, x, sh, shi);
@@ -573,7 +1097,10 @@ __device__ void solve_problem(const BatchProblem &p, const Arenas<R> &ar, const 
                 for (int k = threadIdx.x; k < N; k += blockDim.x) dp[k] = x[k];
                 __syncthreads();
                 double sums[2];
-                stage_back<R>(p, ar, mu, sh, sums);
+                if constexpr (MX)
+                    stage_back_mx(p, ar, mu, sh, sums);
+                else
+                    stage_back<R>(p, ar, mu, sh, sums);
                 const double dp_L2 = sums[0], rho_den = sums[1];
                 if (dp_L2 < shd[1] * o.stop_thresh * o.stop_thresh) {
                     if (threadIdx.x == 0) shi[1] = PSBA_ITER_DP_NO_CHANGE;
@@ -582,9 +1109,16 @@ __device__ void solve_problem(const BatchProblem &p, const Arenas<R> &ar, const 
                     if (threadIdx.x == 0) shi[1] = PSBA_ITER_ERR;
                     decided = 2;
                 } else {
-                    stage_tables<R>(p, ar, dp, tab2);
-                    __syncthreads();
-                    const double new_cost = stage_cost<R>(p, ar, tab2, dp + N, sh);
+                    double new_cost;
+                    if constexpr (MX) {
+                        stage_tables_mx(p, ar, dp, tab2, nullptr, rf2(ar, p.r_tab2f2));
+                        __syncthreads();
+                        new_cost = stage_cost_mx(p, ar, sh);
+                    } else {
+                        stage_tables<R>(p, ar, dp, tab2);
+                        __syncthreads();
+                        new_cost = stage_cost<R>(p, ar, tab2, dp + N, sh);
+                    }
                     const double rho = (shd[2] - new_cost) / rho_den;
                     if (rho > 0) {
                         for (int k = threadIdx.x; k < N; k += blockDim.x) cams[k] = cams[k] + dp[k];
@@ -778,6 +1312,16 @@ bool build_problem_layout(const psba_problem_desc &p, ProblemLayout &L, std::str
     bp.r_B = r_total; r_total += 6LL * no;
     bp.r_W = r_total; r_total += 18LL * no;
     bp.r_Y = r_total; r_total += 18LL * no;
+    // the mixed form's FP32 copies (even counts: FP32 pairs stay 8-byte aligned)
+    bp.r_tab32 = r_total; r_total += (long long)CAMTAB32 * nc;
+    bp.r_tab2f = r_total; r_total += 2LL * RES_TAB2F * nc;
+    bp.r_tab2f2 = r_total; r_total += 2LL * RES_TAB2F * nc;
+    bp.r_meas2f = r_total; r_total += 4LL * no;
+    bp.r_pts2f = r_total; r_total += 6LL * np;
+    bp.r_x2f = r_total; r_total += 6LL * np;
+    bp.r_vinv2f = r_total; r_total += 12LL * np;
+    bp.r_dpa2f = r_total; r_total += 2LL * N;
+    bp.r_gb32 = r_total; r_total += 4LL * np;
     L.nr = r_total;
     bp.d_V = dres(6 * (size_t)np);
     bp.d_Vinv = dres(6 * (size_t)np);
@@ -804,7 +1348,9 @@ void rebase_problem(BatchProblem &bp, long long db, long long ib, long long rb)
     for (long long *f : {&bp.i_obs_pt, &bp.i_obs_cam, &bp.i_pt_start, &bp.i_cam_start, &bp.i_cam_obs,
                          &bp.i_pair_start, &bp.i_pair_kl, &bp.i_pair_a, &bp.i_pair_b})
         *f += ib;
-    for (long long *f : {&bp.r_ex, &bp.r_A, &bp.r_B, &bp.r_W, &bp.r_Y}) *f += rb;
+    for (long long *f : {&bp.r_ex, &bp.r_A, &bp.r_B, &bp.r_W, &bp.r_Y, &bp.r_tab32, &bp.r_tab2f, &bp.r_tab2f2,
+                         &bp.r_meas2f, &bp.r_pts2f, &bp.r_x2f, &bp.r_vinv2f, &bp.r_dpa2f, &bp.r_gb32})
+        *f += rb;
 }
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }

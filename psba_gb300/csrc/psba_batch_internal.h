@@ -19,6 +19,11 @@ struct BatchProblem {
     long long i_obs_pt, i_obs_cam, i_pt_start, i_cam_start, i_cam_obs, i_pair_start, i_pair_kl, i_pair_a,
         i_pair_b;                                                                  // int arena
     long long r_ex, r_A, r_B, r_W, r_Y;                                            // R arena
+    // R arena, used by the mixed form only (as FP32 values and FP32 pairs): the
+    // Jacobian's FP32 camera table, the projection's split tables (current,
+    // trial), the split measurements, current and trial points, V^-1, the
+    // camera step, and gb rounded to FP32
+    long long r_tab32, r_tab2f, r_tab2f2, r_meas2f, r_pts2f, r_x2f, r_vinv2f, r_dpa2f, r_gb32;
     long long d_V, d_Vinv, d_U, d_g, d_uvdiag, d_dp, d_S, d_tab, d_tab2, d_rhs, d_x;  // double arena
 };
 

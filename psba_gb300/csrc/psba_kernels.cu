@@ -224,43 +224,6 @@ void launch_cam_tables(const DeviceProblem &d, const double *cams, const double 
     note_launch(1);
 }
 
-// Double-float arithmetic: a value is an unevaluated sum hi + lo of two
-// FP32 numbers (Dekker, "A floating-point technique for extending the
-// available precision", Numer. Math. 18, 1971; Knuth's TwoSum): products
-// split exactly by an FMA, sums carried with TwoSum, each result renormalised,
-// ~2^-44 relative per operation.
-struct df {
-    float hi, lo;
-};
-__device__ __forceinline__ df df_of(float2 v) { return df{v.x, v.y}; }
-__device__ __forceinline__ df df_renorm(float s, float e)  // |s| >= |e|
-{
-    const float h = __fadd_rn(s, e);
-    return df{h, __fsub_rn(e, __fsub_rn(h, s))};
-}
-__device__ __forceinline__ df df_add(df x, df y)
-{
-    const float s = __fadd_rn(x.hi, y.hi), z = __fsub_rn(s, x.hi);
-    const float e = __fadd_rn(__fsub_rn(x.hi, __fsub_rn(s, z)), __fsub_rn(y.hi, z));
-    return df_renorm(s, e + (x.lo + y.lo));
-}
-__device__ __forceinline__ df df_neg(df x) { return df{-x.hi, -x.lo}; }
-__device__ __forceinline__ df df_mul(df x, df y)
-{
-    const float p = __fmul_rn(x.hi, y.hi);
-    const float e = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, fmaf(x.hi, y.hi, -p)));
-    return df_renorm(p, e);
-}
-// 1 / x: the FP32 reciprocal, then one Newton step r + r (1 - x r) in
-// double-float (doubling its ~24 correct bits)
-__device__ __forceinline__ df df_rcp(df x)
-{
-    const float r = __frcp_rn(x.hi);
-    const df xr = df_mul(x, df{r, 0.0f});
-    const df e = df_add(df{1.0f, 0.0f}, df_neg(xr));
-    return df_add(df{r, 0.0f}, df_mul(df{r, 0.0f}, e));
-}
-
 // ---------------------------------------------------------------------------
 // Linearization, one thread per observation: residual (compute_exQT.cl),
 // Jacobian blocks A = d(x,y)/d(v,t), B = d(x,y)/dX (compute_jacobiQT.cl) by
@@ -652,13 +615,6 @@ void launch_residual(const DeviceProblem &d, const double *tab, const double *pt
     note_launch(1);
 }
 
-// s + e = a + b exactly (Knuth's TwoSum), FP32
-__device__ __forceinline__ void two_sum_f(float a, float b, float &s, float &e)
-{
-    s = __fadd_rn(a, b);
-    const float z = __fsub_rn(s, a);
-    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, z)), __fsub_rn(b, z));
-}
 
 // ---------------------------------------------------------------------------
 // Per-point sums: V_i = coeff sum B^T B (compute_V.cl:24-37) and
@@ -1137,23 +1093,6 @@ void launch_vinv(const DeviceProblem &d, double mu, cudaStream_t s)
 }
 
 
-// w0 v0 + w1 v1 + w2 v2 with each v = hi + lo (two FP32 values), rounded
-// once to FP32: the products w hi split exactly by an FMA, the w lo products
-// and the errors summed beside a TwoSum chain, so the result is the FP32
-// rounding of the sum computed to ~2^-44 of its terms (double-float
-// arithmetic), as if formed in FP64 and rounded on store.
-__device__ __forceinline__ float dot3_df(float w0, float w1, float w2, float2 v0, float2 v1, float2 v2)
-{
-    const float p0 = __fmul_rn(w0, v0.x), p1 = __fmul_rn(w1, v1.x), p2 = __fmul_rn(w2, v2.x);
-    float lo = fmaf(w0, v0.x, -p0) + fmaf(w1, v1.x, -p1) + fmaf(w2, v2.x, -p2);
-    lo = fmaf(w0, v0.y, lo);
-    lo = fmaf(w1, v1.y, lo);
-    lo = fmaf(w2, v2.y, lo);
-    float s1, t1, s2, t2;
-    two_sum_f(p0, p1, s1, t1);
-    two_sum_f(s1, p2, s2, t2);
-    return __fadd_rn(s2, (t1 + t2) + lo);
-}
 
 // Y = W V^-1 (compute_Yblks.cl:26-37), one thread per observation, the
 // mixed form: W in FP32, V^-1 inverted in FP64 and carried as FP32 pairs

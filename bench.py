@@ -118,6 +118,8 @@ def parse():
     ap.add_argument("--serve-large-cams", type=int, default=None, help="server large_cams (default: library's)")
     ap.add_argument("--serve-large-chol", type=int, default=None,
                     help="server large_chol_ctas (default: library's)")
+    ap.add_argument("--serve-fp64-intrinsics", type=int, default=None, choices=[0, 1],
+                    help="server fp64_intrinsics: 11/16-parameter requests in FP64 (default: library's)")
     return ap.parse_args()
 
 
@@ -632,12 +634,13 @@ def serving_leg(P, args):
     out = {"workload": "Poisson arrivals; %d distinct request scenes cycled: cameras log-U[5,138], points "
                        "log-U[500,60000], 4-6 views/point, half 6-param and half 11-param cameras; each request "
                        "solved to the reference's stopping rule (at most %d LM iterations); mixed form for "
-                       "6-param cameras, FP64 for 11-param; 120 GB HBM budget" % (len(pool), cap),
+                       "6-param cameras, %s for 11-param; 120 GB HBM budget"
+                       % (len(pool), cap, "mixed" if args.serve_fp64_intrinsics == 0 else "FP64"),
            "mean_observations": float(np.mean([sc.n_obs for sc in pool])), "rates": []}
     rel_all = []
     with S.Server(precision=P.PREC_MIXED, max_iter=cap, hbm_budget_bytes=120e9, large_cams=args.serve_large_cams,
                   large_lanes=args.serve_large_lanes, large_obs=args.serve_large_obs,
-                  large_chol_ctas=args.serve_large_chol) as srv:
+                  large_chol_ctas=args.serve_large_chol, fp64_intrinsics=args.serve_fp64_intrinsics) as srv:
         S.run_poisson(srv, pool[:4], rate=1000.0, n_requests=4, seed=1)
         for rate in rates:
             n = int(min(max(rate * args.serve_seconds, 20), args.serve_max))

@@ -215,3 +215,33 @@ def autotune(batch, precision=PREC_MIXED, n_buckets=3, lane_options=(8, 16, 32),
                                    for b in range(n_buckets)},
               "bucket_edges_mean_common_points": [float(e) for e in edges]}
     return choice, table
+
+
+def main(argv=None):
+    """``python -m psba_gb300.batch --problems 64 --iters 15``: the bench's
+    batch workload (seeded scenes: 5-30 cameras, 200-3,000 points, 3-8 views
+    per point) in one batch, solved once untimed and once timed in each form
+    (mixed, then FP64); prints solves/s and the launch's device time.  It is
+    the command the batched kernel's ncu summary is captured under."""
+    import argparse
+
+    from . import scenes
+    ap = argparse.ArgumentParser(description="batched LM solves of seeded small problems")
+    ap.add_argument("--problems", type=int, default=64)
+    ap.add_argument("--iters", type=int, default=15, help="LM iteration cap of every problem")
+    ap.add_argument("--seed", type=int, default=1000)
+    a = ap.parse_args(argv)
+    probs = scenes.batch_scenes(a.problems, seed=a.seed)
+    with Batch(probs) as b:
+        for tag, prec in (("mixed", PREC_MIXED), ("fp64", PREC_FP64)):
+            o = default_opts(allow_switch=0, max_iter=a.iters, precision=prec)
+            b.reset()
+            b.levmar(o)
+            b.reset()
+            res, ms = b.levmar(o)
+            print("%s: %d problems, %.3f ms, %.1f solves/s, median final cost %.6e"
+                  % (tag, b.n, ms, b.n / ms * 1e3, float(np.median(res["final_cost"]))))
+
+
+if __name__ == "__main__":
+    main()

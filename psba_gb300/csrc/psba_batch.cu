@@ -514,6 +514,42 @@ __device__ __forceinline__ float2 *rf2(const Arenas<float> &ar, long long off)
     return reinterpret_cast<float2 *>(ar.r + off);
 }
 
+// vector loads and stores of FP32 rows (8-byte aligned: every R-arena region
+// offset is even; A's rows 16-byte aligned)
+__device__ __forceinline__ void ld2n(const float *p, float *out, int n)
+{
+    const float2 *q = reinterpret_cast<const float2 *>(p);
+    for (int k = 0; k < n / 2; ++k) {
+        const float2 v = q[k];
+        out[2 * k] = v.x;
+        out[2 * k + 1] = v.y;
+    }
+}
+__device__ __forceinline__ void st2n(float *p, const float *in, int n)
+{
+    float2 *q = reinterpret_cast<float2 *>(p);
+    for (int k = 0; k < n / 2; ++k) q[k] = make_float2(in[2 * k], in[2 * k + 1]);
+}
+// nine consecutive floats of a 72-byte row starting at float 9 h (h = 0, 1):
+// four 8-byte pairs and one scalar
+__device__ __forceinline__ void ld_half9(const float *row, int h, float (&v)[9])
+{
+    const float *p = row + 9 * h;
+    const float single = p[h ? 0 : 8];
+    const float2 *q = reinterpret_cast<const float2 *>(p + (h ? 1 : 0));
+    float pr[8];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float2 t = q[k];
+        pr[2 * k] = t.x;
+        pr[2 * k + 1] = t.y;
+    }
+    v[0] = h ? single : pr[0];
+#pragma unroll
+    for (int e = 1; e < 8; ++e) v[e] = h ? pr[e - 1] : pr[e];
+    v[8] = h ? pr[7] : single;
+}
+
 // df accumulator: h + l += x (x an FP32 value)
 __device__ __forceinline__ void dacc(float &h, float &l, float x)
 {
@@ -593,8 +629,7 @@ __device__ void stage_linearize_mx(const BatchProblem &p, const Arenas<float> &a
         const df Xa = df_of(X2[3 * i]), Xb = df_of(X2[3 * i + 1]), Xc = df_of(X2[3 * i + 2]);
         df e0, e1, ycv, izv, nuv;
         proj_df(T2 + (size_t)RES_TAB2F * j, Xa, Xb, Xc, M4[o], e0, e1, ycv, izv, nuv);
-        ex[2 * (size_t)o] = __fadd_rn(e0.hi, e0.lo);
-        ex[2 * (size_t)o + 1] = __fadd_rn(e1.hi, e1.lo);
+        *reinterpret_cast<float2 *>(ex + 2 * (size_t)o) = make_float2(__fadd_rn(e0.hi, e0.lo), __fadd_rn(e1.hi, e1.lo));
         const float X0 = Xa.hi, X1 = Xb.hi, X2v = Xc.hi;
         const float yc = __fadd_rn(ycv.hi, ycv.lo), iz = __fadd_rn(izv.hi, izv.lo), nu = __fadd_rn(nuv.hi, nuv.lo);
         const float *F = T32 + (size_t)CAMTAB32 * j;
@@ -613,11 +648,16 @@ __device__ void stage_linearize_mx(const BatchProblem &p, const Arenas<float> &a
         }
         a[3] = p00; a[4] = p01; a[5] = p02;
         a[9] = 0.0f; a[10] = p11; a[11] = p12;
-        float *Ao = A + 12 * (size_t)o, *Bo = B + 6 * (size_t)o, *Wo = W + 18 * (size_t)o;
-        for (int e = 0; e < 12; ++e) Ao[e] = a[e];
-        for (int e = 0; e < 6; ++e) Bo[e] = bb[e];
+        float4 *A4 = reinterpret_cast<float4 *>(A + 12 * (size_t)o);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) A4[k] = make_float4(a[4 * k], a[4 * k + 1], a[4 * k + 2], a[4 * k + 3]);
+        st2n(B + 6 * (size_t)o, bb, 6);
+        float wv[18];
+#pragma unroll
         for (int r = 0; r < 6; ++r)
-            for (int c = 0; c < 3; ++c) Wo[r * 3 + c] = a[r] * bb[c] + a[6 + r] * bb[3 + c];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) wv[r * 3 + c] = a[r] * bb[c] + a[6 + r] * bb[3 + c];
+        st2n(W + 18 * (size_t)o, wv, 18);
     }
 }
 
@@ -634,8 +674,10 @@ __device__ void stage_points_mx(const BatchProblem &p, const Arenas<float> &ar)
         float h[9], l[9];
         for (int v = 0; v < 9; ++v) h[v] = l[v] = 0.0f;
         for (int o = ps[i]; o < ps[i + 1]; ++o) {
-            const float *b = B + 6 * (size_t)o;
-            const float e0 = ex[2 * (size_t)o], e1 = ex[2 * (size_t)o + 1];
+            float b[6];
+            ld2n(B + 6 * (size_t)o, b, 6);
+            const float2 ee = *reinterpret_cast<const float2 *>(ex + 2 * (size_t)o);
+            const float e0 = ee.x, e1 = ee.y;
             dacc(h[0], l[0], fmaf(b[0], b[0], b[3] * b[3]));
             dacc(h[1], l[1], fmaf(b[0], b[1], b[3] * b[4]));
             dacc(h[2], l[2], fmaf(b[0], b[2], b[3] * b[5]));
@@ -695,10 +737,18 @@ __device__ void stage_cameras_mx(const BatchProblem &p, const Arenas<float> &ar)
         for (int t = cs[j] + s; t < cs[j + 1]; t += 8) {
             const int o = co[t];
             float a[12];
+            const float4 *A4 = reinterpret_cast<const float4 *>(A + 12 * (size_t)o);
 #pragma unroll
-            for (int e = 0; e < 12; ++e) a[e] = A[12 * (size_t)o + e];
+            for (int k = 0; k < 3; ++k) {
+                const float4 x = A4[k];
+                a[4 * k] = x.x;
+                a[4 * k + 1] = x.y;
+                a[4 * k + 2] = x.z;
+                a[4 * k + 3] = x.w;
+            }
             if (q == 2) {
-                const float e0 = ex[2 * (size_t)o], e1 = ex[2 * (size_t)o + 1];
+                const float2 ee = *reinterpret_cast<const float2 *>(ex + 2 * (size_t)o);
+                const float e0 = ee.x, e1 = ee.y;
 #pragma unroll
                 for (int k = 0; k < 6; ++k) {
                     const float p0 = __fmul_rn(a[k], e0), p1 = __fmul_rn(a[6 + k], e1);
@@ -772,14 +822,16 @@ __device__ void stage_vinv_y_mx(const BatchProblem &p, const Arenas<float> &ar, 
     for (int o = threadIdx.x; o < p.no; o += blockDim.x) {
         const float2 *s = vs + 6 * (size_t)opt[o];
         const float2 s00 = s[0], s01 = s[1], s02 = s[2], s11 = s[3], s12 = s[4], s22 = s[5];
-        const float *w = W + 18 * (size_t)o;
-        float *y = Y + 18 * (size_t)o;
+        float w[18], y[18];
+        ld2n(W + 18 * (size_t)o, w, 18);
+#pragma unroll
         for (int r = 0; r < 6; ++r) {
             const float w0 = w[3 * r], w1 = w[3 * r + 1], w2 = w[3 * r + 2];
             y[3 * r] = dot3_df(w0, w1, w2, s00, s01, s02);
             y[3 * r + 1] = dot3_df(w0, w1, w2, s01, s11, s12);
             y[3 * r + 2] = dot3_df(w0, w1, w2, s02, s12, s22);
         }
+        st2n(Y + 18 * (size_t)o, y, 18);
     }
 }
 
@@ -815,23 +867,22 @@ __device__ void stage_schur_mx(const BatchProblem &p, const Arenas<float> &ar, d
                 const int a = co[t];
                 const float *y = Y + 18 * (size_t)a, *w = W + 18 * (size_t)a;
                 if (qd == 1) {
-                    const float *gb = gb32 + 4 * (size_t)opt[a];
-                    const float g0 = gb[0], g1 = gb[1], g2 = gb[2];
+                    const float4 gb = *reinterpret_cast<const float4 *>(gb32 + 4 * (size_t)opt[a]);
+                    const float g0 = gb.x, g1 = gb.y, g2 = gb.z;
+                    float yr[18];
+                    ld2n(y, yr, 18);
 #pragma unroll
                     for (int r = 0; r < 6; ++r) {
                         float sm = part[r];
-                        sm = fmaf(y[3 * r], g0, sm);
-                        sm = fmaf(y[3 * r + 1], g1, sm);
-                        sm = fmaf(y[3 * r + 2], g2, sm);
+                        sm = fmaf(yr[3 * r], g0, sm);
+                        sm = fmaf(yr[3 * r + 1], g1, sm);
+                        sm = fmaf(yr[3 * r + 2], g2, sm);
                         part[r] = sm;
                     }
                 } else {
                     float yv[9], wv[9];
-#pragma unroll
-                    for (int e = 0; e < 9; ++e) {
-                        yv[e] = y[9 * (r0 / 3) + e];
-                        wv[e] = w[9 * (c0 / 3) + e];
-                    }
+                    ld_half9(y, r0 / 3, yv);
+                    ld_half9(w, c0 / 3, wv);
 #pragma unroll
                     for (int r = 0; r < 3; ++r)
 #pragma unroll
@@ -888,12 +939,9 @@ __device__ void stage_schur_mx(const BatchProblem &p, const Arenas<float> &ar, d
         if (q < p.n_pairs) {
             int n = 0;
             for (int t = pst[q] + s4; t < pst[q + 1]; t += nslot) {
-                const float *y = Y + 18 * (size_t)pa[t] + 9 * qr, *w = W + 18 * (size_t)pb[t] + 9 * qc;
                 float yv[9], wv[9];
-                for (int e = 0; e < 9; ++e) {
-                    yv[e] = y[e];
-                    wv[e] = w[e];
-                }
+                ld_half9(Y + 18 * (size_t)pa[t], qr, yv);
+                ld_half9(W + 18 * (size_t)pb[t], qc, wv);
                 for (int r = 0; r < 3; ++r)
                     for (int c = 0; c < 3; ++c) {
                         float sm = part[3 * r + c];
@@ -950,7 +998,8 @@ __device__ void stage_back_mx(const BatchProblem &p, const Arenas<float> &ar, do
     for (int i = threadIdx.x; i < p.np; i += blockDim.x) {
         float h[3] = {0.0f, 0.0f, 0.0f}, l[3] = {0.0f, 0.0f, 0.0f};
         for (int o = ps[i]; o < ps[i + 1]; ++o) {
-            const float *w = W + 18 * (size_t)o;
+            float w[18];
+            ld2n(W + 18 * (size_t)o, w, 18);
             const float2 *da = da2 + 6 * (size_t)ocam[o];
             for (int k = 0; k < 6; ++k) {
                 const float2 d2 = da[k];
@@ -1307,11 +1356,13 @@ bool build_problem_layout(const psba_problem_desc &p, ProblemLayout &L, std::str
     bp.i_pair_a = iput(pa.data(), pa.size());
     bp.i_pair_b = iput(pb.data(), pb.size());
     long long r_total = 0;
-    bp.r_ex = r_total; r_total += 2LL * no;
+    // A first: its 48-byte rows stay 16-byte aligned (every region and the
+    // problem's total are multiples of four elements), the others 8-byte
     bp.r_A = r_total; r_total += 12LL * no;
-    bp.r_B = r_total; r_total += 6LL * no;
     bp.r_W = r_total; r_total += 18LL * no;
     bp.r_Y = r_total; r_total += 18LL * no;
+    bp.r_B = r_total; r_total += 6LL * no;
+    bp.r_ex = r_total; r_total += 2LL * no;
     // the mixed form's FP32 copies (even counts: FP32 pairs stay 8-byte aligned)
     bp.r_tab32 = r_total; r_total += (long long)CAMTAB32 * nc;
     bp.r_tab2f = r_total; r_total += 2LL * RES_TAB2F * nc;

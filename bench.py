@@ -366,6 +366,52 @@ def timed_cut(P, torch, flush, solver, precision, k, reps):
             "iterations_per_s": k / (m / 1e3)}
 
 
+def predictability_horizon(trace_ref, trace_ctl, tol=MATCH_TOL):
+    """The last outer iteration k >= 1 up to which the costs of a run and of
+    its control (the same run with the points moved by one ulp) agree to tol
+    relative, and the run's cost there; (0, None) if they part at once."""
+    cr, cn = cost_by_iteration(trace_ref), cost_by_iteration(trace_ctl)
+    kh = 0
+    for k in range(1, min(len(cr), len(cn))):
+        if not abs(cr[k] - cn[k]) <= tol * cr[k]:
+            break
+        kh = k
+    return (kh, float(cr[kh])) if kh > 0 else (0, None)
+
+
+def summarize_matched(recs):
+    """Summary over per-problem matched-cost records (matched_cost_leg): how
+    many reached the FP64 converged cost in both forms, the speed-ups there
+    and at the predictability horizon, and the other minima the mixed form
+    ended in."""
+    both = [r for r in recs if r["fp64"]["reached"] and r["mixed"]["reached"]]
+    other = [r for r in recs if not r["mixed"]["reached"]]
+    hz = [r["horizon"] for r in recs if "horizon" in r and "speedup_mixed_vs_fp64" in r["horizon"]]
+    summary = {"problems": len(recs), "mixed_reached_fp64_minimum": len(both),
+               "mixed_ended_in_another_minimum": len(other),
+               "fp64_points_1ulp_same_minimum": sum(bool(r["fp64_points_1ulp"]["same_minimum"]) for r in recs)}
+    if both:
+        sp = [r["fp64"]["ms"] / r["mixed"]["ms"] for r in both]
+        summary.update({
+            "speedup_mixed_vs_fp64_geomean": float(np.exp(np.mean(np.log(sp)))),
+            "speedup_mixed_vs_fp64_min": float(min(sp)), "speedup_mixed_vs_fp64_max": float(max(sp)),
+            "fp64_ms_total": sum(r["fp64"]["ms"] for r in both),
+            "mixed_ms_total": sum(r["mixed"]["ms"] for r in both)})
+    if hz:
+        sp = [h["speedup_mixed_vs_fp64"] for h in hz]
+        summary["horizon"] = {
+            "problems_reached": len(hz), "iterations": [h["iteration"] for h in hz],
+            "speedup_mixed_vs_fp64_geomean": float(np.exp(np.mean(np.log(sp)))),
+            "speedup_mixed_vs_fp64_min": float(min(sp)), "speedup_mixed_vs_fp64_max": float(max(sp)),
+            "fp64_ms_total": sum(h["fp64"]["ms"] for h in hz), "mixed_ms_total": sum(h["mixed"]["ms"] for h in hz)}
+    if other:
+        summary["other_minima"] = [{"seed": r["seed"], "rel_vs_fp64": r["mixed"]["to_stopping_rule"]["rel_vs_fp64"],
+                                    "fp64_polish_rel_decrease":
+                                        r["mixed"]["to_stopping_rule"]["fp64_polish_rel_decrease"]}
+                                   for r in other]
+    return summary
+
+
 def cost_by_iteration(trace):
     """cost[k] = the cost after k outer iterations (accepted steps only
     change it), from a trace; cost[0] is not recorded and stays NaN."""
@@ -429,15 +475,8 @@ def matched_cost_leg(P, torch, flush, sc, args, reps, solver=None):
                                    "final_cost_rel_vs_fp64": (nud.final_cost - cstar) / cstar,
                                    "same_minimum": bool(abs(nud.final_cost - cstar) <= MATCH_TOL * cstar)}
         # the predictability horizon and the cost target there
-        cr, cn = cost_by_iteration(ref.trace), cost_by_iteration(nud.trace)
-        n = min(len(cr), len(cn))
-        kh = 0
-        for k in range(1, n):
-            if not abs(cr[k] - cn[k]) <= MATCH_TOL * cr[k]:
-                break
-            kh = k
+        kh, th = predictability_horizon(ref.trace, nud.trace)
         if kh > 0:
-            th = cr[kh]
             hz = {"iteration": kh, "cost": th}
             for tag, prec in (("fp64", P.PREC_FP64), ("mixed", P.PREC_MIXED)):
                 k = first_iteration_at(runs[tag].trace, th * (1.0 + MATCH_TOL))
@@ -468,31 +507,7 @@ def matched_cost_instances(P, torch, flush, scenes, args, reps, solver):
             r = matched_cost_leg(P, torch, flush, sc, args, reps)
         r["seed"] = seed
         recs.append(r)
-    both = [r for r in recs if r["fp64"]["reached"] and r["mixed"]["reached"]]
-    other = [r for r in recs if not r["mixed"]["reached"]]
-    hz = [r["horizon"] for r in recs if "horizon" in r and "speedup_mixed_vs_fp64" in r["horizon"]]
-    summary = {"problems": len(recs), "mixed_reached_fp64_minimum": len(both),
-               "mixed_ended_in_another_minimum": len(other),
-               "fp64_points_1ulp_same_minimum": sum(bool(r["fp64_points_1ulp"]["same_minimum"]) for r in recs)}
-    if both:
-        sp = [r["fp64"]["ms"] / r["mixed"]["ms"] for r in both]
-        summary.update({
-            "speedup_mixed_vs_fp64_geomean": float(np.exp(np.mean(np.log(sp)))),
-            "speedup_mixed_vs_fp64_min": float(min(sp)), "speedup_mixed_vs_fp64_max": float(max(sp)),
-            "fp64_ms_total": sum(r["fp64"]["ms"] for r in both),
-            "mixed_ms_total": sum(r["mixed"]["ms"] for r in both)})
-    if hz:
-        sp = [h["speedup_mixed_vs_fp64"] for h in hz]
-        summary["horizon"] = {
-            "problems_reached": len(hz), "iterations": [h["iteration"] for h in hz],
-            "speedup_mixed_vs_fp64_geomean": float(np.exp(np.mean(np.log(sp)))),
-            "speedup_mixed_vs_fp64_min": float(min(sp)), "speedup_mixed_vs_fp64_max": float(max(sp)),
-            "fp64_ms_total": sum(h["fp64"]["ms"] for h in hz), "mixed_ms_total": sum(h["mixed"]["ms"] for h in hz)}
-    if other:
-        summary["other_minima"] = [{"seed": r["seed"], "rel_vs_fp64": r["mixed"]["to_stopping_rule"]["rel_vs_fp64"],
-                                    "fp64_polish_rel_decrease":
-                                        r["mixed"]["to_stopping_rule"]["fp64_polish_rel_decrease"]}
-                                   for r in other]
+    summary = summarize_matched(recs)
     return {"summary": summary, "problems": recs}
 
 
